@@ -1,0 +1,304 @@
+"""GB300-native cell-centred TPFA porous-flow hot path (residual/Jacobian assembly by
+numeric differentiation, Newton, ILU(0)-preconditioned BiCGSTAB) behind the C ABI of
+include/dumux_gb300.h.
+
+The compute path is the CUDA library dumux_gb300/_lib/libdumux_gb300.so (built by
+dumux_gb300/build.py).  There is no CPU fallback: every entry point raises when the
+library or a CUDA device is missing.
+
+Python mirror of the reference interfaces (same method names and meaning):
+    FVAssembler            dumux/assembly/fvassembler.hh
+    ILUBiCGSTABIstlSolver  dumux/linear/istlsolvers.hh:635-642
+    NewtonSolver           dumux/nonlinear/newtonsolver.hh
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (DXG_PRECISION_FP64, DXG_PRECISION_MIXED, STATUS_NAMES, LinearResultC, NewtonParamsC,
+                  NewtonReportC, ProblemDesc, ProblemDescC, newton_params)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libdumux_gb300.so")
+_lib = None
+
+
+class DxgError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+
+
+class NumericalProblem(DxgError):
+    """Recoverable failure (linear breakdown / non-convergence), Dumux::NumericalProblem."""
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run dumux_gb300/build.py (nvcc, sm_103a)")
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        vp = C.c_void_p
+        L.dxg_num_boundary_faces.argtypes = [C.POINTER(ProblemDescC)]
+        L.dxg_num_boundary_faces.restype = C.c_int64
+        L.dxg_ctx_create.argtypes = [C.POINTER(vp), C.c_int]
+        L.dxg_ctx_destroy.argtypes = [vp]
+        L.dxg_last_error.argtypes = [vp]
+        L.dxg_last_error.restype = C.c_char_p
+        L.dxg_set_precision.argtypes = [vp, C.c_int]
+        L.dxg_problem_upload.argtypes = [vp, C.POINTER(ProblemDescC)]
+        L.dxg_sizes.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+        for name in ("dxg_set_solution", "dxg_get_solution", "dxg_set_prev_solution", "dxg_get_residual",
+                     "dxg_get_update"):
+            getattr(L, name).argtypes = [vp, dp]
+        L.dxg_set_time_step.argtypes = [vp, C.c_double]
+        L.dxg_assemble_jacobian_and_residual.argtypes = [vp]
+        L.dxg_assemble_residual.argtypes = [vp]
+        L.dxg_get_jacobian.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), dp]
+        L.dxg_set_linear_system.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), dp, dp]
+        L.dxg_linear_solve.argtypes = [vp, C.c_double, C.c_int32, C.POINTER(LinearResultC)]
+        L.dxg_residual_norm.argtypes = [vp, dp]
+        L.dxg_newton_default_params.argtypes = [C.POINTER(NewtonParamsC)]
+        L.dxg_newton_default_params.restype = None
+        L.dxg_newton_solve.argtypes = [vp, C.c_double, C.POINTER(NewtonParamsC), C.POINTER(NewtonReportC)]
+        L.dxg_suggest_time_step.argtypes = [vp, C.c_double, C.POINTER(NewtonParamsC)]
+        L.dxg_suggest_time_step.restype = C.c_double
+        L.dxg_advance_time_step.argtypes = [vp]
+        L.dxg_kernel_launch_count.argtypes = [vp]
+        L.dxg_kernel_launch_count.restype = C.c_int64
+        L.dxg_sync.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Context:
+    """One problem resident on one GPU (dxg_ctx)."""
+
+    def __init__(self, desc=None, device=0, precision="fp64"):
+        L = lib()
+        h = C.c_void_p()
+        st = L.dxg_ctx_create(C.byref(h), int(device))
+        if st != 0:
+            raise DxgError(st, L.dxg_last_error(None).decode())
+        self._h = h
+        self._L = L
+        prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
+        self._check(L.dxg_set_precision(h, prec))
+        self.precision = precision
+        self.desc = None
+        if desc is not None:
+            self.upload(desc)
+
+    def _check(self, st, recoverable=False):
+        if st != 0:
+            msg = self._L.dxg_last_error(self._h).decode()
+            if recoverable and st in (5, 6, 7, 8):
+                raise NumericalProblem(st, msg)
+            raise DxgError(st, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dxg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- problem / state ---------------------------------------------------------
+    def upload(self, desc):
+        self.desc = desc
+        d = desc.c
+        self._check(self._L.dxg_problem_upload(self._h, C.byref(d)))
+        n = C.c_int64(); b = C.c_int32(); nnzb = C.c_int64()
+        self._check(self._L.dxg_sizes(self._h, C.byref(n), C.byref(b), C.byref(nnzb)))
+        self.num_cells, self.num_eq, self.num_blocks = n.value, b.value, nnzb.value
+        self.num_dofs = self.num_cells * self.num_eq
+
+    def _vec(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        if a.size != self.num_dofs:
+            raise ValueError(f"expected {self.num_dofs} values, got {a.size}")
+        return a
+
+    def set_solution(self, u):
+        self._check(self._L.dxg_set_solution(self._h, _dp(self._vec(u))))
+
+    def solution(self):
+        out = np.empty(self.num_dofs)
+        self._check(self._L.dxg_get_solution(self._h, _dp(out)))
+        return out
+
+    def set_prev_solution(self, u):
+        self._check(self._L.dxg_set_prev_solution(self._h, _dp(self._vec(u))))
+
+    def set_time_step(self, dt):
+        self._check(self._L.dxg_set_time_step(self._h, float(dt)))
+
+    def advance_time_step(self):
+        self._check(self._L.dxg_advance_time_step(self._h))
+
+    # -- assembler ---------------------------------------------------------------
+    def assemble_jacobian_and_residual(self):
+        self._check(self._L.dxg_assemble_jacobian_and_residual(self._h), recoverable=True)
+
+    def assemble_residual(self):
+        self._check(self._L.dxg_assemble_residual(self._h), recoverable=True)
+
+    def residual(self):
+        out = np.empty(self.num_dofs)
+        self._check(self._L.dxg_get_residual(self._h, _dp(out)))
+        return out
+
+    def jacobian(self):
+        """(row_ptr, col_idx, values) in BCRS layout, blocks row-major."""
+        b = self.num_eq
+        row_ptr = np.empty(self.num_cells + 1, dtype=np.int64)
+        col = np.empty(self.num_blocks, dtype=np.int32)
+        vals = np.empty(self.num_blocks * b * b)
+        self._check(self._L.dxg_get_jacobian(self._h, row_ptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             col.ctypes.data_as(C.POINTER(C.c_int32)), _dp(vals)))
+        return row_ptr, col, vals
+
+    def set_linear_system(self, row_ptr, col, vals, rhs):
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self._L.dxg_set_linear_system(self._h, row_ptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                  col.ctypes.data_as(C.POINTER(C.c_int32)), _dp(vals),
+                                                  _dp(self._vec(rhs))))
+
+    # -- linear solver -----------------------------------------------------------
+    def linear_solve(self, reduction=1e-13, max_iter=250, raise_on_failure=False):
+        res = LinearResultC()
+        st = self._L.dxg_linear_solve(self._h, float(reduction), int(max_iter), C.byref(res))
+        if st not in (0, 6) or (raise_on_failure and st != 0):
+            self._check(st, recoverable=True)
+        return {"converged": bool(res.converged), "iterations": res.iterations, "reduction": res.reduction,
+                "initial_defect": res.initial_defect, "final_defect": res.final_defect}
+
+    def update(self):
+        out = np.empty(self.num_dofs)
+        self._check(self._L.dxg_get_update(self._h, _dp(out)))
+        return out
+
+    def residual_norm(self):
+        v = C.c_double()
+        self._check(self._L.dxg_residual_norm(self._h, C.byref(v)))
+        return v.value
+
+    # -- Newton ------------------------------------------------------------------
+    def newton_solve(self, dt=0.0, params=None, raise_on_failure=True):
+        p = params if params is not None else newton_params()
+        rep = NewtonReportC()
+        st = self._L.dxg_newton_solve(self._h, float(dt), C.byref(p), C.byref(rep))
+        if st != 0 and raise_on_failure:
+            self._check(st, recoverable=True)
+        out = rep.as_dict()
+        out["status"] = st
+        return out
+
+    def suggest_time_step(self, old_dt, params=None):
+        p = params if params is not None else newton_params()
+        return self._L.dxg_suggest_time_step(self._h, float(old_dt), C.byref(p))
+
+    def kernel_launches(self):
+        return int(self._L.dxg_kernel_launch_count(self._h))
+
+    def sync(self):
+        self._check(self._L.dxg_sync(self._h))
+
+
+# ---------------------------------------------------------------- reference-named mirror
+class FVAssembler:
+    """dumux/assembly/fvassembler.hh:101-662 over a device-resident problem."""
+
+    def __init__(self, desc, prev_sol=None, dt=None, device=0, precision="fp64"):
+        self.ctx = Context(desc, device=device, precision=precision)
+        if prev_sol is not None:
+            self.set_previous_solution(prev_sol)
+        if dt is not None:
+            self.ctx.set_time_step(dt)
+
+    def is_stationary_problem(self):
+        return self.ctx.desc is not None and not hasattr(self, "_dt")
+
+    def set_previous_solution(self, u):
+        self.ctx.set_prev_solution(u)
+
+    def assemble_jacobian_and_residual(self, u):
+        self.ctx.set_solution(u)
+        self.ctx.assemble_jacobian_and_residual()
+
+    def assemble_residual(self, u):
+        self.ctx.set_solution(u)
+        self.ctx.assemble_residual()
+
+    def jacobian(self):
+        return self.ctx.jacobian()
+
+    def residual(self):
+        return self.ctx.residual()
+
+    assembleJacobianAndResidual = assemble_jacobian_and_residual
+    assembleResidual = assemble_residual
+
+
+class ILUBiCGSTABIstlSolver:
+    """dumux/linear/istlsolvers.hh:635-642: ILU(0)-preconditioned BiCGSTAB."""
+
+    def __init__(self, residual_reduction=1e-13, max_iter=250):
+        self.reduction = residual_reduction
+        self.max_iter = max_iter
+
+    def set_residual_reduction(self, r):
+        self.reduction = r
+
+    def set_max_iter(self, n):
+        self.max_iter = n
+
+    def solve(self, assembler):
+        """Solves the assembler's J x = r on the device; returns (converged, x)."""
+        res = assembler.ctx.linear_solve(self.reduction, self.max_iter)
+        return res["converged"], assembler.ctx.update()
+
+    def norm(self, assembler):
+        return assembler.ctx.residual_norm()
+
+    setResidualReduction = set_residual_reduction
+
+
+class NewtonSolver:
+    """dumux/nonlinear/newtonsolver.hh: solve(x, dt) with dt halving, solve(x) stationary."""
+
+    def __init__(self, assembler, linear_solver=None, **params):
+        self.assembler = assembler
+        self.params = newton_params(**params)
+        if linear_solver is not None:
+            self.params.linear_max_iter = linear_solver.max_iter
+        self.last_report = None
+
+    def solve(self, u, dt=0.0):
+        ctx = self.assembler.ctx
+        ctx.set_solution(u)
+        self.last_report = ctx.newton_solve(dt, self.params)
+        return ctx.solution()
+
+    def suggest_time_step_size(self, old_dt):
+        return self.assembler.ctx.suggest_time_step(old_dt, self.params)
+
+    suggestTimeStepSize = suggest_time_step_size
+
+
+__all__ = ["Context", "FVAssembler", "ILUBiCGSTABIstlSolver", "NewtonSolver", "ProblemDesc", "newton_params",
+           "DxgError", "NumericalProblem", "lib", "LIB_PATH"]

@@ -1,0 +1,1180 @@
+// api.cu -- C ABI of the GB300 cc-TPFA hot path: context, problem tabulation,
+// assembler, ILU(0)-BiCGSTAB driver and the Newton driver.
+//
+// Host code in this file is compiled with FP contraction disabled: the tabulated
+// transmissibilities, gravity terms and Dirichlet ghost states are computed with the
+// reference's operation order (dumux/flux/cctpfa/darcyslaw.hh:153-259,
+// dumux/discretization/cellcentered/tpfa/computetransmissibility.hh:66-80) and so are
+// bit-identical to what the reference evaluates for every face.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+
+using namespace dxg;
+
+namespace {
+
+std::string g_createError;
+
+// ---------------------------------------------------------------- host geometry
+struct HostGrid {
+    int dim;
+    int64_t n[3];
+    const double* x[3];
+    void ijk(int64_t c, int64_t* id) const
+    {
+        id[0] = c % n[0];
+        id[1] = (c / n[0]) % n[1];
+        id[2] = c / (n[0] * n[1]);
+    }
+    double lo(int a, int64_t i) const { return x[a][i]; }
+    double hi(int a, int64_t i) const { return x[a][i + 1]; }
+    void center(const int64_t* id, double* c) const
+    {
+        for (int a = 0; a < 3; ++a) c[a] = 0.0;
+        for (int a = 0; a < dim; ++a) c[a] = 0.5 * (lo(a, id[a]) + hi(a, id[a]));
+    }
+    double volume(const int64_t* id) const
+    {
+        double v = 1.0;
+        for (int a = 0; a < dim; ++a) v *= hi(a, id[a]) - lo(a, id[a]);
+        return v;
+    }
+    double faceArea(const int64_t* id, int axis) const
+    {
+        double ar = 1.0;
+        for (int k = 0; k < dim; ++k)
+            if (k != axis) ar *= hi(k, id[k]) - lo(k, id[k]);
+        return ar;
+    }
+};
+
+// computeTpfaTransmissibility with a scalar permeability: K*extr*((ip-c)/|ip-c|^2 . n)
+double tpfaT(int dim, const double* ip, const double* n, const double* c, double K, double extr)
+{
+    double d[3];
+    for (int i = 0; i < dim; ++i) d[i] = ip[i] - c[i];
+    double n2 = 0.0;
+    for (int i = 0; i < dim; ++i) n2 += d[i] * d[i];
+    for (int i = 0; i < dim; ++i) d[i] /= n2;
+    double dot = 0.0;
+    for (int i = 0; i < dim; ++i) dot += d[i] * n[i];
+    return K * extr * dot;
+}
+
+double dotN(int dim, const double* n, const double* g)
+{
+    double s = 0.0;
+    for (int i = 0; i < dim; ++i) s += n[i] * g[i];
+    return s;
+}
+
+// BrooksCoreyDefault evaluated on the host (Dirichlet ghost states, law constants)
+MaterialLaw makeLaw(const double* prm)
+{
+    MaterialLaw m{};
+    m.pe = prm[0];
+    m.lambda = prm[1];
+    m.swr = prm[2];
+    m.snr = prm[3];
+    m.pcLowSwe = prm[4];
+    m.denom = 1.0 - m.swr - m.snr;
+    m.expPc = -1.0 / m.lambda;
+    m.expKrw = 2.0 / m.lambda + 3.0;
+    m.expKrn = 2.0 / m.lambda + 1.0;
+    auto swToSwe = [&](double sw) { return (sw - m.swr) / (1.0 - m.swr - m.snr); };
+    auto sweToSw = [&](double swe) { return swe * (1.0 - m.swr - m.snr) + m.swr; };
+    auto clamp01 = [](double v) { return std::clamp(v, 0.0, 1.0); };
+    auto dpc_dswe = [&](double swe) { swe = clamp01(swe); return -m.pe / m.lambda * std::pow(swe, -1.0 / m.lambda - 1.0); };
+    const double dswe_dsw = 1.0 / (1.0 - m.swr - m.snr);
+    const double dsw_dswe = 1.0 - m.swr - m.snr;
+    const double lowSw = sweToSw(m.pcLowSwe);
+    const double highSw = sweToSw(1.0);
+    m.entryPressure = m.pe;
+    m.pcDerivativeLowSw = dpc_dswe(swToSwe(lowSw)) * dswe_dsw * dsw_dswe;
+    m.pcDerivativeHighSwEnd = dpc_dswe(swToSwe(highSw)) * dswe_dsw * dsw_dswe;
+    m.pcLowSwePcValue = m.pe * std::pow(clamp01(swToSwe(lowSw)), -1.0 / m.lambda);
+    return m;
+}
+double hostPc(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
+    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0) + m.entryPressure;
+    return m.pe * std::pow(std::clamp(swe, 0.0, 1.0), m.expPc);
+}
+double hostKrw(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0) return 0.0;
+    else if (swe >= 1.0) return 1.0;
+    return std::pow(std::clamp(swe, 0.0, 1.0), m.expKrw);
+}
+double hostKrn(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0) return 1.0;
+    else if (swe >= 1.0) return 0.0;
+    const double s = std::clamp(swe, 0.0, 1.0);
+    const double sne = 1.0 - s;
+    return sne * sne * (1.0 - std::pow(s, m.expKrn));
+}
+
+template <class T>
+void upload(DevBuf<T>& buf, const std::vector<T>& h, cudaStream_t st)
+{
+    buf.alloc(h.size());
+    if (!h.empty()) DXG_CUDA(cudaMemcpyAsync(buf.get(), h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+int fail(dxg_ctx* ctx, const Error& e)
+{
+    if (ctx) ctx->err = e.what();
+    return e.status;
+}
+
+template <class F>
+int guarded(dxg_ctx* ctx, F&& f)
+{
+    try {
+        return f();
+    } catch (const Error& e) {
+        return fail(ctx, e);
+    } catch (const std::bad_alloc&) {
+        if (ctx) ctx->err = "host allocation failed";
+        return DXG_ERR_OOM;
+    } catch (const std::exception& e) {
+        if (ctx) ctx->err = e.what();
+        return DXG_ERR_ARG;
+    }
+}
+
+void requireUploaded(const dxg_ctx* ctx)
+{
+    if (!ctx || !ctx->uploaded) throw Error(DXG_ERR_STATE, "no problem uploaded");
+}
+
+}  // namespace
+
+dxg::AssemblyArgs dxg_ctx::asmArgs() const
+{
+    AssemblyArgs a{};
+    a.pc = pcDev.get();
+    a.N = N;
+    a.nb = nb;
+    a.vol = vol.get();
+    a.phi = phi.get();
+    a.extr = extr.get();
+    a.mat = mat.get();
+    a.srcterm = srcterm.get();
+    a.tijPlus = tijPlus.get();
+    a.G1 = G1.get();
+    a.G2 = G2.get();
+    a.btype = btype.get();
+    a.bTij = bTij.get();
+    a.bG1 = bG1.get();
+    a.bP = bP.get();
+    a.bU = bU.get();
+    a.bNeu = bNeu.get();
+    a.vvP = vvP.get();
+    a.vvU = vvU.get();
+    a.vvS = vvS.get();
+    a.eps = eps.get();
+    a.stPrev = stPrev.get();
+    a.A = A.get();
+    a.r = r.get();
+    a.dt = dt;
+    return a;
+}
+
+namespace {
+
+// ---------------------------------------------------------------- tabulation
+void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
+{
+    if (!d) throw Error(DXG_ERR_ARG, "null problem description");
+    if (d->dim != 2 && d->dim != 3) throw Error(DXG_ERR_ARG, "dim must be 2 or 3");
+    if (d->num_eq != 1 && d->num_eq != 2) throw Error(DXG_ERR_ARG, "num_eq must be 1 or 2");
+    for (int a = 0; a < d->dim; ++a)
+        if (d->cells[a] < 1 || !d->coords[a]) throw Error(DXG_ERR_ARG, "invalid cells/coords");
+    if (!d->permeability || !d->porosity || !d->bc_type || !d->bc_values) throw Error(DXG_ERR_ARG, "missing tables");
+    const int method = d->numeric_difference_method;
+    if (method != 1 && method != 0 && method != -1)
+        throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0 or -1 on the device");
+    if (d->num_eq == 2 && (d->num_materials < 1 || d->num_materials > kMaxMaterials || !d->material_params))
+        throw Error(DXG_ERR_ARG, "2p needs 1..16 Brooks-Corey parameter sets");
+
+    const int dim = d->dim, b = d->num_eq;
+    HostGrid g{};
+    g.dim = dim;
+    for (int a = 0; a < 3; ++a) g.n[a] = a < dim ? d->cells[a] : 1;
+    for (int a = 0; a < dim; ++a) g.x[a] = d->coords[a];
+    const int64_t N = g.n[0] * g.n[1] * g.n[2];
+    if (N > (int64_t)INT32_MAX) throw Error(DXG_ERR_ARG, "too many cells");
+
+    c->dim = dim;
+    c->b = b;
+    c->N = N;
+    c->M = N * b;
+    c->slots = 2 * dim + 1;
+    c->bb = b * b;
+    c->method = method;
+    c->gravity = d->enable_gravity != 0;
+    c->fullUpwind = d->upwind_weight != 1.0;
+
+    double grav[3] = {0, 0, 0};
+    if (c->gravity)
+        for (int a = 0; a < dim; ++a) grav[a] = d->gravity[a];
+    const int va = dim - 1;
+    for (int a = 0; a < dim - 1; ++a)
+        if (grav[a] != 0.0) throw Error(DXG_ERR_ARG, "gravity must act along the last axis");
+
+    // problem constants
+    ProblemConsts& pc = c->pcHost;
+    pc = ProblemConsts{};
+    pc.dim = dim;
+    pc.b = b;
+    pc.nx = (int)g.n[0];
+    pc.ny = (int)g.n[1];
+    pc.nz = (int)g.n[2];
+    pc.N = N;
+    pc.sideOffset[0] = 0;
+    for (int f = 0; f < 2 * dim; ++f) {
+        const int a = f / 2;
+        int64_t cnt = 1;
+        for (int k = 0; k < dim; ++k)
+            if (k != a) cnt *= g.n[k];
+        pc.sideOffset[f + 1] = pc.sideOffset[f] + cnt;
+    }
+    const int64_t nb = pc.sideOffset[2 * dim];
+    c->nb = nb;
+    pc.gravity = c->gravity;
+    pc.gravAxisMask = (c->gravity && grav[va] != 0.0) ? (1 << va) : 0;
+    for (int p = 0; p < 2; ++p) {
+        pc.density[p] = d->density[p];
+        pc.viscosity[p] = d->viscosity[p];
+        pc.magnitude[p] = d->privar_magnitude[p];
+    }
+    pc.mobility1p = 1.0 / d->viscosity[0];
+    pc.upwindWeight = d->upwind_weight;
+    pc.upwindFull = c->fullUpwind;
+    pc.method = method;
+    pc.baseEps = d->base_epsilon > 0 ? d->base_epsilon : 1e-10;
+    pc.numMaterials = b == 2 ? d->num_materials : 0;
+    pc.hasSource = d->source != nullptr;
+    for (int m = 0; m < pc.numMaterials; ++m) pc.law[m] = makeLaw(d->material_params + 5 * m);
+
+    const int64_t strides[3] = {1, g.n[0], g.n[0] * g.n[1]};
+    for (int s = 0; s < c->slots; ++s) c->off[s] = 0;
+    for (int a = 0; a < dim; ++a) {
+        c->off[dim - 1 - a] = -strides[a];
+        c->off[dim + 1 + a] = strides[a];
+    }
+
+    // per-cell tables
+    std::vector<double> vol(N), phi(N), extr(N), srcterm((size_t)b * N, 0.0), tijPlus((size_t)dim * N, 0.0);
+    std::vector<double> G1((size_t)2 * b * N, 0.0), G2((size_t)2 * b * N, 0.0);
+    std::vector<int32_t> mat(N, 0);
+    std::vector<uint8_t> nbmask(N, 0);
+    auto K = [&](int64_t i) { return d->permeability[i]; };
+    auto EX = [&](int64_t i) { return d->extrusion ? d->extrusion[i] : 1.0; };
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t id[3];
+        g.ijk(i, id);
+        vol[i] = g.volume(id);
+        phi[i] = d->porosity[i];
+        extr[i] = EX(i);
+        if (b == 2) {
+            mat[i] = d->material ? d->material[i] : 0;
+            if (mat[i] < 0 || mat[i] >= pc.numMaterials) throw Error(DXG_ERR_ARG, "material index out of range");
+        }
+        const double s = vol[i] * extr[i];
+        for (int e = 0; e < b; ++e) {
+            double src = 0.0;
+            if (d->source) src += d->source[i * b + e];
+            src *= s;
+            srcterm[(size_t)e * N + i] = src;
+        }
+        unsigned m = 0;
+        for (int f = 0; f < 2 * dim; ++f) {
+            const int a = f / 2;
+            const bool interior = (f & 1) ? id[a] < g.n[a] - 1 : id[a] > 0;
+            if (interior) m |= 1u << f;
+        }
+        nbmask[i] = (uint8_t)m;
+    }
+    // interior faces: transmissibility of the + face of every axis, gravity terms of the
+    // vertical faces (both orientations)
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t id[3];
+        g.ijk(i, id);
+        double ci[3];
+        g.center(id, ci);
+        for (int a = 0; a < dim; ++a) {
+            if (id[a] >= g.n[a] - 1) continue;
+            const int64_t j = i + strides[a];
+            int64_t jd[3] = {id[0], id[1], id[2]};
+            jd[a] += 1;
+            double cj[3];
+            g.center(jd, cj);
+            double ip[3] = {ci[0], ci[1], ci[2]};
+            ip[a] = g.hi(a, id[a]);
+            double n[3] = {0, 0, 0};
+            n[a] = 1.0;
+            const double area = g.faceArea(id, a);
+            const double ti = tpfaT(dim, ip, n, ci, K(i), EX(i));
+            const double tj = -1.0 * tpfaT(dim, ip, n, cj, K(j), EX(j));
+            const double tij = (ti * tj <= 0.0) ? 0 : area * (ti * tj) / (ti + tj);
+            tijPlus[(size_t)a * N + i] = tij;
+            if (c->gravity && a == va && grav[va] != 0.0) {
+                // directed from i (+ face of i) and from j (- face of j)
+                for (int side = 0; side < 2; ++side) {
+                    const int64_t in = side == 0 ? i : j, out = side == 0 ? j : i;
+                    const double* cin = side == 0 ? ci : cj;
+                    const double* cout = side == 0 ? cj : ci;
+                    double nn[3] = {0, 0, 0};
+                    nn[a] = side == 0 ? 1.0 : -1.0;
+                    // recompute the transmissibility from this side, as the reference does
+                    const double tIn = tpfaT(dim, ip, nn, cin, K(in), EX(in));
+                    const double tOut = -1.0 * tpfaT(dim, ip, nn, cout, K(out), EX(out));
+                    const double tijS = (tIn * tOut <= 0.0) ? 0 : area * (tIn * tOut) / (tIn + tOut);
+                    if (tijS != tij) throw Error(DXG_ERR_ARG, "asymmetric transmissibility");
+                    const double ng = dotN(dim, nn, grav);
+                    const double alphaIn = K(in) * ng * EX(in);
+                    const double alphaOut = K(out) * ng * EX(out);
+                    const double outsideTi = -1.0 * tpfaT(dim, ip, nn, cout, K(out), EX(out));
+                    for (int ph = 0; ph < b; ++ph) {
+                        const double rho = (d->density[ph] + d->density[ph]) * 0.5;
+                        const double g1 = rho * area * alphaIn;
+                        const double g2 = rho * tijS / outsideTi * (alphaIn - alphaOut);
+                        // stored at the inside cell under its face side (0: -va face, 1: +va face)
+                        const int fs = side == 0 ? 1 : 0;
+                        G1[((size_t)fs * b + ph) * N + in] = g1;
+                        G2[((size_t)fs * b + ph) * N + in] = g2;
+                    }
+                }
+            }
+        }
+    }
+    // boundary faces
+    std::vector<int8_t> btype(nb);
+    std::vector<double> bTij(nb, 0.0), bG1((size_t)b * nb, 0.0), bP((size_t)b * nb, 0.0), bU((size_t)b * nb, 0.0),
+        bNeu((size_t)b * nb, 0.0);
+    for (int f = 0; f < 2 * dim; ++f) {
+        const int a = f / 2, side = f & 1;
+        int o1 = -1, o2 = -1;
+        for (int k = 0; k < dim; ++k)
+            if (k != a) { if (o1 < 0) o1 = k; else o2 = k; }
+        const int64_t n1 = g.n[o1], n2 = o2 >= 0 ? g.n[o2] : 1;
+        for (int64_t q2 = 0; q2 < n2; ++q2)
+            for (int64_t q1 = 0; q1 < n1; ++q1) {
+                const int64_t bidx = pc.sideOffset[f] + q1 + n1 * q2;
+                int64_t id[3] = {0, 0, 0};
+                id[a] = side ? g.n[a] - 1 : 0;
+                id[o1] = q1;
+                if (o2 >= 0) id[o2] = q2;
+                const int64_t i = id[0] + strides[1] * id[1] + strides[2] * id[2];
+                const int8_t t = d->bc_type[bidx];
+                if (t != 1 && t != 2) throw Error(DXG_ERR_ARG, "boundary type must be 1 (Dirichlet) or 2 (Neumann)");
+                btype[bidx] = t;
+                double ci[3];
+                g.center(id, ci);
+                double ip[3] = {ci[0], ci[1], ci[2]};
+                ip[a] = side ? g.hi(a, id[a]) : g.lo(a, id[a]);
+                double n[3] = {0, 0, 0};
+                n[a] = side ? 1.0 : -1.0;
+                const double area = g.faceArea(id, a);
+                const double* bv = d->bc_values + bidx * b;
+                if (t == 1) {
+                    const double ti = tpfaT(dim, ip, n, ci, K(i), EX(i));
+                    bTij[bidx] = area * ti;
+                    // ghost volume variables from the Dirichlet values with the inside cell's
+                    // spatial parameters (elementvolumevariables.hh:317-342)
+                    if (b == 1) {
+                        bP[bidx] = bv[0];
+                        bU[bidx] = d->density[0] * (1.0 / d->viscosity[0]);
+                    } else {
+                        const MaterialLaw& m = pc.law[mat[i]];
+                        const double Sn = bv[1];
+                        const double Sw = 1 - Sn;
+                        const double pcap = hostPc(m, Sw);
+                        bP[0 * nb + bidx] = bv[0];
+                        bP[1 * nb + bidx] = bv[0] + pcap;
+                        bU[0 * nb + bidx] = d->density[0] * (hostKrw(m, Sw) / d->viscosity[0]);
+                        bU[1 * nb + bidx] = d->density[1] * (hostKrn(m, Sw) / d->viscosity[1]);
+                    }
+                    if (c->gravity && a == va && grav[va] != 0.0) {
+                        const double ng = dotN(dim, n, grav);
+                        const double alphaIn = K(i) * ng * EX(i);
+                        for (int ph = 0; ph < b; ++ph) bG1[(size_t)ph * nb + bidx] = d->density[ph] * area * alphaIn;
+                    }
+                } else {
+                    const double s = area * EX(i);
+                    for (int e = 0; e < b; ++e) {
+                        double q = 0.0;
+                        q += bv[e] * s;
+                        bNeu[(size_t)e * nb + bidx] = q;
+                    }
+                }
+            }
+    }
+    // level schedule of the ILU(0) wavefront
+    const int numLevels = (int)(g.n[0] + g.n[1] + g.n[2] - 2);
+    std::vector<int32_t> cnt(numLevels + 1, 0), perm(N);
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t id[3];
+        g.ijk(i, id);
+        cnt[id[0] + id[1] + id[2] + 1]++;
+    }
+    for (int L = 0; L < numLevels; ++L) cnt[L + 1] += cnt[L];
+    c->levels.numLevels = numLevels;
+    c->levels.ptr = cnt;
+    {
+        std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
+        for (int64_t i = 0; i < N; ++i) {
+            int64_t id[3];
+            g.ijk(i, id);
+            perm[pos[id[0] + id[1] + id[2]]++] = (int32_t)i;
+        }
+    }
+    int64_t nnzb = N;
+    for (int64_t i = 0; i < N; ++i)
+        for (int f = 0; f < 2 * dim; ++f) nnzb += (nbmask[i] >> f) & 1;
+    c->nnzb = nnzb;
+    c->nbmaskHost = nbmask;
+
+    cudaStream_t st = c->stream;
+    c->pcDev.alloc(1);
+    DXG_CUDA(cudaMemcpyAsync(c->pcDev.get(), &c->pcHost, sizeof(ProblemConsts), cudaMemcpyHostToDevice, st));
+    upload(c->vol, vol, st);
+    upload(c->phi, phi, st);
+    upload(c->extr, extr, st);
+    upload(c->srcterm, srcterm, st);
+    upload(c->tijPlus, tijPlus, st);
+    upload(c->G1, G1, st);
+    upload(c->G2, G2, st);
+    upload(c->mat, mat, st);
+    upload(c->nbmask, nbmask, st);
+    upload(c->btype, btype, st);
+    upload(c->bTij, bTij, st);
+    upload(c->bG1, bG1, st);
+    upload(c->bP, bP, st);
+    upload(c->bU, bU, st);
+    upload(c->bNeu, bNeu, st);
+    upload(c->perm, perm, st);
+    DXG_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
+
+    const int NS = 1 + (method == 0 ? 2 * b : b);
+    const int64_t M = N * b;
+    c->u.alloc(M);
+    c->uprev.alloc(M);
+    c->uLast.alloc(M);
+    c->stPrev.alloc((size_t)b * N);
+    c->vvP.alloc((size_t)NS * b * N);
+    c->vvU.alloc((size_t)NS * b * N);
+    c->vvS.alloc((size_t)NS * b * N);
+    c->eps.alloc((size_t)b * N);
+    c->A.alloc((size_t)c->slots * N * c->bb);
+    c->r.alloc(M);
+    c->delta.alloc(M);
+    c->defect.alloc(M);
+    DXG_CUDA(cudaMemsetAsync(c->u.get(), 0, M * sizeof(double), st));
+    DXG_CUDA(cudaMemsetAsync(c->uprev.get(), 0, M * sizeof(double), st));
+    DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, M * sizeof(double), st));
+    if (c->precision == DXG_PRECISION_FP64) {
+        c->L.alloc((size_t)dim * N * c->bb);
+        c->Dinv.alloc((size_t)N * c->bb);
+        for (auto* v : {&c->kx, &c->kr, &c->krt, &c->kp, &c->kv, &c->kt, &c->ky}) v->alloc(M);
+    } else {
+        c->Af.alloc((size_t)c->slots * N * c->bb);
+        c->Lf.alloc((size_t)dim * N * c->bb);
+        c->Dinvf.alloc((size_t)N * c->bb);
+        for (auto* v : {&c->fx, &c->fr, &c->frt, &c->fp, &c->fv, &c->ft, &c->fy}) v->alloc(M);
+    }
+    c->ks.alloc(1);
+    c->partials.alloc(3 * kMaxReduceBlocks);
+    c->counters.alloc(8);
+    c->scal.alloc(4);
+    c->singular.alloc(1);
+    DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
+    DXG_CUDA(cudaStreamSynchronize(st));
+    c->uploaded = true;
+    c->havePrev = false;
+    c->stPrevValid = false;
+    c->haveJac = c->haveRes = c->haveFactor = false;
+}
+
+// ---------------------------------------------------------------- assembly
+void ensurePrevStorage(dxg_ctx* c)
+{
+    if (c->dt > 0.0 && !c->stPrevValid) {
+        launchPrevStorage(c->asmArgs(), c->b, c->uprev.get(), c->stream);
+        c->launches += 1;
+        c->stPrevValid = true;
+    }
+}
+
+void assemble(dxg_ctx* c, bool jac)
+{
+    requireUploaded(c);
+    if (c->dt > 0.0 && !c->havePrev) throw Error(DXG_ERR_STATE, "transient assembly needs the previous solution");
+    ensurePrevStorage(c);
+    const AssemblyArgs a = c->asmArgs();
+    launchVolvars(a, c->b, jac ? c->method : 2, c->u.get(), c->stream);
+    launchRow(a, c->b, c->dim, c->method, jac, c->gravity && c->pcHost.gravAxisMask, c->dt > 0.0, c->fullUpwind,
+              c->stream);
+    c->launches += 2;
+    c->haveRes = true;
+    if (jac) {
+        c->haveJac = true;
+        c->haveFactor = false;
+    }
+}
+
+double deviceNorm(dxg_ctx* c, const double* x)
+{
+    launchNorm2(x, c->M, c->scratch(), c->scal.get() + 1, c->stream);
+    c->launches += 1;
+    DXG_CUDA(cudaMemcpyAsync(c->scalHost + 1, c->scal.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    DXG_CUDA(cudaStreamSynchronize(c->stream));
+    return c->scalHost[1];
+}
+
+// ---------------------------------------------------------------- linear solve
+__global__ void toFloatKernel(const double* __restrict__ x, float* __restrict__ y, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        y[k] = (float)x[k];
+}
+__global__ void axpyDoubleKernel(double* __restrict__ y, const float* __restrict__ x, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        y[k] += (double)x[k];
+}
+// defect = r - A*delta in FP64 (iterative refinement of the mixed-precision solve)
+__global__ void defectKernel(SpmvArgs<double, double> a, const double* __restrict__ rhs, int b, int dim)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned m = a.nbmask[i];
+        double acc[2] = {0.0, 0.0};
+        for (int s = 0; s < 2 * dim + 1; ++s) {
+            if (s != dim) {
+                const int f = s < dim ? 2 * (dim - 1 - s) : 2 * (s - dim - 1) + 1;
+                if (!((m >> f) & 1u)) continue;
+            }
+            const int64_t j = i + a.off[s];
+            const double* blk = a.A + ((int64_t)s * a.N + i) * b * b;
+            for (int rr = 0; rr < b; ++rr)
+                for (int cc = 0; cc < b; ++cc) acc[rr] += blk[rr * b + cc] * a.x[j * b + cc];
+        }
+        for (int rr = 0; rr < b; ++rr) a.y[i * b + rr] = rhs[i * b + rr] - acc[rr];
+    }
+}
+
+template <class T>
+IluArgs<T, T> iluArgs(dxg_ctx* c, const T* A, T* L, T* Dinv)
+{
+    IluArgs<T, T> a{};
+    a.A = A;
+    a.L = L;
+    a.Dinv = Dinv;
+    a.nbmask = c->nbmask.get();
+    a.perm = c->perm.get();
+    a.N = c->N;
+    for (int s = 0; s < 7; ++s) a.off[s] = c->off[s];
+    a.singular = c->singular.get();
+    a.ks = c->ks.get();
+    return a;
+}
+
+// BiCGSTAB with ILU(0) on the device from x = 0 for rhs (FP64 in device memory).
+template <class T>
+dxg_linear_result bicgstab(dxg_ctx* c, const T* A, T* L, T* Dinv, T* x, T* r, T* rt, T* p, T* v, T* t, T* y,
+                           const double* rhs, double reduction, int maxit, bool refactor)
+{
+    cudaStream_t st = c->stream;
+    IluArgs<T, T> ia = iluArgs<T>(c, A, L, Dinv);
+    if (refactor) {
+        DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, sizeof(int), st));
+        c->launches += launchIluFactor<T>(ia, c->levels, c->b, c->dim, st);
+    }
+    BicgArgs<T> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch()};
+    KrylovState init{};
+    init.reduction = reduction;
+    init.maxHalf = 2 * maxit;
+    DXG_CUDA(cudaMemcpyAsync(c->ks.get(), &init, sizeof(KrylovState), cudaMemcpyHostToDevice, st));
+    launchBicgInit<T>(ba, rhs, st);
+    c->launches += 1;
+    SpmvArgs<T, T> sv{};
+    sv.A = A;
+    sv.nbmask = c->nbmask.get();
+    sv.N = c->N;
+    for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
+    sv.ks = c->ks.get();
+    sv.scratch = c->scratch();
+    const int chunk = 4;
+    int done = 0;
+    while (true) {
+        for (int k = 0; k < chunk; ++k) {
+            launchBicgRho<T>(ba, st);
+            launchBicgUpdateP<T>(ba, st);
+            c->launches += 2 + launchIluApply<T, T>(ia, c->levels, c->b, c->dim, p, y, st);
+            sv.x = y; sv.y = v; sv.w = rt;
+            launchSpmv<T, T>(sv, c->b, c->dim, 1, st);
+            launchBicgAxpyNorm<T>(ba, 0, st);
+            c->launches += 2 + launchIluApply<T, T>(ia, c->levels, c->b, c->dim, r, y, st);
+            sv.x = y; sv.y = t; sv.w = r;
+            launchSpmv<T, T>(sv, c->b, c->dim, 2, st);
+            launchBicgAxpyNorm<T>(ba, 1, st);
+            c->launches += 2;
+        }
+        done += chunk;
+        DXG_CUDA(cudaMemcpyAsync(c->ksHost, c->ks.get(), sizeof(KrylovState), cudaMemcpyDeviceToHost, st));
+        DXG_CUDA(cudaStreamSynchronize(st));
+        if (c->ksHost->status != KS_RUNNING || done > maxit + chunk) break;
+    }
+    int sing = 0;
+    if (refactor) {
+        DXG_CUDA(cudaMemcpy(&sing, c->singular.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    const KrylovState& ks = *c->ksHost;
+    dxg_linear_result res{};
+    res.converged = ks.status == KS_CONVERGED;
+    res.iterations = (ks.halfsteps + 1) / 2;
+    res.initial_defect = ks.def0;
+    res.final_defect = ks.def;
+    res.reduction = ks.def0 > 0 ? ks.def / ks.def0 : 0.0;
+    if (sing) {
+        res.converged = 0;
+        throw Error(DXG_ERR_LINEAR_BREAKDOWN, "singular pivot block in ILU(0)");
+    }
+    if (ks.status == KS_BREAKDOWN) throw Error(DXG_ERR_LINEAR_BREAKDOWN, "BiCGSTAB breakdown");
+    if (ks.status == KS_NAN) throw Error(DXG_ERR_NAN, "non-finite defect in BiCGSTAB");
+    return res;
+}
+
+// Solves J delta = r into c->delta (FP64), in the context's precision.
+dxg_linear_result linearSolve(dxg_ctx* c, double reduction, int maxit)
+{
+    requireUploaded(c);
+    if (!c->haveJac || !c->haveRes) throw Error(DXG_ERR_STATE, "assemble before solving");
+    cudaStream_t st = c->stream;
+    const int g = reduceBlocks(c->M);
+    if (c->precision == DXG_PRECISION_FP64) {
+        auto res = bicgstab<double>(c, c->A.get(), c->L.get(), c->Dinv.get(), c->kx.get(), c->kr.get(), c->krt.get(),
+                                    c->kp.get(), c->kv.get(), c->kt.get(), c->ky.get(), c->r.get(), reduction, maxit,
+                                    !c->haveFactor);
+        c->haveFactor = true;
+        DXG_CUDA(cudaMemcpyAsync(c->delta.get(), c->kx.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        return res;
+    }
+    // mixed precision: FP32 matrix, ILU(0) and BiCGSTAB; FP64 defect and accumulation
+    // (iterative refinement when the requested reduction is below FP32 resolution)
+    if (!c->haveFactor) {
+        const int64_t nA = (int64_t)c->slots * c->N * c->bb;
+        toFloatKernel<<<reduceBlocks(nA), kReduceThreads, 0, st>>>(c->A.get(), c->Af.get(), nA);
+        c->launches += 1;
+    }
+    const double innerRed = std::max(reduction, 1e-5);
+    DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, c->M * sizeof(double), st));
+    const double r0 = deviceNorm(c, c->r.get());
+    dxg_linear_result total{};
+    total.initial_defect = r0;
+    const double* rhs = c->r.get();
+    double defNorm = r0;
+    for (int pass = 0; pass < 20; ++pass) {
+        auto res = bicgstab<float>(c, c->Af.get(), c->Lf.get(), c->Dinvf.get(), c->fx.get(), c->fr.get(), c->frt.get(),
+                                   c->fp.get(), c->fv.get(), c->ft.get(), c->fy.get(), rhs, innerRed, maxit,
+                                   !c->haveFactor);
+        c->haveFactor = true;
+        total.iterations += res.iterations;
+        axpyDoubleKernel<<<g, kReduceThreads, 0, st>>>(c->delta.get(), c->fx.get(), c->M);
+        c->launches += 1;
+        if (!res.converged) {
+            total.converged = 0;
+            total.final_defect = res.final_defect;
+            total.reduction = r0 > 0 ? res.final_defect / r0 : 0;
+            return total;
+        }
+        if (reduction >= innerRed) {
+            total.converged = 1;
+            total.final_defect = res.final_defect;
+            total.reduction = r0 > 0 ? res.final_defect / r0 : 0;
+            return total;
+        }
+        SpmvArgs<double, double> sv{};
+        sv.A = c->A.get();
+        sv.nbmask = c->nbmask.get();
+        sv.x = c->delta.get();
+        sv.y = c->defect.get();
+        sv.N = c->N;
+        for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
+        defectKernel<<<g, kReduceThreads, 0, st>>>(sv, c->r.get(), c->b, c->dim);
+        c->launches += 1;
+        defNorm = deviceNorm(c, c->defect.get());
+        if (defNorm < reduction * r0 || defNorm < 1e-30) {
+            total.converged = 1;
+            total.final_defect = defNorm;
+            total.reduction = r0 > 0 ? defNorm / r0 : 0;
+            return total;
+        }
+        rhs = c->defect.get();
+    }
+    total.converged = 0;
+    total.final_defect = defNorm;
+    total.reduction = r0 > 0 ? defNorm / r0 : 0;
+    return total;
+}
+
+// ---------------------------------------------------------------- Newton
+struct NumericalProblem {};
+
+struct NewtonRun {
+    dxg_ctx* c;
+    const dxg_newton_params& p;
+    dxg_newton_report* rep;
+    int numSteps = 0;
+    double shift = 0, lastShift = 0, reduction = 0, lastReduction = 1, residualNorm = 0, initialResidual = 0;
+
+    bool converged() const
+    {
+        if (!p.enable_residual_criterion) return shift <= p.max_relative_shift;
+        return shift <= p.max_relative_shift || reduction <= p.residual_reduction;
+    }
+    bool proceed(bool conv) const
+    {
+        if (numSteps < p.min_steps) return true;
+        else if (conv) return false;
+        else if (numSteps >= p.max_steps) return shift * 4.0 < lastShift;
+        return true;
+    }
+    double update(double lambda)
+    {
+        launchNewtonUpdate(c->uLast.get(), c->delta.get(), c->u.get(), lambda, c->M, c->scratch(), c->scal.get(),
+                           c->stream);
+        c->launches += 1;
+        DXG_CUDA(cudaMemcpyAsync(c->scalHost, c->scal.get(), sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        return c->scalHost[0];
+    }
+    void residualReduction()
+    {
+        assemble(c, false);
+        residualNorm = deviceNorm(c, c->r.get());
+        reduction = residualNorm / initialResidual;
+    }
+    // NewtonSolver::solveImpl_ (newtonsolver.hh:976-1072); false on NumericalProblem
+    bool run()
+    {
+        using clk = std::chrono::steady_clock;
+        numSteps = 0;
+        bool conv = false;
+        DXG_CUDA(cudaMemcpyAsync(c->uLast.get(), c->u.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        try {
+            while (proceed(conv)) {
+                lastShift = shift;
+                lastReduction = numSteps == 0 ? 1.0 : reduction;
+                if (numSteps > 0)
+                    DXG_CUDA(cudaMemcpyAsync(c->uLast.get(), c->u.get(), c->M * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, c->stream));
+                auto t0 = clk::now();
+                assemble(c, true);
+                if (numSteps == 0) initialResidual = deviceNorm(c, c->r.get());
+                auto t1 = clk::now();
+                dxg_linear_result lr{};
+                bool lconv = false;
+                try {
+                    lr = linearSolve(c, p.linear_reduction, p.linear_max_iter);
+                    lconv = lr.converged != 0;
+                } catch (const Error& e) {
+                    if (e.status != DXG_ERR_LINEAR_BREAKDOWN && e.status != DXG_ERR_NAN) throw;
+                    lconv = false;
+                }
+                if (!lconv) throw NumericalProblem{};
+                auto t2 = clk::now();
+                if (p.use_line_search) {
+                    double lambda = 1.0;
+                    while (true) {
+                        shift = update(lambda);
+                        residualReduction();
+                        if (reduction < lastReduction || lambda <= p.line_search_min_relaxation) break;
+                        lambda *= 0.5;
+                    }
+                } else {
+                    shift = update(1.0);
+                    if (p.enable_residual_criterion) residualReduction();
+                }
+                auto t3 = clk::now();
+                if (numSteps < DXG_MAX_NEWTON_RECORD) {
+                    rep->shift[numSteps] = shift;
+                    rep->linear_iters[numSteps] = lr.iterations;
+                    if (p.record_residual_norms) {
+                        if (!(p.use_line_search || p.enable_residual_criterion)) {
+                            assemble(c, false);
+                            residualNorm = deviceNorm(c, c->r.get());
+                        }
+                        rep->residual_norm[numSteps] = residualNorm;
+                    }
+                }
+                rep->linear_iterations += lr.iterations;
+                rep->time_assemble += std::chrono::duration<double>(t1 - t0).count();
+                rep->time_solve += std::chrono::duration<double>(t2 - t1).count();
+                rep->time_update += std::chrono::duration<double>(t3 - t2).count();
+                ++numSteps;
+                conv = converged();
+            }
+        } catch (const NumericalProblem&) {
+            return false;
+        }
+        return converged();
+    }
+};
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+int64_t dxg_num_boundary_faces(const dxg_problem_desc* d)
+{
+    if (!d || (d->dim != 2 && d->dim != 3)) return -1;
+    int64_t n[3];
+    for (int a = 0; a < 3; ++a) n[a] = a < d->dim ? d->cells[a] : 1;
+    int64_t total = 0;
+    for (int a = 0; a < d->dim; ++a) {
+        int64_t cnt = 1;
+        for (int k = 0; k < d->dim; ++k)
+            if (k != a) cnt *= n[k];
+        total += 2 * cnt;
+    }
+    return total;
+}
+
+int dxg_ctx_create(dxg_ctx** out, int device)
+{
+    if (!out) return DXG_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        g_createError = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        return DXG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) {
+        g_createError = "device index out of range";
+        return DXG_ERR_ARG;
+    }
+    auto* c = new dxg_ctx();
+    int st = guarded(c, [&] {
+        c->device = device;
+        DXG_CUDA(cudaSetDevice(device));
+        DXG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        DXG_CUDA(cudaMallocHost(&c->ksHost, sizeof(KrylovState)));
+        DXG_CUDA(cudaMallocHost(&c->scalHost, 4 * sizeof(double)));
+        return DXG_OK;
+    });
+    if (st != DXG_OK) {
+        g_createError = c->err;
+        delete c;
+        return st;
+    }
+    *out = c;
+    return DXG_OK;
+}
+
+int dxg_ctx_destroy(dxg_ctx* c)
+{
+    if (!c) return DXG_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ksHost) cudaFreeHost(c->ksHost);
+    if (c->scalHost) cudaFreeHost(c->scalHost);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return DXG_OK;
+}
+
+const char* dxg_last_error(const dxg_ctx* c) { return c ? c->err.c_str() : g_createError.c_str(); }
+
+int dxg_set_precision(dxg_ctx* c, int precision)
+{
+    if (!c || (precision != DXG_PRECISION_FP64 && precision != DXG_PRECISION_MIXED)) return DXG_ERR_ARG;
+    if (c->uploaded) {
+        c->err = "precision must be set before dxg_problem_upload";
+        return DXG_ERR_STATE;
+    }
+    c->precision = precision;
+    return DXG_OK;
+}
+
+int dxg_problem_upload(dxg_ctx* c, const dxg_problem_desc* d)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        DXG_CUDA(cudaSetDevice(c->device));
+        tabulate(c, d);
+        return DXG_OK;
+    });
+}
+
+int dxg_sizes(const dxg_ctx* c, int64_t* n, int32_t* b, int64_t* nnzb)
+{
+    if (!c || !c->uploaded) return DXG_ERR_STATE;
+    if (n) *n = c->N;
+    if (b) *b = c->b;
+    if (nnzb) *nnzb = c->nnzb;
+    return DXG_OK;
+}
+
+static int copyIn(dxg_ctx* c, DevBuf<double>& dst, const double* src)
+{
+    return guarded(c, [&] {
+        requireUploaded(c);
+        if (!src) throw Error(DXG_ERR_ARG, "null host buffer");
+        DXG_CUDA(cudaMemcpyAsync(dst.get(), src, c->M * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        return DXG_OK;
+    });
+}
+static int copyOut(dxg_ctx* c, const double* src, double* dst)
+{
+    return guarded(c, [&] {
+        requireUploaded(c);
+        if (!dst) throw Error(DXG_ERR_ARG, "null host buffer");
+        DXG_CUDA(cudaMemcpyAsync(dst, src, c->M * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        return DXG_OK;
+    });
+}
+
+int dxg_set_solution(dxg_ctx* c, const double* u)
+{
+    if (!c) return DXG_ERR_ARG;
+    const int st = copyIn(c, c->u, u);
+    if (st == DXG_OK) c->haveJac = c->haveRes = c->haveFactor = false;
+    return st;
+}
+int dxg_get_solution(dxg_ctx* c, double* u) { return c ? copyOut(c, c->u.get(), u) : DXG_ERR_ARG; }
+int dxg_set_prev_solution(dxg_ctx* c, const double* up)
+{
+    if (!c) return DXG_ERR_ARG;
+    const int st = copyIn(c, c->uprev, up);
+    if (st == DXG_OK) {
+        c->havePrev = true;
+        c->stPrevValid = false;
+    }
+    return st;
+}
+int dxg_set_time_step(dxg_ctx* c, double dt)
+{
+    if (!c) return DXG_ERR_ARG;
+    c->dt = dt > 0.0 ? dt : 0.0;
+    c->haveJac = c->haveRes = c->haveFactor = false;
+    return DXG_OK;
+}
+
+int dxg_assemble_jacobian_and_residual(dxg_ctx* c)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        assemble(c, true);
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        return DXG_OK;
+    });
+}
+int dxg_assemble_residual(dxg_ctx* c)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        assemble(c, false);
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        return DXG_OK;
+    });
+}
+int dxg_get_residual(dxg_ctx* c, double* r) { return c ? copyOut(c, c->r.get(), r) : DXG_ERR_ARG; }
+int dxg_get_update(dxg_ctx* c, double* d) { return c ? copyOut(c, c->delta.get(), d) : DXG_ERR_ARG; }
+
+int dxg_get_jacobian(dxg_ctx* c, int64_t* row_ptr, int32_t* col_idx, double* values)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        requireUploaded(c);
+        if (!c->haveJac) throw Error(DXG_ERR_STATE, "no Jacobian assembled");
+        std::vector<double> h((size_t)c->slots * c->N * c->bb);
+        DXG_CUDA(cudaMemcpyAsync(h.data(), c->A.get(), h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        int64_t k = 0;
+        for (int64_t i = 0; i < c->N; ++i) {
+            if (row_ptr) row_ptr[i] = k;
+            const unsigned m = c->nbmaskHost[i];
+            for (int s = 0; s < c->slots; ++s) {
+                if (s != c->dim) {
+                    const int f = s < c->dim ? 2 * (c->dim - 1 - s) : 2 * (s - c->dim - 1) + 1;
+                    if (!((m >> f) & 1u)) continue;
+                }
+                if (col_idx) col_idx[k] = (int32_t)(i + c->off[s]);
+                if (values)
+                    std::memcpy(values + k * c->bb, h.data() + ((size_t)s * c->N + i) * c->bb, sizeof(double) * c->bb);
+                ++k;
+            }
+        }
+        if (row_ptr) row_ptr[c->N] = k;
+        return DXG_OK;
+    });
+}
+
+int dxg_set_linear_system(dxg_ctx* c, const int64_t* row_ptr, const int32_t* col_idx, const double* values,
+                          const double* rhs)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        requireUploaded(c);
+        if (!row_ptr || !col_idx || !values || !rhs) throw Error(DXG_ERR_ARG, "null buffer");
+        std::vector<double> h((size_t)c->slots * c->N * c->bb, 0.0);
+        for (int64_t i = 0; i < c->N; ++i)
+            for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+                const int64_t dc = (int64_t)col_idx[k] - i;
+                int slot = -1;
+                for (int s = 0; s < c->slots; ++s)
+                    if (c->off[s] == dc) slot = s;
+                if (slot < 0) throw Error(DXG_ERR_ARG, "entry outside the stencil pattern");
+                std::memcpy(h.data() + ((size_t)slot * c->N + i) * c->bb, values + k * c->bb, sizeof(double) * c->bb);
+            }
+        DXG_CUDA(cudaMemcpyAsync(c->A.get(), h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        DXG_CUDA(cudaMemcpyAsync(c->r.get(), rhs, c->M * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        c->haveJac = c->haveRes = true;
+        c->haveFactor = false;
+        return DXG_OK;
+    });
+}
+
+int dxg_linear_solve(dxg_ctx* c, double reduction, int32_t max_iter, dxg_linear_result* res)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        DXG_CUDA(cudaSetDevice(c->device));
+        dxg_linear_result r = linearSolve(c, reduction, max_iter);
+        if (res) *res = r;
+        return r.converged ? DXG_OK : DXG_ERR_LINEAR_NOT_CONVERGED;
+    });
+}
+
+int dxg_residual_norm(dxg_ctx* c, double* norm)
+{
+    if (!c || !norm) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        requireUploaded(c);
+        if (!c->haveRes) throw Error(DXG_ERR_STATE, "no residual assembled");
+        *norm = deviceNorm(c, c->r.get());
+        return DXG_OK;
+    });
+}
+
+void dxg_newton_default_params(dxg_newton_params* p)
+{
+    if (!p) return;
+    p->max_relative_shift = 1e-8;
+    p->min_steps = 2;
+    p->max_steps = 18;
+    p->target_steps = 10;
+    p->use_line_search = 0;
+    p->line_search_min_relaxation = 0.125;
+    p->enable_residual_criterion = 0;
+    p->residual_reduction = 1e-5;
+    p->max_time_step_divisions = 10;
+    p->retry_time_step_reduction = 0.5;
+    p->linear_reduction = 1e-6;
+    p->linear_max_iter = 250;
+    p->record_residual_norms = 0;
+}
+
+int dxg_newton_solve(dxg_ctx* c, double dt, const dxg_newton_params* params, dxg_newton_report* report)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        requireUploaded(c);
+        DXG_CUDA(cudaSetDevice(c->device));
+        dxg_newton_params p;
+        if (params) p = *params;
+        else dxg_newton_default_params(&p);
+        dxg_newton_report local{};
+        dxg_newton_report* rep = report ? report : &local;
+        std::memset(rep, 0, sizeof(*rep));
+        const bool transient = dt > 0.0;
+        if (transient && !c->havePrev) throw Error(DXG_ERR_STATE, "transient solve needs the previous solution");
+        const int divisions = transient ? p.max_time_step_divisions : 0;
+        int wasted = 0;
+        for (int i = 0; i <= divisions; ++i) {
+            c->dt = transient ? dt : 0.0;
+            dxg_newton_report attempt{};
+            NewtonRun run{c, p, &attempt};
+            const bool conv = run.run();
+            attempt.iterations = run.numSteps;
+            attempt.initial_residual = run.initialResidual;
+            attempt.dt_used = dt;
+            attempt.converged = conv;
+            attempt.time_step_divisions = i;
+            attempt.wasted_iterations = wasted;
+            c->lastNewtonSteps = run.numSteps;
+            *rep = attempt;
+            if (conv) return DXG_OK;
+            wasted += run.numSteps;
+            rep->wasted_iterations = wasted;
+            if (transient) {
+                // reset to the previous solution and retry with a reduced time step
+                DXG_CUDA(cudaMemcpyAsync(c->u.get(), c->uprev.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice,
+                                         c->stream));
+                dt *= p.retry_time_step_reduction;
+            }
+        }
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        c->err = "Newton solver did not converge";
+        return DXG_ERR_NEWTON_NOT_CONVERGED;
+    });
+}
+
+double dxg_suggest_time_step(const dxg_ctx* c, double oldTimeStep, const dxg_newton_params* params)
+{
+    dxg_newton_params p;
+    if (params) p = *params;
+    else dxg_newton_default_params(&p);
+    const int numSteps = c ? c->lastNewtonSteps : p.target_steps;
+    if (numSteps > p.target_steps) {
+        const double percent = double(numSteps - p.target_steps) / p.target_steps;
+        return oldTimeStep / (1.0 + percent);
+    }
+    const double percent = double(p.target_steps - numSteps) / p.target_steps;
+    return oldTimeStep * (1.0 + percent / 1.2);
+}
+
+int dxg_advance_time_step(dxg_ctx* c)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        requireUploaded(c);
+        DXG_CUDA(cudaMemcpyAsync(c->uprev.get(), c->u.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        c->havePrev = true;
+        c->stPrevValid = false;
+        return DXG_OK;
+    });
+}
+
+int64_t dxg_kernel_launch_count(const dxg_ctx* c) { return c ? c->launches : -1; }
+
+int dxg_sync(dxg_ctx* c)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        DXG_CUDA(cudaStreamSynchronize(c->stream));
+        DXG_CUDA(cudaGetLastError());
+        return DXG_OK;
+    });
+}
+
+}  // extern "C"

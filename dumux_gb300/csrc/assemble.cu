@@ -1,0 +1,437 @@
+// assemble.cu -- residual and numeric-difference Jacobian of the cc-TPFA scheme.
+//
+// Two kernels per assembly:
+//   volvarsKernel   one thread per cell: volume variables of the cell at its own
+//                   solution and at every perturbed state of the numeric
+//                   differentiation (OnePVolumeVariables / TwoPVolumeVariables::update,
+//                   dumux/porousmediumflow/{1p,2p}/volumevariables.hh), plus the
+//                   epsilon of each primary variable (dumux/assembly/numericepsilon.hh:49-53).
+//   rowKernel       one thread per cell I: the local residual r_I at the cell's own
+//                   states and the whole block row I of the Jacobian.
+//
+// The reference assembles block columns (CCLocalAssembler<numeric>::assembleJacobian-
+// AndResidualImpl, dumux/assembly/cclocalassembler.hh:164-348): element I perturbs its
+// own unknowns and differences its own residual (diagonal block A[I][I]) and the
+// fluxes of each neighbour J's face towards I, evaluated with J as the inside element
+// (off-diagonal block A[J][I]).  Each of those numbers is a function of the two cells'
+// volume variables only, so the same value can be produced in row order: A[I][J] is
+// the difference of I's flux through the face towards J, with J perturbed, divided by
+// J's epsilon.  Evaluating every flux with the reference's operation sequence (no FMA
+// contraction in this file) yields the reference's values for every block while each
+// volume variable is computed once per (cell, state) instead of once per element that
+// binds it, and the rows are written coalesced.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace dxg {
+
+// ---------------------------------------------------------------- constitutive laws
+// Regularised Brooks-Corey (brookscorey.hh:99-503 with TwoPEffToAbsDefaultPolicy).
+__device__ __forceinline__ double bcPc(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
+    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0) + m.entryPressure;
+    const double s = fmin(fmax(swe, 0.0), 1.0);
+    return m.pe * pow(s, m.expPc);
+}
+__device__ __forceinline__ double bcKrw(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0) return 0.0;
+    else if (swe >= 1.0) return 1.0;
+    return pow(fmin(fmax(swe, 0.0), 1.0), m.expKrw);
+}
+__device__ __forceinline__ double bcKrn(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0) return 1.0;
+    else if (swe >= 1.0) return 0.0;
+    const double s = fmin(fmax(swe, 0.0), 1.0);
+    const double sne = 1.0 - s;
+    return sne * sne * (1.0 - pow(s, m.expKrn));
+}
+
+// Volume variables needed by the residual: phase pressure, upwind term rho*lambda and
+// the storage term (phi*rho*S)*extrusion (immiscible/localresidual.hh:64-86,
+// fvlocalresidual.hh:293-297).
+template <int B>
+__device__ __forceinline__ void volVars(const ProblemConsts& pc, const double* pv, double phi, double extr,
+                                        int mat, double* p, double* up, double* st)
+{
+    if (B == 1) {
+        const double mob = 1.0 / pc.viscosity[0];
+        p[0] = pv[0];
+        up[0] = pc.density[0] * mob;
+        double s = phi * pc.density[0] * 1.0;
+        s *= extr;
+        st[0] = s;
+    } else {
+        const MaterialLaw& m = pc.law[mat];
+        const double Sn = pv[1];
+        const double Sw = 1 - Sn;
+        const double pcap = bcPc(m, Sw);
+        p[0] = pv[0];
+        p[1] = pv[0] + pcap;
+        const double mobW = bcKrw(m, Sw) / pc.viscosity[0];
+        const double mobN = bcKrn(m, Sw) / pc.viscosity[1];
+        up[0] = pc.density[0] * mobW;
+        up[1] = pc.density[1] * mobN;
+        double sW = phi * pc.density[0] * Sw;
+        double sN = phi * pc.density[1] * Sn;
+        sW *= extr;
+        sN *= extr;
+        st[0] = sW;
+        st[1] = sN;
+    }
+}
+
+__device__ __forceinline__ double numericEps(const ProblemConsts& pc, double x, int pv)
+{
+    return pc.magnitude[pv] > 0.0 ? pc.baseEps * pc.magnitude[pv] : pc.baseEps * (fabs(x) + 1.0);
+}
+
+// States per cell: 0 = own solution; forward/backward: 1+pv = x[pv] +/- eps;
+// central: 1+2pv = x+eps, 2+2pv = x-eps.  METHOD 2 selects state 0 only (residual).
+template <int B, int METHOD>
+__global__ void volvarsKernel(const ProblemConsts* __restrict__ pcp, const double* __restrict__ u,
+                              const double* __restrict__ phi, const double* __restrict__ extr,
+                              const int32_t* __restrict__ mat, double* __restrict__ vvP, double* __restrict__ vvU,
+                              double* __restrict__ vvS, double* __restrict__ eps, int64_t N)
+{
+    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : (METHOD == 2 ? 0 : B));
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const ProblemConsts& pc = *pcp;
+    double x[B];
+#pragma unroll
+    for (int e = 0; e < B; ++e) x[e] = u[i * B + e];
+    const double ph = phi[i], ex = extr[i];
+    const int m = (B == 2) ? mat[i] : 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        double q[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) q[e] = x[e];
+        if (s > 0) {
+            const int pv = (METHOD == 0) ? (s - 1) / 2 : s - 1;
+            const double ep = numericEps(pc, x[pv], pv);
+            const bool minus = (METHOD == -1) || (METHOD == 0 && ((s - 1) & 1));
+            q[pv] = minus ? x[pv] - ep : x[pv] + ep;
+            if (METHOD != 0 || !((s - 1) & 1)) eps[pv * N + i] = ep;
+        }
+        double p[B], up[B], st[B];
+        volVars<B>(pc, q, ph, ex, m, p, up, st);
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            vvP[(s * B + k) * N + i] = p[k];
+            vvU[(s * B + k) * N + i] = up[k];
+            vvS[(s * B + k) * N + i] = st[k];
+        }
+    }
+}
+
+// Storage of the previous time level, ((phi*rho*S)*extr) at u_prev.
+template <int B>
+__global__ void prevStorageKernel(const ProblemConsts* __restrict__ pcp, const double* __restrict__ uprev,
+                                  const double* __restrict__ phi, const double* __restrict__ extr,
+                                  const int32_t* __restrict__ mat, double* __restrict__ stPrev, int64_t N)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double x[B], p[B], up[B], st[B];
+#pragma unroll
+    for (int e = 0; e < B; ++e) x[e] = uprev[i * B + e];
+    volVars<B>(*pcp, x, phi[i], extr[i], (B == 2) ? mat[i] : 0, p, up, st);
+#pragma unroll
+    for (int k = 0; k < B; ++k) stPrev[k * N + i] = st[k];
+}
+
+// Darcy flux times upwinded rho*lambda of one phase across one face
+// (darcyslaw.hh:153-213, upwindscheme.hh:35-54, fluxvariables.hh:75-98).
+// g1 = rho*area*alpha_inside, g2 = rho*tij/outsideTi*(alpha_inside-alpha_outside).
+template <bool GRAV, bool FULLUP>
+__device__ __forceinline__ double phaseFlux(double tij, double pin, double pout, double upin, double upout,
+                                            double g1, double g2, double w)
+{
+    double flux = tij * (pin - pout);
+    if (GRAV) {
+        flux = flux + g1;
+        flux = flux - g2;
+    }
+    double mult;
+    if (FULLUP) mult = signbit(flux) ? (w * upout + (1.0 - w) * upin) : (w * upin + (1.0 - w) * upout);
+    else mult = signbit(flux) ? upout : upin;
+    return flux * mult;
+}
+
+template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP, bool WANT_JAC>
+__global__ void __launch_bounds__(128) rowKernel(AssemblyArgs a)
+{
+    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : B);
+    constexpr int BB = B * B;
+    constexpr int NF = 2 * DIM;
+    constexpr int VA = DIM - 1;                 // vertical axis (gravity)
+    const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t N = a.N;
+    if (I >= N) return;
+    const ProblemConsts& pc = *a.pc;
+    const double w = pc.upwindWeight;
+
+    // own states
+    double pI[NS][B], uI[NS][B];
+#pragma unroll
+    for (int s = 0; s < (WANT_JAC ? NS : 1); ++s)
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            pI[s][k] = a.vvP[(s * B + k) * N + I];
+            uI[s][k] = a.vvU[(s * B + k) * N + I];
+        }
+    constexpr int NR = WANT_JAC ? NS : 1;
+    double r[NS][B];
+#pragma unroll
+    for (int s = 0; s < NR; ++s)
+#pragma unroll
+        for (int e = 0; e < B; ++e) r[s][e] = 0.0 - a.srcterm[e * N + I];
+
+    const int nx = pc.nx, ny = pc.ny;
+    const int64_t strides[3] = {1, (int64_t)nx, (int64_t)nx * ny};
+    const int ix = (int)(I % nx);
+    const int iy = (int)((I / nx) % ny);
+    const int iz = (DIM == 3) ? (int)(I / ((int64_t)nx * ny)) : 0;
+    const int idx[3] = {ix, iy, iz};
+    const int nn[3] = {nx, ny, pc.nz};
+
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        const int ax = f >> 1, side = f & 1;
+        const bool interior = side ? (idx[ax] < nn[ax] - 1) : (idx[ax] > 0);
+        const int slot = (side ? DIM + 1 + ax : DIM - 1 - ax);
+        if (interior) {
+            const int64_t J = side ? I + strides[ax] : I - strides[ax];
+            const double tij = a.tijPlus[ax * N + (side ? I : J)];
+            double g1[B], g2[B];
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                g1[k] = 0.0;
+                g2[k] = 0.0;
+                if (GRAV && ax == VA) {
+                    g1[k] = a.G1[(side * B + k) * N + I];
+                    g2[k] = a.G2[(side * B + k) * N + I];
+                }
+            }
+            double pJ[B], uJ[B];
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                pJ[k] = a.vvP[k * N + J];
+                uJ[k] = a.vvU[k * N + J];
+            }
+            double F0[B];
+#pragma unroll
+            for (int s = 0; s < NR; ++s)
+#pragma unroll
+                for (int k = 0; k < B; ++k) {
+                    const double F = (GRAV && ax == VA)
+                                         ? phaseFlux<true, FULLUP>(tij, pI[s][k], pJ[k], uI[s][k], uJ[k], g1[k], g2[k], w)
+                                         : phaseFlux<false, FULLUP>(tij, pI[s][k], pJ[k], uI[s][k], uJ[k], 0.0, 0.0, w);
+                    if (s == 0) F0[k] = F;
+                    r[s][k] += F;
+                }
+            if (WANT_JAC) {
+                double blk[BB];
+#pragma unroll
+                for (int pv = 0; pv < B; ++pv) {
+                    const double epsJ = a.eps[pv * N + J];
+                    double Fa[B], Fb[B];
+#pragma unroll
+                    for (int t = 0; t < (METHOD == 0 ? 2 : 1); ++t) {
+                        const int sJ = (METHOD == 0) ? 1 + 2 * pv + t : 1 + pv;
+                        double pJs[B], uJs[B];
+#pragma unroll
+                        for (int k = 0; k < B; ++k) {
+                            pJs[k] = a.vvP[(sJ * B + k) * N + J];
+                            uJs[k] = a.vvU[(sJ * B + k) * N + J];
+                        }
+#pragma unroll
+                        for (int k = 0; k < B; ++k) {
+                            const double F = (GRAV && ax == VA)
+                                ? phaseFlux<true, FULLUP>(tij, pI[0][k], pJs[k], uI[0][k], uJs[k], g1[k], g2[k], w)
+                                : phaseFlux<false, FULLUP>(tij, pI[0][k], pJs[k], uI[0][k], uJs[k], 0.0, 0.0, w);
+                            if (t == 0) Fa[k] = F;
+                            else Fb[k] = F;
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        double d;
+                        if (METHOD == 1) d = (Fa[e] - F0[e]) / epsJ;
+                        else if (METHOD == -1) d = (F0[e] - Fa[e]) / epsJ;
+                        else d = (Fa[e] - Fb[e]) / (epsJ + epsJ);
+                        blk[e * B + pv] = d;
+                    }
+                }
+                double* dst = a.A + ((int64_t)slot * N + I) * BB;
+#pragma unroll
+                for (int e = 0; e < BB; ++e) dst[e] = blk[e];
+            }
+        } else {
+            // boundary face: index among the faces of this side
+            int64_t pos;
+            if (ax == 0) pos = iy + (int64_t)ny * iz;
+            else if (ax == 1) pos = ix + (int64_t)nx * iz;
+            else pos = ix + (int64_t)nx * iy;
+            const int64_t bidx = pc.sideOffset[f] + pos;
+            const int8_t type = a.btype[bidx];
+            if (type == 1) {
+                const double tij = a.bTij[bidx];
+#pragma unroll
+                for (int k = 0; k < B; ++k) {
+                    const double gp = a.bP[k * a.nb + bidx];
+                    const double gu = a.bU[k * a.nb + bidx];
+                    const double g1 = a.bG1[k * a.nb + bidx];
+#pragma unroll
+                    for (int s = 0; s < NR; ++s) {
+                        const double F = (GRAV && ax == VA)
+                                             ? phaseFlux<true, FULLUP>(tij, pI[s][k], gp, uI[s][k], gu, g1, 0.0, w)
+                                             : phaseFlux<false, FULLUP>(tij, pI[s][k], gp, uI[s][k], gu, 0.0, 0.0, w);
+                        r[s][k] += F;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < B; ++e) {
+                    const double q = a.bNeu[e * a.nb + bidx];
+#pragma unroll
+                    for (int s = 0; s < NR; ++s) r[s][e] += q;
+                }
+            }
+            if (WANT_JAC) {
+                double* dst = a.A + ((int64_t)slot * N + I) * BB;
+#pragma unroll
+                for (int e = 0; e < BB; ++e) dst[e] = 0.0;
+            }
+        }
+    }
+
+    if (TRANSIENT) {
+        const double V = a.vol[I];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const double sp = a.stPrev[k * N + I];
+#pragma unroll
+            for (int s = 0; s < NR; ++s) {
+                double st = a.vvS[(s * B + k) * N + I];
+                st -= sp;
+                st *= V;
+                st /= a.dt;
+                r[s][k] += st;
+            }
+        }
+    }
+
+#pragma unroll
+    for (int e = 0; e < B; ++e) a.r[I * B + e] = r[0][e];
+
+    if (WANT_JAC) {
+        double blk[BB];
+#pragma unroll
+        for (int pv = 0; pv < B; ++pv) {
+            const double epsI = a.eps[pv * N + I];
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                double d;
+                if (METHOD == 1) d = (r[1 + pv][e] - r[0][e]) / epsI;
+                else if (METHOD == -1) d = (r[0][e] - r[1 + pv][e]) / epsI;
+                else d = (r[1 + 2 * pv][e] - r[2 + 2 * pv][e]) / (epsI + epsI);
+                blk[e * B + pv] = d;
+            }
+        }
+        double* dst = a.A + ((int64_t)DIM * N + I) * BB;
+#pragma unroll
+        for (int e = 0; e < BB; ++e) dst[e] = blk[e];
+    }
+}
+
+// ---------------------------------------------------------------- host launchers
+static int blocksFor(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+template <int B, int METHOD>
+static void launchVolvars(const AssemblyArgs& a, const double* u, cudaStream_t st)
+{
+    volvarsKernel<B, METHOD><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, u, a.phi, a.extr, a.mat, a.vvP, a.vvU,
+                                                                  a.vvS, a.eps, a.N);
+}
+
+void launchPrevStorage(const AssemblyArgs& a, int b, const double* uprev, cudaStream_t st)
+{
+    if (b == 1) prevStorageKernel<1><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, uprev, a.phi, a.extr, a.mat, a.stPrev, a.N);
+    else prevStorageKernel<2><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, uprev, a.phi, a.extr, a.mat, a.stPrev, a.N);
+    DXG_CUDA(cudaGetLastError());
+}
+
+void launchVolvars(const AssemblyArgs& a, int b, int method, const double* u, cudaStream_t st)
+{
+    if (b == 1) {
+        if (method == 2) launchVolvars<1, 2>(a, u, st);
+        else if (method == 1) launchVolvars<1, 1>(a, u, st);
+        else if (method == -1) launchVolvars<1, -1>(a, u, st);
+        else launchVolvars<1, 0>(a, u, st);
+    } else {
+        if (method == 2) launchVolvars<2, 2>(a, u, st);
+        else if (method == 1) launchVolvars<2, 1>(a, u, st);
+        else if (method == -1) launchVolvars<2, -1>(a, u, st);
+        else launchVolvars<2, 0>(a, u, st);
+    }
+    DXG_CUDA(cudaGetLastError());
+}
+
+template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP>
+static void launchRow3(const AssemblyArgs& a, bool jac, cudaStream_t st)
+{
+    if (jac) rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, true><<<blocksFor(a.N, 128), 128, 0, st>>>(a);
+    else rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, false><<<blocksFor(a.N, 128), 128, 0, st>>>(a);
+}
+template <int B, int DIM, int METHOD>
+static void launchRow2(const AssemblyArgs& a, bool jac, bool grav, bool transient, bool fullup, cudaStream_t st)
+{
+    if (fullup) {
+        if (grav) {
+            if (transient) launchRow3<B, DIM, METHOD, true, true, true>(a, jac, st);
+            else launchRow3<B, DIM, METHOD, true, false, true>(a, jac, st);
+        } else {
+            if (transient) launchRow3<B, DIM, METHOD, false, true, true>(a, jac, st);
+            else launchRow3<B, DIM, METHOD, false, false, true>(a, jac, st);
+        }
+    } else {
+        if (grav) {
+            if (transient) launchRow3<B, DIM, METHOD, true, true, false>(a, jac, st);
+            else launchRow3<B, DIM, METHOD, true, false, false>(a, jac, st);
+        } else {
+            if (transient) launchRow3<B, DIM, METHOD, false, true, false>(a, jac, st);
+            else launchRow3<B, DIM, METHOD, false, false, false>(a, jac, st);
+        }
+    }
+}
+template <int B, int DIM>
+static void launchRow1(const AssemblyArgs& a, int method, bool jac, bool grav, bool transient, bool fullup,
+                       cudaStream_t st)
+{
+    if (method == 1) launchRow2<B, DIM, 1>(a, jac, grav, transient, fullup, st);
+    else if (method == -1) launchRow2<B, DIM, -1>(a, jac, grav, transient, fullup, st);
+    else launchRow2<B, DIM, 0>(a, jac, grav, transient, fullup, st);
+}
+
+void launchRow(const AssemblyArgs& a, int b, int dim, int method, bool jac, bool grav, bool transient, bool fullup,
+               cudaStream_t st)
+{
+    if (b == 1) {
+        if (dim == 2) launchRow1<1, 2>(a, method, jac, grav, transient, fullup, st);
+        else launchRow1<1, 3>(a, method, jac, grav, transient, fullup, st);
+    } else {
+        if (dim == 2) launchRow1<2, 2>(a, method, jac, grav, transient, fullup, st);
+        else launchRow1<2, 3>(a, method, jac, grav, transient, fullup, st);
+    }
+    DXG_CUDA(cudaGetLastError());
+}
+
+}  // namespace dxg

@@ -1,0 +1,94 @@
+// common.cuh -- shared device/host helpers of the GB300 cc-TPFA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/dumux_gb300.h"
+
+namespace dxg {
+
+// Thrown inside the library only; converted to a status code at the C ABI.
+struct Error : std::runtime_error {
+    int status;
+    Error(int st, const std::string& msg) : std::runtime_error(msg), status(st) {}
+};
+
+#define DXG_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            throw ::dxg::Error(e_ == cudaErrorMemoryAllocation ? DXG_ERR_OOM : DXG_ERR_CUDA, \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        DXG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    T* get() const { return p; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+constexpr int kMaxMaterials = 16;
+
+// Derived constants of one regularised Brooks-Corey parameter set
+// (BrooksCoreyRegularization::initPcParameters_, brookscorey.hh:477-486).
+struct MaterialLaw {
+    double pe, lambda, swr, snr, pcLowSwe;
+    double denom;                  // 1.0 - swr - snr
+    double expPc;                  // -1.0/lambda
+    double expKrw;                 // 2.0/lambda + 3.0
+    double expKrn;                 // 2.0/lambda + 1.0
+    double pcLowSwePcValue, pcDerivativeLowSw, pcDerivativeHighSwEnd, entryPressure;
+};
+
+// Problem constants visible to the kernels.
+struct ProblemConsts {
+    int dim, b;
+    int nx, ny, nz;
+    int64_t N;
+    int64_t sideOffset[7];
+    int gravity;                   // Problem.EnableGravity
+    int gravAxisMask;              // bit a set: faces normal to axis a carry gravity terms
+    double density[2], viscosity[2];
+    double mobility1p;             // 1.0/viscosity (1p)
+    double upwindWeight;
+    int upwindFull;                // upwind weight != 1
+    int method;                    // numeric difference method
+    double baseEps;
+    double magnitude[2];
+    int numMaterials;
+    int hasSource;
+    MaterialLaw law[kMaxMaterials];
+};
+
+__host__ __device__ inline int slotOfFace(int dim, int f)
+{
+    const int a = f >> 1;
+    return (f & 1) ? dim + 1 + a : dim - 1 - a;
+}
+
+}  // namespace dxg

@@ -1,0 +1,61 @@
+// context.h -- the opaque dxg_ctx behind the C ABI.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "linalg_kernels.cuh"
+
+struct dxg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    int precision = DXG_PRECISION_FP64;
+    bool uploaded = false;
+
+    // problem
+    dxg::ProblemConsts pcHost{};
+    dxg::DevBuf<dxg::ProblemConsts> pcDev;
+    int dim = 0, b = 0, slots = 0, bb = 0, method = 1;
+    int64_t N = 0, nb = 0, M = 0, nnzb = 0;
+    bool gravity = false, fullUpwind = false;
+    int64_t off[7] = {0, 0, 0, 0, 0, 0, 0};
+    dxg::LevelSchedule levels;
+    std::vector<uint8_t> nbmaskHost;
+
+    dxg::DevBuf<double> vol, phi, extr, srcterm, tijPlus, G1, G2;
+    dxg::DevBuf<int32_t> mat, perm;
+    dxg::DevBuf<int8_t> btype;
+    dxg::DevBuf<double> bTij, bG1, bP, bU, bNeu;
+    dxg::DevBuf<uint8_t> nbmask;
+
+    // state
+    dxg::DevBuf<double> u, uprev, uLast, stPrev;
+    dxg::DevBuf<double> vvP, vvU, vvS, eps;
+    dxg::DevBuf<double> A, r;
+    double dt = 0.0;
+    bool havePrev = false, stPrevValid = false, haveJac = false, haveRes = false, haveFactor = false;
+
+    // linear solver (FP64)
+    dxg::DevBuf<double> L, Dinv;
+    dxg::DevBuf<double> kx, kr, krt, kp, kv, kt, ky;
+    // mixed precision copies
+    dxg::DevBuf<float> Af, Lf, Dinvf, fx, fr, frt, fp, fv, ft, fy;
+    dxg::DevBuf<double> delta, defect;
+
+    dxg::DevBuf<dxg::KrylovState> ks;
+    dxg::DevBuf<double> partials;
+    dxg::DevBuf<unsigned> counters;
+    dxg::DevBuf<double> scal;         // [0] shift, [1] norm
+    dxg::DevBuf<int> singular;
+    dxg::KrylovState* ksHost = nullptr;   // pinned
+    double* scalHost = nullptr;           // pinned
+
+    int lastNewtonSteps = 0;
+
+    dxg::AssemblyArgs asmArgs() const;
+    dxg::ReduceScratch scratch() const { return {partials.get(), counters.get()}; }
+};

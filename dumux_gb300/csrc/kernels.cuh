@@ -1,0 +1,45 @@
+// kernels.cuh -- kernel argument blocks and launcher declarations.
+#pragma once
+
+#include "common.cuh"
+
+namespace dxg {
+
+// Everything the assembly kernels read or write (device pointers).
+struct AssemblyArgs {
+    const ProblemConsts* pc;
+    int64_t N, nb;
+    // per cell
+    const double* vol;
+    const double* phi;
+    const double* extr;
+    const int32_t* mat;
+    const double* srcterm;      // [b][N]: (0 + source)*(V*extrusion)
+    const double* tijPlus;      // [dim][N]: transmissibility of the + face of each axis
+    const double* G1;           // [2 sides][b][N]: gravity terms of the vertical faces
+    const double* G2;
+    // boundary faces
+    const int8_t* btype;
+    const double* bTij;         // [nb]
+    const double* bG1;          // [b][nb]
+    const double* bP;           // [b][nb] Dirichlet ghost phase pressures
+    const double* bU;           // [b][nb] Dirichlet ghost rho*lambda
+    const double* bNeu;         // [b][nb] Neumann flux * area * extrusion
+    // volume variables
+    double* vvP;                // [states][b][N]
+    double* vvU;
+    double* vvS;
+    double* eps;                // [b][N]
+    double* stPrev;             // [b][N]
+    // outputs
+    double* A;                  // [slots][N][b*b]
+    double* r;                  // [N][b]
+    double dt;
+};
+
+void launchVolvars(const AssemblyArgs& a, int b, int method, const double* u, cudaStream_t st);
+void launchPrevStorage(const AssemblyArgs& a, int b, const double* uprev, cudaStream_t st);
+void launchRow(const AssemblyArgs& a, int b, int dim, int method, bool jac, bool grav, bool transient, bool fullup,
+               cudaStream_t st);
+
+}  // namespace dxg

@@ -1,0 +1,583 @@
+// linalg.cu -- block SpMV, natural-order ILU(0) and BiCGSTAB on the device.
+//
+// Replaces the dune-istl path bound by ILUBiCGSTABIstlSolver
+// (dumux/linear/istlsolvers.hh:635-642): SeqILU with n = 0, relaxation 1 (block ILU(0)
+// of the assembled matrix in its natural, lexicographic order) and BiCGSTABSolver.
+//
+// ILU(0) on the cc-TPFA stencil: for row i every lower neighbour j = i - stride has,
+// in its own row, exactly one upper block inside row i's pattern -- the one pointing
+// back at i -- so the factorisation only rewrites pivots:
+//     L_ij = A_ij * D_j^{-1},   D_i = A_ii - sum_j L_ij * A_ji   (j in increasing order)
+// and the upper factor is the upper part of A itself.  Row i depends on rows i-1,
+// i-nx, i-nx*ny, so all cells with equal ix+iy+iz (one "level") are independent.
+//
+// BiCGSTAB keeps its scalars on the device (KrylovState); every kernel returns at
+// once when the solve has stopped, so a fixed sequence of launches can be queued or
+// captured without a host round trip per half step.  Reductions are deterministic:
+// per-block partial sums in a fixed grid, combined in block order by the last block.
+#include <cuda/atomic>
+
+#include "common.cuh"
+#include "linalg.cuh"
+#include "linalg_kernels.cuh"
+
+namespace dxg {
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double warpSum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warpMax(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum of NV values per thread; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void blockSum(double (&v)[NV])
+{
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = warpSum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][wid] = v[k];
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = lane < nw ? sh[k][lane] : 0.0;
+            v[k] = warpSum(t);
+        }
+    }
+}
+
+// Writes this block's partials; returns true in thread 0 of the last block to finish,
+// which then holds the grid totals (summed in block order) in v.
+template <int NV>
+__device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsigned* counter)
+{
+    blockSum<NV>(v);
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) partials[k * kMaxReduceBlocks + blockIdx.x] = v[k];
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        amLast = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    // the last block combines the partials in block order
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (unsigned bI = threadIdx.x; bI < gridDim.x; bI += 32)
+                s += ((volatile double*)partials)[k * kMaxReduceBlocks + bI];
+            v[k] = warpSum(s);
+        }
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+    return threadIdx.x == 0;
+}
+
+// ---------------------------------------------------------------- block helpers
+template <int B, class MT, class VT>
+__device__ __forceinline__ void blkMv(const MT* __restrict__ blk, const VT* x, VT* acc)
+{
+#pragma unroll
+    for (int r = 0; r < B; ++r)
+#pragma unroll
+        for (int c = 0; c < B; ++c) acc[r] += (VT)blk[r * B + c] * x[c];
+}
+template <int B, class MT, class VT>
+__device__ __forceinline__ void blkMvSub(const MT* __restrict__ blk, const VT* x, VT* acc)
+{
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+        VT s = 0;
+#pragma unroll
+        for (int c = 0; c < B; ++c) s += (VT)blk[r * B + c] * x[c];
+        acc[r] -= s;
+    }
+}
+
+template <int B, class T>
+__device__ __forceinline__ void loadVec(const T* p, int64_t i, T* v)
+{
+#pragma unroll
+    for (int e = 0; e < B; ++e) v[e] = p[i * B + e];
+}
+template <int B, class T>
+__device__ __forceinline__ void storeVec(T* p, int64_t i, const T* v)
+{
+#pragma unroll
+    for (int e = 0; e < B; ++e) p[i * B + e] = v[e];
+}
+
+__device__ __forceinline__ bool slotValid(unsigned mask, int dim, int s)
+{
+    if (s == dim) return true;
+    const int f = s < dim ? 2 * (dim - 1 - s) : 2 * (s - dim - 1) + 1;
+    return (mask >> f) & 1u;
+}
+
+// ---------------------------------------------------------------- SpMV
+// y = A x; MODE 0: plain; MODE 1: also dot(w, y) -> h, alpha; MODE 2: dots (y,w),(y,y) -> omega
+template <int B, int DIM, class MT, class VT, int MODE>
+__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    constexpr int S = 2 * DIM + 1;
+    constexpr int BB = B * B;
+    double part[2] = {0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned m = a.nbmask[i];
+        VT acc[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) acc[e] = 0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (!slotValid(m, DIM, s)) continue;
+            const int64_t j = i + a.off[s];
+            VT xj[B];
+            loadVec<B>(a.x, j, xj);
+            blkMv<B>(a.A + ((int64_t)s * a.N + i) * BB, xj, acc);
+        }
+        storeVec<B>(a.y, i, acc);
+        if (MODE == 1) {
+            VT w[B];
+            loadVec<B>(a.w, i, w);
+#pragma unroll
+            for (int e = 0; e < B; ++e) part[0] += (double)w[e] * (double)acc[e];
+        } else if (MODE == 2) {
+            VT w[B];
+            loadVec<B>(a.w, i, w);
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                part[0] += (double)acc[e] * (double)w[e];
+                part[1] += (double)acc[e] * (double)acc[e];
+            }
+        }
+    }
+    if (MODE == 0) return;
+    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE)) {
+        KrylovState& ks = *a.ks;
+        if (MODE == 1) {
+            ks.h = part[0];
+            if (fabs(ks.h) < 1e-80) ks.status = KS_BREAKDOWN;
+            else ks.alpha = ks.rho_new / ks.h;
+        } else {
+            ks.tr = part[0];
+            ks.tt = part[1];
+            ks.omega = ks.tr / ks.tt;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- ILU(0)
+template <int B, class T>
+__device__ __forceinline__ bool blkInvert(const T* A, T* inv)
+{
+    if (B == 1) {
+        inv[0] = (T)1 / A[0];
+        return A[0] != (T)0;
+    } else {
+        const T det = A[0] * A[3] - A[1] * A[2];
+        if (det == (T)0) return false;
+        const T detInv = (T)1 / det;
+        inv[0] = A[3] * detInv;
+        inv[1] = -A[1] * detInv;
+        inv[2] = -A[2] * detInv;
+        inv[3] = A[0] * detInv;
+        return true;
+    }
+}
+template <int B, class T>
+__device__ __forceinline__ void blkMul(const T* X, const T* Y, T* Z)
+{
+#pragma unroll
+    for (int r = 0; r < B; ++r)
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+            T s = 0;
+#pragma unroll
+            for (int k = 0; k < B; ++k) s += X[r * B + k] * Y[k * B + c];
+            Z[r * B + c] = s;
+        }
+}
+
+template <int B, int DIM, class MT>
+__global__ void iluFactorLevel(IluArgs<MT, MT> a, int begin, int count)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    constexpr int BB = B * B;
+    const int64_t i = a.perm[begin + k];
+    const unsigned m = a.nbmask[i];
+    MT D[BB];
+#pragma unroll
+    for (int e = 0; e < BB; ++e) D[e] = a.A[((int64_t)DIM * a.N + i) * BB + e];
+#pragma unroll
+    for (int s = 0; s < DIM; ++s) {
+        MT* Ls = a.L + ((int64_t)s * a.N + i) * BB;
+        if (!slotValid(m, DIM, s)) {
+#pragma unroll
+            for (int e = 0; e < BB; ++e) Ls[e] = 0;
+            continue;
+        }
+        const int64_t j = i + a.off[s];
+        MT Aij[BB], Dj[BB], Lij[BB], Uji[BB], P[BB];
+#pragma unroll
+        for (int e = 0; e < BB; ++e) {
+            Aij[e] = a.A[((int64_t)s * a.N + i) * BB + e];
+            Dj[e] = a.Dinv[j * BB + e];
+            Uji[e] = a.A[((int64_t)(2 * DIM - s) * a.N + j) * BB + e];
+        }
+        blkMul<B>(Aij, Dj, Lij);
+#pragma unroll
+        for (int e = 0; e < BB; ++e) Ls[e] = Lij[e];
+        blkMul<B>(Lij, Uji, P);
+#pragma unroll
+        for (int e = 0; e < BB; ++e) D[e] -= P[e];
+    }
+    MT inv[BB];
+    if (!blkInvert<B>(D, inv)) *a.singular = 1;
+#pragma unroll
+    for (int e = 0; e < BB; ++e) a.Dinv[i * BB + e] = inv[e];
+}
+
+template <int B, int DIM, class MT, class VT>
+__global__ void iluForwardLevel(IluArgs<MT, VT> a, const VT* __restrict__ d, VT* v, int begin, int count)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    constexpr int BB = B * B;
+    const int64_t i = a.perm[begin + k];
+    const unsigned m = a.nbmask[i];
+    VT rhs[B];
+    loadVec<B>(d, i, rhs);
+#pragma unroll
+    for (int s = 0; s < DIM; ++s) {
+        if (!slotValid(m, DIM, s)) continue;
+        const int64_t j = i + a.off[s];
+        VT vj[B];
+        loadVec<B>(v, j, vj);
+        blkMvSub<B>(a.L + ((int64_t)s * a.N + i) * BB, vj, rhs);
+    }
+    storeVec<B>(v, i, rhs);
+}
+
+template <int B, int DIM, class MT, class VT>
+__global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    constexpr int BB = B * B;
+    const int64_t i = a.perm[begin + k];
+    const unsigned m = a.nbmask[i];
+    VT rhs[B];
+    loadVec<B>(v, i, rhs);
+#pragma unroll
+    for (int s = DIM + 1; s < 2 * DIM + 1; ++s) {
+        if (!slotValid(m, DIM, s)) continue;
+        const int64_t j = i + a.off[s];
+        VT vj[B];
+        loadVec<B>(v, j, vj);
+        blkMvSub<B>(a.A + ((int64_t)s * a.N + i) * BB, vj, rhs);
+    }
+    VT out[B];
+#pragma unroll
+    for (int e = 0; e < B; ++e) out[e] = 0;
+    blkMv<B>(a.Dinv + i * BB, rhs, out);
+    storeVec<B>(v, i, out);
+}
+
+// ---------------------------------------------------------------- BiCGSTAB vector kernels
+template <class VT>
+__global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a, const double* __restrict__ rhs)
+{
+    double part[1] = {0.0};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
+        const VT rv = (VT)rhs[k];
+        a.r[k] = rv;
+        a.rt[k] = rv;
+        a.x[k] = 0;
+        a.p[k] = 0;
+        a.v[k] = 0;
+        part[0] += (double)rv * (double)rv;
+    }
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 4)) {
+        KrylovState& ks = *a.ks;
+        ks.def0 = ks.def = sqrt(part[0]);
+        ks.rho = ks.alpha = ks.omega = 1.0;
+        ks.halfsteps = 0;
+        if (!isfinite(ks.def)) ks.status = KS_NAN;
+        else if (ks.def < 1e-30) ks.status = KS_CONVERGED;
+        else ks.status = KS_RUNNING;
+    }
+}
+
+// rho_new = <rt, r>, breakdown checks and beta (first half of an iteration)
+template <class VT>
+__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a)
+{
+    if (a.ks->status != KS_RUNNING) return;
+    double part[1] = {0.0};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x)
+        part[0] += (double)a.rt[k] * (double)a.r[k];
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5)) {
+        KrylovState& ks = *a.ks;
+        if (ks.halfsteps + 1 >= ks.maxHalf) { ks.status = KS_MAXIT; return; }
+        ks.rho_new = part[0];
+        if (fabs(ks.rho) <= 1e-80 || fabs(ks.omega) <= 1e-80) { ks.status = KS_BREAKDOWN; return; }
+        if (ks.halfsteps > 0) ks.beta = (ks.rho_new / ks.rho) * (ks.alpha / ks.omega);
+    }
+}
+
+// p = r (first iteration) or p = (p - omega v) * beta + r
+template <class VT>
+__global__ void bicgUpdateP(BicgArgs<VT> a)
+{
+    const KrylovState& ks = *a.ks;
+    if (ks.status != KS_RUNNING) return;
+    const bool first = ks.halfsteps == 0;
+    const VT omega = (VT)ks.omega, beta = (VT)ks.beta;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
+        if (first) a.p[k] = a.r[k];
+        else {
+            VT pk = a.p[k];
+            pk += -omega * a.v[k];
+            pk *= beta;
+            pk += a.r[k];
+            a.p[k] = pk;
+        }
+    }
+}
+
+// x += s*y; r -= s*q; def = ||r||; STAGE 0: s = alpha, q = v; STAGE 1: s = omega, q = t
+template <class VT, int STAGE>
+__global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a)
+{
+    const KrylovState& ksr = *a.ks;
+    if (ksr.status != KS_RUNNING) return;
+    const double sd = STAGE == 0 ? ksr.alpha : ksr.omega;
+    const VT s = (VT)sd;
+    const VT* q = STAGE == 0 ? a.v : a.t;
+    double part[1] = {0.0};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
+        a.x[k] += s * a.y[k];
+        const VT rk = a.r[k] + (-s) * q[k];
+        a.r[k] = rk;
+        part[0] += (double)rk * (double)rk;
+    }
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6)) {
+        KrylovState& ks = *a.ks;
+        ks.def = sqrt(part[0]);
+        ks.halfsteps += 1;
+        if (STAGE == 1) ks.rho = ks.rho_new;
+        if (!isfinite(ks.def)) ks.status = KS_NAN;
+        else if (ks.def < ks.def0 * ks.reduction || ks.def < 1e-30) ks.status = KS_CONVERGED;
+    }
+}
+
+// ---------------------------------------------------------------- Newton helpers
+// u = uLast - lambda*delta (uLast keeps the iterate), shift = max relative shift
+// (maxRelativeShift, dumux/nonlinear/newtonsolver.hh:110-128)
+__global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(const double* __restrict__ uLast,
+                                                                      const double* __restrict__ delta, double* u,
+                                                                      double lambda, int64_t M, double* partials,
+                                                                      unsigned* counter, double* shiftOut)
+{
+    double mx = 0.0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x) {
+        const double a = uLast[k];
+        const double b = a + (-lambda) * delta[k];
+        u[k] = b;
+        const double s = fabs(a - b) / fmax(1.0, fabs(a + b) * 0.5);
+        mx = fmax(mx, s);
+    }
+    // block max
+    __shared__ double sh[32];
+    mx = warpMax(mx);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = mx;
+    __syncthreads();
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+        double bm = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) bm = fmax(bm, sh[k]);
+        partials[blockIdx.x] = bm;
+        __threadfence();
+        amLast = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (amLast && threadIdx.x == 0) {
+        __threadfence();
+        double g = 0.0;
+        for (unsigned bI = 0; bI < gridDim.x; ++bI) g = fmax(g, ((volatile double*)partials)[bI]);
+        *shiftOut = g;
+        *counter = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kReduceThreads) norm2Kernel(const double* __restrict__ x, int64_t M,
+                                                               double* partials, unsigned* counter, double* out)
+{
+    double part[1] = {0.0};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x)
+        part[0] += x[k] * x[k];
+    if (gridSum<1>(part, partials, counter)) *out = sqrt(part[0]);
+}
+
+template <class VT>
+__global__ void copyToDouble(const VT* __restrict__ x, double* y, int64_t M)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x)
+        y[k] = (double)x[k];
+}
+
+// ---------------------------------------------------------------- host launchers
+int reduceBlocks(int64_t M)
+{
+    int64_t b = (M + kReduceThreads - 1) / kReduceThreads;
+    if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <int B, int DIM, class MT, class VT>
+void spmvT(const SpmvArgs<MT, VT>& a, int mode, cudaStream_t st)
+{
+    const int g = reduceBlocks(a.N);
+    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a);
+    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a);
+    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a);
+}
+
+template <class MT, class VT>
+void launchSpmv(const SpmvArgs<MT, VT>& a, int b, int dim, int mode, cudaStream_t st)
+{
+    if (b == 1) { if (dim == 2) spmvT<1, 2>(a, mode, st); else spmvT<1, 3>(a, mode, st); }
+    else { if (dim == 2) spmvT<2, 2>(a, mode, st); else spmvT<2, 3>(a, mode, st); }
+    DXG_CUDA(cudaGetLastError());
+}
+
+template <class MT>
+int64_t launchIluFactor(const IluArgs<MT, MT>& a, const LevelSchedule& ls, int b, int dim, cudaStream_t st)
+{
+    int64_t launches = 0;
+    for (int L = 0; L < ls.numLevels; ++L) {
+        const int begin = ls.ptr[L], count = ls.ptr[L + 1] - ls.ptr[L];
+        const int g = (count + 127) / 128;
+        if (b == 1) {
+            if (dim == 2) iluFactorLevel<1, 2, MT><<<g, 128, 0, st>>>(a, begin, count);
+            else iluFactorLevel<1, 3, MT><<<g, 128, 0, st>>>(a, begin, count);
+        } else {
+            if (dim == 2) iluFactorLevel<2, 2, MT><<<g, 128, 0, st>>>(a, begin, count);
+            else iluFactorLevel<2, 3, MT><<<g, 128, 0, st>>>(a, begin, count);
+        }
+        ++launches;
+    }
+    DXG_CUDA(cudaGetLastError());
+    return launches;
+}
+
+template <int B, int DIM, class MT, class VT>
+static int64_t iluApplyT(const IluArgs<MT, VT>& a, const LevelSchedule& ls, const VT* d, VT* v, cudaStream_t st)
+{
+    for (int L = 0; L < ls.numLevels; ++L) {
+        const int begin = ls.ptr[L], count = ls.ptr[L + 1] - ls.ptr[L];
+        iluForwardLevel<B, DIM, MT, VT><<<(count + 127) / 128, 128, 0, st>>>(a, d, v, begin, count);
+    }
+    for (int L = ls.numLevels - 1; L >= 0; --L) {
+        const int begin = ls.ptr[L], count = ls.ptr[L + 1] - ls.ptr[L];
+        iluBackwardLevel<B, DIM, MT, VT><<<(count + 127) / 128, 128, 0, st>>>(a, v, begin, count);
+    }
+    return 2 * (int64_t)ls.numLevels;
+}
+
+template <class MT, class VT>
+int64_t launchIluApply(const IluArgs<MT, VT>& a, const LevelSchedule& ls, int b, int dim, const VT* d, VT* v,
+                       cudaStream_t st)
+{
+    int64_t n;
+    if (b == 1) n = dim == 2 ? iluApplyT<1, 2>(a, ls, d, v, st) : iluApplyT<1, 3>(a, ls, d, v, st);
+    else n = dim == 2 ? iluApplyT<2, 2>(a, ls, d, v, st) : iluApplyT<2, 3>(a, ls, d, v, st);
+    DXG_CUDA(cudaGetLastError());
+    return n;
+}
+
+template <class VT>
+void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st)
+{
+    bicgInit<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, rhs);
+    DXG_CUDA(cudaGetLastError());
+}
+template <class VT>
+void launchBicgRho(const BicgArgs<VT>& a, cudaStream_t st)
+{
+    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+}
+template <class VT>
+void launchBicgUpdateP(const BicgArgs<VT>& a, cudaStream_t st)
+{
+    bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+}
+template <class VT>
+void launchBicgAxpyNorm(const BicgArgs<VT>& a, int stage, cudaStream_t st)
+{
+    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+    else bicgAxpyNorm<VT, 1><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+}
+template <class VT>
+void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st)
+{
+    copyToDouble<VT><<<reduceBlocks(M), kReduceThreads, 0, st>>>(x, y, M);
+}
+
+void launchNewtonUpdate(const double* uLast, const double* delta, double* u, double lambda, int64_t M,
+                        const ReduceScratch& sc, double* shiftOut, cudaStream_t st)
+{
+    newtonUpdateKernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(uLast, delta, u, lambda, M, sc.partials,
+                                                                  sc.counter + 7, shiftOut);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st)
+{
+    norm2Kernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(x, M, sc.partials, sc.counter + 3, out);
+    DXG_CUDA(cudaGetLastError());
+}
+
+// explicit instantiations
+template void launchSpmv<double, double>(const SpmvArgs<double, double>&, int, int, int, cudaStream_t);
+template void launchSpmv<float, float>(const SpmvArgs<float, float>&, int, int, int, cudaStream_t);
+template int64_t launchIluFactor<double>(const IluArgs<double, double>&, const LevelSchedule&, int, int, cudaStream_t);
+template int64_t launchIluFactor<float>(const IluArgs<float, float>&, const LevelSchedule&, int, int, cudaStream_t);
+template int64_t launchIluApply<double, double>(const IluArgs<double, double>&, const LevelSchedule&, int, int,
+                                                const double*, double*, cudaStream_t);
+template int64_t launchIluApply<float, float>(const IluArgs<float, float>&, const LevelSchedule&, int, int,
+                                              const float*, float*, cudaStream_t);
+template void launchBicgInit<double>(const BicgArgs<double>&, const double*, cudaStream_t);
+template void launchBicgInit<float>(const BicgArgs<float>&, const double*, cudaStream_t);
+template void launchBicgRho<double>(const BicgArgs<double>&, cudaStream_t);
+template void launchBicgRho<float>(const BicgArgs<float>&, cudaStream_t);
+template void launchBicgUpdateP<double>(const BicgArgs<double>&, cudaStream_t);
+template void launchBicgUpdateP<float>(const BicgArgs<float>&, cudaStream_t);
+template void launchBicgAxpyNorm<double>(const BicgArgs<double>&, int, cudaStream_t);
+template void launchBicgAxpyNorm<float>(const BicgArgs<float>&, int, cudaStream_t);
+template void launchCopyToDouble<double>(const double*, double*, int64_t, cudaStream_t);
+template void launchCopyToDouble<float>(const float*, double*, int64_t, cudaStream_t);
+
+}  // namespace dxg

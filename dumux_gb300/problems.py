@@ -1,0 +1,139 @@
+"""Tabulated problems: the reference's test problems and the benchmark workloads.
+
+Each builder evaluates the problem's ``*AtPos`` callbacks at cell and face centres and
+returns a :class:`dumux_gb300.abi.ProblemDesc` (the input of ``dxg_problem_upload``)
+plus the initial solution.  This is the Python counterpart of the C++ tabulation in
+``include/dumux_gb300/tabulate.hh``.
+"""
+import numpy as np
+
+from .abi import ProblemDesc, boundary_face_centers, cell_centers, num_boundary_faces
+
+# SimpleH2O (dumux/material/components/simpleh2o.hh:265-267, 309) and
+# Trichloroethene (dumux/material/components/trichloroethene.hh:148-171)
+WATER_DENSITY, WATER_VISCOSITY = 1000.0, 1e-3
+DNAPL_DENSITY, DNAPL_VISCOSITY = 1460.0, 5.7e-4
+
+
+def equidistant(lower, upper, cells):
+    """Vertex coordinates of a YaspGrid with EquidistantOffsetCoordinates: x_i = lower + i*h."""
+    h = (upper - lower) / cells
+    return lower + np.arange(cells + 1, dtype=np.float64) * h
+
+
+def onep_lens_problem(cells=(10, 10), numeric_epsilon=True):
+    """test/porousmediumflow/1p/incompressible (problem.hh, spatialparams.hh, params.input):
+    unit square, lens [0.2,0.8]^2 with K=1e-12 in K=1e-10, Dirichlet top/bottom with
+    p = 1e5 - 1e5*(y - ymax), no-flow left/right, gravity on, stationary."""
+    coords = [equidistant(0.0, 1.0, n) for n in cells]
+    cc = cell_centers(coords)
+    eps = 1.5e-7
+    lens_lo, lens_hi = (0.2, 0.2), (0.8, 0.8)
+    in_lens = np.ones(len(cc), dtype=bool)
+    for a in range(2):
+        in_lens &= (cc[:, a] >= lens_lo[a] + eps) & (cc[:, a] <= lens_hi[a] - eps)
+    K = np.where(in_lens, 1e-12, 1e-10)
+    fc = boundary_face_centers(2, coords)
+    ymax = coords[1][-1]
+    dirichlet = (fc[:, 1] < 1e-6) | (fc[:, 1] > ymax - 1e-6)
+    bc_type = np.where(dirichlet, 1, 2).astype(np.int8)
+    bc_values = np.where(dirichlet, 1.0e5 + (-1.0e5) * (fc[:, 1] - ymax), 0.0)
+    desc = ProblemDesc(coords=coords, num_eq=1, permeability=K, porosity=np.full(len(cc), 0.4),
+                       bc_type=bc_type, bc_values=bc_values, enable_gravity=True,
+                       density=(WATER_DENSITY, WATER_DENSITY), viscosity=(WATER_VISCOSITY, WATER_VISCOSITY),
+                       base_epsilon=0.1 if numeric_epsilon else 1e-10,
+                       privar_magnitude=(1e5, -1.0) if numeric_epsilon else (-1.0, -1.0))
+    return desc, np.zeros(desc.num_dofs)
+
+
+def gaussian_lnk_field(cells, mean, sigma, corr_len, seed):
+    """Stationary Gaussian random field with exponential covariance
+    C(h) = sigma^2 exp(-|h|/corr_len) (|h| in cells), sampled by circulant embedding
+    on a grid padded to twice the size in every axis (numpy PCG64 from `seed`)."""
+    cells = tuple(int(c) for c in cells)
+    pad = tuple(2 * c for c in cells)
+    axes = [np.minimum(np.arange(p), p - np.arange(p)).astype(np.float64) for p in pad]
+    grids = np.meshgrid(*axes, indexing="ij")
+    dist = np.sqrt(sum(g * g for g in grids))
+    cov = sigma * sigma * np.exp(-dist / corr_len)
+    lam = np.real(np.fft.fftn(cov))
+    lam = np.maximum(lam, 0.0)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xi = rng.standard_normal(pad) + 1j * rng.standard_normal(pad)
+    field = np.fft.ifftn(np.sqrt(lam) * xi) * np.sqrt(np.prod(pad))
+    f = np.real(field)[tuple(slice(0, c) for c in cells)]
+    # index order (x, y, z) -> flatten x fastest
+    return mean + f.flatten(order="F")
+
+
+def darcy_1p(cells=(100, 100), seed=1, sigma=1.0, corr_len=8.0, mean_lnk=np.log(1e-10),
+             enable_gravity=False, lnk=None):
+    """1p incompressible Darcy on [0,1]^2: ln K Gaussian field, porosity 0.4, water,
+    Dirichlet p=2e5 left / 1e5 right, no-flow top/bottom, one Newton step (stationary)."""
+    dim = len(cells)
+    coords = [equidistant(0.0, 1.0, n) for n in cells]
+    if lnk is None:
+        lnk = gaussian_lnk_field(cells, mean_lnk, sigma, corr_len, seed)
+    K = np.exp(lnk)
+    n = int(np.prod(cells))
+    fc = boundary_face_centers(dim, coords)
+    nb = num_boundary_faces(dim, list(cells) + [1] * (3 - dim))
+    left = fc[:, 0] < 1e-6
+    right = fc[:, 0] > coords[0][-1] - 1e-6
+    bc_type = np.where(left | right, 1, 2).astype(np.int8)
+    bc_values = np.zeros(nb)
+    bc_values[left] = 2e5
+    bc_values[right] = 1e5
+    desc = ProblemDesc(coords=coords, num_eq=1, permeability=K, porosity=np.full(n, 0.4),
+                       bc_type=bc_type, bc_values=bc_values, enable_gravity=enable_gravity,
+                       density=(WATER_DENSITY, WATER_DENSITY), viscosity=(WATER_VISCOSITY, WATER_VISCOSITY))
+    return desc, np.full(desc.num_dofs, 1e5)
+
+
+def dnapl_2p(cells=(64, 64, 32), extent=(6.0, 4.0, 1.0), seed=2, sigma=1.0, corr_len=6.0,
+             mean_lnk=np.log(5e-11), inflow=0.04, pe=500.0, lam=2.0, swr=0.05, snr=0.0,
+             pc_low_swe=0.01, enable_gravity=True, lnk=None):
+    """2p immiscible water-DNAPL (p_w, S_n), the 2p incompressible test problem
+    (test/porousmediumflow/2p/incompressible/problem.hh:59-180) on a 2D or 3D box with
+    the vertical axis last: hydrostatic Dirichlet left/right (alpha-scaled), DNAPL
+    Neumann inflow on the top strip 0.5 < (xmax-x)/width < 2/3, Brooks-Corey default law,
+    Gaussian ln K field."""
+    dim = len(cells)
+    coords = [equidistant(0.0, float(extent[a]), cells[a]) for a in range(dim)]
+    if lnk is None:
+        lnk = gaussian_lnk_field(cells, mean_lnk, sigma, corr_len, seed)
+    K = np.exp(lnk)
+    n = int(np.prod(cells))
+    v = dim - 1                       # vertical axis
+    g = -9.81 if enable_gravity else 0.0
+    fc = boundary_face_centers(dim, coords)
+    nb = len(fc)
+    xmin, xmax = coords[0][0], coords[0][-1]
+    vmin, vmax = coords[v][0], coords[v][-1]
+    eps = 1e-6
+    on_left = fc[:, 0] < xmin + eps
+    on_right = fc[:, 0] > xmax - eps
+    on_upper = fc[:, v] > vmax - eps
+    width = xmax - xmin
+    lam_x = (xmax - fc[:, 0]) / width
+    on_inlet = on_upper & (0.5 < lam_x) & (lam_x < 2.0 / 3.0)
+    dirichlet = on_left | on_right
+    bc_type = np.where(dirichlet, 1, 2).astype(np.int8)
+    bc_values = np.zeros((nb, 2))
+    height = vmax - vmin
+    depth = vmax - fc[:, v]
+    alpha = 1 + 1.5 / height
+    factor = (width * alpha + (1.0 - alpha) * fc[:, 0]) / width
+    pw_dir = 1e5 - factor * WATER_DENSITY * g * depth
+    bc_values[dirichlet, 0] = pw_dir[dirichlet]
+    bc_values[dirichlet, 1] = 0.0
+    bc_values[on_inlet & ~dirichlet, 1] = -inflow
+    cc = cell_centers(coords)
+    u0 = np.zeros((n, 2))
+    u0[:, 0] = 1e5 - WATER_DENSITY * g * (vmax - cc[:, v])
+    u0[:, 1] = 0.0
+    desc = ProblemDesc(coords=coords, num_eq=2, permeability=K, porosity=np.full(n, 0.4),
+                       bc_type=bc_type, bc_values=bc_values.reshape(-1), enable_gravity=enable_gravity,
+                       density=(WATER_DENSITY, DNAPL_DENSITY), viscosity=(WATER_VISCOSITY, DNAPL_VISCOSITY),
+                       material_params=np.array([[pe, lam, swr, snr, pc_low_swe]]))
+    return desc, u0.reshape(-1)

@@ -1,0 +1,223 @@
+/*
+ * dumux_gb300.h -- C ABI of the GB300-native cell-centred TPFA porous-flow hot path.
+ *
+ * One opaque context (dxg_ctx) owns one problem resident in device memory: the
+ * tabulated problem / spatial parameters, the solution vectors, the block Jacobian,
+ * the ILU(0) factors and the Krylov work vectors.  Every entry point returns an int
+ * status (DXG_OK == 0); no C++ exception crosses this boundary.  Host buffers are
+ * owned by the caller; device buffers are owned by the context.  A context is not
+ * re-entrant; distinct contexts may be used from distinct threads.
+ *
+ * Each entry point names the reference interface it replaces (paths are relative to
+ * the DuMux source tree).
+ */
+#ifndef DUMUX_GB300_H
+#define DUMUX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+enum {
+    DXG_OK = 0,
+    DXG_ERR_ARG = 1,             /* invalid argument / unsupported configuration      */
+    DXG_ERR_CUDA = 2,            /* CUDA runtime error (message via dxg_last_error)   */
+    DXG_ERR_OOM = 3,             /* device allocation failed                          */
+    DXG_ERR_STATE = 4,           /* call order violated (e.g. solve before assemble)  */
+    DXG_ERR_LINEAR_BREAKDOWN = 5,/* BiCGSTAB breakdown (|rho| or |h| below 1e-80)     */
+    DXG_ERR_LINEAR_NOT_CONVERGED = 6, /* BiCGSTAB hit maxit                           */
+    DXG_ERR_NAN = 7,             /* non-finite residual / defect                      */
+    DXG_ERR_NEWTON_NOT_CONVERGED = 8, /* Newton failed after all dt divisions         */
+    DXG_ERR_TIMEOUT = 9,         /* a bounded device-side wait gave up                */
+    DXG_ERR_NO_DEVICE = 10       /* no CUDA device / extension built without GPU      */
+};
+
+/* ---- problem description (tabulated Problem + SpatialParams) ------------------
+ * A structured tensor-product grid (YaspGrid semantics): cells are numbered
+ * lexicographically with x fastest; the local faces of a cell are ordered
+ * -x, +x, -y, +y, -z, +z (dune-grid reference-element numbering, used through
+ * dumux/discretization/cellcentered/tpfa/fvgridgeometry.hh:239-330).
+ *
+ * Boundary faces are listed side by side in the order -x, +x, -y, +y, -z, +z; on
+ * each side they are numbered lexicographically over the two remaining axes (the
+ * lower axis fastest).  For dim == 2 there are four sides.
+ *
+ * All pointers are host pointers read during dxg_problem_upload only.            */
+typedef struct dxg_problem_desc {
+    int32_t dim;                 /* 2 or 3                                          */
+    int32_t cells[3];            /* cells per axis (cells[2] == 1 when dim == 2)    */
+    const double* coords[3];     /* vertex coordinates per axis, cells[d]+1 values  */
+    int32_t num_eq;              /* 1: 1p (p), 2: 2p immiscible p0s1 (p_w, S_n)     */
+    int32_t enable_gravity;      /* Problem.EnableGravity (reference default true)  */
+    double gravity[3];           /* used when enable_gravity != 0                   */
+    double density[2];           /* constant liquid density per phase [kg/m^3]      */
+    double viscosity[2];         /* constant liquid viscosity per phase [Pa s]      */
+    /* per-cell spatial parameters, N = cells[0]*cells[1]*cells[2] entries          */
+    const double* permeability;  /* isotropic intrinsic permeability [m^2]          */
+    const double* porosity;      /* [-]                                             */
+    const double* extrusion;     /* extrusion factor, NULL -> 1                     */
+    const int32_t* material;     /* material-law index per cell, NULL -> 0          */
+    const double* source;        /* N*num_eq source rates [kg/m^3/s], NULL -> 0     */
+    /* regularised Brooks-Corey parameter sets, 5 doubles each:
+     * pcEntry, lambda, Swr, Snr, pcLowSwe (BrooksCoreyDefault)                     */
+    int32_t num_materials;
+    const double* material_params;
+    /* boundary faces (see ordering above)                                          */
+    const int8_t* bc_type;       /* 1 = Dirichlet, 2 = Neumann                      */
+    const double* bc_values;     /* num_eq values per boundary face: Dirichlet
+                                    primary variables or Neumann mass flux
+                                    [kg/m^2/s] (positive = outflow)                  */
+    /* numeric differentiation (dumux/assembly/numericepsilon.hh)                   */
+    double base_epsilon;         /* Assembly.NumericDifference.BaseEpsilon (1e-10)  */
+    double privar_magnitude[2];  /* Assembly.NumericDifference.PriVarMagnitude (<=0: |x|+1) */
+    int32_t numeric_difference_method; /* Assembly.NumericDifferenceMethod: 1 forward, 0 central, -1 backward */
+    double upwind_weight;        /* Flux.UpwindWeight (1.0)                         */
+} dxg_problem_desc;
+
+/* Number of boundary faces implied by the grid of desc. */
+int64_t dxg_num_boundary_faces(const dxg_problem_desc* desc);
+
+/* ---- context lifecycle --------------------------------------------------------- */
+typedef struct dxg_ctx dxg_ctx;
+
+/* Creates a context on CUDA device `device`.  Replaces the construction of
+ * FVAssembler + ILUBiCGSTABIstlSolver + NewtonSolver
+ * (dumux/assembly/fvassembler.hh:154-172, dumux/linear/istlsolvers.hh:635-642,
+ *  dumux/nonlinear/newtonsolver.hh:210-237). */
+int dxg_ctx_create(dxg_ctx** out, int device);
+int dxg_ctx_destroy(dxg_ctx* ctx);
+/* Human-readable description of the last error of this context (or of the last
+ * failed dxg_ctx_create when ctx == NULL). */
+const char* dxg_last_error(const dxg_ctx* ctx);
+
+/* Precision of the linear system: FP64 everywhere (the plain drop-in), or the
+ * mixed form (FP32 Jacobian / ILU(0) / inner BiCGSTAB inside an FP64 residual,
+ * FP64 numeric differentiation, update and norms).  Must be set before upload. */
+enum { DXG_PRECISION_FP64 = 0, DXG_PRECISION_MIXED = 1 };
+int dxg_set_precision(dxg_ctx* ctx, int precision);
+
+/* Tabulates the problem into device memory and builds the sparsity pattern.
+ * Replaces CCTpfaFVGridGeometry::update_ (dumux/discretization/cellcentered/tpfa/
+ * fvgridgeometry.hh:216), CCSimpleConnectivityMap::update (dumux/discretization/
+ * cellcentered/connectivitymap.hh:66-114), getJacobianPattern (dumux/assembly/
+ * jacobianpattern.hh:25-53) and FVAssembler::setLinearSystem
+ * (dumux/assembly/fvassembler.hh:294-302). */
+int dxg_problem_upload(dxg_ctx* ctx, const dxg_problem_desc* desc);
+
+/* Sizes: cells, equations per cell, nonzero blocks of the Jacobian. */
+int dxg_sizes(const dxg_ctx* ctx, int64_t* num_cells, int32_t* num_eq, int64_t* num_blocks);
+
+/* ---- state ----------------------------------------------------------------------- */
+/* Current solution (N*num_eq doubles, cell-major: u[cell*num_eq + pv]).
+ * dxg_set_solution replaces FVAssembler::updateGridVariables
+ * (dumux/assembly/fvassembler.hh:379-382). */
+int dxg_set_solution(dxg_ctx* ctx, const double* u);
+int dxg_get_solution(dxg_ctx* ctx, double* u);
+/* Previous time level.  Replaces FVAssembler::setPreviousSolution / resetTimeStep
+ * (dumux/assembly/fvassembler.hh:360-390). */
+int dxg_set_prev_solution(dxg_ctx* ctx, const double* u_prev);
+/* Time step size for the storage term; dt <= 0 selects the stationary residual
+ * (FVAssembler::isStationaryProblem, dumux/assembly/fvassembler.hh:340). */
+int dxg_set_time_step(dxg_ctx* ctx, double dt);
+
+/* ---- assembler (dumux/assembly/fvassembler.hh) ----------------------------------- */
+/* Residual and numeric-differentiation Jacobian at the current solution.
+ * Replaces FVAssembler::assembleJacobianAndResidual (fvassembler.hh:178-207) with
+ * CCLocalAssembler<numeric, implicit> (dumux/assembly/cclocalassembler.hh:164-348). */
+int dxg_assemble_jacobian_and_residual(dxg_ctx* ctx);
+/* Residual only.  Replaces FVAssembler::assembleResidual (fvassembler.hh:240-267). */
+int dxg_assemble_residual(dxg_ctx* ctx);
+/* Copies of the device residual / Jacobian.  The Jacobian is exported in BCRS form:
+ * row_ptr[N+1], col_idx[num_blocks], values[num_blocks*num_eq*num_eq] (row-major
+ * blocks, columns sorted), the layout of Dune::BCRSMatrix<FieldMatrix<double,b,b>>
+ * (dumux/discretization/fvproperties.hh:66-75). */
+int dxg_get_residual(dxg_ctx* ctx, double* r);
+int dxg_get_jacobian(dxg_ctx* ctx, int64_t* row_ptr, int32_t* col_idx, double* values);
+/* Loads a host BCRS matrix with the context's sparsity pattern (same layout as
+ * dxg_get_jacobian) and a right-hand side, for stand-alone linear solves. */
+int dxg_set_linear_system(dxg_ctx* ctx, const int64_t* row_ptr, const int32_t* col_idx,
+                          const double* values, const double* rhs);
+
+/* ---- linear solver (dumux/linear/istlsolvers.hh) ----------------------------------- */
+typedef struct dxg_linear_result {
+    int32_t converged;           /* IstlSolverResult::converged                      */
+    int32_t iterations;          /* BiCGSTAB iterations (half steps rounded up)      */
+    double reduction;            /* final defect / initial defect                    */
+    double initial_defect;
+    double final_defect;
+} dxg_linear_result;
+/* Solves J x = r with ILU(0)-preconditioned BiCGSTAB from x = 0 on the device (the
+ * assembled Jacobian and residual), stopping when defect < reduction * defect0 or
+ * after max_iter iterations.  Replaces ILUBiCGSTABIstlSolver::solve
+ * (dumux/linear/istlsolvers.hh:273, 457-491, 635-642).  The solution stays on the
+ * device as the Newton update; dxg_get_update copies it out. */
+int dxg_linear_solve(dxg_ctx* ctx, double reduction, int32_t max_iter, dxg_linear_result* res);
+int dxg_get_update(dxg_ctx* ctx, double* delta);
+/* Euclidean norm of the device residual.  Replaces IstlIterativeLinearSolver::norm
+ * (dumux/linear/istlsolvers.hh:306-337). */
+int dxg_residual_norm(dxg_ctx* ctx, double* norm);
+
+/* ---- Newton (dumux/nonlinear/newtonsolver.hh) ---------------------------------------- */
+typedef struct dxg_newton_params {
+    double max_relative_shift;   /* Newton.MaxRelativeShift (1e-8)                   */
+    int32_t min_steps;           /* Newton.MinSteps (2)                              */
+    int32_t max_steps;           /* Newton.MaxSteps (18)                             */
+    int32_t target_steps;        /* Newton.TargetSteps (10)                          */
+    int32_t use_line_search;     /* Newton.UseLineSearch (false)                     */
+    double line_search_min_relaxation; /* Newton.LineSearchMinRelaxationFactor (0.125) */
+    int32_t enable_residual_criterion; /* Newton.EnableResidualCriterion (false)     */
+    double residual_reduction;   /* Newton.ResidualReduction (1e-5)                  */
+    int32_t max_time_step_divisions;   /* Newton.MaxTimeStepDivisions (10)           */
+    double retry_time_step_reduction;  /* Newton.RetryTimeStepReductionFactor (0.5)  */
+    double linear_reduction;     /* LinearSolver.ResidualReduction used in Newton (1e-6) */
+    int32_t linear_max_iter;     /* LinearSolver.MaxIterations (250)                 */
+    int32_t record_residual_norms; /* compute ||r|| after each update as a diagnostic */
+} dxg_newton_params;
+
+/* Fills p with the reference defaults (newtonsolver.hh:1213-1247). */
+void dxg_newton_default_params(dxg_newton_params* p);
+
+#define DXG_MAX_NEWTON_RECORD 64
+typedef struct dxg_newton_report {
+    int32_t converged;
+    int32_t iterations;          /* Newton iterations of the last (successful) attempt */
+    int32_t time_step_divisions; /* retries with reduced dt                            */
+    double dt_used;              /* dt of the last attempt                             */
+    int32_t linear_iterations;   /* summed over the successful attempt                 */
+    int32_t wasted_iterations;   /* iterations of failed attempts                      */
+    double initial_residual;     /* ||r(u^0)||                                         */
+    double shift[DXG_MAX_NEWTON_RECORD];          /* max relative shift per iteration  */
+    double residual_norm[DXG_MAX_NEWTON_RECORD];  /* ||r(u^{k+1})|| (when recorded)    */
+    int32_t linear_iters[DXG_MAX_NEWTON_RECORD];  /* BiCGSTAB iterations per Newton step */
+    double time_assemble, time_solve, time_update; /* seconds, host clock            */
+} dxg_newton_report;
+
+/* Solves one implicit-Euler time step u^{n+1} from the current solution (used as
+ * initial guess) and the previous solution, with dt halving on failure.  On success
+ * the solution is u^{n+1} and dt_used is reported; on failure the solution is reset
+ * to the previous solution and DXG_ERR_NEWTON_NOT_CONVERGED is returned.
+ * Replaces NewtonSolver::solve(x, timeLoop) (newtonsolver.hh:309-355).
+ * dt <= 0: stationary problem, NewtonSolver::solve(x) (newtonsolver.hh:362-368). */
+int dxg_newton_solve(dxg_ctx* ctx, double dt, const dxg_newton_params* params,
+                     dxg_newton_report* report);
+/* Time-step size proposal from the last Newton iteration count.
+ * Replaces NewtonSolver::suggestTimeStepSize (newtonsolver.hh:784-798). */
+double dxg_suggest_time_step(const dxg_ctx* ctx, double old_dt, const dxg_newton_params* params);
+/* Accepts the current solution as the new previous solution (advanceTimeStep,
+ * dumux/discretization/fvgridvariables.hh:54-129). */
+int dxg_advance_time_step(dxg_ctx* ctx);
+
+/* ---- diagnostics --------------------------------------------------------------------- */
+/* Kernel launches issued by this context since creation (all of them ours). */
+int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
+/* Synchronises the context stream and reports any pending CUDA error. */
+int dxg_sync(dxg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DUMUX_GB300_H */

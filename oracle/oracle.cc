@@ -1,0 +1,1023 @@
+// oracle.cc -- CPU oracle for the cc-TPFA hot path.  TEST INFRASTRUCTURE ONLY:
+// the checker for the product's CUDA path (tests, smoke check, CPU baseline of
+// bench.py).  Never linked into the product.
+//
+// A faithful FP64 restatement of the reference's element-wise algorithm:
+//   * element loop and numeric-difference Jacobian: dumux/assembly/fvassembler.hh:461-510,
+//     dumux/assembly/cclocalassembler.hh:164-348 (column-wise scatter, neighbour fluxes
+//     evaluated with the neighbour as inside element);
+//   * local residual: dumux/assembly/fvlocalresidual.hh:132-333,
+//     dumux/assembly/cclocalresidual.hh:49-105,
+//     dumux/porousmediumflow/immiscible/localresidual.hh:64-126;
+//   * TPFA Darcy flux with gravity and upwinding: dumux/flux/cctpfa/darcyslaw.hh:153-259,
+//     dumux/discretization/cellcentered/tpfa/computetransmissibility.hh:66-80,
+//     dumux/flux/upwindscheme.hh:35-54;
+//   * element volume variables incl. Dirichlet ghosts built with the inside cell's
+//     spatial parameters: dumux/discretization/cellcentered/tpfa/elementvolumevariables.hh:277-342,
+//     dumux/porousmediumflow/2p/volumevariables.hh:74-191, 1p/volumevariables.hh:65-179;
+//   * regularised Brooks-Corey: dumux/material/fluidmatrixinteractions/2p/brookscorey.hh:99-503,
+//     materiallaw.hh:103-223, efftoabsdefaultpolicy.hh:106-151;
+//   * numeric differentiation: dumux/common/numericdifferentiation.hh:36-123,
+//     dumux/assembly/numericepsilon.hh:37-53;
+//   * Newton driver: dumux/nonlinear/newtonsolver.hh:110-128, 309-382, 428-701, 784-798,
+//     917-1072, 1138-1178, 1213-1254;
+//   * linear solver: dune-istl >= 2.10 (not vendored in the reference) SeqILU(n=0, w=1) and
+//     BiCGSTABSolver as bound by dumux/linear/istlsolvers.hh:535-568, 635-642 with the
+//     defaults of dumux/linear/linearsolverparameters.hh:56-73.  ILU(0) follows the
+//     published block ILU(0) algorithm (Saad 2003, Alg. 10.4, row-wise "IKJ" variant,
+//     pivots stored inverted); BiCGSTAB follows van der Vorst (1992) with dune-istl's
+//     half-step convergence tests (def < reduction*def0 or def < 1e-30) and breakdown
+//     threshold 1e-80.
+// Compiled with -ffp-contract=off so x86 and Arm hosts give identical bits.
+#include "oracle.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+struct NumericalProblem : std::runtime_error { using std::runtime_error::runtime_error; };
+struct SolverAbort : std::runtime_error { using std::runtime_error::runtime_error; };
+
+static int g_threads = 0;
+}  // namespace orc
+extern "C" int orc_get_threads(void);
+namespace orc {
+
+// ---------------------------------------------------------------- Brooks-Corey
+struct BrooksCoreyDefault {
+    double pe, lambda, swr, snr, pcLowSwe;
+    double pcLowSwePcValue = 0, pcDerivativeLowSw = 0, pcDerivativeHighSwEnd = 0, entryPressure = 0;
+
+    explicit BrooksCoreyDefault(const double* prm)
+        : pe(prm[0]), lambda(prm[1]), swr(prm[2]), snr(prm[3]), pcLowSwe(prm[4])
+    {
+        // BrooksCoreyRegularization::init / initPcParameters_ (brookscorey.hh:347-354, 477-486)
+        entryPressure = pe;
+        const double lowSw = sweToSw(pcLowSwe);
+        const double highSw = sweToSw(1.0);
+        const double dsw_dswe = 1.0 - swr - snr;
+        pcDerivativeLowSw = dpc_dsw_noreg(lowSw) * dsw_dswe;
+        pcDerivativeHighSwEnd = dpc_dsw_noreg(highSw) * dsw_dswe;
+        pcLowSwePcValue = pc_noreg(lowSw);
+    }
+    double swToSwe(double sw) const { return (sw - swr) / (1.0 - swr - snr); }
+    double sweToSw(double swe) const { return swe * (1.0 - swr - snr) + swr; }
+    double dswe_dsw() const { return 1.0 / (1.0 - swr - snr); }
+    static double clamp01(double x) { return std::clamp(x, 0.0, 1.0); }
+    double base_pc(double swe) const { swe = clamp01(swe); return pe * std::pow(swe, -1.0 / lambda); }
+    double base_dpc_dswe(double swe) const
+    {
+        swe = clamp01(swe);
+        return -pe / lambda * std::pow(swe, -1.0 / lambda - 1.0);
+    }
+    double pc_noreg(double sw) const { return base_pc(swToSwe(sw)); }
+    double dpc_dsw_noreg(double sw) const { return base_dpc_dswe(swToSwe(sw)) * dswe_dsw(); }
+
+    double pc(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= pcLowSwe) return pcLowSwePcValue + pcDerivativeLowSw * (swe - pcLowSwe);
+        else if (swe >= 1.0) return pcDerivativeHighSwEnd * (swe - 1.0) + entryPressure;
+        return base_pc(swe);
+    }
+    double krw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0) return 0.0;
+        else if (swe >= 1.0) return 1.0;
+        return std::pow(clamp01(swe), 2.0 / lambda + 3.0);
+    }
+    double krn(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0) return 1.0;
+        else if (swe >= 1.0) return 0.0;
+        const double s = clamp01(swe);
+        const double exponent = 2.0 / lambda + 1.0;
+        const double sne = 1.0 - s;
+        return sne * sne * (1.0 - std::pow(s, exponent));
+    }
+};
+
+// ---------------------------------------------------------------- grid / geometry
+struct Face {
+    int axis, side;            // local face f = 2*axis + side
+    bool boundary;
+    int64_t outside;           // neighbour cell (interior faces)
+    int64_t bidx;              // boundary face index (boundary faces)
+    double ip[3], n[3], area;
+};
+
+struct Problem {
+    const dxg_problem_desc& d;
+    int dim, b;
+    int64_t n[3], N;
+    int64_t side_offset[7];
+    std::vector<BrooksCoreyDefault> laws;
+    double g[3] = {0, 0, 0};
+
+    explicit Problem(const dxg_problem_desc& desc) : d(desc)
+    {
+        dim = d.dim;
+        b = d.num_eq;
+        if (dim < 2 || dim > 3 || (b != 1 && b != 2)) throw std::invalid_argument("unsupported dim/num_eq");
+        for (int a = 0; a < 3; ++a) n[a] = (a < dim) ? d.cells[a] : 1;
+        N = n[0] * n[1] * n[2];
+        side_offset[0] = 0;
+        for (int f = 0; f < 2 * dim; ++f) {
+            const int a = f / 2;
+            int64_t cnt = 1;
+            for (int c = 0; c < dim; ++c) if (c != a) cnt *= n[c];
+            side_offset[f + 1] = side_offset[f] + cnt;
+        }
+        if (b == 2) for (int m = 0; m < d.num_materials; ++m) laws.emplace_back(d.material_params + 5 * m);
+        if (d.enable_gravity) for (int a = 0; a < dim; ++a) g[a] = d.gravity[a];
+    }
+    void ijk(int64_t c, int64_t* id) const { id[0] = c % n[0]; id[1] = (c / n[0]) % n[1]; id[2] = c / (n[0] * n[1]); }
+    double lo(int a, int64_t i) const { return d.coords[a][i]; }
+    double hi(int a, int64_t i) const { return d.coords[a][i + 1]; }
+    void center(int64_t c, double* x) const
+    {
+        int64_t id[3]; ijk(c, id);
+        for (int a = 0; a < 3; ++a) x[a] = 0.0;
+        for (int a = 0; a < dim; ++a) x[a] = 0.5 * (lo(a, id[a]) + hi(a, id[a]));
+    }
+    double volume(int64_t c) const
+    {
+        int64_t id[3]; ijk(c, id);
+        double v = 1.0;
+        for (int a = 0; a < dim; ++a) v *= hi(a, id[a]) - lo(a, id[a]);
+        return v;
+    }
+    Face face(int64_t c, int f) const
+    {
+        Face fc{};
+        int64_t id[3]; ijk(c, id);
+        fc.axis = f / 2; fc.side = f % 2;
+        const int a = fc.axis;
+        center(c, fc.ip);
+        fc.ip[a] = fc.side == 0 ? lo(a, id[a]) : hi(a, id[a]);
+        for (int k = 0; k < 3; ++k) fc.n[k] = 0.0;
+        fc.n[a] = fc.side == 0 ? -1.0 : 1.0;
+        fc.area = 1.0;
+        for (int k = 0; k < dim; ++k) if (k != a) fc.area *= hi(k, id[k]) - lo(k, id[k]);
+        const bool bnd = fc.side == 0 ? id[a] == 0 : id[a] == n[a] - 1;
+        fc.boundary = bnd;
+        if (!bnd) {
+            int64_t stride = 1;
+            for (int k = 0; k < a; ++k) stride *= n[k];
+            fc.outside = c + (fc.side == 0 ? -stride : stride);
+            fc.bidx = -1;
+        } else {
+            fc.outside = -1;
+            int64_t pos = 0, mul = 1;
+            for (int k = 0; k < dim; ++k) if (k != a) { pos += id[k] * mul; mul *= n[k]; }
+            fc.bidx = side_offset[f] + pos;
+        }
+        return fc;
+    }
+    double perm(int64_t c) const { return d.permeability[c]; }
+    double poro(int64_t c) const { return d.porosity[c]; }
+    double extr(int64_t c) const { return d.extrusion ? d.extrusion[c] : 1.0; }
+    const BrooksCoreyDefault& law(int64_t c) const { return laws[d.material ? d.material[c] : 0]; }
+};
+
+struct VolVars {
+    double p[2], rho[2], mob[2], S[2];
+    double phi, extr, K;
+};
+
+// OnePVolumeVariables::update / TwoPVolumeVariables::update + completeFluidState (p0s1,
+// water wetting).  Spatial parameters are those of cell c.
+static VolVars volVars(const Problem& P, const double* pv, int64_t c)
+{
+    VolVars v{};
+    v.phi = P.poro(c);
+    v.extr = P.extr(c);
+    v.K = P.perm(c);
+    if (P.b == 1) {
+        v.p[0] = pv[0];
+        v.rho[0] = P.d.density[0];
+        v.mob[0] = 1.0 / P.d.viscosity[0];
+        v.S[0] = 1.0;
+    } else {
+        const auto& law = P.law(c);
+        const double Sn = pv[1];
+        v.S[1] = Sn;
+        v.S[0] = 1 - Sn;
+        const double pc = law.pc(v.S[0]);
+        v.p[0] = pv[0];
+        v.p[1] = pv[0] + pc;
+        v.rho[0] = P.d.density[0];
+        v.rho[1] = P.d.density[1];
+        v.mob[0] = law.krw(v.S[0]) / P.d.viscosity[0];
+        v.mob[1] = law.krn(v.S[0]) / P.d.viscosity[1];
+    }
+    return v;
+}
+
+// computeTpfaTransmissibility for a scalar permeability
+static double tpfaT(const Problem& P, const Face& f, int64_t scvCell, double K, double extr)
+{
+    double c[3]; P.center(scvCell, c);
+    double dv[3];
+    for (int i = 0; i < P.dim; ++i) dv[i] = f.ip[i] - c[i];
+    double n2 = 0.0;
+    for (int i = 0; i < P.dim; ++i) n2 += dv[i] * dv[i];
+    for (int i = 0; i < P.dim; ++i) dv[i] /= n2;
+    double dot = 0.0;
+    for (int i = 0; i < P.dim; ++i) dot += dv[i] * f.n[i];
+    return K * extr * dot;
+}
+
+static double nDotG(const Problem& P, const Face& f)
+{
+    double s = 0.0;
+    for (int i = 0; i < P.dim; ++i) s += f.n[i] * P.g[i];
+    return s;
+}
+
+// ImmiscibleLocalResidual::computeFlux for the face f of cell `inside`
+static void computeFlux(const Problem& P, int64_t inside, const Face& f,
+                        const VolVars& vin, const VolVars& vout, double* F)
+{
+    // flux variables cache: TPFA transmissibility (darcyslaw.hh:217-259)
+    const double ti = tpfaT(P, f, inside, vin.K, vin.extr);
+    double tij;
+    if (f.boundary)
+        tij = f.area * ti;
+    else {
+        const double tj = -1.0 * tpfaT(P, f, f.outside, vout.K, vout.extr);
+        if (ti * tj <= 0.0) tij = 0;
+        else tij = f.area * (ti * tj) / (ti + tj);
+    }
+    const double w = P.d.upwind_weight;
+    for (int ph = 0; ph < P.b; ++ph) {
+        double flux;
+        if (P.d.enable_gravity) {
+            const double rho = f.boundary ? vout.rho[ph] : (vin.rho[ph] + vout.rho[ph]) * 0.5;
+            const double alpha_inside = vin.K * nDotG(P, f) * vin.extr;
+            flux = tij * (vin.p[ph] - vout.p[ph]) + rho * f.area * alpha_inside;
+            if (!f.boundary) {
+                const double outsideTi = -1.0 * tpfaT(P, f, f.outside, vout.K, vout.extr);
+                const double alpha_outside = vout.K * nDotG(P, f) * vout.extr;
+                flux -= rho * tij / outsideTi * (alpha_inside - alpha_outside);
+            }
+        } else {
+            flux = tij * (vin.p[ph] - vout.p[ph]);
+        }
+        const double upIn = vin.rho[ph] * vin.mob[ph];
+        const double upOut = vout.rho[ph] * vout.mob[ph];
+        double mult;
+        if (std::signbit(flux)) mult = w * upOut + (1.0 - w) * upIn;
+        else mult = w * upIn + (1.0 - w) * upOut;
+        F[ph] = flux * mult;
+    }
+}
+
+// element-local view: volume variables of the element, its neighbours and the
+// Dirichlet ghosts, bound at the current solution
+struct ElemView {
+    int64_t I;
+    VolVars vI;
+    VolVars vOut[6];           // per local face: neighbour vv or Dirichlet ghost
+    Face faces[6];
+    VolVars vPrev;
+    bool transient;
+    double dt;
+};
+
+// CCLocalResidual::evalFlux (boundary handling, cclocalresidual.hh:58-101)
+static void evalFlux(const Problem& P, int64_t inside, const Face& f, const VolVars& vin,
+                     const VolVars& vout, double* out)
+{
+    double flux[2] = {0.0, 0.0};
+    if (!f.boundary) {
+        double F[2]; computeFlux(P, inside, f, vin, vout, F);
+        for (int e = 0; e < P.b; ++e) flux[e] += F[e];
+    } else {
+        const int8_t t = P.d.bc_type[f.bidx];
+        if (t == 1) {
+            double F[2]; computeFlux(P, inside, f, vin, vout, F);
+            for (int e = 0; e < P.b; ++e) flux[e] += F[e];
+        } else if (t == 2) {
+            const double s = f.area * vin.extr;
+            for (int e = 0; e < P.b; ++e) flux[e] += P.d.bc_values[f.bidx * P.b + e] * s;
+        } else throw std::invalid_argument("mixed/unknown boundary condition");
+    }
+    for (int e = 0; e < P.b; ++e) out[e] = flux[e];
+}
+
+// FVLocalAssemblerBase::evalLocalResidual for element I with (possibly deflected) vI
+static void localResidual(const Problem& P, const ElemView& ev, const VolVars& vI, double* res)
+{
+    const int b = P.b;
+    const int64_t I = ev.I;
+    const double V = P.volume(I);
+    double r[2] = {0.0, 0.0};
+    // evalSource: residual -= source*V*extrusion
+    {
+        double src[2] = {0.0, 0.0};
+        if (P.d.source) for (int e = 0; e < b; ++e) src[e] += P.d.source[I * b + e];
+        const double s = V * vI.extr;
+        for (int e = 0; e < b; ++e) { src[e] *= s; r[e] -= src[e]; }
+    }
+    // evalFlux over all faces of I
+    for (int f = 0; f < 2 * P.dim; ++f) {
+        double fl[2];
+        evalFlux(P, I, ev.faces[f], vI, ev.vOut[f], fl);
+        for (int e = 0; e < b; ++e) r[e] += fl[e];
+    }
+    if (ev.transient) {
+        double st[2] = {0.0, 0.0};
+        for (int ph = 0; ph < b; ++ph) {
+            double prevS = ev.vPrev.phi * ev.vPrev.rho[ph] * ev.vPrev.S[ph];
+            double curS = vI.phi * vI.rho[ph] * vI.S[ph];
+            prevS *= ev.vPrev.extr;
+            curS *= vI.extr;
+            curS -= prevS;
+            curS *= V;
+            curS /= ev.dt;
+            st[ph] += curS;
+        }
+        for (int e = 0; e < b; ++e) r[e] += st[e];
+    }
+    for (int e = 0; e < b; ++e) res[e] = r[e];
+}
+
+static int oppositeFace(int f) { return f ^ 1; }
+
+// flux of neighbour J's face touching I, J as inside element (cclocalassembler.hh:186-218)
+static void neighbourFlux(const Problem& P, const ElemView& ev, int f, const VolVars& vI, double* out)
+{
+    const Face& fI = ev.faces[f];
+    const int64_t J = fI.outside;
+    const Face fJ = P.face(J, oppositeFace(f));
+    double r[2] = {0.0, 0.0};
+    double fl[2];
+    evalFlux(P, J, fJ, ev.vOut[f], vI, fl);
+    for (int e = 0; e < P.b; ++e) r[e] += fl[e];
+    for (int e = 0; e < P.b; ++e) out[e] = r[e];
+}
+
+static void bindElement(const Problem& P, int64_t I, const double* u, const double* uprev, double dt, ElemView& ev)
+{
+    const int b = P.b;
+    ev.I = I;
+    ev.vI = volVars(P, u + I * b, I);
+    for (int f = 0; f < 2 * P.dim; ++f) {
+        ev.faces[f] = P.face(I, f);
+        const Face& fc = ev.faces[f];
+        if (!fc.boundary) ev.vOut[f] = volVars(P, u + fc.outside * b, fc.outside);
+        else if (P.d.bc_type[fc.bidx] == 1) ev.vOut[f] = volVars(P, P.d.bc_values + fc.bidx * b, I);
+        else ev.vOut[f] = ev.vI;   // unused for Neumann faces
+    }
+    ev.transient = dt > 0.0;
+    ev.dt = dt;
+    if (ev.transient) ev.vPrev = volVars(P, uprev + I * b, I);
+}
+
+static double numericEpsilon(const Problem& P, double x, int pv)
+{
+    const double mag = P.d.privar_magnitude[pv];
+    const double base = P.d.base_epsilon > 0 ? P.d.base_epsilon : 1e-10;
+    if (mag > 0.0) return base * mag;
+    return base * (std::abs(x) + 1.0);
+}
+
+struct Pattern {
+    std::vector<int64_t> rowPtr;
+    std::vector<int32_t> col;
+    std::vector<int64_t> diag;               // block index of (I,I)
+    std::vector<int64_t> colBlock;           // per cell I, per face f: block index of (J,I), -1 if none
+};
+
+static Pattern buildPattern(const Problem& P)
+{
+    Pattern pt;
+    const int nf = 2 * P.dim;
+    std::vector<std::vector<int32_t>> rows(P.N);
+    for (int64_t I = 0; I < P.N; ++I) {
+        rows[I].push_back((int32_t)I);
+        for (int f = 0; f < nf; ++f) {
+            const Face fc = P.face(I, f);
+            if (!fc.boundary) rows[fc.outside].push_back((int32_t)I);
+        }
+    }
+    pt.rowPtr.resize(P.N + 1);
+    pt.rowPtr[0] = 0;
+    for (int64_t I = 0; I < P.N; ++I) {
+        std::sort(rows[I].begin(), rows[I].end());
+        rows[I].erase(std::unique(rows[I].begin(), rows[I].end()), rows[I].end());
+        pt.rowPtr[I + 1] = pt.rowPtr[I] + (int64_t)rows[I].size();
+    }
+    pt.col.resize(pt.rowPtr[P.N]);
+    for (int64_t I = 0; I < P.N; ++I) std::copy(rows[I].begin(), rows[I].end(), pt.col.begin() + pt.rowPtr[I]);
+    auto find = [&](int64_t row, int64_t c) -> int64_t {
+        auto b0 = pt.col.begin() + pt.rowPtr[row], b1 = pt.col.begin() + pt.rowPtr[row + 1];
+        auto it = std::lower_bound(b0, b1, (int32_t)c);
+        return (it != b1 && *it == c) ? (int64_t)(it - pt.col.begin()) : -1;
+    };
+    pt.diag.resize(P.N);
+    pt.colBlock.assign(P.N * nf, -1);
+    for (int64_t I = 0; I < P.N; ++I) {
+        pt.diag[I] = find(I, I);
+        for (int f = 0; f < nf; ++f) {
+            const Face fc = P.face(I, f);
+            if (!fc.boundary) pt.colBlock[I * nf + f] = find(fc.outside, I);
+        }
+    }
+    return pt;
+}
+
+// CCLocalAssembler<numeric, implicit>::assembleJacobianAndResidualImpl for element I
+static void assembleElement(const Problem& P, const Pattern& pt, int64_t I, const double* u, const double* uprev,
+                            double dt, double* values, double* r)
+{
+    const int b = P.b, nf = 2 * P.dim;
+    ElemView ev;
+    bindElement(P, I, u, uprev, dt, ev);
+    double orig0[2];
+    localResidual(P, ev, ev.vI, orig0);
+    if (values) {
+        double origJ[6][2] = {};
+        for (int f = 0; f < nf; ++f)
+            if (!ev.faces[f].boundary) neighbourFlux(P, ev, f, ev.vI, origJ[f]);
+
+        const int method = P.d.numeric_difference_method;
+        for (int pv = 0; pv < b; ++pv) {
+            double pvs[2] = {u[I * b], b > 1 ? u[I * b + 1] : 0.0};
+            const double x0 = pvs[pv];
+            // evaluates own residual and neighbour fluxes with u_I[pv] = x
+            auto eval = [&](double x, double* d0, double (*dJ)[2]) {
+                double q[2] = {pvs[0], pvs[1]};
+                q[pv] = x;
+                const VolVars vDef = volVars(P, q, I);
+                localResidual(P, ev, vDef, d0);
+                for (int f = 0; f < nf; ++f) {
+                    dJ[f][0] = dJ[f][1] = 0.0;
+                    if (!ev.faces[f].boundary) neighbourFlux(P, ev, f, vDef, dJ[f]);
+                }
+            };
+            const double eps = numericEpsilon(P, x0, pv);
+            double d0[2], dJ[6][2];
+            // NumericDifferentiation::partialDerivative (numericdifferentiation.hh:67-123)
+            if (method == 5) {
+                double a0[2], aJ[6][2];
+                eval(x0 + eps, d0, dJ);
+                eval(x0 - eps, a0, aJ);
+                for (int e = 0; e < b; ++e) { d0[e] -= a0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] -= aJ[f][e]; }
+                for (int e = 0; e < b; ++e) { d0[e] *= 8.0; for (int f = 0; f < nf; ++f) dJ[f][e] *= 8.0; }
+                eval(x0 - 2.0 * eps, a0, aJ);
+                for (int e = 0; e < b; ++e) { d0[e] += a0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] += aJ[f][e]; }
+                eval(x0 + 2.0 * eps, a0, aJ);
+                for (int e = 0; e < b; ++e) { d0[e] -= a0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] -= aJ[f][e]; }
+                const double den = 12.0 * eps;
+                for (int e = 0; e < b; ++e) { d0[e] /= den; for (int f = 0; f < nf; ++f) dJ[f][e] /= den; }
+            } else {
+                double delta = 0.0;
+                if (method >= 0) {
+                    delta += eps;
+                    eval(x0 + eps, d0, dJ);
+                } else {
+                    for (int e = 0; e < b; ++e) { d0[e] = orig0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] = origJ[f][e]; }
+                }
+                if (method <= 0) {
+                    delta += eps;
+                    double a0[2], aJ[6][2];
+                    eval(x0 - eps, a0, aJ);
+                    for (int e = 0; e < b; ++e) { d0[e] -= a0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] -= aJ[f][e]; }
+                } else {
+                    for (int e = 0; e < b; ++e) { d0[e] -= orig0[e]; for (int f = 0; f < nf; ++f) dJ[f][e] -= origJ[f][e]; }
+                }
+                for (int e = 0; e < b; ++e) { d0[e] /= delta; for (int f = 0; f < nf; ++f) dJ[f][e] /= delta; }
+            }
+            // scatter column pv of block column I
+            const int64_t di = pt.diag[I];
+            for (int e = 0; e < b; ++e) {
+                values[(di * b + e) * b + pv] += d0[e];
+                for (int f = 0; f < nf; ++f) {
+                    const int64_t blk = pt.colBlock[I * nf + f];
+                    if (blk >= 0) values[(blk * b + e) * b + pv] += dJ[f][e];
+                }
+            }
+        }
+    }
+    for (int e = 0; e < b; ++e) r[I * b + e] = orig0[e];
+}
+
+static void assemble(const Problem& P, const Pattern& pt, const double* u, const double* uprev, double dt,
+                     double* values, double* r)
+{
+    const int b = P.b;
+    if (values) std::fill(values, values + pt.rowPtr[P.N] * b * b, 0.0);
+    // Column-wise scatter: element I writes only block column I and r[I], so the
+    // element loop is race free without colouring.
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t I = 0; I < P.N; ++I) assembleElement(P, pt, I, u, uprev, dt, values, r);
+}
+
+// ---------------------------------------------------------------- dune-istl restatement
+struct BCRS {
+    int64_t n; int b;
+    const int64_t* rowPtr; const int32_t* col;
+    std::vector<double> val;   // ILU copy
+};
+
+static void blkMul(int b, const double* A, const double* B, double* C)   // C = A*B
+{
+    for (int i = 0; i < b; ++i)
+        for (int j = 0; j < b; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < b; ++k) s += A[i * b + k] * B[k * b + j];
+            C[i * b + j] = s;
+        }
+}
+
+static void blkInvert(int b, double* A)
+{
+    if (b == 1) { A[0] = 1.0 / A[0]; return; }
+    const double det = A[0] * A[3] - A[1] * A[2];
+    if (det == 0.0) throw SolverAbort("singular pivot in ILU(0)");
+    const double detInv = 1.0 / det;
+    const double a00 = A[0], a01 = A[1], a10 = A[2], a11 = A[3];
+    A[0] = a11 * detInv;
+    A[1] = -a01 * detInv;
+    A[2] = -a10 * detInv;
+    A[3] = a00 * detInv;
+}
+
+// block ILU(0) in place; diagonal blocks hold the inverted pivots afterwards
+static void ilu0Decompose(BCRS& M)
+{
+    const int b = M.b, bb = b * b;
+    double tmp[4], L[4];
+    for (int64_t i = 0; i < M.n; ++i) {
+        int64_t ij = M.rowPtr[i];
+        const int64_t endi = M.rowPtr[i + 1];
+        for (; ij < endi && M.col[ij] < i; ++ij) {
+            const int64_t j = M.col[ij];
+            int64_t jj = M.rowPtr[j];
+            while (M.col[jj] != j) ++jj;
+            blkMul(b, &M.val[ij * bb], &M.val[jj * bb], L);      // L_ij = A_ij * D_j^{-1}
+            std::memcpy(&M.val[ij * bb], L, sizeof(double) * bb);
+            int64_t ik = ij + 1, jk = jj + 1;
+            const int64_t endj = M.rowPtr[j + 1];
+            while (ik < endi && jk < endj) {
+                if (M.col[ik] == M.col[jk]) {
+                    blkMul(b, L, &M.val[jk * bb], tmp);            // A_ik -= L_ij * A_jk
+                    for (int e = 0; e < bb; ++e) M.val[ik * bb + e] -= tmp[e];
+                    ++ik; ++jk;
+                } else if (M.col[ik] < M.col[jk]) ++ik;
+                else ++jk;
+            }
+        }
+        if (ij >= endi || M.col[ij] != i) throw SolverAbort("ILU: missing diagonal");
+        blkInvert(b, &M.val[ij * bb]);
+    }
+}
+
+static void ilu0Apply(const BCRS& M, const double* d, double* v)
+{
+    const int b = M.b, bb = b * b;
+    for (int64_t i = 0; i < M.n; ++i) {
+        double rhs[2] = {d[i * b], b > 1 ? d[i * b + 1] : 0.0};
+        for (int64_t ij = M.rowPtr[i]; ij < M.rowPtr[i + 1] && M.col[ij] < i; ++ij) {
+            const double* L = &M.val[ij * bb];
+            const double* vj = &v[(int64_t)M.col[ij] * b];
+            for (int r = 0; r < b; ++r) {
+                double s = 0.0;
+                for (int c = 0; c < b; ++c) s += L[r * b + c] * vj[c];
+                rhs[r] -= s;
+            }
+        }
+        for (int r = 0; r < b; ++r) v[i * b + r] = rhs[r];
+    }
+    for (int64_t i = M.n - 1; i >= 0; --i) {
+        double rhs[2] = {v[i * b], b > 1 ? v[i * b + 1] : 0.0};
+        int64_t ii = -1;
+        for (int64_t ij = M.rowPtr[i]; ij < M.rowPtr[i + 1]; ++ij) {
+            const int64_t j = M.col[ij];
+            if (j == i) { ii = ij; continue; }
+            if (j < i) continue;
+            const double* U = &M.val[ij * bb];
+            const double* vj = &v[j * b];
+            for (int r = 0; r < b; ++r) {
+                double s = 0.0;
+                for (int c = 0; c < b; ++c) s += U[r * b + c] * vj[c];
+                rhs[r] -= s;
+            }
+        }
+        const double* Dinv = &M.val[ii * bb];
+        for (int r = 0; r < b; ++r) {
+            double s = 0.0;
+            for (int c = 0; c < b; ++c) s += Dinv[r * b + c] * rhs[c];
+            v[i * b + r] = s;
+        }
+    }
+}
+
+static void spmv(int64_t n, int b, const int64_t* rowPtr, const int32_t* col, const double* A, const double* x, double* y)
+{
+    const int bb = b * b;
+    for (int64_t i = 0; i < n; ++i) {
+        double acc[2] = {0.0, 0.0};
+        for (int64_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const double* blk = A + k * bb;
+            const double* xj = x + (int64_t)col[k] * b;
+            for (int r = 0; r < b; ++r)
+                for (int c = 0; c < b; ++c) acc[r] += blk[r * b + c] * xj[c];
+        }
+        for (int r = 0; r < b; ++r) y[i * b + r] = acc[r];
+    }
+}
+
+static double dot(int64_t m, const double* a, const double* c)
+{
+    double s = 0.0;
+    for (int64_t i = 0; i < m; ++i) s += a[i] * c[i];
+    return s;
+}
+
+static dxg_linear_result bicgstab(int64_t n, int b, const int64_t* rowPtr, const int32_t* col, const double* A,
+                                  const double* rhs, double* x, double reduction, int maxit)
+{
+    const int64_t m = n * b;
+    BCRS M{n, b, rowPtr, col, std::vector<double>(A, A + rowPtr[n] * b * b)};
+    ilu0Decompose(M);
+    std::vector<double> r(rhs, rhs + m), rt(m), p(m, 0.0), v(m, 0.0), t(m), y(m);
+    std::fill(x, x + m, 0.0);
+    const double EPSILON = 1e-80;
+    dxg_linear_result res{};
+    double def = std::sqrt(dot(m, r.data(), r.data()));
+    const double def0 = def;
+    res.initial_defect = def0;
+    auto converged = [&](double d) { return d < def0 * reduction || d < 1e-30; };
+    auto finish = [&](bool conv, double it, double d) {
+        res.converged = conv;
+        res.iterations = (int)std::ceil(it);
+        res.final_defect = d;
+        res.reduction = def0 > 0 ? d / def0 : 0.0;
+        return res;
+    };
+    if (!std::isfinite(def)) throw SolverAbort("non-finite defect");
+    if (converged(def)) return finish(true, 0.0, def);
+    rt = r;
+    double rho = 1, alpha = 1, omega = 1, rho_new, beta, h;
+    double it;
+    for (it = 0.5; it < maxit; it += .5) {
+        rho_new = dot(m, rt.data(), r.data());
+        if (std::abs(rho) <= EPSILON) throw SolverAbort("breakdown in BiCGSTAB - rho");
+        if (std::abs(omega) <= EPSILON) throw SolverAbort("breakdown in BiCGSTAB - omega");
+        if (it < 1)
+            p = r;
+        else {
+            beta = (rho_new / rho) * (alpha / omega);
+            for (int64_t i = 0; i < m; ++i) p[i] += -omega * v[i];
+            for (int64_t i = 0; i < m; ++i) p[i] *= beta;
+            for (int64_t i = 0; i < m; ++i) p[i] += r[i];
+        }
+        ilu0Apply(M, p.data(), y.data());
+        spmv(n, b, rowPtr, col, A, y.data(), v.data());
+        h = dot(m, rt.data(), v.data());
+        if (std::abs(h) < EPSILON) throw SolverAbort("breakdown in BiCGSTAB - h");
+        alpha = rho_new / h;
+        for (int64_t i = 0; i < m; ++i) x[i] += alpha * y[i];
+        for (int64_t i = 0; i < m; ++i) r[i] += -alpha * v[i];
+        def = std::sqrt(dot(m, r.data(), r.data()));
+        if (!std::isfinite(def)) throw SolverAbort("non-finite defect");
+        if (converged(def)) return finish(true, it, def);
+        it += .5;
+        ilu0Apply(M, r.data(), y.data());
+        spmv(n, b, rowPtr, col, A, y.data(), t.data());
+        omega = dot(m, t.data(), r.data()) / dot(m, t.data(), t.data());
+        for (int64_t i = 0; i < m; ++i) x[i] += omega * y[i];
+        for (int64_t i = 0; i < m; ++i) r[i] += -omega * t[i];
+        rho = rho_new;
+        def = std::sqrt(dot(m, r.data(), r.data()));
+        if (!std::isfinite(def)) throw SolverAbort("non-finite defect");
+        if (converged(def)) return finish(true, it, def);
+    }
+    return finish(false, it, def);
+}
+
+// ---------------------------------------------------------------- Newton driver
+// The reference NewtonSolver<Assembler, LinearSolver> restated over an abstract
+// assembler exposing the calls Newton makes (newtonsolver.hh:466-475, 488-524, 869-881).
+struct NewtonAssembler {
+    virtual ~NewtonAssembler() = default;
+    virtual int64_t size() const = 0;                         // scalar entries of u
+    virtual void assembleJacobianAndResidual(const std::vector<double>& u) = 0;
+    virtual void assembleResidual(const std::vector<double>& u) = 0;
+    virtual double residualNorm() const = 0;
+    // solves J delta = r, returns converged (throws SolverAbort on breakdown)
+    virtual bool solveLinear(std::vector<double>& delta, double reduction, int maxit, int* iters) = 0;
+};
+
+struct Newton {
+    dxg_newton_params prm;
+    int numSteps = 0;
+    double shift = 0, lastShift = 0, reduction = 0, lastReduction = 1, residualNorm = 0, initialResidual = 0;
+    std::vector<double> uLastIter;
+    dxg_newton_report* rep = nullptr;
+
+    bool converged() const
+    {
+        if (!prm.enable_residual_criterion) return shift <= prm.max_relative_shift;
+        return shift <= prm.max_relative_shift || reduction <= prm.residual_reduction;
+    }
+    bool proceed(bool conv) const
+    {
+        if (numSteps < prm.min_steps) return true;
+        else if (conv) return false;
+        else if (numSteps >= prm.max_steps) return shift * 4.0 < lastShift;
+        return true;
+    }
+    static double maxRelShift(const std::vector<double>& a, const std::vector<double>& c)
+    {
+        double s = 0.0;
+        for (size_t i = 0; i < a.size(); ++i) {
+            const double v = std::abs(a[i] - c[i]) / std::max<double>(1.0, std::abs(a[i] + c[i]) * 0.5);
+            s = std::max(s, v);
+        }
+        return s;
+    }
+    void computeResidualReduction(NewtonAssembler& A, const std::vector<double>& u)
+    {
+        A.assembleResidual(u);
+        residualNorm = A.residualNorm();
+        reduction = residualNorm / initialResidual;
+    }
+    // solveImpl_ (newtonsolver.hh:976-1072); throws NumericalProblem
+    bool solveImpl(NewtonAssembler& A, std::vector<double>& u)
+    {
+        numSteps = 0;
+        uLastIter = u;
+        std::vector<double> deltaU(u.size(), 0.0);
+        bool conv = false;
+        using clk = std::chrono::steady_clock;
+        while (proceed(conv)) {
+            lastShift = shift;
+            lastReduction = numSteps == 0 ? 1.0 : reduction;
+            if (numSteps > 0) uLastIter = u;
+            auto t0 = clk::now();
+            A.assembleJacobianAndResidual(u);
+            auto t1 = clk::now();
+            std::fill(deltaU.begin(), deltaU.end(), 0.0);
+            if (numSteps == 0) initialResidual = A.residualNorm();
+            int iters = 0;
+            bool lconv = false;
+            try { lconv = A.solveLinear(deltaU, prm.linear_reduction, prm.linear_max_iter, &iters); }
+            catch (const SolverAbort&) { lconv = false; }
+            if (!lconv) throw NumericalProblem("Linear solver did not converge");
+            auto t2 = clk::now();
+            if (prm.use_line_search) {
+                double lambda = 1.0;
+                std::vector<double> uCur = uLastIter;
+                while (true) {
+                    for (size_t i = 0; i < u.size(); ++i) uCur[i] += -lambda * deltaU[i];
+                    u = uCur;
+                    computeResidualReduction(A, u);
+                    if (reduction < lastReduction || lambda <= prm.line_search_min_relaxation) break;
+                    lambda *= 0.5;
+                    uCur = uLastIter;
+                }
+            } else {
+                std::vector<double> uCur = uLastIter;
+                for (size_t i = 0; i < u.size(); ++i) uCur[i] += -1.0 * deltaU[i];
+                u = uCur;
+                if (prm.enable_residual_criterion) computeResidualReduction(A, u);
+            }
+            shift = maxRelShift(uLastIter, u);
+            auto t3 = clk::now();
+            if (rep && numSteps < DXG_MAX_NEWTON_RECORD) {
+                rep->shift[numSteps] = shift;
+                rep->linear_iters[numSteps] = iters;
+                if (prm.record_residual_norms) {
+                    if (!(prm.use_line_search || prm.enable_residual_criterion)) {
+                        A.assembleResidual(u);
+                        residualNorm = A.residualNorm();
+                    }
+                    rep->residual_norm[numSteps] = residualNorm;
+                }
+            }
+            if (rep) {
+                rep->linear_iterations += iters;
+                rep->time_assemble += std::chrono::duration<double>(t1 - t0).count();
+                rep->time_solve += std::chrono::duration<double>(t2 - t1).count();
+                rep->time_update += std::chrono::duration<double>(t3 - t2).count();
+            }
+            ++numSteps;
+            conv = converged();
+        }
+        return converged();
+    }
+    bool solve_(NewtonAssembler& A, std::vector<double>& u)
+    {
+        bool conv = false;
+        try { conv = solveImpl(A, u); }
+        catch (const NumericalProblem&) { conv = false; }
+        return conv;
+    }
+};
+
+// FVAssembler + ILUBiCGSTABIstlSolver over the problem
+struct FVAssembler final : NewtonAssembler {
+    const Problem& P;
+    const Pattern& pt;
+    const double* uprev;
+    double dt;
+    std::vector<double> J, r;
+    FVAssembler(const Problem& p, const Pattern& pat, const double* up, double dt_)
+        : P(p), pt(pat), uprev(up), dt(dt_), J(pat.rowPtr[p.N] * p.b * p.b), r(p.N * p.b) {}
+    int64_t size() const override { return P.N * P.b; }
+    void assembleJacobianAndResidual(const std::vector<double>& u) override { assemble(P, pt, u.data(), uprev, dt, J.data(), r.data()); }
+    void assembleResidual(const std::vector<double>& u) override { assemble(P, pt, u.data(), uprev, dt, nullptr, r.data()); }
+    double residualNorm() const override { return std::sqrt(dot((int64_t)r.size(), r.data(), r.data())); }
+    bool solveLinear(std::vector<double>& delta, double reduction, int maxit, int* iters) override
+    {
+        auto res = bicgstab(P.N, P.b, pt.rowPtr.data(), pt.col.data(), J.data(), r.data(), delta.data(), reduction, maxit);
+        *iters = res.iterations;
+        return res.converged;
+    }
+};
+
+struct ScalarMock final : NewtonAssembler {
+    double jac = 0, res = 0;
+    int64_t size() const override { return 1; }
+    void assembleResidual(const std::vector<double>& u) override { res = u[0] * u[0] - 5.0; }
+    void assembleJacobianAndResidual(const std::vector<double>& u) override { assembleResidual(u); jac = 2.0 * u[0]; }
+    double residualNorm() const override { return std::abs(res); }
+    bool solveLinear(std::vector<double>& delta, double, int, int* iters) override { delta[0] = res / jac; *iters = 1; return true; }
+};
+
+} // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void orc_set_threads(int n) { g_threads = n; }
+int orc_get_threads(void)
+{
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int orc_num_blocks(const dxg_problem_desc* d, int64_t* nnzb)
+{
+    try {
+        Problem P(*d);
+        int64_t cnt = P.N;
+        for (int64_t I = 0; I < P.N; ++I)
+            for (int f = 0; f < 2 * P.dim; ++f) if (!P.face(I, f).boundary) ++cnt;
+        *nnzb = cnt;
+        return 0;
+    } catch (...) { return DXG_ERR_ARG; }
+}
+
+int orc_pattern(const dxg_problem_desc* d, int64_t* row_ptr, int32_t* col_idx)
+{
+    try {
+        Problem P(*d);
+        Pattern pt = buildPattern(P);
+        std::copy(pt.rowPtr.begin(), pt.rowPtr.end(), row_ptr);
+        std::copy(pt.col.begin(), pt.col.end(), col_idx);
+        return 0;
+    } catch (...) { return DXG_ERR_ARG; }
+}
+
+int orc_assemble(const dxg_problem_desc* d, const double* u, const double* u_prev, double dt, double* values, double* r)
+{
+    try {
+        Problem P(*d);
+        Pattern pt = buildPattern(P);
+        assemble(P, pt, u, u_prev, dt, values, r);
+        return 0;
+    } catch (...) { return DXG_ERR_ARG; }
+}
+
+int orc_linear_solve(int64_t n, int32_t b, const int64_t* row_ptr, const int32_t* col_idx, const double* values,
+                     const double* rhs, double* x, double reduction, int32_t max_iter, dxg_linear_result* res)
+{
+    try {
+        *res = bicgstab(n, b, row_ptr, col_idx, values, rhs, x, reduction, max_iter);
+        return res->converged ? 0 : DXG_ERR_LINEAR_NOT_CONVERGED;
+    } catch (const SolverAbort&) {
+        std::memset(res, 0, sizeof(*res));
+        return DXG_ERR_LINEAR_BREAKDOWN;
+    }
+}
+
+int orc_newton_solve(const dxg_problem_desc* d, double* u, const double* u_prev, double dt,
+                     const dxg_newton_params* p, dxg_newton_report* rep)
+{
+    try {
+        Problem P(*d);
+        Pattern pt = buildPattern(P);
+        std::memset(rep, 0, sizeof(*rep));
+        std::vector<double> x(u, u + P.N * P.b);
+        const std::vector<double> x0 = x;
+        Newton nw;
+        nw.prm = *p;
+        const int divisions = dt > 0 ? p->max_time_step_divisions : 0;
+        int wasted = 0;
+        dxg_newton_report attempt{};
+        for (int i = 0; i <= divisions; ++i) {
+            FVAssembler A(P, pt, u_prev, dt);
+            attempt = dxg_newton_report{};
+            nw.rep = &attempt;
+            const bool conv = nw.solve_(A, x);
+            attempt.iterations = nw.numSteps;
+            attempt.initial_residual = nw.initialResidual;
+            attempt.dt_used = dt;
+            attempt.converged = conv;
+            attempt.time_step_divisions = i;
+            attempt.wasted_iterations = wasted;
+            if (conv) {
+                *rep = attempt;
+                std::copy(x.begin(), x.end(), u);
+                return 0;
+            }
+            wasted += nw.numSteps;
+            // reset to the previous solution and retry with a reduced time step
+            const double* src = u_prev ? u_prev : x0.data();
+            x.assign(src, src + P.N * P.b);
+            dt *= p->retry_time_step_reduction;
+        }
+        *rep = attempt;
+        rep->converged = 0;
+        rep->wasted_iterations = wasted;
+        if (u_prev) std::copy(u_prev, u_prev + P.N * P.b, u);
+        return DXG_ERR_NEWTON_NOT_CONVERGED;
+    } catch (...) { return DXG_ERR_ARG; }
+}
+
+double orc_suggest_time_step(int32_t numSteps, double oldTimeStep, const dxg_newton_params* p)
+{
+    if (numSteps > p->target_steps) {
+        const double percent = double(numSteps - p->target_steps) / p->target_steps;
+        return oldTimeStep / (1.0 + percent);
+    }
+    const double percent = double(p->target_steps - numSteps) / p->target_steps;
+    return oldTimeStep * (1.0 + percent / 1.2);
+}
+
+int orc_brooks_corey(const double* params, int32_t what, int64_t n, const double* sw, double* out)
+{
+    BrooksCoreyDefault law(params);
+    for (int64_t i = 0; i < n; ++i) {
+        if (what == 0) out[i] = law.pc(sw[i]);
+        else if (what == 1) out[i] = law.krw(sw[i]);
+        else out[i] = law.krn(sw[i]);
+    }
+    return 0;
+}
+
+double orc_numdiff_poly(int32_t method, double eps, double x0)
+{
+    auto f = [](double x) { return 1.0 / 24.0 * x * x * x * x + 1.0 / 6.0 * x * x * x + 1.0 / 2.0 * x * x + x; };
+    const double fx0 = f(x0);
+    if (method == 5) {
+        double d = f(x0 + eps);
+        d -= f(x0 - eps);
+        d *= 8.0;
+        d += f(x0 - 2.0 * eps);
+        d -= f(x0 + 2.0 * eps);
+        d /= 12.0 * eps;
+        return d;
+    }
+    double delta = 0.0, d;
+    if (method >= 0) { delta += eps; d = f(x0 + eps); }
+    else d = fx0;
+    if (method <= 0) { delta += eps; d -= f(x0 - eps); }
+    else d -= fx0;
+    d /= delta;
+    return d;
+}
+
+int orc_newton_scalar(double x0, const dxg_newton_params* p, double* x_out, int32_t* iterations)
+{
+    ScalarMock A;
+    Newton nw;
+    nw.prm = *p;
+    std::vector<double> x{x0};
+    const bool conv = nw.solve_(A, x);
+    *x_out = x[0];
+    *iterations = nw.numSteps;
+    return conv ? 0 : DXG_ERR_NEWTON_NOT_CONVERGED;
+}
+
+} // extern "C"

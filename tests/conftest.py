@@ -1,0 +1,22 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built library")
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The product library on a GPU host; building it on first use."""
+    from dumux_gb300 import build as _build
+    _build.build()
+    import dumux_gb300
+    return dumux_gb300.lib()
