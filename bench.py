@@ -1,0 +1,313 @@
+"""Benchmark: cell*Newton-steps/s of the implicit cc-TPFA 2p hot path on one GB300.
+
+Workload (default): 2p immiscible water-DNAPL (p_w, S_n), cc-TPFA, 3D 64x64x32 cells on
+6x4x1 m, seeded ln K Gaussian field (mean ln 5e-11, sigma 1, correlation length 6 cells),
+porosity 0.4, regularised Brooks-Corey (pe=500 Pa, lambda=2, Swr=0.05, Snr=0), hydrostatic
+Dirichlet left/right, DNAPL inflow 0.04 kg/m^2/s on the top strip, implicit Euler
+dt = 250 s, Newton MaxRelativeShift 1e-8, ILU(0)-BiCGSTAB with the Newton's linear
+reduction 1e-6, plain FP64 path.  One "step" = one implicit-Euler time step (a full
+Newton solve).  Synthetic inputs: the ln K field is generated from a seed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--precision fp64|mixed] [--cells 64,64,32]
+
+N > 1 (torchrun): every rank solves its own replica of the workload (weak scaling, no
+collective on the data path); rank 0 prints the line.  --impl reference times the
+reference algorithm's CPU implementation (the oracle restatement; DuMux/DUNE cannot be
+built here) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell*Newton-steps/s (2p cc-TPFA, numeric-diff assembly + ILU0-BiCGSTAB + Newton)"
+UNIT = "cell*Newton-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cells", default="64,64,32")
+    ap.add_argument("--dt", type=float, default=250.0)
+    ap.add_argument("--cpu-sample-iters", type=int, default=2)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(cells, seed=2):
+    from dumux_gb300 import problems
+    return problems.dnapl_2p(cells=cells, seed=seed)
+
+
+def workload_name(cells, precision):
+    return (f"2p water-DNAPL cc-TPFA {'x'.join(map(str, cells))} cells, implicit Euler dt=250 s, "
+            f"Newton shift 1e-8, ILU0-BiCGSTAB reduction 1e-6, {precision.upper()} linear system")
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                           "-i", str(self.index), "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+        def reader():
+            for line in self._proc.stdout:
+                self.samples.append([v.strip() for v in line.split(",")])
+        self._t = threading.Thread(target=reader, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace('.', '', 1).isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace('.', '', 1).isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) < 9:
+                continue
+            for k, n in enumerate(names):
+                if s[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
+# of the 64x64x32 FP64 system, from the ncu capture summarised in
+# profiles/ilu_sweep_64x64x32_fp64.md (cold-cache, serialised launches).
+ILU_TRAFFIC_PER_APPLY_64x64x32 = 14546688 + 18746624
+
+
+def cpu_sample(desc, u0, dt, iters):
+    """The oracle (restated reference algorithm) on the host cores: the first `iters`
+    Newton iterations of the first time step; returns (cell*Newton-steps/s, seconds)."""
+    import oracle
+    from dumux_gb300.abi import newton_params
+    # exactly `iters` iterations: the shift criterion is satisfied once MinSteps are done
+    p = newton_params(min_steps=iters, max_steps=iters, max_relative_shift=1e300, max_time_step_divisions=0)
+    t0 = time.perf_counter()
+    st, u, rep = oracle.newton_solve(desc, u0, u0, dt, p)
+    sec = time.perf_counter() - t0
+    n = rep["iterations"] + rep["wasted_iterations"]
+    if n == 0:
+        n = iters
+    return desc.num_cells * n / sec, sec, n
+
+
+def run_reference(args, cells):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    import oracle
+    desc, u0 = workload(cells)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    for _ in range(args.warmup):
+        cpu_sample(desc, u0, args.dt, args.cpu_sample_iters)
+    t0 = time.perf_counter()
+    work = 0
+    for _ in range(args.steps):
+        _, sec, n = cpu_sample(desc, u0, args.dt, args.cpu_sample_iters)
+        work += desc.num_cells * n
+    total = time.perf_counter() - t0
+    value = work / total
+    sample = (f"first {args.cpu_sample_iters} Newton iterations of the first time step per step "
+              f"(assembly on {threads} OpenMP threads, ILU0-BiCGSTAB sequential as dune-istl SeqILU)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(cells, "fp64"), "cells": int(np.prod(cells)),
+                   "unknowns": int(np.prod(cells)) * 2, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "DuMux needs DUNE (not installed, no network): the reference arm runs the oracle's "
+                "restatement of the same algorithm on the host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    cells = tuple(int(c) for c in args.cells.split(","))
+    if args.impl == "reference":
+        return run_reference(args, cells)
+
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    import dumux_gb300
+    desc, u0 = workload(cells, seed=2 + rank)
+    ctx = dumux_gb300.Context(desc, device=local, precision=args.precision)
+    params = dumux_gb300.newton_params()
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up time steps (advance the simulation)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    for _ in range(args.warmup):
+        ctx.newton_solve(args.dt, params)
+        ctx.advance_time_step()
+    u_start = ctx.solution()
+
+    # ---- device-resident timed region
+    ctx.set_kernel_timing(True)
+    launches0 = ctx.kernel_launches()
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    work = 0
+    newton_iters = []
+    for _ in range(args.steps):
+        rep = ctx.newton_solve(args.dt, params)
+        ctx.advance_time_step()
+        newton_iters.append(rep["iterations"] + rep["wasted_iterations"])
+        work += ctx.num_cells * newton_iters[-1]
+        with torch.cuda.stream(stream):
+            flush.zero_()          # L2 flush between timed steps (256 MiB > 129 MB L2)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = ctx.kernel_launches() - launches0
+    sweep_n, sweep_ms, sweep_bytes = ctx.kernel_timing("ilu_sweep")
+    asm_n, asm_ms, asm_bytes = ctx.kernel_timing("assembly")
+    spmv_n, spmv_ms, spmv_bytes = ctx.kernel_timing("spmv")
+    ctx.set_kernel_timing(False)
+    sec = ms / 1e3
+    if world > 1:
+        t = torch.tensor([sec, float(work)], device=f"cuda:{local}", dtype=torch.float64)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        sec, work = float(mx[0]), float(t[1])
+    value = work / sec
+
+    # ---- end to end through the C ABI with host buffers (h2d + d2h inside the region)
+    ctx.set_solution(u_start)
+    ctx.set_prev_solution(u_start)
+    host_u = np.array(u_start)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_work = 0
+    for _ in range(args.steps):
+        ctx.set_solution(host_u)            # h2d: initial guess of the step
+        rep = ctx.newton_solve(args.dt, params)
+        host_u = ctx.solution()             # d2h: result of the step
+        ctx.advance_time_step()
+        e2e_work += ctx.num_cells * (rep["iterations"] + rep["wasted_iterations"])
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_sec, float(e2e_work)], device=f"cuda:{local}", dtype=torch.float64)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        e2e_sec, e2e_work = float(mx[0]), float(t[1])
+    e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(ctx.num_dofs * 8),
+           "d2h_bytes_per_step": int(ctx.num_dofs * 8)}
+
+    peak, peak_kind = measured_peaks()
+    achieved = (sweep_bytes / sweep_n) / (sweep_ms / sweep_n / 1e3) / 1e9 if sweep_n else None
+    traffic = ILU_TRAFFIC_PER_APPLY_64x64x32 if (cells == (64, 64, 32) and args.precision == "fp64") else None
+    roofline = {"kernel": "waveKernel (ILU(0) forward+backward sweep, one apply)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic, "algorithmic_bytes": sweep_bytes / sweep_n if sweep_n else None,
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "share_of_timed": (sweep_ms / ms) if ms else None,
+                "note": "latency/FP64-bound wavefront (nx+ny+nz-2 dependent levels), far below the HBM roof"}
+    kernels = {
+        "ilu_sweep": {"launches": sweep_n, "ms": sweep_ms, "gbs": achieved},
+        "assembly": {"launches": asm_n, "ms": asm_ms,
+                     "gbs": (asm_bytes / (asm_ms / 1e3) / 1e9) if asm_ms else None},
+        "spmv": {"launches": spmv_n, "ms": spmv_ms, "gbs": (spmv_bytes / (spmv_ms / 1e3) / 1e9) if spmv_ms else None},
+    }
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded ln K Gaussian field)",
+        "config": {"workload": workload_name(cells, args.precision), "cells": int(np.prod(cells)),
+                   "unknowns": ctx.num_dofs, "newton_iterations": newton_iters, "global_batch": world,
+                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)"},
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
+    }
+    if rank == 0:
+        rate, sec_cpu, n_cpu = cpu_sample(desc, u_start, args.dt, args.cpu_sample_iters)
+        import oracle
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
+                                "sample": f"first {n_cpu} Newton iterations of one time step "
+                                          f"({sec_cpu:.1f} s; threaded assembly, sequential ILU0-BiCGSTAB)"}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

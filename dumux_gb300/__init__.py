@@ -68,6 +68,12 @@ def lib():
         L.dxg_suggest_time_step.argtypes = [vp, C.c_double, C.POINTER(NewtonParamsC)]
         L.dxg_suggest_time_step.restype = C.c_double
         L.dxg_advance_time_step.argtypes = [vp]
+        L.dxg_set_ilu_kernel.argtypes = [vp, C.c_int]
+        L.dxg_stream_handle.argtypes = [vp]
+        L.dxg_stream_handle.restype = C.c_void_p
+        L.dxg_set_kernel_timing.argtypes = [vp, C.c_int]
+        L.dxg_get_kernel_timing.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]
         L.dxg_kernel_launch_count.argtypes = [vp]
         L.dxg_kernel_launch_count.restype = C.c_int64
         L.dxg_sync.argtypes = [vp]
@@ -211,6 +217,24 @@ class Context:
     def suggest_time_step(self, old_dt, params=None):
         p = params if params is not None else newton_params()
         return self._L.dxg_suggest_time_step(self._h, float(old_dt), C.byref(p))
+
+    def set_ilu_kernel(self, kind):
+        """'auto' / 'wavefront' (one cluster launch per sweep) or 'levels' (one launch per level)."""
+        self._check(self._L.dxg_set_ilu_kernel(self._h, {"auto": 0, "wavefront": 1, "levels": 2}[kind]))
+
+    def stream_handle(self):
+        """cudaStream_t of this context (as an int) for event timing by the caller."""
+        return int(self._L.dxg_stream_handle(self._h) or 0)
+
+    def set_kernel_timing(self, enable=True):
+        self._check(self._L.dxg_set_kernel_timing(self._h, int(bool(enable))))
+
+    def kernel_timing(self, kind):
+        """(launches, total device ms, algorithmic bytes) of 'ilu_sweep' / 'assembly' / 'spmv'."""
+        k = {"ilu_sweep": 0, "assembly": 1, "spmv": 2}[kind]
+        n = C.c_int64(); ms = C.c_double(); by = C.c_double()
+        self._check(self._L.dxg_get_kernel_timing(self._h, k, C.byref(n), C.byref(ms), C.byref(by)))
+        return n.value, ms.value, by.value
 
     def kernel_launches(self):
         return int(self._L.dxg_kernel_launch_count(self._h))

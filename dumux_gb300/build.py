@@ -22,6 +22,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "assemble.cu": ["--fmad=false"],
     "linalg.cu": [],
+    "wave.cu": [],
     "api.cu": [],
 }
 

@@ -158,6 +158,56 @@ void requireUploaded(const dxg_ctx* ctx)
     if (!ctx || !ctx->uploaded) throw Error(DXG_ERR_STATE, "no problem uploaded");
 }
 
+cudaEvent_t takeEvent(dxg_ctx* c)
+{
+    if (!c->eventPool.empty()) {
+        cudaEvent_t e = c->eventPool.back();
+        c->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    DXG_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void resolveTimings(dxg_ctx* c)
+{
+    for (auto& t : c->pending) {
+        DXG_CUDA(cudaEventSynchronize(t.stop));
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, t.start, t.stop));
+        c->kcLaunches[t.kclass] += 1;
+        c->kcMs[t.kclass] += ms;
+        c->kcBytes[t.kclass] += t.bytes;
+        c->eventPool.push_back(t.start);
+        c->eventPool.push_back(t.stop);
+    }
+    c->pending.clear();
+}
+
+// brackets one launch (or launch group) of a kernel class with events when timing is on
+struct TimedScope {
+    dxg_ctx* c;
+    int kclass;
+    double bytes;
+    cudaEvent_t start = nullptr;
+    TimedScope(dxg_ctx* ctx, int kc, double b) : c(ctx), kclass(kc), bytes(b)
+    {
+        if (c->timing) {
+            start = takeEvent(c);
+            DXG_CUDA(cudaEventRecord(start, c->stream));
+        }
+    }
+    ~TimedScope() noexcept(false)
+    {
+        if (!start) return;
+        cudaEvent_t stop = takeEvent(c);
+        DXG_CUDA(cudaEventRecord(stop, c->stream));
+        c->pending.push_back({start, stop, kclass, bytes});
+        if (c->pending.size() >= 2048) resolveTimings(c);
+    }
+};
+
 }  // namespace
 
 dxg::AssemblyArgs dxg_ctx::asmArgs() const
@@ -446,6 +496,20 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
         for (int f = 0; f < 2 * dim; ++f) nnzb += (nbmask[i] >> f) & 1;
     c->nnzb = nnzb;
     c->nbmaskHost = nbmask;
+    {
+        // algorithmic bytes per launch with 8-byte values: every block / entry once
+        const double bb8 = 8.0 * b * b, v8 = 8.0 * b;
+        const double offBlocks = (double)(nnzb - N);      // = lower + upper blocks
+        // forward: lower blocks + rhs + z; backward: upper blocks + Dinv + z + y
+        c->bytesSweep = (offBlocks * bb8 + N * (v8 + v8)) + (N * bb8 + N * (v8 + v8));
+        // SpMV: all blocks + neighbour mask + x + y
+        c->bytesSpmv = nnzb * bb8 + N * 1.0 + 2.0 * N * v8;
+        // assembly: u read, volume variables written and read back, coefficients,
+        // Jacobian rows and residual written
+        const int NS = 1 + (method == 0 ? 2 * b : b);
+        c->bytesAssembly = N * v8 + 3.0 * N * NS * v8 + N * b * 8.0 /*eps*/ + N * (8.0 * dim + 2.0 * 2 * b * 8.0) +
+                           N * (3 * 8.0 + 1 + b * 8.0) + (double)c->slots * N * bb8 + N * v8;
+    }
 
     cudaStream_t st = c->stream;
     c->pcDev.alloc(1);
@@ -499,7 +563,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->partials.alloc(3 * kMaxReduceBlocks);
     c->counters.alloc(8);
     c->scal.alloc(4);
-    c->singular.alloc(1);
+    c->singular.alloc(2);
+    c->wavePlan = makeWavePlan(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b, c->precision == DXG_PRECISION_FP64);
     DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
     DXG_CUDA(cudaStreamSynchronize(st));
     c->uploaded = true;
@@ -524,6 +589,7 @@ void assemble(dxg_ctx* c, bool jac)
     if (c->dt > 0.0 && !c->havePrev) throw Error(DXG_ERR_STATE, "transient assembly needs the previous solution");
     ensurePrevStorage(c);
     const AssemblyArgs a = c->asmArgs();
+    TimedScope ts(c, DXG_KC_ASSEMBLY, jac ? c->bytesAssembly : 0.0);
     launchVolvars(a, c->b, jac ? c->method : 2, c->u.get(), c->stream);
     launchRow(a, c->b, c->dim, c->method, jac, c->gravity && c->pcHost.gravAxisMask, c->dt > 0.0, c->fullUpwind,
               c->stream);
@@ -576,6 +642,43 @@ __global__ void defectKernel(SpmvArgs<double, double> a, const double* __restric
 }
 
 template <class T>
+WaveArgs<T> waveArgs(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* rhs, T* v)
+{
+    WaveArgs<T> w{};
+    w.dim = c->dim;
+    w.nx = c->pcHost.nx;
+    w.ny = c->pcHost.ny;
+    w.nz = c->pcHost.nz;
+    w.N = c->N;
+    w.ctas = c->wavePlan.ctas;
+    w.linesPerCta = c->wavePlan.linesPerCta;
+    w.haloLines = c->wavePlan.haloLines;
+    w.A = A;
+    w.L = L;
+    w.Dinv = Dinv;
+    w.rhs = rhs;
+    w.v = v;
+    w.err = c->singular.get() + 1;
+    w.singular = c->singular.get();
+    w.ks = c->ks.get();
+    return w;
+}
+
+bool useWave(const dxg_ctx* c) { return c->iluKernel != DXG_ILU_LEVELS && c->wavePlan.ok; }
+
+template <class T>
+int64_t iluApply(dxg_ctx* c, const IluArgs<T, T>& ia, const T* A, T* L, T* Dinv, const T* d, T* v)
+{
+    TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(T) / 8.0);
+    if (useWave(c)) {
+        launchWaveApply<T>(c->wavePlan, waveArgs<T>(c, A, L, Dinv, d, v), waveArgs<T>(c, A, L, Dinv, d, v), c->b,
+                           c->stream);
+        return 2;
+    }
+    return launchIluApply<T, T>(ia, c->levels, c->b, c->dim, d, v, c->stream);
+}
+
+template <class T>
 IluArgs<T, T> iluArgs(dxg_ctx* c, const T* A, T* L, T* Dinv)
 {
     IluArgs<T, T> a{};
@@ -599,8 +702,16 @@ dxg_linear_result bicgstab(dxg_ctx* c, const T* A, T* L, T* Dinv, T* x, T* r, T*
     cudaStream_t st = c->stream;
     IluArgs<T, T> ia = iluArgs<T>(c, A, L, Dinv);
     if (refactor) {
-        DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, sizeof(int), st));
-        c->launches += launchIluFactor<T>(ia, c->levels, c->b, c->dim, st);
+        DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
+        if (useWave(c)) {
+            // the factor kernel must not skip: give it no Krylov state
+            WaveArgs<T> w = waveArgs<T>(c, A, L, Dinv, nullptr, nullptr);
+            w.ks = nullptr;
+            launchWaveFactor<T>(c->wavePlan, w, c->b, st);
+            c->launches += 1;
+        } else {
+            c->launches += launchIluFactor<T>(ia, c->levels, c->b, c->dim, st);
+        }
     }
     BicgArgs<T> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch()};
     KrylovState init{};
@@ -622,13 +733,19 @@ dxg_linear_result bicgstab(dxg_ctx* c, const T* A, T* L, T* Dinv, T* x, T* r, T*
         for (int k = 0; k < chunk; ++k) {
             launchBicgRho<T>(ba, st);
             launchBicgUpdateP<T>(ba, st);
-            c->launches += 2 + launchIluApply<T, T>(ia, c->levels, c->b, c->dim, p, y, st);
+            c->launches += 2 + iluApply<T>(c, ia, A, L, Dinv, p, y);
             sv.x = y; sv.y = v; sv.w = rt;
-            launchSpmv<T, T>(sv, c->b, c->dim, 1, st);
+            {
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * sizeof(T) / 8.0);
+                launchSpmv<T, T>(sv, c->b, c->dim, 1, st);
+            }
             launchBicgAxpyNorm<T>(ba, 0, st);
-            c->launches += 2 + launchIluApply<T, T>(ia, c->levels, c->b, c->dim, r, y, st);
+            c->launches += 2 + iluApply<T>(c, ia, A, L, Dinv, r, y);
             sv.x = y; sv.y = t; sv.w = r;
-            launchSpmv<T, T>(sv, c->b, c->dim, 2, st);
+            {
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * sizeof(T) / 8.0);
+                launchSpmv<T, T>(sv, c->b, c->dim, 2, st);
+            }
             launchBicgAxpyNorm<T>(ba, 1, st);
             c->launches += 2;
         }
@@ -637,10 +754,11 @@ dxg_linear_result bicgstab(dxg_ctx* c, const T* A, T* L, T* Dinv, T* x, T* r, T*
         DXG_CUDA(cudaStreamSynchronize(st));
         if (c->ksHost->status != KS_RUNNING || done > maxit + chunk) break;
     }
-    int sing = 0;
-    if (refactor) {
-        DXG_CUDA(cudaMemcpy(&sing, c->singular.get(), sizeof(int), cudaMemcpyDeviceToHost));
-    }
+    int flags[2] = {0, 0};
+    DXG_CUDA(cudaMemcpyAsync(flags, c->singular.get(), 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    DXG_CUDA(cudaStreamSynchronize(st));
+    const int sing = flags[0];
+    if (flags[1]) throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out");
     const KrylovState& ks = *c->ksHost;
     dxg_linear_result res{};
     res.converged = ks.status == KS_CONVERGED;
@@ -891,6 +1009,11 @@ int dxg_ctx_destroy(dxg_ctx* c)
     if (!c) return DXG_ERR_ARG;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& t : c->pending) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    for (auto e : c->eventPool) cudaEventDestroy(e);
     if (c->ksHost) cudaFreeHost(c->ksHost);
     if (c->scalHost) cudaFreeHost(c->scalHost);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1165,7 +1288,48 @@ int dxg_advance_time_step(dxg_ctx* c)
     });
 }
 
+int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
+{
+    if (!c || kind < DXG_ILU_AUTO || kind > DXG_ILU_LEVELS) return DXG_ERR_ARG;
+    if (kind == DXG_ILU_WAVEFRONT && c->uploaded && !c->wavePlan.ok) {
+        c->err = "no wavefront plan fits this grid";
+        return DXG_ERR_ARG;
+    }
+    c->iluKernel = kind;
+    c->haveFactor = false;
+    return DXG_OK;
+}
+
 int64_t dxg_kernel_launch_count(const dxg_ctx* c) { return c ? c->launches : -1; }
+
+void* dxg_stream_handle(const dxg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int dxg_set_kernel_timing(dxg_ctx* c, int enable)
+{
+    if (!c) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        resolveTimings(c);
+        c->timing = enable != 0;
+        for (int k = 0; k < DXG_KC_COUNT; ++k) {
+            c->kcLaunches[k] = 0;
+            c->kcMs[k] = 0;
+            c->kcBytes[k] = 0;
+        }
+        return DXG_OK;
+    });
+}
+
+int dxg_get_kernel_timing(dxg_ctx* c, int kc, int64_t* launches, double* ms, double* bytes)
+{
+    if (!c || kc < 0 || kc >= DXG_KC_COUNT) return DXG_ERR_ARG;
+    return guarded(c, [&] {
+        resolveTimings(c);
+        if (launches) *launches = c->kcLaunches[kc];
+        if (ms) *ms = c->kcMs[kc];
+        if (bytes) *bytes = c->kcBytes[kc];
+        return DXG_OK;
+    });
+}
 
 int dxg_sync(dxg_ctx* c)
 {

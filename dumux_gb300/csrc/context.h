@@ -7,6 +7,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "linalg_kernels.cuh"
+#include "wave.cuh"
 
 struct dxg_ctx {
     int device = 0;
@@ -50,11 +51,29 @@ struct dxg_ctx {
     dxg::DevBuf<double> partials;
     dxg::DevBuf<unsigned> counters;
     dxg::DevBuf<double> scal;         // [0] shift, [1] norm
-    dxg::DevBuf<int> singular;
+    dxg::DevBuf<int> singular;        // [0] singular pivot, [1] wavefront wait timeout
     dxg::KrylovState* ksHost = nullptr;   // pinned
     double* scalHost = nullptr;           // pinned
 
     int lastNewtonSteps = 0;
+
+    // ILU(0) kernels: cluster wavefront (default) or level-scheduled launches
+    int iluKernel = DXG_ILU_AUTO;
+    dxg::WavePlan wavePlan;
+
+    // optional event timing per kernel class (pairs resolved lazily)
+    struct TimedLaunch {
+        cudaEvent_t start, stop;
+        int kclass;
+        double bytes;
+    };
+    bool timing = false;
+    std::vector<TimedLaunch> pending;
+    std::vector<cudaEvent_t> eventPool;
+    int64_t kcLaunches[DXG_KC_COUNT] = {0, 0, 0};
+    double kcMs[DXG_KC_COUNT] = {0, 0, 0};
+    double kcBytes[DXG_KC_COUNT] = {0, 0, 0};
+    double bytesSweep = 0, bytesAssembly = 0, bytesSpmv = 0;   // algorithmic bytes per launch (FP64 sizes)
 
     dxg::AssemblyArgs asmArgs() const;
     dxg::ReduceScratch scratch() const { return {partials.get(), counters.get()}; }

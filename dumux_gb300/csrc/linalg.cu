@@ -256,6 +256,17 @@ __global__ void iluFactorLevel(IluArgs<MT, MT> a, int begin, int count)
     for (int e = 0; e < BB; ++e) a.Dinv[i * BB + e] = inv[e];
 }
 
+// z -= blk * x as a chain of FMAs, the operation order of the wavefront kernels (wave.cu)
+template <int B, class MT, class VT>
+__device__ __forceinline__ void blkFmaSub(const MT* __restrict__ blk, const VT* x, VT* acc)
+{
+#pragma unroll
+    for (int r = 0; r < B; ++r)
+#pragma unroll
+        for (int c = 0; c < B; ++c) acc[r] = fma(-(VT)blk[r * B + c], x[c], acc[r]);
+}
+
+// forward sweep of one level: z_i = d_i - L_ix z_x - L_iy z_y - L_iz z_z
 template <int B, int DIM, class MT, class VT>
 __global__ void iluForwardLevel(IluArgs<MT, VT> a, const VT* __restrict__ d, VT* v, int begin, int count)
 {
@@ -268,16 +279,17 @@ __global__ void iluForwardLevel(IluArgs<MT, VT> a, const VT* __restrict__ d, VT*
     VT rhs[B];
     loadVec<B>(d, i, rhs);
 #pragma unroll
-    for (int s = 0; s < DIM; ++s) {
+    for (int s = DIM - 1; s >= 0; --s) {
         if (!slotValid(m, DIM, s)) continue;
         const int64_t j = i + a.off[s];
         VT vj[B];
         loadVec<B>(v, j, vj);
-        blkMvSub<B>(a.L + ((int64_t)s * a.N + i) * BB, vj, rhs);
+        blkFmaSub<B>(a.L + ((int64_t)s * a.N + i) * BB, vj, rhs);
     }
     storeVec<B>(v, i, rhs);
 }
 
+// backward sweep of one level: y_i = D_i^{-1} (z_i - U_ix y_x - U_iy y_y - U_iz y_z)
 template <int B, int DIM, class MT, class VT>
 __global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
 {
@@ -287,20 +299,25 @@ __global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
     constexpr int BB = B * B;
     const int64_t i = a.perm[begin + k];
     const unsigned m = a.nbmask[i];
-    VT rhs[B];
-    loadVec<B>(v, i, rhs);
+    VT acc[B];
+    loadVec<B>(v, i, acc);
 #pragma unroll
     for (int s = DIM + 1; s < 2 * DIM + 1; ++s) {
         if (!slotValid(m, DIM, s)) continue;
         const int64_t j = i + a.off[s];
         VT vj[B];
         loadVec<B>(v, j, vj);
-        blkMvSub<B>(a.A + ((int64_t)s * a.N + i) * BB, vj, rhs);
+        blkFmaSub<B>(a.A + ((int64_t)s * a.N + i) * BB, vj, acc);
     }
+    const MT* Di = a.Dinv + i * BB;
     VT out[B];
 #pragma unroll
-    for (int e = 0; e < B; ++e) out[e] = 0;
-    blkMv<B>(a.Dinv + i * BB, rhs, out);
+    for (int r = 0; r < B; ++r) {
+        VT t = (VT)Di[r * B] * acc[0];
+#pragma unroll
+        for (int c = 1; c < B; ++c) t = fma((VT)Di[r * B + c], acc[c], t);
+        out[r] = t;
+    }
     storeVec<B>(v, i, out);
 }
 

@@ -1,0 +1,36 @@
+// wave.cuh -- cluster wavefront ILU(0) kernels (see wave.cu).
+#pragma once
+
+#include "common.cuh"
+#include "linalg.cuh"
+
+namespace dxg {
+
+template <class T>
+struct WaveArgs {
+    int dim, nx, ny, nz;
+    int64_t N;
+    int ctas, linesPerCta, haloLines;
+    const T* A;               // slot matrix (lower slots for the factor, upper for the backward sweep)
+    T* L;                     // lower factor
+    T* Dinv;                  // inverted pivots
+    const T* rhs;             // forward sweep input
+    T* v;                     // forward output / backward in-out
+    int* err;                 // DXG_ERR_TIMEOUT on an expired wait
+    int* singular;            // set on a singular pivot
+    const KrylovState* ks;    // sweeps are skipped once the solve has stopped
+};
+
+struct WavePlan {
+    int ctas = 0, linesPerCta = 0, haloLines = 0, threads = 0, lpt = 0;
+    size_t smemSolve = 0, smemFactor = 0;
+    bool ok = false;
+};
+
+WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64);
+template <class T>
+void launchWaveFactor(const WavePlan& plan, const WaveArgs<T>& a, int b, cudaStream_t st);
+template <class T>
+void launchWaveApply(const WavePlan& plan, const WaveArgs<T>& fwd, const WaveArgs<T>& bwd, int b, cudaStream_t st);
+
+}  // namespace dxg

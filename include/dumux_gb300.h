@@ -211,7 +211,27 @@ double dxg_suggest_time_step(const dxg_ctx* ctx, double old_dt, const dxg_newton
  * dumux/discretization/fvgridvariables.hh:54-129). */
 int dxg_advance_time_step(dxg_ctx* ctx);
 
+/* ---- tuning --------------------------------------------------------------------------- */
+/* Kernels of the ILU(0) factorisation and sweeps (same factors, same sweeps):
+ * DXG_ILU_AUTO / DXG_ILU_WAVEFRONT: one thread-block-cluster wavefront launch per
+ * sweep; DXG_ILU_LEVELS: one launch per wavefront level.  No counterpart in the
+ * reference (dune-istl's SeqILU is sequential). */
+enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2 };
+int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
+
 /* ---- diagnostics --------------------------------------------------------------------- */
+/* The CUDA stream (cudaStream_t) all work of this context runs on, for event timing
+ * by the caller.  No counterpart in the reference. */
+void* dxg_stream_handle(const dxg_ctx* ctx);
+/* Per-kernel-class event timing on the context stream (off by default).  Classes:
+ * DXG_KC_ILU_SWEEP (ILU(0) forward+backward sweeps), DXG_KC_ASSEMBLY (volume
+ * variables + residual/Jacobian rows), DXG_KC_SPMV.  Reports launches, summed device
+ * milliseconds and the algorithmic bytes those launches move (each matrix block,
+ * vector entry and coefficient read or written once).  No counterpart in the
+ * reference. */
+enum { DXG_KC_ILU_SWEEP = 0, DXG_KC_ASSEMBLY = 1, DXG_KC_SPMV = 2, DXG_KC_COUNT = 3 };
+int dxg_set_kernel_timing(dxg_ctx* ctx, int enable);
+int dxg_get_kernel_timing(dxg_ctx* ctx, int kernel_class, int64_t* launches, double* total_ms, double* bytes);
 /* Kernel launches issued by this context since creation (all of them ours). */
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */

@@ -79,8 +79,7 @@ def test_newton_2p_matches_oracle_fp64():
         # ulp; the numeric derivative amplifies that into ~1e-8 relative Jacobian
         # differences, which move the intermediate iterates (not the converged one).
         rn_g, rn_o = np.array(rg["residual_norm"]), np.array(ro["residual_norm"])
-        noise = 1e-10 * rg["initial_residual"]
-        assert np.all(np.abs(rn_g - rn_o) <= 1e-5 * np.abs(rn_o) + noise)
+        assert np.all(np.abs(rn_g - rn_o) <= 1e-6 * rg["initial_residual"])
     scale = np.max(np.abs(u_orc.reshape(-1, 2)), axis=0)
     err = np.max(np.abs((u_gpu - u_orc).reshape(-1, 2)), axis=0) / scale
     assert np.all(err <= 1e-9), err
@@ -97,3 +96,28 @@ def test_newton_2p_mixed_precision_within_1e6():
     uo, um = u_orc.reshape(-1, 2), u_mix.reshape(-1, 2)
     assert np.max(np.abs(um[:, 0] - uo[:, 0])) / np.max(np.abs(uo[:, 0])) <= 1e-6
     assert np.max(np.abs(um[:, 1] - uo[:, 1])) / max(np.max(np.abs(uo[:, 1])), 1e-12) <= 1e-6
+
+
+@pytest.mark.parametrize("dims,precision", [((13, 11), "fp64"), ((7, 6, 9), "fp64"), ((64, 64, 32), "fp64"),
+                                            ((7, 6, 9), "mixed"), ((40, 1, 3), "fp64"), ((1, 5, 4), "fp64")])
+def test_wavefront_ilu_equals_level_scheduled(dims, precision):
+    # the cluster wavefront kernels and the per-level kernels compute the same factor and
+    # sweeps (identical operand order; they may differ only by FMA contraction)
+    d, u0 = problems.dnapl_2p(cells=dims, extent=(6.0, 4.0, 1.0)[:len(dims)], seed=6)
+    u = u0.reshape(-1, 2).copy()
+    u[:, 1] = np.random.default_rng(2).uniform(0, 0.6, len(u))
+    out = {}
+    for kind in ("levels", "wavefront"):
+        ctx = Context(d, precision=precision)
+        ctx.set_ilu_kernel(kind)
+        ctx.set_solution(u.reshape(-1))
+        ctx.set_prev_solution(u0)
+        ctx.set_time_step(250.0)
+        ctx.assemble_jacobian_and_residual()
+        res = ctx.linear_solve(1e-12 if precision == "fp64" else 1e-5, 1000)
+        out[kind] = (res, ctx.update())
+    (rl, xl), (rw, xw) = out["levels"], out["wavefront"]
+    assert rl["converged"] and rw["converged"]
+    assert abs(rl["iterations"] - rw["iterations"]) <= 2
+    tol = 1e-7 if precision == "fp64" else 1e-3
+    assert np.max(np.abs(xl - xw)) <= tol * np.max(np.abs(xl))
