@@ -123,7 +123,7 @@ def measured_peaks():
 # dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
 # of the 64x64x32 FP64 system, from the ncu capture summarised in
 # profiles/ilu_sweep_64x64x32_fp64.md (cold-cache, serialised launches).
-ILU_TRAFFIC_PER_APPLY_64x64x32 = 14546688 + 18746624
+ILU_TRAFFIC_PER_APPLY_64x64x32 = 14511616 + 18709760
 
 
 def cpu_sample(desc, u0, dt, iters):
