@@ -11,7 +11,7 @@ DXG_OK = 0
 STATUS_NAMES = {
     0: "DXG_OK", 1: "DXG_ERR_ARG", 2: "DXG_ERR_CUDA", 3: "DXG_ERR_OOM", 4: "DXG_ERR_STATE",
     5: "DXG_ERR_LINEAR_BREAKDOWN", 6: "DXG_ERR_LINEAR_NOT_CONVERGED", 7: "DXG_ERR_NAN",
-    8: "DXG_ERR_NEWTON_NOT_CONVERGED", 9: "DXG_ERR_TIMEOUT", 10: "DXG_ERR_NO_DEVICE",
+    8: "DXG_ERR_NEWTON_NOT_CONVERGED", 9: "DXG_ERR_TIMEOUT", 10: "DXG_ERR_NO_DEVICE", 11: "DXG_ERR_SIZE",
 }
 DXG_PRECISION_FP64 = 0
 DXG_PRECISION_MIXED = 1

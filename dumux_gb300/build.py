@@ -24,6 +24,7 @@ UNITS = {
     "linalg.cu": [],
     "wave.cu": [],
     "api.cu": [],
+    "noalloc.cu": [],
 }
 
 

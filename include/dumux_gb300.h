@@ -33,7 +33,8 @@ enum {
     DXG_ERR_NAN = 7,             /* non-finite residual / defect                      */
     DXG_ERR_NEWTON_NOT_CONVERGED = 8, /* Newton failed after all dt divisions         */
     DXG_ERR_TIMEOUT = 9,         /* a bounded device-side wait gave up                */
-    DXG_ERR_NO_DEVICE = 10       /* no CUDA device / extension built without GPU      */
+    DXG_ERR_NO_DEVICE = 10,      /* no CUDA device / extension built without GPU      */
+    DXG_ERR_SIZE = 11            /* input larger than a fixed capacity                */
 };
 
 /* ---- problem description (tabulated Problem + SpatialParams) ------------------
@@ -232,6 +233,21 @@ void* dxg_stream_handle(const dxg_ctx* ctx);
 enum { DXG_KC_ILU_SWEEP = 0, DXG_KC_ASSEMBLY = 1, DXG_KC_SPMV = 2, DXG_KC_COUNT = 3 };
 int dxg_set_kernel_timing(dxg_ctx* ctx, int enable);
 int dxg_get_kernel_timing(dxg_ctx* ctx, int kernel_class, int64_t* launches, double* total_ms, double* bytes);
+/* ---- allocation-free norm --------------------------------------------------------------- */
+/* ||x||_2 of n doubles at device address x, written to the device address `result`,
+ * queued on `stream` (a cudaStream_t; NULL selects the default stream).  For callers
+ * that must not allocate device memory while they run (their device memory belongs to
+ * their own allocator or budget, or a cudaMalloc would synchronise the device and stall
+ * other streams): this call allocates nothing.  Its reduction scratch is a fixed 33 KB
+ * array in the library's device memory, held by every GPU that loads the library until
+ * the process exits; vectors longer than 8,388,608 entries are refused with
+ * DXG_ERR_SIZE.  The first call on a device looks up that array's device address (once
+ * per device, with the device current); make that first call before any stream capture.
+ * All calls on a device share the array, so calls whose kernels may overlap on the GPU
+ * (unordered streams) race and must be ordered by the caller.  No counterpart in the
+ * reference (dune-istl's norms run on the host). */
+int dxg_norm2_noalloc(const double* x, int64_t n, double* result, void* stream);
+
 /* Kernel launches issued by this context since creation (all of them ours). */
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */
