@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--cells", default="64,64,32")
     ap.add_argument("--dt", type=float, default=250.0)
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
+    ap.add_argument("--workload", default="2p", choices=["2p", "1p"],
+                    help="2p: transient water-DNAPL (default); 1p: stationary Darcy, 100x100, one Newton step")
     return ap.parse_args()
 
 
@@ -53,14 +55,31 @@ def dist_info():
     return rank, world, local
 
 
+WORKLOAD = "2p"
+
+
 def workload(cells, seed=2):
     from dumux_gb300 import problems
+    if WORKLOAD == "1p":
+        return problems.darcy_1p(cells=cells[:2], seed=seed - 1)
     return problems.dnapl_2p(cells=cells, seed=seed)
 
 
 def workload_name(cells, precision):
+    if WORKLOAD == "1p":
+        return (f"1p incompressible Darcy cc-TPFA {'x'.join(map(str, cells[:2]))} cells on [0,1]^2, stationary, "
+                f"one Newton step, ILU0-BiCGSTAB reduction 1e-12, {precision.upper()} linear system")
     return (f"2p water-DNAPL cc-TPFA {'x'.join(map(str, cells))} cells, implicit Euler dt=250 s, "
             f"Newton shift 1e-8, ILU0-BiCGSTAB reduction 1e-6, {precision.upper()} linear system")
+
+
+def step_params():
+    from dumux_gb300.abi import newton_params
+    if WORKLOAD == "1p":
+        # LinearPDESolver semantics: one assembly, one solve, one update
+        return newton_params(min_steps=1, max_steps=1, max_relative_shift=1e300, linear_reduction=1e-12,
+                             max_time_step_divisions=0)
+    return newton_params()
 
 
 class ClockSampler:
@@ -132,7 +151,10 @@ def cpu_sample(desc, u0, dt, iters):
     import oracle
     from dumux_gb300.abi import newton_params
     # exactly `iters` iterations: the shift criterion is satisfied once MinSteps are done
-    p = newton_params(min_steps=iters, max_steps=iters, max_relative_shift=1e300, max_time_step_divisions=0)
+    p = newton_params(min_steps=iters, max_steps=iters, max_relative_shift=1e300, max_time_step_divisions=0,
+                      linear_reduction=1e-12 if WORKLOAD == "1p" else 1e-6)
+    if WORKLOAD == "1p":
+        dt = 0.0
     t0 = time.perf_counter()
     st, u, rep = oracle.newton_solve(desc, u0, u0, dt, p)
     sec = time.perf_counter() - t0
@@ -143,6 +165,8 @@ def cpu_sample(desc, u0, dt, iters):
 
 
 def run_reference(args, cells):
+    global WORKLOAD
+    WORKLOAD = args.workload
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
@@ -166,7 +190,7 @@ def run_reference(args, cells):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_name(cells, "fp64"), "cells": int(np.prod(cells)),
-                   "unknowns": int(np.prod(cells)) * 2, "parallelism": "host threads"},
+                   "unknowns": int(np.prod(cells)) * (1 if WORKLOAD == "1p" else 2), "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "DuMux needs DUNE (not installed, no network): the reference arm runs the oracle's "
@@ -177,8 +201,15 @@ def run_reference(args, cells):
 
 
 def main():
+    global WORKLOAD
     args = parse()
+    WORKLOAD = args.workload
+    if args.workload == "1p" and args.cells == "64,64,32":
+        args.cells = "100,100"
+        args.cpu_sample_iters = 1
     cells = tuple(int(c) for c in args.cells.split(","))
+    if args.workload == "1p":
+        args.dt = 0.0
     if args.impl == "reference":
         return run_reference(args, cells)
 
@@ -192,7 +223,8 @@ def main():
     import dumux_gb300
     desc, u0 = workload(cells, seed=2 + rank)
     ctx = dumux_gb300.Context(desc, device=local, precision=args.precision)
-    params = dumux_gb300.newton_params()
+    params = step_params()
+    stationary = args.workload == "1p"
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -204,9 +236,11 @@ def main():
     ctx.set_solution(u0)
     ctx.set_prev_solution(u0)
     for _ in range(args.warmup):
+        if stationary:
+            ctx.set_solution(u0)
         ctx.newton_solve(args.dt, params)
         ctx.advance_time_step()
-    u_start = ctx.solution()
+    u_start = u0 if stationary else ctx.solution()
 
     # ---- device-resident timed region
     launches0 = ctx.kernel_launches()
@@ -220,6 +254,8 @@ def main():
     work = 0
     newton_iters = []
     for _ in range(args.steps):
+        if stationary:
+            ctx.set_solution(u0)            # each step solves the same stationary problem
         rep = ctx.newton_solve(args.dt, params)
         ctx.advance_time_step()
         newton_iters.append(rep["iterations"] + rep["wasted_iterations"])
@@ -251,7 +287,7 @@ def main():
     t0 = time.perf_counter()
     e2e_work = 0
     for _ in range(args.steps):
-        ctx.set_solution(host_u)            # h2d: initial guess of the step
+        ctx.set_solution(u0 if stationary else host_u)   # h2d: initial guess of the step
         rep = ctx.newton_solve(args.dt, params)
         host_u = ctx.solution()             # d2h: result of the step
         ctx.advance_time_step()
@@ -269,7 +305,7 @@ def main():
 
     # ---- per-kernel event timing: one more time step from the state after the timed
     # region, outside of it (events around every launch would perturb the timed region)
-    ctx.set_solution(u_after)
+    ctx.set_solution(u0 if stationary else u_after)
     ctx.set_prev_solution(u_after)
     ctx.set_kernel_timing(True)
     ctx.newton_solve(args.dt, params)
@@ -281,7 +317,8 @@ def main():
 
     peak, peak_kind = measured_peaks()
     achieved = (sweep_bytes / sweep_n) / (sweep_ms / sweep_n / 1e3) / 1e9 if sweep_n else None
-    traffic = ILU_TRAFFIC_PER_APPLY_64x64x32 if (cells == (64, 64, 32) and args.precision == "fp64") else None
+    traffic = (ILU_TRAFFIC_PER_APPLY_64x64x32
+               if (args.workload == "2p" and cells == (64, 64, 32) and args.precision == "fp64") else None)
     roofline = {"kernel": "waveKernel (ILU(0) forward+backward sweep, one apply)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                 "traffic": traffic, "algorithmic_bytes": sweep_bytes / sweep_n if sweep_n else None,
@@ -302,7 +339,9 @@ def main():
         "data": "synthetic (seeded ln K Gaussian field)",
         "config": {"workload": workload_name(cells, args.precision), "cells": int(np.prod(cells)),
                    "unknowns": ctx.num_dofs, "newton_iterations": newton_iters, "global_batch": world,
-                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)"},
+                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)",
+                   "step": "one stationary Newton step from the same initial state (includes its 80 KB h2d reset)"
+                           if stationary else "one implicit-Euler time step"},
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
     if rank == 0:

@@ -797,14 +797,21 @@ dxg_linear_result linearSolve(dxg_ctx* c, double reduction, int maxit)
         toFloatKernel<<<reduceBlocks(nA), kReduceThreads, 0, st>>>(c->A.get(), c->Af.get(), nA);
         c->launches += 1;
     }
-    const double innerRed = std::max(reduction, 1e-5);
+    // Each FP32 pass solves J c = d to at most 1e-3 (a reduction FP32 reaches without
+    // stagnating); the FP64 defect d = r - J delta of the accumulated update decides
+    // convergence against the requested reduction.
+    const double innerRed = std::max(reduction, 1e-3);
     DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, c->M * sizeof(double), st));
     const double r0 = deviceNorm(c, c->r.get());
     dxg_linear_result total{};
     total.initial_defect = r0;
     const double* rhs = c->r.get();
     double defNorm = r0;
-    for (int pass = 0; pass < 20; ++pass) {
+    if (r0 < 1e-30) {
+        total.converged = 1;
+        return total;
+    }
+    for (int pass = 0; pass < 30; ++pass) {
         auto res = bicgstab<float>(c, c->Af.get(), c->Lf.get(), c->Dinvf.get(), c->fx.get(), c->fr.get(), c->frt.get(),
                                    c->fp.get(), c->fv.get(), c->ft.get(), c->fy.get(), rhs, innerRed, maxit,
                                    !c->haveFactor);
@@ -812,18 +819,6 @@ dxg_linear_result linearSolve(dxg_ctx* c, double reduction, int maxit)
         total.iterations += res.iterations;
         axpyDoubleKernel<<<g, kReduceThreads, 0, st>>>(c->delta.get(), c->fx.get(), c->M);
         c->launches += 1;
-        if (!res.converged) {
-            total.converged = 0;
-            total.final_defect = res.final_defect;
-            total.reduction = r0 > 0 ? res.final_defect / r0 : 0;
-            return total;
-        }
-        if (reduction >= innerRed) {
-            total.converged = 1;
-            total.final_defect = res.final_defect;
-            total.reduction = r0 > 0 ? res.final_defect / r0 : 0;
-            return total;
-        }
         SpmvArgs<double, double> sv{};
         sv.A = c->A.get();
         sv.nbmask = c->nbmask.get();
@@ -833,13 +828,15 @@ dxg_linear_result linearSolve(dxg_ctx* c, double reduction, int maxit)
         for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
         defectKernel<<<g, kReduceThreads, 0, st>>>(sv, c->r.get(), c->b, c->dim);
         c->launches += 1;
+        const double prevDef = defNorm;
         defNorm = deviceNorm(c, c->defect.get());
+        total.final_defect = defNorm;
+        total.reduction = defNorm / r0;
         if (defNorm < reduction * r0 || defNorm < 1e-30) {
             total.converged = 1;
-            total.final_defect = defNorm;
-            total.reduction = r0 > 0 ? defNorm / r0 : 0;
             return total;
         }
+        if (!(defNorm < 0.9 * prevDef)) break;   // refinement no longer makes progress
         rhs = c->defect.get();
     }
     total.converged = 0;
