@@ -30,6 +30,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell*Newton-steps/s (2p cc-TPFA, numeric-diff assembly + ILU0-BiCGSTAB + Newton)"
+METRIC_ENSEMBLE = "cell*Newton-steps/s, batched ensemble of 2p cc-TPFA problems (engine-wide)"
+METRIC_SERVE = "cell*Newton-steps/s of a served 1p/2p request stream (continuous batching)"
 UNIT = "cell*Newton-steps/s"
 
 
@@ -43,8 +45,13 @@ def parse():
     ap.add_argument("--cells", default="64,64,32")
     ap.add_argument("--dt", type=float, default=250.0)
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
-    ap.add_argument("--workload", default="2p", choices=["2p", "1p"],
-                    help="2p: transient water-DNAPL (default); 1p: stationary Darcy, 100x100, one Newton step")
+    ap.add_argument("--workload", default="2p", choices=["2p", "1p", "ensemble", "serve"],
+                    help="2p: transient water-DNAPL (default); 1p: stationary Darcy, 100x100, one Newton step; "
+                         "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching")
+    ap.add_argument("--problems", type=int, default=256, help="ensemble size")
+    ap.add_argument("--requests", type=int, default=48, help="served-stream length")
+    ap.add_argument("--plain-sample", type=int, default=8,
+                    help="problems / requests of the workload also run alone on the plain FP64 path")
     return ap.parse_args()
 
 
@@ -171,7 +178,20 @@ def run_reference(args, cells):
     if rank != 0:
         return 0
     import oracle
-    desc, u0 = workload(cells)
+    metric, name = METRIC, workload_name(cells, "fp64")
+    if WORKLOAD == "ensemble":
+        from dumux_gb300 import problems
+        desc, u0, _ = problems.ensemble_2p(count=1, seed=4)[0]
+        WORKLOAD = "2p"
+        metric, name = METRIC_ENSEMBLE, f"ensemble problem 0 ({desc.num_cells} cells) on the host"
+    elif WORKLOAD == "serve":
+        from dumux_gb300 import problems
+        req = next(r for r in problems.served_requests(args.requests, seed=5) if r["kind"] == "2p")
+        desc, u0 = problems.make_request_problem(req)
+        WORKLOAD = "2p"
+        metric, name = METRIC_SERVE, f"first 2p request ({desc.num_cells} cells) on the host"
+    else:
+        desc, u0 = workload(cells)
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
     for _ in range(args.warmup):
@@ -186,11 +206,11 @@ def run_reference(args, cells):
     sample = (f"first {args.cpu_sample_iters} Newton iterations of the first time step per step "
               f"(assembly on {threads} OpenMP threads, ILU0-BiCGSTAB sequential as dune-istl SeqILU)")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(cells, "fp64"), "cells": int(np.prod(cells)),
-                   "unknowns": int(np.prod(cells)) * (1 if WORKLOAD == "1p" else 2), "parallelism": "host threads"},
+        "config": {"workload": name, "cells": int(desc.num_cells), "unknowns": int(desc.num_dofs),
+                   "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "DuMux needs DUNE (not installed, no network): the reference arm runs the oracle's "
@@ -200,10 +220,265 @@ def run_reference(args, cells):
     return 0
 
 
+def stats_of(values):
+    return {"p50": float(np.percentile(values, 50)), "p99": float(np.percentile(values, 99)),
+            "mean": float(np.mean(values))} if values else None
+
+
+def plain_fp64_alone(items, params, device):
+    """Each (desc, u0, dt, t_end) alone through one plain FP64 context (the
+    single-problem drop-in path, host time loop): cell*Newton-steps/s over the sample
+    and per-problem service seconds."""
+    import dumux_gb300
+    work, total, service = 0, 0.0, []
+    for desc, u0, dt, t_end in items:
+        t0 = time.perf_counter()
+        ctx = dumux_gb300.Context(desc, device=device, precision="fp64")
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        t, dtc, its = 0.0, min(dt, t_end), 0
+        while True:
+            rep = ctx.newton_solve(dtc, params)
+            its += rep["iterations"] + rep["wasted_iterations"]
+            t += rep["dt_used"]
+            ctx.advance_time_step()
+            remaining = t_end - t
+            if remaining <= 1e-9 * max(1.0, t_end):
+                break
+            dtc = min(ctx.suggest_time_step(rep["dt_used"], params), dt, remaining)
+        ctx.solution()
+        sec = time.perf_counter() - t0
+        ctx.close()
+        work += desc.num_cells * its
+        total += sec
+        service.append(sec)
+    return work / total, service
+
+
+def batch_roofline(batch):
+    """Kernel-class timing of the batched launches -> kernels dict and the roofline of
+    the class with the largest device time."""
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    for kind in ("ilu_sweep", "assembly", "spmv"):
+        n, kms, by = batch.kernel_timing(kind)
+        kernels[kind] = {"launches": n, "ms": kms, "gbs": (by / (kms / 1e3) / 1e9) if kms else None,
+                         "algorithmic_bytes_per_launch": (by / n) if n else None}
+    top = max(kernels, key=lambda k: kernels[k]["ms"])
+    total = sum(v["ms"] for v in kernels.values())
+    names = {"ilu_sweep": "waveKernel (batched ILU(0) forward+backward sweeps, one cluster per problem)",
+             "assembly": "volvarsKernel + rowKernel (batched numeric-diff assembly)",
+             "spmv": "spmvKernel (batched block SpMV)"}
+    a = kernels[top]["gbs"]
+    roofline = {"kernel": names[top], "bound": "hbm", "achieved": a, "peak": peak, "unit": "GB/s",
+                "frac": (a / peak) if a else None, "traffic": None,
+                "algorithmic_bytes": kernels[top]["algorithmic_bytes_per_launch"],
+                "peak_source": f"{peak_kind} hbm_gbs", "share_of_sweep_spmv_assembly": kernels[top]["ms"] / total
+                if total else None}
+    if top == "assembly":
+        roofline["note"] = "assembly is FP64-pipe bound (numeric-diff flux evaluations), reported against HBM"
+    return kernels, roofline
+
+
+def run_ensemble(args):
+    """Batched ensemble: `--problems` independent 2p problems (uneven grids 16..64 per
+    axis, own ln K fields and inflow rates) advanced together by one dxg_batch."""
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import dumux_gb300
+    from dumux_gb300 import problems
+    from dumux_gb300.abi import newton_params
+    params = newton_params()
+    dt = args.dt
+    probs = problems.ensemble_2p(count=args.problems, seed=4 + 100003 * rank)
+    cells_total = sum(d.num_cells for d, _, _ in probs)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    batch = dumux_gb300.Batch(device=local, precision=args.precision)
+    t_end = (args.warmup + args.steps + 1) * dt
+    ids = [batch.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
+    cells_of = {pid: d.num_cells for pid, (d, _, _) in zip(ids, probs)}
+    # warm-up: every problem completes `warmup` time steps (includes the sweep autotuning)
+    while min(batch.info(i)["time_steps"] for i in ids) < args.warmup:
+        batch.iterate()
+    # kernel-class timing: one Newton iteration with events around the batched launches
+    batch.set_kernel_timing(True)
+    batch.iterate()
+    kernels, roofline = batch_roofline(batch)
+    batch.set_kernel_timing(False)
+
+    before = {i: batch.info(i) for i in ids}
+    stream = torch.cuda.ExternalStream(batch.stream_handle(), device=local)
+    launches0 = batch.kernel_launches()
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    iterations = 0
+    while batch.iterate() > 0:
+        iterations += 1
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    sec = ev0.elapsed_time(ev1) / 1e3
+    launches = batch.kernel_launches() - launches0
+    after = {i: batch.info(i) for i in ids}
+    failed = sum(1 for i in ids if after[i]["state"] != "finished")
+    work = sum(cells_of[i] * (after[i]["newton_iterations"] - before[i]["newton_iterations"]) for i in ids)
+    solves = sum(after[i]["time_steps"] - before[i]["time_steps"] for i in ids)
+    if world > 1:
+        t = torch.tensor([sec, float(work), float(solves)], device=f"cuda:{local}", dtype=torch.float64)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        sec, work, solves = float(mx[0]), float(t[1]), float(t[2])
+    batch.close()
+
+    # ---- end to end through the C ABI: admit (tabulate + h2d), solve K steps, read back
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b2 = dumux_gb300.Batch(device=local, precision=args.precision)
+    ids2 = [b2.add(d, u0, dt=dt, t_end=args.steps * dt, params=params) for d, u0, _ in probs]
+    b2.run()
+    sols = [b2.solution(i) for i in ids2]
+    e2e_sec = time.perf_counter() - t0
+    e2e_work = sum(d.num_cells * b2.info(i)["newton_iterations"] for i, (d, _, _) in zip(ids2, probs))
+    b2.close()
+    h2d = sum(d.num_dofs * 8 + d.num_cells * 16 + d.bc_type.size + d.bc_values.size * 8 for d, _, _ in probs)
+    d2h = sum(s.size * 8 for s in sols)
+    if world > 1:
+        t = torch.tensor([e2e_sec, float(e2e_work)], device=f"cuda:{local}", dtype=torch.float64)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        e2e_sec, e2e_work = float(mx[0]), float(t[1])
+    e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+           "d2h_bytes_per_step": int(d2h / args.steps),
+           "note": "fresh batch: admission (tabulation + upload) + all time steps + solution read-back"}
+
+    value = work / sec
+    line = {
+        "metric": METRIC_ENSEMBLE, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded ln K Gaussian fields)",
+        "config": {"workload": f"batched ensemble: {args.problems} independent 2p water-DNAPL problems, grids "
+                               f"16..64 cells per axis (uniform integers), sigma U[0.5,2], corr. length U[3,10] "
+                               f"cells, inflow U[0.01,0.08] kg/m^2/s, dt=250 s, {args.precision} precision",
+                   "problems": args.problems, "cells_total": int(cells_total), "global_batch": world,
+                   "engine_iterations": iterations, "failed_problems": failed,
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, one batched launch per kernel",
+                   "l2": f"inputs larger than L2 (device working set {cells_total * 0.9e-6:.0f} MB+)",
+                   "step": "each problem's next implicit-Euler time step (problems advance independently)"},
+        "ensemble_solves_per_s": solves / sec,
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
+    }
+    if rank == 0:
+        sample = probs[::max(1, len(probs) // max(1, args.plain_sample))][:args.plain_sample]
+        plain, _ = plain_fp64_alone([(d, u0, dt, dt) for d, u0, _ in sample], params, local)
+        line["plain_fp64_same_problems"] = {
+            "value": plain, "unit": UNIT, "sample": f"{len(sample)} of the problems, first time step each, "
+                                                     "alone through one FP64 context",
+            "speedup_of_batched": value / plain}
+        desc0, u00, _ = probs[0]
+        rate, sec_cpu, n_cpu = cpu_sample(desc0, u00, dt, args.cpu_sample_iters)
+        import oracle
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
+                                "sample": f"problem 0 ({desc0.num_cells} cells): first {n_cpu} Newton iterations "
+                                          f"of its first time step ({sec_cpu:.1f} s)"}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_serve(args):
+    """Served stream: Poisson arrivals (200/s) of a 30/70 1p/2p mix, cube grids log-uniform
+    in [1e3, 1e6] cells, 1..20 time steps each, admitted by device-memory budget into a
+    continuously batched engine."""
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from dumux_gb300 import problems
+    from dumux_gb300.abi import newton_params
+    from dumux_gb300.serve import Server
+    params = newton_params()
+    reqs = problems.served_requests(args.requests, rate=200.0, seed=5 + 100003 * rank)
+    built = {r["index"]: problems.make_request_problem(r) for r in reqs}
+    free, _ = torch.cuda.mem_get_info(local)
+    budget = int(0.8 * free)
+    server = Server(device=local, precision=args.precision, memory_budget=budget, params=params)
+    # warm-up: small requests of both kinds (kernel loading, sweep autotuning)
+    warm = problems.served_requests(max(3, args.warmup), rate=1e6, seed=99, n_max=2e4)
+    server.serve(warm, problems.make_request_problem)
+    launches0 = server.batch.kernel_launches()
+    sampler = ClockSampler(local)
+    torch.cuda.synchronize()
+    sampler.start()
+    records, st = server.serve(reqs, lambda r: built[r["index"]])
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = server.batch.kernel_launches() - launches0
+    h2d = sum(d.num_dofs * 8 + d.num_cells * 16 + d.bc_type.size + d.bc_values.size * 8 for d, _ in built.values())
+    d2h = 0
+    line = {
+        "metric": METRIC_SERVE, "value": st["cell_newton_steps_per_s"], "unit": UNIT, "n_gpus": world,
+        "steps": args.requests, "warmup": len(warm), "ms_per_step": st["makespan_s"] * 1e3 / max(1, len(records)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded request stream)",
+        "config": {"workload": f"served stream: {args.requests} requests, Poisson arrivals 200/s, 30/70 1p/2p, "
+                               "cube grids log-uniform 1e3..1e6 cells, 1..20 steps of 250 s, "
+                               f"{args.precision} precision, HBM admission budget {budget / 1e9:.0f} GB",
+                   "step": "one request (ms_per_step = makespan / requests)",
+                   "l2": "inputs larger than L2", "parallelism": "1 GPU, continuous batching"},
+        "serve": st, "solves_per_s": st["solves_per_s"],
+        "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
+        "e2e": {"value": st["cell_newton_steps_per_s"], "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d / max(1, len(records))), "d2h_bytes_per_step": d2h,
+                "note": "the served loop is itself end to end: arrival replay, admission (tabulation + upload), "
+                        "solve, release"},
+        "gpu_launches": int(launches), "clocks": clocks,
+    }
+    if rank == 0:
+        sample = reqs[::max(1, len(reqs) // max(1, args.plain_sample))][:args.plain_sample]
+        items = [(built[r["index"]][0], built[r["index"]][1], r["dt"], r["t_end"]) for r in sample]
+        plain, service = plain_fp64_alone(items, params, local)
+        served_lat = {r["index"]: rec["latency"] for rec in records for r in sample if rec["index"] == r["index"]}
+        line["plain_fp64_alone"] = {
+            "value": plain, "unit": UNIT, "sample": f"{len(sample)} of the requests, each alone through one FP64 "
+                                                     "context (no queueing)",
+            "service_s": stats_of(service), "solves_per_s_sequential": len(service) / sum(service),
+            "served_latency_of_same_requests_s": stats_of(list(served_lat.values())),
+            "speedup_of_served": st["cell_newton_steps_per_s"] / plain}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     global WORKLOAD
     args = parse()
     WORKLOAD = args.workload
+    if args.workload in ("ensemble", "serve") and args.impl == "gb300":
+        if args.precision == "fp64" and "--precision" not in sys.argv:
+            args.precision = "mixed"
+        return run_ensemble(args) if args.workload == "ensemble" else run_serve(args)
     if args.workload == "1p" and args.cells == "64,64,32":
         args.cells = "100,100"
         args.cpu_sample_iters = 1

@@ -16,8 +16,9 @@ import os
 
 import numpy as np
 
-from .abi import (DXG_PRECISION_FP64, DXG_PRECISION_MIXED, STATUS_NAMES, LinearResultC, NewtonParamsC,
-                  NewtonReportC, ProblemDesc, ProblemDescC, newton_params)
+from .abi import (DXG_BATCH_OPT_AUTOTUNE, DXG_BATCH_OPT_GRAPHS, DXG_ERR_BUDGET, DXG_PRECISION_FP64,
+                  DXG_PRECISION_MIXED, STATUS_NAMES, BatchProblemInfoC, LinearResultC, NewtonParamsC, NewtonReportC,
+                  ProblemDesc, ProblemDescC, newton_params)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libdumux_gb300.so")
@@ -77,6 +78,30 @@ def lib():
         L.dxg_kernel_launch_count.argtypes = [vp]
         L.dxg_kernel_launch_count.restype = C.c_int64
         L.dxg_sync.argtypes = [vp]
+        L.dxg_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int]
+        L.dxg_batch_destroy.argtypes = [vp]
+        L.dxg_batch_last_error.argtypes = [vp]
+        L.dxg_batch_last_error.restype = C.c_char_p
+        L.dxg_batch_set_option.argtypes = [vp, C.c_int, C.c_int]
+        L.dxg_problem_device_bytes.argtypes = [C.POINTER(ProblemDescC), C.c_int]
+        L.dxg_problem_device_bytes.restype = C.c_int64
+        L.dxg_batch_set_memory_budget.argtypes = [vp, C.c_int64]
+        L.dxg_batch_device_bytes.argtypes = [vp]
+        L.dxg_batch_device_bytes.restype = C.c_int64
+        L.dxg_batch_add.argtypes = [vp, C.POINTER(ProblemDescC), dp, C.c_double, C.c_double,
+                                    C.POINTER(NewtonParamsC), C.POINTER(C.c_int64)]
+        L.dxg_batch_iterate.argtypes = [vp, C.POINTER(C.c_int32)]
+        L.dxg_batch_run.argtypes = [vp]
+        L.dxg_batch_info.argtypes = [vp, C.c_int64, C.POINTER(BatchProblemInfoC)]
+        L.dxg_batch_get_solution.argtypes = [vp, C.c_int64, dp]
+        L.dxg_batch_remove.argtypes = [vp, C.c_int64]
+        L.dxg_batch_launch_count.argtypes = [vp]
+        L.dxg_batch_launch_count.restype = C.c_int64
+        L.dxg_batch_set_kernel_timing.argtypes = [vp, C.c_int]
+        L.dxg_batch_get_kernel_timing.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                                  C.POINTER(C.c_double)]
+        L.dxg_batch_stream.argtypes = [vp]
+        L.dxg_batch_stream.restype = C.c_void_p
         _lib = L
     return _lib
 
@@ -324,5 +349,110 @@ class NewtonSolver:
     suggestTimeStepSize = suggest_time_step_size
 
 
+def problem_device_bytes(desc, precision="mixed"):
+    """Device memory a problem takes once admitted (dxg_problem_device_bytes)."""
+    prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
+    return int(lib().dxg_problem_device_bytes(C.byref(desc.c), prec))
+
+
+class Batch:
+    """Many independent problems advanced together on one GPU (dxg_batch).
+
+    add() admits a problem (refused with DXG_ERR_BUDGET beyond the memory budget),
+    iterate() runs one Newton iteration of every active problem, run() iterates until
+    none is active.  Each problem follows its own time loop; its result does not
+    depend on what else is in the batch.
+    """
+
+    def __init__(self, device=0, precision="mixed", graphs=True, autotune=True, memory_budget=0):
+        L = lib()
+        h = C.c_void_p()
+        prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
+        st = L.dxg_batch_create(C.byref(h), int(device), prec)
+        if st != 0:
+            raise DxgError(st, L.dxg_batch_last_error(None).decode())
+        self._h = h
+        self._L = L
+        self.precision = precision
+        self._sizes = {}
+        self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_GRAPHS, int(bool(graphs))))
+        self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_AUTOTUNE, int(bool(autotune))))
+        self._check(L.dxg_batch_set_memory_budget(h, int(memory_budget)))
+
+    def _check(self, st):
+        if st != 0:
+            raise DxgError(st, self._L.dxg_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dxg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, desc, u0, dt=0.0, t_end=0.0, params=None):
+        """Admits a problem; returns its id, or None when the memory budget refuses it."""
+        u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
+        if u0.size != desc.num_dofs:
+            raise ValueError(f"u0 has {u0.size} entries, expected {desc.num_dofs}")
+        p = params if params is not None else newton_params()
+        pid = C.c_int64()
+        st = self._L.dxg_batch_add(self._h, C.byref(desc.c), _dp(u0), float(dt), float(t_end), C.byref(p),
+                                   C.byref(pid))
+        if st == DXG_ERR_BUDGET:
+            return None
+        self._check(st)
+        self._sizes[pid.value] = desc.num_dofs
+        return pid.value
+
+    def iterate(self):
+        n = C.c_int32()
+        self._check(self._L.dxg_batch_iterate(self._h, C.byref(n)))
+        return n.value
+
+    def run(self):
+        self._check(self._L.dxg_batch_run(self._h))
+
+    def info(self, pid):
+        i = BatchProblemInfoC()
+        self._check(self._L.dxg_batch_info(self._h, int(pid), C.byref(i)))
+        return i.as_dict()
+
+    def solution(self, pid):
+        u = np.empty(self._sizes[pid], dtype=np.float64)
+        self._check(self._L.dxg_batch_get_solution(self._h, int(pid), _dp(u)))
+        return u
+
+    def remove(self, pid):
+        self._check(self._L.dxg_batch_remove(self._h, int(pid)))
+        self._sizes.pop(pid, None)
+
+    def device_bytes(self):
+        return int(self._L.dxg_batch_device_bytes(self._h))
+
+    def set_memory_budget(self, nbytes):
+        self._check(self._L.dxg_batch_set_memory_budget(self._h, int(nbytes)))
+
+    def kernel_launches(self):
+        return int(self._L.dxg_batch_launch_count(self._h))
+
+    def stream_handle(self):
+        return self._L.dxg_batch_stream(self._h)
+
+    def set_kernel_timing(self, enable=True):
+        self._check(self._L.dxg_batch_set_kernel_timing(self._h, int(bool(enable))))
+
+    def kernel_timing(self, kind):
+        """(launches, device ms, algorithmic bytes) of 'ilu_sweep', 'assembly' or 'spmv'."""
+        kc = {"ilu_sweep": 0, "assembly": 1, "spmv": 2}[kind]
+        n = C.c_int64(); ms = C.c_double(); by = C.c_double()
+        self._check(self._L.dxg_batch_get_kernel_timing(self._h, kc, C.byref(n), C.byref(ms), C.byref(by)))
+        return n.value, ms.value, by.value
+
+
 __all__ = ["Context", "FVAssembler", "ILUBiCGSTABIstlSolver", "NewtonSolver", "ProblemDesc", "newton_params",
-           "DxgError", "NumericalProblem", "lib", "LIB_PATH"]
+           "DxgError", "NumericalProblem", "lib", "LIB_PATH", "Batch", "problem_device_bytes"]

@@ -12,7 +12,11 @@ STATUS_NAMES = {
     0: "DXG_OK", 1: "DXG_ERR_ARG", 2: "DXG_ERR_CUDA", 3: "DXG_ERR_OOM", 4: "DXG_ERR_STATE",
     5: "DXG_ERR_LINEAR_BREAKDOWN", 6: "DXG_ERR_LINEAR_NOT_CONVERGED", 7: "DXG_ERR_NAN",
     8: "DXG_ERR_NEWTON_NOT_CONVERGED", 9: "DXG_ERR_TIMEOUT", 10: "DXG_ERR_NO_DEVICE", 11: "DXG_ERR_SIZE",
+    12: "DXG_ERR_BUDGET",
 }
+DXG_ERR_BUDGET = 12
+DXG_BATCH_OPT_GRAPHS = 0
+DXG_BATCH_OPT_AUTOTUNE = 1
 DXG_PRECISION_FP64 = 0
 DXG_PRECISION_MIXED = 1
 MAX_NEWTON_RECORD = 64
@@ -107,6 +111,37 @@ class NewtonReportC(C.Structure):
             "time_assemble": float(self.time_assemble),
             "time_solve": float(self.time_solve),
             "time_update": float(self.time_update),
+        }
+
+
+class BatchProblemInfoC(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32),
+        ("status", C.c_int32),
+        ("time_steps", C.c_int32),
+        ("time_step_divisions", C.c_int32),
+        ("newton_iterations", C.c_int64),
+        ("linear_iterations", C.c_int64),
+        ("cells", C.c_int64),
+        ("time", C.c_double),
+        ("seconds_admitted", C.c_double),
+        ("seconds_finished", C.c_double),
+    ]
+
+    STATES = {0: "active", 1: "finished", 2: "failed"}
+
+    def as_dict(self):
+        return {
+            "state": self.STATES.get(self.state, self.state),
+            "status": int(self.status),
+            "time_steps": int(self.time_steps),
+            "time_step_divisions": int(self.time_step_divisions),
+            "newton_iterations": int(self.newton_iterations),
+            "linear_iterations": int(self.linear_iterations),
+            "cells": int(self.cells),
+            "time": float(self.time),
+            "seconds_admitted": float(self.seconds_admitted),
+            "seconds_finished": float(self.seconds_finished),
         }
 
 

@@ -25,6 +25,7 @@ UNITS = {
     "wave.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
+    "batch.cu": [],
 }
 
 

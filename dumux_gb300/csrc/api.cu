@@ -545,19 +545,18 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->A.alloc((size_t)c->slots * N * c->bb);
     c->r.alloc(M);
     c->delta.alloc(M);
-    c->defect.alloc(M);
     DXG_CUDA(cudaMemsetAsync(c->u.get(), 0, M * sizeof(double), st));
     DXG_CUDA(cudaMemsetAsync(c->uprev.get(), 0, M * sizeof(double), st));
     DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, M * sizeof(double), st));
+    for (auto* v : {&c->kx, &c->kr, &c->krt, &c->kp, &c->kv, &c->kt, &c->ky}) v->alloc(M);
     if (c->precision == DXG_PRECISION_FP64) {
         c->L.alloc((size_t)dim * N * c->bb);
         c->Dinv.alloc((size_t)N * c->bb);
-        for (auto* v : {&c->kx, &c->kr, &c->krt, &c->kp, &c->kv, &c->kt, &c->ky}) v->alloc(M);
     } else {
         c->Af.alloc((size_t)c->slots * N * c->bb);
         c->Lf.alloc((size_t)dim * N * c->bb);
         c->Dinvf.alloc((size_t)N * c->bb);
-        for (auto* v : {&c->fx, &c->fr, &c->frt, &c->fp, &c->fv, &c->ft, &c->fy}) v->alloc(M);
+        for (auto* v : {&c->fr, &c->fp, &c->fy}) v->alloc(M);
     }
     c->ks.alloc(1);
     c->partials.alloc(3 * kMaxReduceBlocks);
@@ -566,6 +565,9 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->singular.alloc(2);
     c->wavePlan = makeWavePlan(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b, c->precision == DXG_PRECISION_FP64);
     DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
+    DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
+    DXG_CUDA(cudaMemsetAsync(c->ks.get(), 0, sizeof(KrylovState), st));
+    DXG_CUDA(cudaMemsetAsync(c->scal.get(), 0, 4 * sizeof(double), st));
     DXG_CUDA(cudaStreamSynchronize(st));
     c->uploaded = true;
     c->havePrev = false;
@@ -611,36 +613,6 @@ double deviceNorm(dxg_ctx* c, const double* x)
 }
 
 // ---------------------------------------------------------------- linear solve
-__global__ void toFloatKernel(const double* __restrict__ x, float* __restrict__ y, int64_t n)
-{
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-        y[k] = (float)x[k];
-}
-__global__ void axpyDoubleKernel(double* __restrict__ y, const float* __restrict__ x, int64_t n)
-{
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-        y[k] += (double)x[k];
-}
-// defect = r - A*delta in FP64 (iterative refinement of the mixed-precision solve)
-__global__ void defectKernel(SpmvArgs<double, double> a, const double* __restrict__ rhs, int b, int dim)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned m = a.nbmask[i];
-        double acc[2] = {0.0, 0.0};
-        for (int s = 0; s < 2 * dim + 1; ++s) {
-            if (s != dim) {
-                const int f = s < dim ? 2 * (dim - 1 - s) : 2 * (s - dim - 1) + 1;
-                if (!((m >> f) & 1u)) continue;
-            }
-            const int64_t j = i + a.off[s];
-            const double* blk = a.A + ((int64_t)s * a.N + i) * b * b;
-            for (int rr = 0; rr < b; ++rr)
-                for (int cc = 0; cc < b; ++cc) acc[rr] += blk[rr * b + cc] * a.x[j * b + cc];
-        }
-        for (int rr = 0; rr < b; ++rr) a.y[i * b + rr] = rhs[i * b + rr] - acc[rr];
-    }
-}
-
 template <class T>
 WaveArgs<T> waveArgs(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* rhs, T* v)
 {
@@ -694,59 +666,90 @@ IluArgs<T, T> iluArgs(dxg_ctx* c, const T* A, T* L, T* Dinv)
     return a;
 }
 
-// BiCGSTAB with ILU(0) on the device from x = 0 for rhs (FP64 in device memory).
-template <class T>
-dxg_linear_result bicgstab(dxg_ctx* c, const T* A, T* L, T* Dinv, T* x, T* r, T* rt, T* p, T* v, T* t, T* y,
-                           const double* rhs, double reduction, int maxit, bool refactor)
+// BiCGSTAB with ILU(0) on the device from x = 0 for rhs (FP64 in device memory):
+// Krylov vectors and SpMV in FP64 on the FP64 Jacobian; the ILU(0) preconditioner in
+// PT -- FP64 (plain path) or FP32 (mixed precision: FP32 copy of the Jacobian, FP32
+// factors and sweeps, fed by FP32 copies of p and r and widened back to FP64).
+template <class PT>
+dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int maxit, bool refactor)
 {
+    constexpr bool mixed = sizeof(PT) == 4;
     cudaStream_t st = c->stream;
-    IluArgs<T, T> ia = iluArgs<T>(c, A, L, Dinv);
+    const double* A = c->A.get();
+    const PT* PA = mixed ? (const PT*)c->Af.get() : (const PT*)c->A.get();
+    PT* PL = mixed ? (PT*)c->Lf.get() : (PT*)c->L.get();
+    PT* PD = mixed ? (PT*)c->Dinvf.get() : (PT*)c->Dinv.get();
+    IluArgs<PT, PT> ia = iluArgs<PT>(c, PA, PL, PD);
     if (refactor) {
+        if (mixed) {
+            const int64_t nA = (int64_t)c->slots * c->N * c->bb;
+            launchToFloat(ToFloatArgs{c->A.get(), c->Af.get(), nA}, st);
+            c->launches += 1;
+        }
         DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
         if (useWave(c)) {
             // the factor kernel must not skip: give it no Krylov state
-            WaveArgs<T> w = waveArgs<T>(c, A, L, Dinv, nullptr, nullptr);
+            WaveArgs<PT> w = waveArgs<PT>(c, PA, PL, PD, nullptr, nullptr);
             w.ks = nullptr;
-            launchWaveFactor<T>(c->wavePlan, w, c->b, st);
+            launchWaveFactor<PT>(c->wavePlan, w, c->b, st);
             c->launches += 1;
         } else {
-            c->launches += launchIluFactor<T>(ia, c->levels, c->b, c->dim, st);
+            c->launches += launchIluFactor<PT>(ia, c->levels, c->b, c->dim, st);
         }
     }
-    BicgArgs<T> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch()};
+    double *x = c->kx.get(), *r = c->kr.get(), *rt = c->krt.get(), *p = c->kp.get(), *v = c->kv.get(),
+           *t = c->kt.get(), *y = c->ky.get();
+    BicgArgs<double> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr};
+    // preconditioner operands: FP32 copies of p / r and an FP32 result, or the FP64 vectors
+    const PT* pIn = mixed ? (const PT*)c->fp.get() : (const PT*)p;
+    const PT* rIn = mixed ? (const PT*)c->fr.get() : (const PT*)r;
+    PT* yOut = mixed ? (PT*)c->fy.get() : (PT*)y;
+    if (mixed) {
+        ba.pLow = c->fp.get();
+        ba.rLow = c->fr.get();
+    }
     KrylovState init{};
     init.reduction = reduction;
     init.maxHalf = 2 * maxit;
     DXG_CUDA(cudaMemcpyAsync(c->ks.get(), &init, sizeof(KrylovState), cudaMemcpyHostToDevice, st));
-    launchBicgInit<T>(ba, rhs, st);
+    launchBicgInit<double>(ba, rhs, st);
     c->launches += 1;
-    SpmvArgs<T, T> sv{};
+    SpmvArgs<double, double> sv{};
     sv.A = A;
     sv.nbmask = c->nbmask.get();
     sv.N = c->N;
     for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
     sv.ks = c->ks.get();
     sv.scratch = c->scratch();
+    auto precondition = [&](const PT* in) {
+        c->launches += iluApply<PT>(c, ia, PA, PL, PD, in, yOut);
+        if (mixed) {
+            launchToDouble(ToDoubleArgs{c->fy.get(), y, c->M}, st);
+            c->launches += 1;
+        }
+    };
     const int chunk = 4;
     int done = 0;
     while (true) {
         for (int k = 0; k < chunk; ++k) {
-            launchBicgRho<T>(ba, st);
-            launchBicgUpdateP<T>(ba, st);
-            c->launches += 2 + iluApply<T>(c, ia, A, L, Dinv, p, y);
+            launchBicgRho<double>(ba, st);
+            launchBicgUpdateP<double>(ba, st);
+            c->launches += 2;
+            precondition(pIn);
             sv.x = y; sv.y = v; sv.w = rt;
             {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * sizeof(T) / 8.0);
-                launchSpmv<T, T>(sv, c->b, c->dim, 1, st);
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv);
+                launchSpmv<double, double>(sv, c->b, c->dim, 1, st);
             }
-            launchBicgAxpyNorm<T>(ba, 0, st);
-            c->launches += 2 + iluApply<T>(c, ia, A, L, Dinv, r, y);
+            launchBicgAxpyNorm<double>(ba, 0, st);
+            c->launches += 2;
+            precondition(rIn);
             sv.x = y; sv.y = t; sv.w = r;
             {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * sizeof(T) / 8.0);
-                launchSpmv<T, T>(sv, c->b, c->dim, 2, st);
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv);
+                launchSpmv<double, double>(sv, c->b, c->dim, 2, st);
             }
-            launchBicgAxpyNorm<T>(ba, 1, st);
+            launchBicgAxpyNorm<double>(ba, 1, st);
             c->launches += 2;
         }
         done += chunk;
@@ -780,69 +783,13 @@ dxg_linear_result linearSolve(dxg_ctx* c, double reduction, int maxit)
 {
     requireUploaded(c);
     if (!c->haveJac || !c->haveRes) throw Error(DXG_ERR_STATE, "assemble before solving");
-    cudaStream_t st = c->stream;
-    const int g = reduceBlocks(c->M);
-    if (c->precision == DXG_PRECISION_FP64) {
-        auto res = bicgstab<double>(c, c->A.get(), c->L.get(), c->Dinv.get(), c->kx.get(), c->kr.get(), c->krt.get(),
-                                    c->kp.get(), c->kv.get(), c->kt.get(), c->ky.get(), c->r.get(), reduction, maxit,
-                                    !c->haveFactor);
-        c->haveFactor = true;
-        DXG_CUDA(cudaMemcpyAsync(c->delta.get(), c->kx.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        return res;
-    }
-    // mixed precision: FP32 matrix, ILU(0) and BiCGSTAB; FP64 defect and accumulation
-    // (iterative refinement when the requested reduction is below FP32 resolution)
-    if (!c->haveFactor) {
-        const int64_t nA = (int64_t)c->slots * c->N * c->bb;
-        toFloatKernel<<<reduceBlocks(nA), kReduceThreads, 0, st>>>(c->A.get(), c->Af.get(), nA);
-        c->launches += 1;
-    }
-    // Each FP32 pass solves J c = d to at most 1e-3 (a reduction FP32 reaches without
-    // stagnating); the FP64 defect d = r - J delta of the accumulated update decides
-    // convergence against the requested reduction.
-    const double innerRed = std::max(reduction, 1e-3);
-    DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, c->M * sizeof(double), st));
-    const double r0 = deviceNorm(c, c->r.get());
-    dxg_linear_result total{};
-    total.initial_defect = r0;
-    const double* rhs = c->r.get();
-    double defNorm = r0;
-    if (r0 < 1e-30) {
-        total.converged = 1;
-        return total;
-    }
-    for (int pass = 0; pass < 30; ++pass) {
-        auto res = bicgstab<float>(c, c->Af.get(), c->Lf.get(), c->Dinvf.get(), c->fx.get(), c->fr.get(), c->frt.get(),
-                                   c->fp.get(), c->fv.get(), c->ft.get(), c->fy.get(), rhs, innerRed, maxit,
-                                   !c->haveFactor);
-        c->haveFactor = true;
-        total.iterations += res.iterations;
-        axpyDoubleKernel<<<g, kReduceThreads, 0, st>>>(c->delta.get(), c->fx.get(), c->M);
-        c->launches += 1;
-        SpmvArgs<double, double> sv{};
-        sv.A = c->A.get();
-        sv.nbmask = c->nbmask.get();
-        sv.x = c->delta.get();
-        sv.y = c->defect.get();
-        sv.N = c->N;
-        for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
-        defectKernel<<<g, kReduceThreads, 0, st>>>(sv, c->r.get(), c->b, c->dim);
-        c->launches += 1;
-        const double prevDef = defNorm;
-        defNorm = deviceNorm(c, c->defect.get());
-        total.final_defect = defNorm;
-        total.reduction = defNorm / r0;
-        if (defNorm < reduction * r0 || defNorm < 1e-30) {
-            total.converged = 1;
-            return total;
-        }
-        if (!(defNorm < 0.9 * prevDef)) break;   // refinement no longer makes progress
-        rhs = c->defect.get();
-    }
-    total.converged = 0;
-    total.final_defect = defNorm;
-    total.reduction = r0 > 0 ? defNorm / r0 : 0;
-    return total;
+    dxg_linear_result res = c->precision == DXG_PRECISION_FP64
+                                ? bicgstab<double>(c, c->r.get(), reduction, maxit, !c->haveFactor)
+                                : bicgstab<float>(c, c->r.get(), reduction, maxit, !c->haveFactor);
+    c->haveFactor = true;
+    DXG_CUDA(cudaMemcpyAsync(c->delta.get(), c->kx.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice,
+                             c->stream));
+    return res;
 }
 
 // ---------------------------------------------------------------- Newton

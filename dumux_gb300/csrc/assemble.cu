@@ -20,6 +20,8 @@
 // contraction in this file) yields the reference's values for every block while each
 // volume variable is computed once per (cell, state) instead of once per element that
 // binds it, and the rows are written coalesced.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -94,57 +96,55 @@ __device__ __forceinline__ double numericEps(const ProblemConsts& pc, double x, 
 // States per cell: 0 = own solution; forward/backward: 1+pv = x[pv] +/- eps;
 // central: 1+2pv = x+eps, 2+2pv = x-eps.  METHOD 2 selects state 0 only (residual).
 template <int B, int METHOD>
-__global__ void volvarsKernel(const ProblemConsts* __restrict__ pcp, const double* __restrict__ u,
-                              const double* __restrict__ phi, const double* __restrict__ extr,
-                              const int32_t* __restrict__ mat, double* __restrict__ vvP, double* __restrict__ vvU,
-                              double* __restrict__ vvS, double* __restrict__ eps, int64_t N)
+__global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ batch)
 {
     constexpr int NS = 1 + (METHOD == 0 ? 2 * B : (METHOD == 2 ? 0 : B));
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const ProblemConsts& pc = *pcp;
-    double x[B];
+    const AssemblyArgs a = batch ? batch[blockIdx.y] : a0;
+    const ProblemConsts& pc = *a.pc;
+    const int64_t N = a.N;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[B];
 #pragma unroll
-    for (int e = 0; e < B; ++e) x[e] = u[i * B + e];
-    const double ph = phi[i], ex = extr[i];
-    const int m = (B == 2) ? mat[i] : 0;
+        for (int e = 0; e < B; ++e) x[e] = a.u[i * B + e];
+        const double ph = a.phi[i], ex = a.extr[i];
+        const int m = (B == 2) ? a.mat[i] : 0;
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        double q[B];
+        for (int s = 0; s < NS; ++s) {
+            double q[B];
 #pragma unroll
-        for (int e = 0; e < B; ++e) q[e] = x[e];
-        if (s > 0) {
-            const int pv = (METHOD == 0) ? (s - 1) / 2 : s - 1;
-            const double ep = numericEps(pc, x[pv], pv);
-            const bool minus = (METHOD == -1) || (METHOD == 0 && ((s - 1) & 1));
-            q[pv] = minus ? x[pv] - ep : x[pv] + ep;
-            if (METHOD != 0 || !((s - 1) & 1)) eps[pv * N + i] = ep;
-        }
-        double p[B], up[B], st[B];
-        volVars<B>(pc, q, ph, ex, m, p, up, st);
+            for (int e = 0; e < B; ++e) q[e] = x[e];
+            if (s > 0) {
+                const int pv = (METHOD == 0) ? (s - 1) / 2 : s - 1;
+                const double ep = numericEps(pc, x[pv], pv);
+                const bool minus = (METHOD == -1) || (METHOD == 0 && ((s - 1) & 1));
+                q[pv] = minus ? x[pv] - ep : x[pv] + ep;
+                if (METHOD != 0 || !((s - 1) & 1)) a.eps[pv * N + i] = ep;
+            }
+            double p[B], up[B], st[B];
+            volVars<B>(pc, q, ph, ex, m, p, up, st);
 #pragma unroll
-        for (int k = 0; k < B; ++k) {
-            vvP[(s * B + k) * N + i] = p[k];
-            vvU[(s * B + k) * N + i] = up[k];
-            vvS[(s * B + k) * N + i] = st[k];
+            for (int k = 0; k < B; ++k) {
+                a.vvP[(s * B + k) * N + i] = p[k];
+                a.vvU[(s * B + k) * N + i] = up[k];
+                a.vvS[(s * B + k) * N + i] = st[k];
+            }
         }
     }
 }
 
 // Storage of the previous time level, ((phi*rho*S)*extr) at u_prev.
 template <int B>
-__global__ void prevStorageKernel(const ProblemConsts* __restrict__ pcp, const double* __restrict__ uprev,
-                                  const double* __restrict__ phi, const double* __restrict__ extr,
-                                  const int32_t* __restrict__ mat, double* __restrict__ stPrev, int64_t N)
+__global__ void prevStorageKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ batch)
 {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    double x[B], p[B], up[B], st[B];
+    const AssemblyArgs a = batch ? batch[blockIdx.y] : a0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[B], p[B], up[B], st[B];
 #pragma unroll
-    for (int e = 0; e < B; ++e) x[e] = uprev[i * B + e];
-    volVars<B>(*pcp, x, phi[i], extr[i], (B == 2) ? mat[i] : 0, p, up, st);
+        for (int e = 0; e < B; ++e) x[e] = a.uprev[i * B + e];
+        volVars<B>(*a.pc, x, a.phi[i], a.extr[i], (B == 2) ? a.mat[i] : 0, p, up, st);
 #pragma unroll
-    for (int k = 0; k < B; ++k) stPrev[k * N + i] = st[k];
+        for (int k = 0; k < B; ++k) a.stPrev[k * a.N + i] = st[k];
+    }
 }
 
 // Darcy flux times upwinded rho*lambda of one phase across one face
@@ -166,15 +166,13 @@ __device__ __forceinline__ double phaseFlux(double tij, double pin, double pout,
 }
 
 template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP, bool WANT_JAC>
-__global__ void __launch_bounds__(128) rowKernel(AssemblyArgs a)
+__device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
 {
     constexpr int NS = 1 + (METHOD == 0 ? 2 * B : B);
     constexpr int BB = B * B;
     constexpr int NF = 2 * DIM;
     constexpr int VA = DIM - 1;                 // vertical axis (gravity)
-    const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t N = a.N;
-    if (I >= N) return;
     const ProblemConsts& pc = *a.pc;
     const double w = pc.upwindWeight;
 
@@ -352,86 +350,138 @@ __global__ void __launch_bounds__(128) rowKernel(AssemblyArgs a)
     }
 }
 
+template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP, bool WANT_JAC>
+__global__ void __launch_bounds__(128) rowKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ batch)
+{
+    const AssemblyArgs a = batch ? batch[blockIdx.y] : a0;
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < a.N; I += (int64_t)gridDim.x * blockDim.x)
+        rowCell<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, WANT_JAC>(a, I);
+}
+
 // ---------------------------------------------------------------- host launchers
 static int blocksFor(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
-template <int B, int METHOD>
-static void launchVolvars(const AssemblyArgs& a, const double* u, cudaStream_t st)
+// launch geometry: single problem -> one thread per cell; batch -> blockIdx.y selects
+// the problem, grid-stride loops cover problems of different sizes
+struct Geo {
+    dim3 grid;
+    const AssemblyArgs* batch;
+};
+static Geo geo(int64_t n, int count, const AssemblyArgs* batch)
 {
-    volvarsKernel<B, METHOD><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, u, a.phi, a.extr, a.mat, a.vvP, a.vvU,
-                                                                  a.vvS, a.eps, a.N);
+    if (!batch) return {dim3(blocksFor(n, 128)), nullptr};
+    const int gx = std::max(1, std::min(blocksFor(n, 128), 1184));
+    return {dim3(gx, count), batch};
 }
 
-void launchPrevStorage(const AssemblyArgs& a, int b, const double* uprev, cudaStream_t st)
+template <int B, int METHOD>
+static void volvarsT(const AssemblyArgs& a, const Geo& g, cudaStream_t st)
 {
-    if (b == 1) prevStorageKernel<1><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, uprev, a.phi, a.extr, a.mat, a.stPrev, a.N);
-    else prevStorageKernel<2><<<blocksFor(a.N, 128), 128, 0, st>>>(a.pc, uprev, a.phi, a.extr, a.mat, a.stPrev, a.N);
+    volvarsKernel<B, METHOD><<<g.grid, 128, 0, st>>>(a, g.batch);
+}
+
+static void volvarsDispatch(const AssemblyArgs& a, const Geo& g, int b, int method, cudaStream_t st)
+{
+    if (b == 1) {
+        if (method == 2) volvarsT<1, 2>(a, g, st);
+        else if (method == 1) volvarsT<1, 1>(a, g, st);
+        else if (method == -1) volvarsT<1, -1>(a, g, st);
+        else volvarsT<1, 0>(a, g, st);
+    } else {
+        if (method == 2) volvarsT<2, 2>(a, g, st);
+        else if (method == 1) volvarsT<2, 1>(a, g, st);
+        else if (method == -1) volvarsT<2, -1>(a, g, st);
+        else volvarsT<2, 0>(a, g, st);
+    }
     DXG_CUDA(cudaGetLastError());
 }
 
 void launchVolvars(const AssemblyArgs& a, int b, int method, const double* u, cudaStream_t st)
 {
-    if (b == 1) {
-        if (method == 2) launchVolvars<1, 2>(a, u, st);
-        else if (method == 1) launchVolvars<1, 1>(a, u, st);
-        else if (method == -1) launchVolvars<1, -1>(a, u, st);
-        else launchVolvars<1, 0>(a, u, st);
-    } else {
-        if (method == 2) launchVolvars<2, 2>(a, u, st);
-        else if (method == 1) launchVolvars<2, 1>(a, u, st);
-        else if (method == -1) launchVolvars<2, -1>(a, u, st);
-        else launchVolvars<2, 0>(a, u, st);
-    }
+    AssemblyArgs aa = a;
+    aa.u = u;
+    volvarsDispatch(aa, geo(a.N, 1, nullptr), b, method, st);
+}
+void launchVolvarsBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, int method, cudaStream_t st)
+{
+    volvarsDispatch(AssemblyArgs{}, geo(maxN, count, batch), b, method, st);
+}
+
+static void prevDispatch(const AssemblyArgs& a, const Geo& g, int b, cudaStream_t st)
+{
+    if (b == 1) prevStorageKernel<1><<<g.grid, 128, 0, st>>>(a, g.batch);
+    else prevStorageKernel<2><<<g.grid, 128, 0, st>>>(a, g.batch);
     DXG_CUDA(cudaGetLastError());
+}
+void launchPrevStorage(const AssemblyArgs& a, int b, const double* uprev, cudaStream_t st)
+{
+    AssemblyArgs aa = a;
+    aa.uprev = uprev;
+    prevDispatch(aa, geo(a.N, 1, nullptr), b, st);
+}
+void launchPrevStorageBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, cudaStream_t st)
+{
+    prevDispatch(AssemblyArgs{}, geo(maxN, count, batch), b, st);
 }
 
 template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP>
-static void launchRow3(const AssemblyArgs& a, bool jac, cudaStream_t st)
+static void launchRow3(const AssemblyArgs& a, const Geo& g, bool jac, cudaStream_t st)
 {
-    if (jac) rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, true><<<blocksFor(a.N, 128), 128, 0, st>>>(a);
-    else rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, false><<<blocksFor(a.N, 128), 128, 0, st>>>(a);
+    if (jac) rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, true><<<g.grid, 128, 0, st>>>(a, g.batch);
+    else rowKernel<B, DIM, METHOD, GRAV, TRANSIENT, FULLUP, false><<<g.grid, 128, 0, st>>>(a, g.batch);
 }
 template <int B, int DIM, int METHOD>
-static void launchRow2(const AssemblyArgs& a, bool jac, bool grav, bool transient, bool fullup, cudaStream_t st)
+static void launchRow2(const AssemblyArgs& a, const Geo& g, bool jac, bool grav, bool transient, bool fullup,
+                       cudaStream_t st)
 {
     if (fullup) {
         if (grav) {
-            if (transient) launchRow3<B, DIM, METHOD, true, true, true>(a, jac, st);
-            else launchRow3<B, DIM, METHOD, true, false, true>(a, jac, st);
+            if (transient) launchRow3<B, DIM, METHOD, true, true, true>(a, g, jac, st);
+            else launchRow3<B, DIM, METHOD, true, false, true>(a, g, jac, st);
         } else {
-            if (transient) launchRow3<B, DIM, METHOD, false, true, true>(a, jac, st);
-            else launchRow3<B, DIM, METHOD, false, false, true>(a, jac, st);
+            if (transient) launchRow3<B, DIM, METHOD, false, true, true>(a, g, jac, st);
+            else launchRow3<B, DIM, METHOD, false, false, true>(a, g, jac, st);
         }
     } else {
         if (grav) {
-            if (transient) launchRow3<B, DIM, METHOD, true, true, false>(a, jac, st);
-            else launchRow3<B, DIM, METHOD, true, false, false>(a, jac, st);
+            if (transient) launchRow3<B, DIM, METHOD, true, true, false>(a, g, jac, st);
+            else launchRow3<B, DIM, METHOD, true, false, false>(a, g, jac, st);
         } else {
-            if (transient) launchRow3<B, DIM, METHOD, false, true, false>(a, jac, st);
-            else launchRow3<B, DIM, METHOD, false, false, false>(a, jac, st);
+            if (transient) launchRow3<B, DIM, METHOD, false, true, false>(a, g, jac, st);
+            else launchRow3<B, DIM, METHOD, false, false, false>(a, g, jac, st);
         }
     }
 }
 template <int B, int DIM>
-static void launchRow1(const AssemblyArgs& a, int method, bool jac, bool grav, bool transient, bool fullup,
-                       cudaStream_t st)
+static void launchRow1(const AssemblyArgs& a, const Geo& g, int method, bool jac, bool grav, bool transient,
+                       bool fullup, cudaStream_t st)
 {
-    if (method == 1) launchRow2<B, DIM, 1>(a, jac, grav, transient, fullup, st);
-    else if (method == -1) launchRow2<B, DIM, -1>(a, jac, grav, transient, fullup, st);
-    else launchRow2<B, DIM, 0>(a, jac, grav, transient, fullup, st);
+    if (method == 1) launchRow2<B, DIM, 1>(a, g, jac, grav, transient, fullup, st);
+    else if (method == -1) launchRow2<B, DIM, -1>(a, g, jac, grav, transient, fullup, st);
+    else launchRow2<B, DIM, 0>(a, g, jac, grav, transient, fullup, st);
+}
+static void rowDispatch(const AssemblyArgs& a, const Geo& g, int b, int dim, int method, bool jac, bool grav,
+                        bool transient, bool fullup, cudaStream_t st)
+{
+    if (b == 1) {
+        if (dim == 2) launchRow1<1, 2>(a, g, method, jac, grav, transient, fullup, st);
+        else launchRow1<1, 3>(a, g, method, jac, grav, transient, fullup, st);
+    } else {
+        if (dim == 2) launchRow1<2, 2>(a, g, method, jac, grav, transient, fullup, st);
+        else launchRow1<2, 3>(a, g, method, jac, grav, transient, fullup, st);
+    }
+    DXG_CUDA(cudaGetLastError());
 }
 
 void launchRow(const AssemblyArgs& a, int b, int dim, int method, bool jac, bool grav, bool transient, bool fullup,
                cudaStream_t st)
 {
-    if (b == 1) {
-        if (dim == 2) launchRow1<1, 2>(a, method, jac, grav, transient, fullup, st);
-        else launchRow1<1, 3>(a, method, jac, grav, transient, fullup, st);
-    } else {
-        if (dim == 2) launchRow1<2, 2>(a, method, jac, grav, transient, fullup, st);
-        else launchRow1<2, 3>(a, method, jac, grav, transient, fullup, st);
-    }
-    DXG_CUDA(cudaGetLastError());
+    rowDispatch(a, geo(a.N, 1, nullptr), b, dim, method, jac, grav, transient, fullup, st);
+}
+void launchRowBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, int dim, int method, bool jac, bool grav,
+                    bool transient, bool fullup, cudaStream_t st)
+{
+    rowDispatch(AssemblyArgs{}, geo(maxN, count, batch), b, dim, method, jac, grav, transient, fullup, st);
 }
 
 }  // namespace dxg

@@ -1,0 +1,1183 @@
+// batch.cu -- batched and served forms: many independent problems advanced together.
+//
+// The single-problem path (api.cu) leaves most of the GPU idle on small and medium
+// grids: the ILU(0) sweeps are a wavefront whose critical path is one dependent block
+// update per level, so one problem occupies one cluster of at most 16 SMs and spends
+// its time waiting on latency.  The engine here advances all active problems by one
+// tick per call: problems that begin a Newton iteration are assembled and factorised,
+// every problem runs a chunk of BiCGSTAB iterations, and problems whose solve ended
+// take their update.  Each kernel (volume variables, Jacobian rows, FP64->FP32 copy,
+// ILU(0) factor and sweeps, SpMV, BiCGSTAB vector updates, Newton update) is launched
+// once for all problems of a kind, each problem reading its own argument block
+// (blockIdx.y, or the cluster index in the sweeps).  Every problem keeps its own
+// reduction scratch and Krylov scalars, and a problem reduces over the same block
+// count as when it runs alone, so its arithmetic -- and its result -- is the same
+// alone and in any mix.  Problems whose solve has ended skip inside the chunk, so a
+// slow problem costs the others nothing but its own sweeps.
+//
+// Control stays per problem on the host: after each chunk one gathered status record
+// per problem (Krylov status, shift, flags) is read back, and each problem follows
+// the reference's Newton / time-loop logic (NewtonSolver::solve_ and solveImpl_,
+// dumux/nonlinear/newtonsolver.hh:309-382, 917-1072; newtonProceed / newtonConverged
+// :428-446, 657-701; suggestTimeStepSize :784-798; TimeLoop::setTimeStepSize capped by
+// the maximum, common/timeloop.hh:323).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "context.h"
+
+using namespace dxg;
+
+namespace {
+
+// ---------------------------------------------------------------- small batched kernels
+struct SlotReport {
+    double def0, def, shift, norm;
+    int status, halfsteps, singular, timeout;
+};
+struct GatherArgs {
+    const KrylovState* ks;
+    const double* scal;   // [0] shift, [1] norm
+    int* flags;           // [0] singular pivot, [1] sweep wait timeout
+};
+
+__global__ void gatherKernel(const GatherArgs* __restrict__ g, SlotReport* __restrict__ out, int count)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count) return;
+    const GatherArgs a = g[p];
+    SlotReport r;
+    r.def0 = a.ks->def0;
+    r.def = a.ks->def;
+    r.status = a.ks->status;
+    r.halfsteps = a.ks->halfsteps;
+    r.shift = a.scal[0];
+    r.norm = a.scal[1];
+    r.singular = a.flags[0];
+    r.timeout = a.flags[1];
+    out[p] = r;
+}
+__global__ void clearFlagsKernel(const GatherArgs* __restrict__ g, int count)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count) return;
+    g[p].flags[0] = 0;
+    g[p].flags[1] = 0;
+}
+
+// y = x (x != nullptr) or y = 0, one problem per blockIdx.y
+struct CopyArgs {
+    double* y;
+    const double* x;
+    int64_t n;
+};
+__global__ void copyKernel(const CopyArgs* __restrict__ batch)
+{
+    const CopyArgs a = batch[blockIdx.y];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
+        a.y[k] = a.x ? a.x[k] : 0.0;
+}
+
+// ---------------------------------------------------------------- argument arena
+// Argument blocks are staged in pinned host memory and copied to device memory in
+// the stream order of the launches that read them.  Space is handed out append-only
+// during one iteration and recycled at the start of the next (after its final sync).
+struct Arena {
+    struct Block {
+        unsigned char* host = nullptr;
+        unsigned char* dev = nullptr;
+        size_t cap = 0, used = 0;
+    };
+    std::vector<Block> blocks;
+    size_t cur = 0;
+
+    void reset()
+    {
+        for (auto& b : blocks) b.used = 0;
+        cur = 0;
+    }
+    template <class T>
+    T* put(const std::vector<T>& v, cudaStream_t st)
+    {
+        const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+        const size_t need = (bytes + 255) & ~(size_t)255;
+        while (cur < blocks.size() && blocks[cur].used + need > blocks[cur].cap) ++cur;
+        if (cur == blocks.size()) {
+            Block b;
+            b.cap = std::max<size_t>(need, 4u << 20);
+            DXG_CUDA(cudaMallocHost(&b.host, b.cap));
+            if (cudaMalloc(&b.dev, b.cap) != cudaSuccess) {
+                cudaGetLastError();
+                cudaFreeHost(b.host);
+                throw Error(DXG_ERR_OOM, "argument arena allocation failed");
+            }
+            blocks.push_back(b);
+        }
+        Block& b = blocks[cur];
+        unsigned char* h = b.host + b.used;
+        unsigned char* d = b.dev + b.used;
+        if (!v.empty()) std::memcpy(h, v.data(), v.size() * sizeof(T));
+        DXG_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
+        b.used += need;
+        return reinterpret_cast<T*>(d);
+    }
+    ~Arena()
+    {
+        for (auto& b : blocks) {
+            cudaFreeHost(b.host);
+            cudaFree(b.dev);
+        }
+    }
+};
+
+enum { SLOT_ACTIVE = 0, SLOT_DONE = 1, SLOT_FAILED = 2 };
+
+// problems sharing kernels: num_eq, dim, difference method, gravity, transient, upwind
+using GroupKey = std::tuple<int, int, int, int, int, int>;
+struct GroupState;
+
+struct Slot {
+    int64_t id = 0;
+    dxg_ctx* c = nullptr;
+    dxg_newton_params p{};
+    int64_t bytes = 0;
+    // time loop
+    bool transient = false;
+    double t = 0.0, tEnd = 0.0, dtMax = 0.0, dt = 0.0;
+    int steps = 0;
+    // Newton state of the current attempt
+    int numSteps = 0, divisions = 0;
+    double shift = 0.0, lastShift = 0.0;
+    // linear solve of the current iteration
+    bool solving = false, linConv = false;
+    int chunks = 0, linIters = 0;
+    int linStatus = DXG_OK;
+    // outcome
+    int state = SLOT_ACTIVE;
+    int status = DXG_OK;
+    int totalDivisions = 0;
+    int64_t newtonIters = 0, linearIters = 0;
+    double tAdmit = 0.0, tFinish = -1.0;
+
+    ~Slot()
+    {
+        if (c) dxg_ctx_destroy(c);
+    }
+};
+
+}  // namespace
+
+struct dxg_batch {
+    int device = 0;
+    int precision = DXG_PRECISION_MIXED;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool graphs = true, autotune = true;
+    int64_t budget = 0, bytesInUse = 0;
+    int64_t nextId = 1;
+    int64_t launches = 0;
+    std::map<int64_t, std::unique_ptr<Slot>> slots;
+    Arena arena;
+    DevBuf<SlotReport> reports;
+    DevBuf<int> tuneFlags;
+    SlotReport* reportsHost = nullptr;
+    size_t reportsCap = 0;
+    std::map<std::tuple<int, int, int, int, int>, WaveBatchPlan> plans;   // autotuned sweep shapes
+    std::map<GroupKey, std::unique_ptr<GroupState>> groups;              // per kind: chunk arguments, graph
+    std::chrono::steady_clock::time_point epoch = std::chrono::steady_clock::now();
+
+    // optional event timing per kernel class (direct launches while it is on)
+    struct Timed {
+        cudaEvent_t start, stop;
+        int kclass;
+        double bytes;
+    };
+    bool timing = false;
+    std::vector<Timed> pending;
+    std::vector<cudaEvent_t> eventPool;
+    int64_t kcLaunches[DXG_KC_COUNT] = {0, 0, 0};
+    double kcMs[DXG_KC_COUNT] = {0, 0, 0};
+    double kcBytes[DXG_KC_COUNT] = {0, 0, 0};
+
+    double clock() const
+    {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - epoch).count();
+    }
+};
+
+namespace {
+
+std::string g_batchCreateError;
+
+template <class F>
+int guardedB(dxg_batch* b, F&& f)
+{
+    try {
+        return f();
+    } catch (const Error& e) {
+        b->err = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        b->err = "host allocation failed";
+        return DXG_ERR_OOM;
+    } catch (const std::exception& e) {
+        b->err = e.what();
+        return DXG_ERR_CUDA;
+    }
+}
+
+using Members = std::vector<Slot*>;
+
+cudaEvent_t takeEventB(dxg_batch* B)
+{
+    if (!B->eventPool.empty()) {
+        cudaEvent_t e = B->eventPool.back();
+        B->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    DXG_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void resolveTimingsB(dxg_batch* B)
+{
+    if (B->pending.empty()) return;
+    DXG_CUDA(cudaStreamSynchronize(B->stream));
+    for (auto& t : B->pending) {
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, t.start, t.stop));
+        B->kcLaunches[t.kclass] += 1;
+        B->kcMs[t.kclass] += ms;
+        B->kcBytes[t.kclass] += t.bytes;
+        B->eventPool.push_back(t.start);
+        B->eventPool.push_back(t.stop);
+    }
+    B->pending.clear();
+}
+
+// Brackets the launches of one kernel class with events while timing is on.
+struct TimedB {
+    dxg_batch* B;
+    cudaEvent_t e0 = nullptr;
+    int kc;
+    double bytes;
+    TimedB(dxg_batch* b, int kclass, double by) : B(b), kc(kclass), bytes(by)
+    {
+        if (!B->timing) return;
+        e0 = takeEventB(B);
+        DXG_CUDA(cudaEventRecord(e0, B->stream));
+    }
+    ~TimedB()
+    {
+        if (!e0) return;
+        cudaEvent_t e1 = takeEventB(B);
+        cudaEventRecord(e1, B->stream);
+        B->pending.push_back({e0, e1, kc, bytes});
+    }
+};
+
+// Algorithmic bytes of one launch over the members (per-problem FP64 figures, scaled
+// to the operand size of the launch).
+double bytesOf(const std::vector<Slot*>& S, double dxg_ctx::*field, double scale)
+{
+    double t = 0.0;
+    for (Slot* s : S) t += s->c->*field;
+    return t * scale;
+}
+
+void ensureReports(dxg_batch* B, size_t n)
+{
+    if (n <= B->reportsCap) return;
+    const size_t cap = std::max<size_t>(n, 2 * B->reportsCap);
+    DXG_CUDA(cudaStreamSynchronize(B->stream));
+    if (B->reportsHost) cudaFreeHost(B->reportsHost);
+    B->reportsHost = nullptr;
+    DXG_CUDA(cudaMallocHost(&B->reportsHost, cap * sizeof(SlotReport)));
+    B->reports.alloc(cap);
+    B->reportsCap = cap;
+}
+
+// Gathers one status record per member into reportsHost (synchronises the stream).
+void gather(dxg_batch* B, const Members& S)
+{
+    ensureReports(B, S.size());
+    std::vector<GatherArgs> g(S.size());
+    for (size_t k = 0; k < S.size(); ++k) g[k] = {S[k]->c->ks.get(), S[k]->c->scal.get(), S[k]->c->singular.get()};
+    GatherArgs* dg = B->arena.put(g, B->stream);
+    gatherKernel<<<(unsigned)((S.size() + 127) / 128), 128, 0, B->stream>>>(dg, B->reports.get(), (int)S.size());
+    DXG_CUDA(cudaGetLastError());
+    B->launches += 1;
+    DXG_CUDA(cudaMemcpyAsync(B->reportsHost, B->reports.get(), S.size() * sizeof(SlotReport), cudaMemcpyDeviceToHost,
+                             B->stream));
+    DXG_CUDA(cudaStreamSynchronize(B->stream));
+}
+
+void batchCopy(dxg_batch* B, const std::vector<CopyArgs>& v)
+{
+    if (v.empty()) return;
+    int64_t mx = 1;
+    for (const auto& a : v) mx = std::max(mx, a.n);
+    const unsigned gx = (unsigned)std::min<int64_t>((mx + 255) / 256, 1184);
+    copyKernel<<<dim3(gx, (unsigned)v.size()), 256, 0, B->stream>>>(B->arena.put(v, B->stream));
+    DXG_CUDA(cudaGetLastError());
+    B->launches += 1;
+}
+
+int64_t maxCells(const Members& S)
+{
+    int64_t m = 1;
+    for (Slot* s : S) m = std::max(m, s->c->N);
+    return m;
+}
+int64_t maxDofs(const Members& S)
+{
+    int64_t m = 1;
+    for (Slot* s : S) m = std::max(m, s->c->M);
+    return m;
+}
+
+// ---------------------------------------------------------------- sweep shape
+std::vector<WaveGeom> geomsFor(const Members& S, int ctas)
+{
+    std::vector<WaveGeom> g;
+    g.reserve(S.size());
+    for (Slot* s : S) g.push_back(waveGeom(s->c->dim, s->c->pcHost.nx, s->c->pcHost.ny, s->c->pcHost.nz, ctas));
+    return g;
+}
+
+// Candidate launch shapes: cluster sizes 1..16, the fewest threads that keep every
+// problem at <= 2 lines per thread (and twice that), prefetch depths 1..8.
+std::vector<WaveBatchPlan> candidates(const Members& S, int dim, int b, bool fp64)
+{
+    std::vector<WaveBatchPlan> out;
+    for (int ctas : {1, 2, 4, 8, 16}) {
+        const std::vector<WaveGeom> g = geomsFor(S, ctas);
+        int maxLines = 0;
+        for (const auto& x : g) maxLines = std::max(maxLines, x.linesPerCta);
+        const int t2 = ((maxLines + 1) / 2 + 31) / 32 * 32;
+        for (int threads : {t2, 2 * t2}) {
+            if (threads < 32 || threads > 1024) continue;
+            for (int pf : {1, 2, 4, 8}) {
+                WaveBatchPlan p;
+                p.ctas = ctas;
+                p.threads = threads;
+                p.pf = pf;
+                if (completeWaveBatchPlan(p, g, dim, b, fp64) > 0) out.push_back(p);
+            }
+        }
+    }
+    return out;
+}
+
+template <class T>
+WaveArgs<T> waveArgsOf(const dxg_ctx* c, const WaveGeom& g, const T* A, T* L, T* Dinv, const T* rhs, T* v,
+                       const KrylovState* ks)
+{
+    WaveArgs<T> w{};
+    w.dim = c->dim;
+    w.nx = c->pcHost.nx;
+    w.ny = c->pcHost.ny;
+    w.nz = c->pcHost.nz;
+    w.N = c->N;
+    w.ctas = g.ctas;
+    w.linesPerCta = g.linesPerCta;
+    w.haloLines = g.haloLines;
+    w.A = A;
+    w.L = L;
+    w.Dinv = Dinv;
+    w.rhs = rhs;
+    w.v = v;
+    w.err = c->singular.get() + 1;
+    w.singular = c->singular.get();
+    w.ks = ks;
+    return w;
+}
+
+// Per-problem operands of the ILU(0) preconditioner in precision PT: the FP64 Jacobian
+// and factors (plain path), or the FP32 Jacobian copy, factors and operand copies
+// (mixed precision).  Krylov vectors and SpMV are FP64 in both.
+template <class PT>
+struct Pre;
+template <>
+struct Pre<double> {
+    static const double* A(dxg_ctx* c) { return c->A.get(); }
+    static double* L(dxg_ctx* c) { return c->L.get(); }
+    static double* Dinv(dxg_ctx* c) { return c->Dinv.get(); }
+    static const double* pIn(dxg_ctx* c) { return c->kp.get(); }
+    static const double* rIn(dxg_ctx* c) { return c->kr.get(); }
+    static double* yOut(dxg_ctx* c) { return c->ky.get(); }
+};
+template <>
+struct Pre<float> {
+    static const float* A(dxg_ctx* c) { return c->Af.get(); }
+    static float* L(dxg_ctx* c) { return c->Lf.get(); }
+    static float* Dinv(dxg_ctx* c) { return c->Dinvf.get(); }
+    static const float* pIn(dxg_ctx* c) { return c->fp.get(); }
+    static const float* rIn(dxg_ctx* c) { return c->fr.get(); }
+    static float* yOut(dxg_ctx* c) { return c->fy.get(); }
+};
+
+BicgArgs<double> krylovArgs(dxg_ctx* c, bool mixed)
+{
+    BicgArgs<double> a{c->kx.get(), c->kr.get(), c->krt.get(), c->kp.get(), c->kv.get(), c->kt.get(), c->ky.get(),
+                       c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr};
+    if (mixed) {
+        a.pLow = c->fp.get();
+        a.rLow = c->fr.get();
+    }
+    return a;
+}
+
+// Times the forward + backward sweep pair of every candidate shape on the members'
+// own factors (Krylov state detached, so nothing is skipped) and keeps the fastest.
+// The sweeps read the members' preconditioner inputs and write only their
+// preconditioner outputs, which hold no state between BiCGSTAB half steps.
+template <class PT>
+WaveBatchPlan tunePlan(dxg_batch* B, const Members& S, int dim, int b)
+{
+    const bool fp64 = sizeof(PT) == 8;
+    std::vector<WaveBatchPlan> cand = candidates(S, dim, b, fp64);
+    if (cand.empty()) throw Error(DXG_ERR_ARG, "no batched ILU(0) sweep shape fits these grids");
+    if (!B->autotune || cand.size() == 1) {
+        // fixed rule: the largest cluster with the fewest threads and the deepest prefetch
+        WaveBatchPlan best = cand.front();
+        for (const auto& p : cand)
+            if (p.ctas > best.ctas || (p.ctas == best.ctas && p.threads < best.threads) ||
+                (p.ctas == best.ctas && p.threads == best.threads && p.pf > best.pf))
+                best = p;
+        return best;
+    }
+    cudaStream_t st = B->stream;
+    // the tuning sweeps report expired waits into the batch's own flags, not the members'
+    if (!B->tuneFlags.get()) B->tuneFlags.alloc(2);
+    DXG_CUDA(cudaMemsetAsync(B->tuneFlags.get(), 0, 2 * sizeof(int), st));
+    cudaEvent_t e0, e1;
+    DXG_CUDA(cudaEventCreate(&e0));
+    DXG_CUDA(cudaEventCreate(&e1));
+    float bestMs = 1e30f;
+    WaveBatchPlan best = cand.front();
+    for (const WaveBatchPlan& p : cand) {
+        const std::vector<WaveGeom> g = geomsFor(S, p.ctas);
+        std::vector<WaveArgs<PT>> fw(S.size()), bw(S.size());
+        for (size_t k = 0; k < S.size(); ++k) {
+            dxg_ctx* c = S[k]->c;
+            fw[k] = waveArgsOf<PT>(c, g[k], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c),
+                                   Pre<PT>::yOut(c), nullptr);
+            bw[k] = waveArgsOf<PT>(c, g[k], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr,
+                                   Pre<PT>::yOut(c), nullptr);
+            fw[k].singular = bw[k].singular = B->tuneFlags.get();
+            fw[k].err = bw[k].err = B->tuneFlags.get() + 1;
+        }
+        const WaveArgs<PT>* dfw = B->arena.put(fw, st);
+        const WaveArgs<PT>* dbw = B->arena.put(bw, st);
+        launchWaveApplyBatch<PT>(p, dfw, dbw, (int)S.size(), dim, b, st);   // warm-up
+        DXG_CUDA(cudaEventRecord(e0, st));
+        for (int rep = 0; rep < 2; ++rep) launchWaveApplyBatch<PT>(p, dfw, dbw, (int)S.size(), dim, b, st);
+        DXG_CUDA(cudaEventRecord(e1, st));
+        DXG_CUDA(cudaEventSynchronize(e1));
+        B->launches += 6;
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < bestMs) {
+            bestMs = ms;
+            best = p;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int flags[2] = {0, 0};
+    DXG_CUDA(cudaMemcpy(flags, B->tuneFlags.get(), sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[1]) throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out while tuning");
+    return best;
+}
+
+template <class PT>
+WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
+{
+    int mx[3] = {0, 0, 0};
+    for (Slot* s : S) {
+        mx[0] = std::max(mx[0], s->c->pcHost.nx);
+        mx[1] = std::max(mx[1], s->c->pcHost.ny);
+        mx[2] = std::max(mx[2], s->c->pcHost.nz);
+    }
+    int cnt = 1;
+    while (cnt < (int)S.size()) cnt *= 2;
+    // batch shape: kind, member count (next power of two), largest extents (multiples of 16)
+    const auto key = std::make_tuple(b * 100 + dim * 10 + (int)sizeof(PT), cnt, (mx[0] + 15) / 16,
+                                     (mx[1] + 15) / 16, (mx[2] + 15) / 16);
+    auto it = B->plans.find(key);
+    if (it != B->plans.end()) {
+        WaveBatchPlan p = it->second;
+        if (completeWaveBatchPlan(p, geomsFor(S, p.ctas), dim, b, sizeof(PT) == 8) > 0) return p;
+    }
+    WaveBatchPlan p = tunePlan<PT>(B, S, dim, b);
+    B->plans[key] = p;
+    return p;
+}
+
+// ---------------------------------------------------------------- group state
+// The members of one kind and the argument blocks of their BiCGSTAB chunk, kept at
+// fixed device addresses while the membership is unchanged, so that the chunk is
+// captured once as a CUDA graph and replayed every tick.  Members whose solve has
+// ended (Krylov status not running) skip inside every kernel of the chunk.
+constexpr int kChunk = 8;    // BiCGSTAB iterations per tick
+
+struct GroupState {
+    std::vector<int64_t> ids;
+    WaveBatchPlan plan;
+    std::vector<WaveGeom> geo;
+    DevBuf<unsigned char> args;
+    const BicgArgs<double>* dBicg = nullptr;
+    const SpmvArgs<double, double>* dSv1 = nullptr;
+    const SpmvArgs<double, double>* dSv2 = nullptr;
+    const void* dFwP = nullptr;
+    const void* dFwR = nullptr;
+    const void* dBw = nullptr;
+    const ToDoubleArgs* dTd = nullptr;
+    int64_t maxN = 1, maxM = 1;
+    double sweepBytes = 0, spmvBytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    bool graphTried = false;
+    ~GroupState()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+template <class T>
+size_t pack(std::vector<unsigned char>& buf, const std::vector<T>& v)
+{
+    const size_t off = (buf.size() + 255) & ~(size_t)255;
+    buf.resize(off + v.size() * sizeof(T));
+    std::memcpy(buf.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+}
+
+// (Re)builds the group's chunk arguments when its membership changed.
+template <class PT>
+GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
+{
+    auto& slot = B->groups[key];
+    std::vector<int64_t> ids;
+    for (Slot* s : S) ids.push_back(s->id);
+    if (slot && slot->ids == ids) return *slot;
+    constexpr bool mixed = sizeof(PT) == 4;
+    cudaStream_t st = B->stream;
+    DXG_CUDA(cudaStreamSynchronize(st));     // the previous arguments may still be read
+    slot.reset(new GroupState());
+    GroupState& G = *slot;
+    G.ids = ids;
+    const int n = (int)S.size();
+    const int dim = S[0]->c->dim, b = S[0]->c->b;
+    G.plan = planFor<PT>(B, S, dim, b);
+    G.geo = geomsFor(S, G.plan.ctas);
+    G.maxN = maxCells(S);
+    G.maxM = maxDofs(S);
+    G.sweepBytes = bytesOf(S, &dxg_ctx::bytesSweep, sizeof(PT) / 8.0);
+    G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, 1.0);
+    std::vector<BicgArgs<double>> ba(n);
+    std::vector<SpmvArgs<double, double>> sv1(n), sv2(n);
+    std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);
+    std::vector<ToDoubleArgs> td(n);
+    for (int k = 0; k < n; ++k) {
+        dxg_ctx* c = S[k]->c;
+        ba[k] = krylovArgs(c, mixed);
+        SpmvArgs<double, double> sv{};
+        sv.A = c->A.get();
+        sv.nbmask = c->nbmask.get();
+        sv.N = c->N;
+        for (int q = 0; q < 7; ++q) sv.off[q] = c->off[q];
+        sv.ks = c->ks.get();
+        sv.scratch = c->scratch();
+        sv.x = ba[k].y;
+        sv.y = ba[k].v;
+        sv.w = ba[k].rt;
+        sv1[k] = sv;
+        sv.y = ba[k].t;
+        sv.w = ba[k].r;
+        sv2[k] = sv;
+        const PT* PA = Pre<PT>::A(c);
+        fwP[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::pIn(c), Pre<PT>::yOut(c),
+                                c->ks.get());
+        fwR[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c), Pre<PT>::yOut(c),
+                                c->ks.get());
+        bw[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr, Pre<PT>::yOut(c),
+                               c->ks.get());
+        td[k] = {c->fy.get(), c->ky.get(), c->M};
+    }
+    std::vector<unsigned char> host;
+    const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oP = pack(host, fwP),
+                 oR = pack(host, fwR), oW = pack(host, bw), oT = pack(host, td);
+    G.args.alloc(host.size());
+    DXG_CUDA(cudaMemcpy(G.args.get(), host.data(), host.size(), cudaMemcpyHostToDevice));
+    unsigned char* d = G.args.get();
+    G.dBicg = reinterpret_cast<const BicgArgs<double>*>(d + oB);
+    G.dSv1 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o1);
+    G.dSv2 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o2);
+    G.dFwP = d + oP;
+    G.dFwR = d + oR;
+    G.dBw = d + oW;
+    G.dTd = reinterpret_cast<const ToDoubleArgs*>(d + oT);
+    return G;
+}
+
+// One chunk of BiCGSTAB iterations for every member of the group.
+template <class PT>
+void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
+{
+    constexpr bool mixed = sizeof(PT) == 4;
+    cudaStream_t st = B->stream;
+    const auto* fwP = static_cast<const WaveArgs<PT>*>(G.dFwP);
+    const auto* fwR = static_cast<const WaveArgs<PT>*>(G.dFwR);
+    const auto* bw = static_cast<const WaveArgs<PT>*>(G.dBw);
+    auto precondition = [&](const WaveArgs<PT>* fw) {
+        {
+            TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
+            launchWaveApplyBatch<PT>(G.plan, fw, bw, n, dim, b, st);
+        }
+        if (mixed) launchToDoubleBatch(G.dTd, n, G.maxM, st);
+    };
+    for (int it = 0; it < kChunk; ++it) {
+        launchBicgRhoBatch<double>(G.dBicg, n, G.maxM, st);
+        launchBicgUpdatePBatch<double>(G.dBicg, n, G.maxM, st);
+        precondition(fwP);
+        {
+            TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
+            launchSpmvBatch<double, double>(G.dSv1, n, G.maxN, b, dim, 1, st);
+        }
+        launchBicgAxpyNormBatch<double>(G.dBicg, n, G.maxM, 0, st);
+        precondition(fwR);
+        {
+            TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
+            launchSpmvBatch<double, double>(G.dSv2, n, G.maxN, b, dim, 2, st);
+        }
+        launchBicgAxpyNormBatch<double>(G.dBicg, n, G.maxM, 1, st);
+    }
+}
+
+template <class PT>
+void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
+{
+    constexpr int launchesPerIt = sizeof(PT) == 4 ? 12 : 10;
+    cudaStream_t st = B->stream;
+    if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
+        G.graphTried = true;
+        cudaGraph_t graph = nullptr;
+        bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+        if (ok) {
+            try {
+                enqueueChunk<PT>(B, G, n, dim, b);
+            } catch (const Error&) {
+                ok = false;
+            }
+            ok = (cudaStreamEndCapture(st, &graph) == cudaSuccess) && ok && graph;
+        }
+        if (ok && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) {
+            G.exec = nullptr;
+            ok = false;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (!ok) {
+            cudaGetLastError();
+            G.exec = nullptr;
+        }
+    }
+    if (G.exec && !B->timing) DXG_CUDA(cudaGraphLaunch(G.exec, st));
+    else enqueueChunk<PT>(B, G, n, dim, b);
+    B->launches += (int64_t)kChunk * launchesPerIt;
+}
+
+// Status of a member's finished BiCGSTAB run.
+int krylovFailure(const SlotReport& r)
+{
+    if (r.timeout) return DXG_ERR_TIMEOUT;
+    if (r.singular) return DXG_ERR_LINEAR_BREAKDOWN;
+    if (r.status == KS_BREAKDOWN) return DXG_ERR_LINEAR_BREAKDOWN;
+    if (r.status == KS_NAN) return DXG_ERR_NAN;
+    return DXG_OK;
+}
+
+// ---------------------------------------------------------------- Newton control
+// newtonProceed (newtonsolver.hh:428-446)
+bool proceed(const Slot& s, bool conv)
+{
+    if (s.numSteps < s.p.min_steps) return true;
+    if (conv) return false;
+    if (s.numSteps >= s.p.max_steps) return s.shift * 4.0 < s.lastShift;
+    return true;
+}
+
+// suggestTimeStepSize (newtonsolver.hh:784-798)
+double suggest(const Slot& s, double dt)
+{
+    const int target = s.p.target_steps;
+    if (s.numSteps > target) return dt / (1.0 + double(s.numSteps - target) / target);
+    return dt * (1.0 + double(target - s.numSteps) / target / 1.2);
+}
+
+void finish(dxg_batch* B, Slot* s, int state, int status)
+{
+    s->state = state;
+    s->status = status;
+    s->tFinish = B->clock();
+}
+
+// Assembly, ILU(0) factorisation and BiCGSTAB start for members that begin a Newton
+// iteration (FVAssembler::assembleJacobianAndResidual + the solver's setup).
+template <class PT>
+void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const std::vector<int>& idx)
+{
+    constexpr bool mixed = sizeof(PT) == 4;
+    cudaStream_t st = B->stream;
+    const int n = (int)idx.size();
+    dxg_ctx* c0 = S[idx[0]]->c;
+    const int b = c0->b, dim = c0->dim, method = c0->method;
+    const bool grav = c0->gravity && c0->pcHost.gravAxisMask;
+    const bool transient = S[idx[0]]->transient;
+    Members A;
+    for (int k : idx) A.push_back(S[k]);
+    const int64_t maxN = maxCells(A), maxM = maxDofs(A);
+
+    // storage of the previous time level for members that start a time step
+    std::vector<AssemblyArgs> pv;
+    for (Slot* s : A) {
+        s->c->dt = s->transient ? s->dt : 0.0;
+        if (s->transient && !s->c->stPrevValid) {
+            AssemblyArgs a = s->c->asmArgs();
+            a.uprev = s->c->uprev.get();
+            pv.push_back(a);
+            s->c->stPrevValid = true;
+        }
+    }
+    if (!pv.empty()) {
+        launchPrevStorageBatch(B->arena.put(pv, st), (int)pv.size(), maxN, b, st);
+        B->launches += 1;
+    }
+    std::vector<AssemblyArgs> aa(n);
+    std::vector<ToFloatArgs> tf(n);
+    std::vector<GatherArgs> fl(n);
+    std::vector<WaveArgs<PT>> fa(n);
+    std::vector<BicgArgs<double>> bi(n);
+    int64_t maxA = 1;
+    for (int k = 0; k < n; ++k) {
+        Slot* s = A[k];
+        dxg_ctx* c = s->c;
+        aa[k] = c->asmArgs();
+        aa[k].u = c->u.get();
+        const int64_t nA = (int64_t)c->slots * c->N * c->bb;
+        maxA = std::max(maxA, nA);
+        tf[k] = {c->A.get(), c->Af.get(), nA};
+        fl[k] = {c->ks.get(), c->scal.get(), c->singular.get()};
+        // the factor must not skip: no Krylov state
+        fa[k] = waveArgsOf<PT>(c, G.geo[idx[k]], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr, nullptr,
+                               nullptr);
+        BicgArgs<double> a = krylovArgs(c, mixed);
+        a.rhs = c->r.get();
+        a.reduction = s->p.linear_reduction;
+        a.maxHalf = 2 * s->p.linear_max_iter;
+        bi[k] = a;
+    }
+    const AssemblyArgs* daa = B->arena.put(aa, st);
+    {
+        TimedB tb(B, DXG_KC_ASSEMBLY, bytesOf(A, &dxg_ctx::bytesAssembly, 1.0));
+        launchVolvarsBatch(daa, n, maxN, b, method, st);
+        launchRowBatch(daa, n, maxN, b, dim, method, true, grav, transient, c0->fullUpwind, st);
+    }
+    if (mixed) {
+        launchToFloatBatch(B->arena.put(tf, st), n, maxA, st);
+        B->launches += 1;
+    }
+    clearFlagsKernel<<<(n + 127) / 128, 128, 0, st>>>(B->arena.put(fl, st), n);
+    DXG_CUDA(cudaGetLastError());
+    launchWaveFactorBatch<PT>(G.plan, B->arena.put(fa, st), n, dim, b, st);
+    launchBicgInitBatch<double>(B->arena.put(bi, st), n, maxM, st);
+    B->launches += 5;
+    for (Slot* s : A) {
+        s->solving = true;
+        s->chunks = 0;
+    }
+}
+
+// One tick of a group: start Newton iterations, one BiCGSTAB chunk for every member,
+// then the update and the Newton / time-loop decisions of members whose solve ended.
+template <class PT>
+void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
+{
+    cudaStream_t st = B->stream;
+    GroupState& G = groupState<PT>(B, key, S);
+    const int n = (int)S.size();
+    const int dim = S[0]->c->dim, b = S[0]->c->b;
+    std::vector<int> starting;
+    for (int k = 0; k < n; ++k)
+        if (!S[k]->solving) starting.push_back(k);
+    if (!starting.empty()) beginIterations<PT>(B, G, S, starting);
+
+    runChunk<PT>(B, G, n, dim, b);
+    gather(B, S);
+
+    Members U;
+    std::vector<int> ended;
+    for (int k = 0; k < n; ++k) {
+        Slot* s = S[k];
+        const SlotReport& r = B->reportsHost[k];
+        s->chunks += 1;
+        const bool stopped = r.status != KS_RUNNING || r.timeout || s->chunks * kChunk > s->p.linear_max_iter + kChunk;
+        if (!stopped) continue;
+        s->solving = false;
+        s->linIters = (r.halfsteps + 1) / 2;
+        s->linStatus = krylovFailure(r);
+        s->linConv = s->linStatus == DXG_OK && r.status == KS_CONVERGED;
+        ended.push_back(k);
+        if (s->linConv) U.push_back(s);
+    }
+    if (ended.empty()) return;
+    // u -= delta and the relative shift for members whose solve converged
+    if (!U.empty()) {
+        std::vector<NewtonUpdArgs> ua;
+        for (Slot* s : U)
+            ua.push_back({s->c->u.get(), s->c->kx.get(), s->c->u.get(), 1.0, s->c->M, s->c->scratch(),
+                          s->c->scal.get()});
+        launchNewtonUpdateBatch(B->arena.put(ua, st), (int)U.size(), maxDofs(U), st);
+        B->launches += 1;
+        gather(B, U);
+    }
+    std::map<Slot*, double> shifts;
+    for (size_t k = 0; k < U.size(); ++k) shifts[U[k]] = B->reportsHost[k].shift;
+
+    std::vector<CopyArgs> restore, advance;
+    for (int k : ended) {
+        Slot* s = S[k];
+        // iterations are counted as the reference reports them: those that reached the
+        // update (an iteration whose linear solve failed ends the attempt uncounted)
+        if (s->linConv) s->newtonIters += 1;
+        s->linearIters += s->linIters;
+        if (s->linStatus == DXG_ERR_TIMEOUT) {
+            finish(B, s, SLOT_FAILED, DXG_ERR_TIMEOUT);
+            continue;
+        }
+        bool failed = false;
+        if (!s->linConv) failed = true;   // NumericalProblem: the linear solver did not converge
+        else {
+            s->lastShift = s->shift;
+            s->shift = shifts[s];
+            s->numSteps += 1;
+            const bool conv = s->shift <= s->p.max_relative_shift;
+            if (!std::isfinite(s->shift)) failed = true;
+            else if (!proceed(*s, conv)) {
+                if (!conv) failed = true;
+                else {
+                    // converged time step (or the stationary solve)
+                    s->steps += 1;
+                    if (!s->transient) {
+                        finish(B, s, SLOT_DONE, DXG_OK);
+                        continue;
+                    }
+                    s->t += s->dt;
+                    advance.push_back({s->c->uprev.get(), s->c->u.get(), s->c->M});
+                    s->c->stPrevValid = false;
+                    const double remaining = s->tEnd - s->t;
+                    if (remaining <= 1e-9 * std::max(1.0, s->tEnd)) {
+                        finish(B, s, SLOT_DONE, DXG_OK);
+                        continue;
+                    }
+                    s->dt = std::min(std::min(suggest(*s, s->dt), s->dtMax), remaining);
+                    s->numSteps = 0;
+                    s->shift = s->lastShift = 0.0;
+                    s->divisions = 0;
+                }
+            }
+        }
+        if (failed) {
+            // NewtonSolver::solve: back to the previous time level, reduced dt, retry
+            if (!s->transient || s->divisions >= s->p.max_time_step_divisions) {
+                finish(B, s, SLOT_FAILED, s->linStatus != DXG_OK ? s->linStatus : DXG_ERR_NEWTON_NOT_CONVERGED);
+                continue;
+            }
+            s->divisions += 1;
+            s->totalDivisions += 1;
+            s->dt *= s->p.retry_time_step_reduction;
+            s->numSteps = 0;
+            s->shift = s->lastShift = 0.0;
+            restore.push_back({s->c->u.get(), s->c->uprev.get(), s->c->M});
+        }
+    }
+    batchCopy(B, restore);
+    batchCopy(B, advance);
+}
+
+GroupKey keyOf(const Slot* s)
+{
+    const dxg_ctx* c = s->c;
+    return GroupKey{c->b, c->dim, c->method, (c->gravity && c->pcHost.gravAxisMask) ? 1 : 0, s->transient ? 1 : 0,
+                    c->fullUpwind ? 1 : 0};
+}
+
+int64_t problemBytes(int64_t N, int64_t nb, int b, int dim, int method, int precision)
+{
+    const int64_t bb = (int64_t)b * b, slots = 2 * dim + 1, M = N * b;
+    const int NS = 1 + (method == 0 ? 2 * b : b);
+    int64_t by = 0;
+    by += (3 + dim) * N * 8 + b * N * 8 + 2 * (2 * b * N * 8) + N * 4 * 2 + N;   // cell tables, mask, level order
+    by += nb * (1 + 8 + 4 * 8 * b);                                             // boundary tables
+    by += 5 * M * 8 + b * N * 8 + 3 * (int64_t)NS * b * N * 8 + b * N * 8;       // state, volume variables, eps
+    by += slots * N * bb * 8;                                                    // Jacobian
+    by += 7 * M * 8;                                                             // Krylov vectors
+    if (precision == DXG_PRECISION_FP64) by += (dim + 1) * N * bb * 8;           // L, D^-1
+    else by += (slots + dim + 1) * N * bb * 4 + 3 * M * 4;                       // FP32 copy, L, D^-1, operands
+    by += 3 * kMaxReduceBlocks * 8 + 4096;                                       // scratch and scalars
+    return by + 64 * 1024;                                                       // allocation granularity
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+int dxg_batch_create(dxg_batch** out, int device, int precision)
+{
+    if (!out || (precision != DXG_PRECISION_FP64 && precision != DXG_PRECISION_MIXED)) return DXG_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        g_batchCreateError = "no CUDA device";
+        return DXG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return DXG_ERR_ARG;
+    auto* b = new dxg_batch();
+    b->device = device;
+    b->precision = precision;
+    const int st = guardedB(b, [&] {
+        DXG_CUDA(cudaSetDevice(device));
+        DXG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        return DXG_OK;
+    });
+    if (st != DXG_OK) {
+        g_batchCreateError = b->err;
+        delete b;
+        return st;
+    }
+    *out = b;
+    return DXG_OK;
+}
+
+int dxg_batch_destroy(dxg_batch* b)
+{
+    if (!b) return DXG_ERR_ARG;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (auto& t : b->pending) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    for (auto e : b->eventPool) cudaEventDestroy(e);
+    b->groups.clear();
+    b->slots.clear();
+    if (b->reportsHost) cudaFreeHost(b->reportsHost);
+    b->reports.release();
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return DXG_OK;
+}
+
+const char* dxg_batch_last_error(const dxg_batch* b) { return b ? b->err.c_str() : g_batchCreateError.c_str(); }
+
+int dxg_batch_set_option(dxg_batch* b, int option, int value)
+{
+    if (!b) return DXG_ERR_ARG;
+    if (option == DXG_BATCH_OPT_GRAPHS) b->graphs = value != 0;
+    else if (option == DXG_BATCH_OPT_AUTOTUNE) {
+        b->autotune = value != 0;
+        b->plans.clear();
+    } else return DXG_ERR_ARG;
+    return DXG_OK;
+}
+
+int64_t dxg_problem_device_bytes(const dxg_problem_desc* d, int precision)
+{
+    if (!d || (d->dim != 2 && d->dim != 3) || (d->num_eq != 1 && d->num_eq != 2)) return -1;
+    int64_t N = 1;
+    for (int a = 0; a < d->dim; ++a) {
+        if (d->cells[a] <= 0) return -1;
+        N *= d->cells[a];
+    }
+    const int64_t nb = dxg_num_boundary_faces(d);
+    return problemBytes(N, nb, d->num_eq, d->dim, d->numeric_difference_method, precision);
+}
+
+int dxg_batch_set_memory_budget(dxg_batch* b, int64_t bytes)
+{
+    if (!b || bytes < 0) return DXG_ERR_ARG;
+    b->budget = bytes;
+    return DXG_OK;
+}
+
+int64_t dxg_batch_device_bytes(const dxg_batch* b) { return b ? b->bytesInUse : -1; }
+
+int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, double dt, double t_end,
+                  const dxg_newton_params* params, int64_t* id)
+{
+    if (!b || !d || !u0 || !id) return DXG_ERR_ARG;
+    const int64_t need = dxg_problem_device_bytes(d, b->precision);
+    if (need < 0) {
+        b->err = "invalid problem description";
+        return DXG_ERR_ARG;
+    }
+    if (b->budget > 0 && b->bytesInUse + need > b->budget) {
+        b->err = "admission would exceed the device-memory budget";
+        return DXG_ERR_BUDGET;
+    }
+    auto s = std::make_unique<Slot>();
+    int st = dxg_ctx_create(&s->c, b->device);
+    if (st != DXG_OK) {
+        b->err = dxg_last_error(nullptr);
+        return st;
+    }
+    auto step = [&](int status) {
+        if (status != DXG_OK && b->err.empty()) b->err = dxg_last_error(s->c);
+        return status;
+    };
+    b->err.clear();
+    if ((st = step(dxg_set_precision(s->c, b->precision))) != DXG_OK) return st;
+    if ((st = step(dxg_problem_upload(s->c, d))) != DXG_OK) return st;
+    if ((st = step(dxg_set_solution(s->c, u0))) != DXG_OK) return st;
+    if ((st = step(dxg_set_prev_solution(s->c, u0))) != DXG_OK) return st;
+    if (params) s->p = *params;
+    else dxg_newton_default_params(&s->p);
+    if (s->p.use_line_search || s->p.enable_residual_criterion) {
+        b->err = "batched problems use the shift criterion without line search";
+        return DXG_ERR_ARG;
+    }
+    s->transient = t_end > 0.0 && dt > 0.0;
+    s->tEnd = s->transient ? t_end : 0.0;
+    s->dtMax = s->dt = s->transient ? std::min(dt, t_end) : 0.0;
+    s->bytes = need;
+    s->tAdmit = b->clock();
+    s->id = b->nextId++;
+    *id = s->id;
+    b->bytesInUse += need;
+    b->slots[s->id] = std::move(s);
+    return DXG_OK;
+}
+
+int dxg_batch_iterate(dxg_batch* b, int32_t* active)
+{
+    if (!b) return DXG_ERR_ARG;
+    return guardedB(b, [&] {
+        DXG_CUDA(cudaSetDevice(b->device));
+        std::map<GroupKey, Members> groups;
+        for (auto& kv : b->slots)
+            if (kv.second->state == SLOT_ACTIVE) groups[keyOf(kv.second.get())].push_back(kv.second.get());
+        b->arena.reset();
+        // release the chunk arguments and graphs of kinds without active members
+        for (auto it = b->groups.begin(); it != b->groups.end();) {
+            if (groups.count(it->first)) ++it;
+            else {
+                DXG_CUDA(cudaStreamSynchronize(b->stream));
+                it = b->groups.erase(it);
+            }
+        }
+        for (auto& g : groups) {
+            if (b->precision == DXG_PRECISION_FP64) tickGroup<double>(b, g.first, g.second);
+            else tickGroup<float>(b, g.first, g.second);
+        }
+        DXG_CUDA(cudaStreamSynchronize(b->stream));
+        int n = 0;
+        for (auto& kv : b->slots) n += kv.second->state == SLOT_ACTIVE;
+        if (active) *active = n;
+        return DXG_OK;
+    });
+}
+
+int dxg_batch_run(dxg_batch* b)
+{
+    if (!b) return DXG_ERR_ARG;
+    while (true) {
+        int32_t n = 0;
+        const int st = dxg_batch_iterate(b, &n);
+        if (st != DXG_OK) return st;
+        if (n == 0) return DXG_OK;
+    }
+}
+
+int dxg_batch_info(const dxg_batch* b, int64_t id, dxg_batch_problem_info* info)
+{
+    if (!b || !info) return DXG_ERR_ARG;
+    auto it = b->slots.find(id);
+    if (it == b->slots.end()) return DXG_ERR_ARG;
+    const Slot& s = *it->second;
+    info->state = s.state;
+    info->status = s.status;
+    info->time_steps = s.steps;
+    info->time_step_divisions = s.totalDivisions;
+    info->newton_iterations = s.newtonIters;
+    info->linear_iterations = s.linearIters;
+    info->cells = s.c->N;
+    info->time = s.t;
+    info->seconds_admitted = s.tAdmit;
+    info->seconds_finished = s.tFinish;
+    return DXG_OK;
+}
+
+int dxg_batch_get_solution(dxg_batch* b, int64_t id, double* u)
+{
+    if (!b || !u) return DXG_ERR_ARG;
+    auto it = b->slots.find(id);
+    if (it == b->slots.end()) return DXG_ERR_ARG;
+    const int st = dxg_get_solution(it->second->c, u);
+    if (st != DXG_OK) b->err = dxg_last_error(it->second->c);
+    return st;
+}
+
+int dxg_batch_remove(dxg_batch* b, int64_t id)
+{
+    if (!b) return DXG_ERR_ARG;
+    auto it = b->slots.find(id);
+    if (it == b->slots.end()) return DXG_ERR_ARG;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    b->bytesInUse -= it->second->bytes;
+    b->slots.erase(it);
+    return DXG_OK;
+}
+
+int64_t dxg_batch_launch_count(const dxg_batch* b) { return b ? b->launches : -1; }
+
+int dxg_batch_set_kernel_timing(dxg_batch* b, int enable)
+{
+    if (!b) return DXG_ERR_ARG;
+    return guardedB(b, [&] {
+        resolveTimingsB(b);
+        b->timing = enable != 0;
+        for (int k = 0; k < DXG_KC_COUNT; ++k) {
+            b->kcLaunches[k] = 0;
+            b->kcMs[k] = 0;
+            b->kcBytes[k] = 0;
+        }
+        return DXG_OK;
+    });
+}
+
+int dxg_batch_get_kernel_timing(dxg_batch* b, int kc, int64_t* launches, double* ms, double* bytes)
+{
+    if (!b || kc < 0 || kc >= DXG_KC_COUNT) return DXG_ERR_ARG;
+    return guardedB(b, [&] {
+        resolveTimingsB(b);
+        if (launches) *launches = b->kcLaunches[kc];
+        if (ms) *ms = b->kcMs[kc];
+        if (bytes) *bytes = b->kcBytes[kc];
+        return DXG_OK;
+    });
+}
+
+void* dxg_batch_stream(const dxg_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+}  // extern "C"

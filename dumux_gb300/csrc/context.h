@@ -43,9 +43,9 @@ struct dxg_ctx {
     // linear solver (FP64)
     dxg::DevBuf<double> L, Dinv;
     dxg::DevBuf<double> kx, kr, krt, kp, kv, kt, ky;
-    // mixed precision copies
-    dxg::DevBuf<float> Af, Lf, Dinvf, fx, fr, frt, fp, fv, ft, fy;
-    dxg::DevBuf<double> delta, defect;
+    // mixed precision: FP32 Jacobian copy, ILU(0) factors and preconditioner operands
+    dxg::DevBuf<float> Af, Lf, Dinvf, fr, fp, fy;
+    dxg::DevBuf<double> delta;
 
     dxg::DevBuf<dxg::KrylovState> ks;
     dxg::DevBuf<double> partials;

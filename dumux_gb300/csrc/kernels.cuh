@@ -35,11 +35,21 @@ struct AssemblyArgs {
     double* A;                  // [slots][N][b*b]
     double* r;                  // [N][b]
     double dt;
+    // state read by the volume-variable kernels
+    const double* u;            // current solution [N][b]
+    const double* uprev;        // previous time level [N][b]
 };
 
 void launchVolvars(const AssemblyArgs& a, int b, int method, const double* u, cudaStream_t st);
 void launchPrevStorage(const AssemblyArgs& a, int b, const double* uprev, cudaStream_t st);
 void launchRow(const AssemblyArgs& a, int b, int dim, int method, bool jac, bool grav, bool transient, bool fullup,
                cudaStream_t st);
+// Batched forms: one launch over `count` problems of the same kind (b, dim, method,
+// gravity, transient, upwind); problem p reads batch[p] (device array), blockIdx.y = p.
+// maxN is the largest cell count of the batch (sizes the grid).
+void launchVolvarsBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, int method, cudaStream_t st);
+void launchPrevStorageBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, cudaStream_t st);
+void launchRowBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, int dim, int method, bool jac, bool grav,
+                    bool transient, bool fullup, cudaStream_t st);
 
 }  // namespace dxg

@@ -59,10 +59,20 @@ __device__ __forceinline__ void blockSum(double (&v)[NV])
     }
 }
 
-// Writes this block's partials; returns true in thread 0 of the last block to finish,
-// which then holds the grid totals (summed in block order) in v.
+// Blocks a reduction over M entries uses (host: reduceBlocks).
+__host__ __device__ __forceinline__ int reduceBlocksFor(int64_t M)
+{
+    int64_t b = (M + kReduceThreads - 1) / kReduceThreads;
+    if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// Writes this block's partials; returns true in thread 0 of the last of the nblk
+// participating blocks to finish, which then holds the totals (summed in block
+// order) in v.
 template <int NV>
-__device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsigned* counter)
+__device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsigned* counter, unsigned nblk)
 {
     blockSum<NV>(v);
     __shared__ bool amLast;
@@ -71,7 +81,7 @@ __device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsig
         for (int k = 0; k < NV; ++k) partials[k * kMaxReduceBlocks + blockIdx.x] = v[k];
         __threadfence();
         const unsigned t = atomicAdd(counter, 1u);
-        amLast = (t == gridDim.x - 1);
+        amLast = (t == nblk - 1);
     }
     __syncthreads();
     if (!amLast) return false;
@@ -81,7 +91,7 @@ __device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsig
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             double s = 0.0;
-            for (unsigned bI = threadIdx.x; bI < gridDim.x; bI += 32)
+            for (unsigned bI = threadIdx.x; bI < nblk; bI += 32)
                 s += ((volatile double*)partials)[k * kMaxReduceBlocks + bI];
             v[k] = warpSum(s);
         }
@@ -134,13 +144,16 @@ __device__ __forceinline__ bool slotValid(unsigned mask, int dim, int s)
 // ---------------------------------------------------------------- SpMV
 // y = A x; MODE 0: plain; MODE 1: also dot(w, y) -> h, alpha; MODE 2: dots (y,w),(y,y) -> omega
 template <int B, int DIM, class MT, class VT, int MODE>
-__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a)
+__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0, const SpmvArgs<MT, VT>* batch)
 {
+    const SpmvArgs<MT, VT> a = batch ? batch[blockIdx.y] : a0;
+    const unsigned nblk = reduceBlocksFor(a.N);
+    if (blockIdx.x >= nblk) return;
     if (a.ks && a.ks->status != KS_RUNNING) return;
     constexpr int S = 2 * DIM + 1;
     constexpr int BB = B * B;
     double part[2] = {0.0, 0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
         const unsigned m = a.nbmask[i];
         VT acc[B];
 #pragma unroll
@@ -170,7 +183,7 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a)
         }
     }
     if (MODE == 0) return;
-    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE)) {
+    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE, nblk)) {
         KrylovState& ks = *a.ks;
         if (MODE == 1) {
             ks.h = part[0];
@@ -322,12 +335,21 @@ __global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
 }
 
 // ---------------------------------------------------------------- BiCGSTAB vector kernels
+// Each kernel takes a single argument block, or (batch != nullptr) one per problem
+// selected by blockIdx.y; a problem's blocks are the first reduceBlocksFor(M) of the row.
+#define DXG_PROBLEM_BLOCKS(ARGT)                                  \
+    const ARGT a = batch ? batch[blockIdx.y] : a0;                \
+    const unsigned nblk = reduceBlocksFor(a.M);                   \
+    if (blockIdx.x >= nblk) return;                               \
+    const int64_t stride = (int64_t)nblk * blockDim.x;
+
 template <class VT>
-__global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a, const double* __restrict__ rhs)
+__global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
 {
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
-        const VT rv = (VT)rhs[k];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+        const VT rv = (VT)a.rhs[k];
         a.r[k] = rv;
         a.rt[k] = rv;
         a.x[k] = 0;
@@ -335,8 +357,12 @@ __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a, const
         a.v[k] = 0;
         part[0] += (double)rv * (double)rv;
     }
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 4)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 4, nblk)) {
         KrylovState& ks = *a.ks;
+        if (a.maxHalf > 0) {
+            ks.reduction = a.reduction;
+            ks.maxHalf = a.maxHalf;
+        }
         ks.def0 = ks.def = sqrt(part[0]);
         ks.rho = ks.alpha = ks.omega = 1.0;
         ks.halfsteps = 0;
@@ -348,13 +374,14 @@ __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a, const
 
 // rho_new = <rt, r>, breakdown checks and beta (first half of an iteration)
 template <class VT>
-__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a)
+__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
 {
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
     if (a.ks->status != KS_RUNNING) return;
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride)
         part[0] += (double)a.rt[k] * (double)a.r[k];
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5, nblk)) {
         KrylovState& ks = *a.ks;
         if (ks.halfsteps + 1 >= ks.maxHalf) { ks.status = KS_MAXIT; return; }
         ks.rho_new = part[0];
@@ -365,41 +392,47 @@ __global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a)
 
 // p = r (first iteration) or p = (p - omega v) * beta + r
 template <class VT>
-__global__ void bicgUpdateP(BicgArgs<VT> a)
+__global__ void bicgUpdateP(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
 {
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
     const KrylovState& ks = *a.ks;
     if (ks.status != KS_RUNNING) return;
     const bool first = ks.halfsteps == 0;
     const VT omega = (VT)ks.omega, beta = (VT)ks.beta;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
-        if (first) a.p[k] = a.r[k];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+        VT pk;
+        if (first) pk = a.r[k];
         else {
-            VT pk = a.p[k];
+            pk = a.p[k];
             pk += -omega * a.v[k];
             pk *= beta;
             pk += a.r[k];
-            a.p[k] = pk;
         }
+        a.p[k] = pk;
+        if (a.pLow) a.pLow[k] = (float)pk;
     }
 }
 
 // x += s*y; r -= s*q; def = ||r||; STAGE 0: s = alpha, q = v; STAGE 1: s = omega, q = t
 template <class VT, int STAGE>
-__global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a)
+__global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
 {
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
     const KrylovState& ksr = *a.ks;
     if (ksr.status != KS_RUNNING) return;
     const double sd = STAGE == 0 ? ksr.alpha : ksr.omega;
     const VT s = (VT)sd;
     const VT* q = STAGE == 0 ? a.v : a.t;
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += (int64_t)gridDim.x * blockDim.x) {
+    float* rLow = STAGE == 0 ? a.rLow : nullptr;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
         a.x[k] += s * a.y[k];
         const VT rk = a.r[k] + (-s) * q[k];
         a.r[k] = rk;
+        if (rLow) rLow[k] = (float)rk;
         part[0] += (double)rk * (double)rk;
     }
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6, nblk)) {
         KrylovState& ks = *a.ks;
         ks.def = sqrt(part[0]);
         ks.halfsteps += 1;
@@ -412,17 +445,15 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a)
 // ---------------------------------------------------------------- Newton helpers
 // u = uLast - lambda*delta (uLast keeps the iterate), shift = max relative shift
 // (maxRelativeShift, dumux/nonlinear/newtonsolver.hh:110-128)
-__global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(const double* __restrict__ uLast,
-                                                                      const double* __restrict__ delta, double* u,
-                                                                      double lambda, int64_t M, double* partials,
-                                                                      unsigned* counter, double* shiftOut)
+__global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(NewtonUpdArgs a0, const NewtonUpdArgs* batch)
 {
+    DXG_PROBLEM_BLOCKS(NewtonUpdArgs)
     double mx = 0.0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x) {
-        const double a = uLast[k];
-        const double b = a + (-lambda) * delta[k];
-        u[k] = b;
-        const double s = fabs(a - b) / fmax(1.0, fabs(a + b) * 0.5);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+        const double x = a.uLast[k];
+        const double y = x + (-a.lambda) * a.delta[k];
+        a.u[k] = y;
+        const double s = fabs(x - y) / fmax(1.0, fabs(x + y) * 0.5);
         mx = fmax(mx, s);
     }
     // block max
@@ -432,30 +463,32 @@ __global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(const doubl
     if (lane == 0) sh[wid] = mx;
     __syncthreads();
     __shared__ bool amLast;
+    double* partials = a.scratch.partials;
+    unsigned* counter = a.scratch.counter + 7;
     if (threadIdx.x == 0) {
         double bm = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) bm = fmax(bm, sh[k]);
         partials[blockIdx.x] = bm;
         __threadfence();
-        amLast = atomicAdd(counter, 1u) == gridDim.x - 1;
+        amLast = atomicAdd(counter, 1u) == nblk - 1;
     }
     __syncthreads();
     if (amLast && threadIdx.x == 0) {
         __threadfence();
         double g = 0.0;
-        for (unsigned bI = 0; bI < gridDim.x; ++bI) g = fmax(g, ((volatile double*)partials)[bI]);
-        *shiftOut = g;
+        for (unsigned bI = 0; bI < nblk; ++bI) g = fmax(g, ((volatile double*)partials)[bI]);
+        *a.shiftOut = g;
         *counter = 0u;
     }
 }
 
-__global__ void __launch_bounds__(kReduceThreads) norm2Kernel(const double* __restrict__ x, int64_t M,
-                                                               double* partials, unsigned* counter, double* out)
+__global__ void __launch_bounds__(kReduceThreads) norm2Kernel(NormArgs a0, const NormArgs* batch)
 {
+    DXG_PROBLEM_BLOCKS(NormArgs)
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x)
-        part[0] += x[k] * x[k];
-    if (gridSum<1>(part, partials, counter)) *out = sqrt(part[0]);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride)
+        part[0] += a.x[k] * a.x[k];
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 3, nblk)) *a.out = sqrt(part[0]);
 }
 
 template <class VT>
@@ -465,30 +498,90 @@ __global__ void copyToDouble(const VT* __restrict__ x, double* y, int64_t M)
         y[k] = (double)x[k];
 }
 
-// ---------------------------------------------------------------- host launchers
-int reduceBlocks(int64_t M)
+// ---------------------------------------------------------------- mixed-precision helpers
+__global__ void toFloatKernel(ToFloatArgs a0, const ToFloatArgs* batch)
 {
-    int64_t b = (M + kReduceThreads - 1) / kReduceThreads;
-    if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
-    if (b < 1) b = 1;
-    return (int)b;
+    const ToFloatArgs a = batch ? batch[blockIdx.y] : a0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
+        a.dst[k] = (float)a.src[k];
+}
+__global__ void toDoubleKernel(ToDoubleArgs a0, const ToDoubleArgs* batch)
+{
+    const ToDoubleArgs a = batch ? batch[blockIdx.y] : a0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
+        a.dst[k] = (double)a.src[k];
+}
+__global__ void accumKernel(AccumArgs a0, const AccumArgs* batch)
+{
+    const AccumArgs a = batch ? batch[blockIdx.y] : a0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
+        a.y[k] += (double)a.x[k];
+}
+// defect = rhs - A*x in FP64 (iterative refinement of the mixed-precision solve)
+template <int B, int DIM>
+__global__ void defectKernel(DefectArgs a0, const DefectArgs* batch)
+{
+    const DefectArgs a = batch ? batch[blockIdx.y] : a0;
+    constexpr int BB = B * B;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned m = a.nbmask[i];
+        double acc[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) acc[e] = 0.0;
+#pragma unroll
+        for (int s = 0; s < 2 * DIM + 1; ++s) {
+            if (!slotValid(m, DIM, s)) continue;
+            const int64_t j = i + a.off[s];
+            const double* blk = a.A + ((int64_t)s * a.N + i) * BB;
+#pragma unroll
+            for (int rr = 0; rr < B; ++rr)
+#pragma unroll
+                for (int cc = 0; cc < B; ++cc) acc[rr] += blk[rr * B + cc] * a.x[j * B + cc];
+        }
+#pragma unroll
+        for (int rr = 0; rr < B; ++rr) a.y[i * B + rr] = a.rhs[i * B + rr] - acc[rr];
+    }
 }
 
-template <int B, int DIM, class MT, class VT>
-void spmvT(const SpmvArgs<MT, VT>& a, int mode, cudaStream_t st)
+// ---------------------------------------------------------------- host launchers
+int reduceBlocks(int64_t M) { return reduceBlocksFor(M); }
+
+// grid of a batched grid-stride launch: x covers the largest problem (capped), y = problems
+static dim3 batchGrid(int64_t maxN, int count, int threads, int cap)
 {
-    const int g = reduceBlocks(a.N);
-    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a);
-    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a);
-    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a);
+    int64_t gx = (maxN + threads - 1) / threads;
+    if (gx > cap) gx = cap;
+    if (gx < 1) gx = 1;
+    return dim3((unsigned)gx, (unsigned)count);
+}
+static dim3 reduceGrid(int64_t maxM, int count) { return dim3((unsigned)reduceBlocksFor(maxM), (unsigned)count); }
+
+template <int B, int DIM, class MT, class VT>
+static void spmvT(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, dim3 g, int mode, cudaStream_t st)
+{
+    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a, batch);
+    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a, batch);
+    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a, batch);
+}
+template <class MT, class VT>
+static void spmvDispatch(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, dim3 g, int b, int dim, int mode,
+                         cudaStream_t st)
+{
+    if (b == 1) { if (dim == 2) spmvT<1, 2>(a, batch, g, mode, st); else spmvT<1, 3>(a, batch, g, mode, st); }
+    else { if (dim == 2) spmvT<2, 2>(a, batch, g, mode, st); else spmvT<2, 3>(a, batch, g, mode, st); }
+    DXG_CUDA(cudaGetLastError());
 }
 
 template <class MT, class VT>
 void launchSpmv(const SpmvArgs<MT, VT>& a, int b, int dim, int mode, cudaStream_t st)
 {
-    if (b == 1) { if (dim == 2) spmvT<1, 2>(a, mode, st); else spmvT<1, 3>(a, mode, st); }
-    else { if (dim == 2) spmvT<2, 2>(a, mode, st); else spmvT<2, 3>(a, mode, st); }
-    DXG_CUDA(cudaGetLastError());
+    spmvDispatch<MT, VT>(a, nullptr, dim3(reduceBlocks(a.N)), b, dim, mode, st);
+}
+template <class MT, class VT>
+void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, int count, int64_t maxN, int b, int dim, int mode,
+                     cudaStream_t st)
+{
+    spmvDispatch<MT, VT>(SpmvArgs<MT, VT>{}, batch, reduceGrid(maxN, count), b, dim, mode, st);
 }
 
 template <class MT>
@@ -539,24 +632,48 @@ int64_t launchIluApply(const IluArgs<MT, VT>& a, const LevelSchedule& ls, int b,
 template <class VT>
 void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st)
 {
-    bicgInit<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, rhs);
+    BicgArgs<VT> aa = a;
+    aa.rhs = rhs;
+    bicgInit<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(aa, nullptr);
     DXG_CUDA(cudaGetLastError());
 }
 template <class VT>
 void launchBicgRho(const BicgArgs<VT>& a, cudaStream_t st)
 {
-    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
 }
 template <class VT>
 void launchBicgUpdateP(const BicgArgs<VT>& a, cudaStream_t st)
 {
-    bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+    bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
 }
 template <class VT>
 void launchBicgAxpyNorm(const BicgArgs<VT>& a, int stage, cudaStream_t st)
 {
-    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
-    else bicgAxpyNorm<VT, 1><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a);
+    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
+    else bicgAxpyNorm<VT, 1><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
+}
+template <class VT>
+void launchBicgInitBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+{
+    bicgInit<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    DXG_CUDA(cudaGetLastError());
+}
+template <class VT>
+void launchBicgRhoBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+{
+    bicgRho<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+}
+template <class VT>
+void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+{
+    bicgUpdateP<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+}
+template <class VT>
+void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, int stage, cudaStream_t st)
+{
+    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    else bicgAxpyNorm<VT, 1><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
 }
 template <class VT>
 void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st)
@@ -567,19 +684,90 @@ void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st)
 void launchNewtonUpdate(const double* uLast, const double* delta, double* u, double lambda, int64_t M,
                         const ReduceScratch& sc, double* shiftOut, cudaStream_t st)
 {
-    newtonUpdateKernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(uLast, delta, u, lambda, M, sc.partials,
-                                                                  sc.counter + 7, shiftOut);
+    const NewtonUpdArgs a{uLast, delta, u, lambda, M, sc, shiftOut};
+    newtonUpdateKernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, int count, int64_t maxM, cudaStream_t st)
+{
+    newtonUpdateKernel<<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(NewtonUpdArgs{}, batch);
     DXG_CUDA(cudaGetLastError());
 }
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st)
 {
-    norm2Kernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(x, M, sc.partials, sc.counter + 3, out);
+    const NormArgs a{x, M, sc, out};
+    norm2Kernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr);
     DXG_CUDA(cudaGetLastError());
+}
+void launchNorm2Batch(const NormArgs* batch, int count, int64_t maxM, cudaStream_t st)
+{
+    norm2Kernel<<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(NormArgs{}, batch);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchToFloat(const ToFloatArgs& a, cudaStream_t st)
+{
+    toFloatKernel<<<reduceBlocks(a.n), kReduceThreads, 0, st>>>(a, nullptr);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchToFloatBatch(const ToFloatArgs* batch, int count, int64_t maxN, cudaStream_t st)
+{
+    toFloatKernel<<<batchGrid(maxN, count, kReduceThreads, 1184), kReduceThreads, 0, st>>>(ToFloatArgs{}, batch);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchToDouble(const ToDoubleArgs& a, cudaStream_t st)
+{
+    toDoubleKernel<<<reduceBlocks(a.n), kReduceThreads, 0, st>>>(a, nullptr);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchToDoubleBatch(const ToDoubleArgs* batch, int count, int64_t maxN, cudaStream_t st)
+{
+    toDoubleKernel<<<batchGrid(maxN, count, kReduceThreads, 1184), kReduceThreads, 0, st>>>(ToDoubleArgs{}, batch);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchAccum(const AccumArgs& a, cudaStream_t st)
+{
+    accumKernel<<<reduceBlocks(a.n), kReduceThreads, 0, st>>>(a, nullptr);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchAccumBatch(const AccumArgs* batch, int count, int64_t maxN, cudaStream_t st)
+{
+    accumKernel<<<batchGrid(maxN, count, kReduceThreads, 1184), kReduceThreads, 0, st>>>(AccumArgs{}, batch);
+    DXG_CUDA(cudaGetLastError());
+}
+static void defectDispatch(const DefectArgs& a, const DefectArgs* batch, dim3 g, int b, int dim, cudaStream_t st)
+{
+    if (b == 1) {
+        if (dim == 2) defectKernel<1, 2><<<g, kReduceThreads, 0, st>>>(a, batch);
+        else defectKernel<1, 3><<<g, kReduceThreads, 0, st>>>(a, batch);
+    } else {
+        if (dim == 2) defectKernel<2, 2><<<g, kReduceThreads, 0, st>>>(a, batch);
+        else defectKernel<2, 3><<<g, kReduceThreads, 0, st>>>(a, batch);
+    }
+    DXG_CUDA(cudaGetLastError());
+}
+void launchDefect(const DefectArgs& a, int b, int dim, cudaStream_t st)
+{
+    defectDispatch(a, nullptr, dim3(reduceBlocks(a.N * b)), b, dim, st);
+}
+void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, int dim, cudaStream_t st)
+{
+    defectDispatch(DefectArgs{}, batch, batchGrid(maxN, count, kReduceThreads, 1184), b, dim, st);
 }
 
 // explicit instantiations
 template void launchSpmv<double, double>(const SpmvArgs<double, double>&, int, int, int, cudaStream_t);
 template void launchSpmv<float, float>(const SpmvArgs<float, float>&, int, int, int, cudaStream_t);
+template void launchSpmvBatch<double, double>(const SpmvArgs<double, double>*, int, int64_t, int, int, int,
+                                              cudaStream_t);
+template void launchSpmvBatch<float, float>(const SpmvArgs<float, float>*, int, int64_t, int, int, int, cudaStream_t);
+template void launchBicgInitBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
+template void launchBicgInitBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
+template void launchBicgRhoBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
+template void launchBicgRhoBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
+template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
+template void launchBicgUpdatePBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
+template void launchBicgAxpyNormBatch<double>(const BicgArgs<double>*, int, int64_t, int, cudaStream_t);
+template void launchBicgAxpyNormBatch<float>(const BicgArgs<float>*, int, int64_t, int, cudaStream_t);
 template int64_t launchIluFactor<double>(const IluArgs<double, double>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluFactor<float>(const IluArgs<float, float>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluApply<double, double>(const IluArgs<double, double>&, const LevelSchedule&, int, int,

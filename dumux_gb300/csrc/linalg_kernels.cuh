@@ -37,6 +37,56 @@ struct BicgArgs {
     int64_t M;                // N*b scalars
     KrylovState* ks;
     ReduceScratch scratch;
+    const double* rhs;        // right-hand side read by the init kernel
+    double reduction;         // init kernel: written to ks when maxHalf > 0
+    int maxHalf;
+    // FP32 copies of p (written by the p update) and r (written by the first-half
+    // update): the inputs of an FP32 preconditioner inside an FP64 iteration
+    float* pLow;
+    float* rLow;
+};
+
+struct ToDoubleArgs {
+    const float* src;
+    double* dst;
+    int64_t n;
+};
+
+// u = uLast - lambda*delta and the maximum relative shift
+struct NewtonUpdArgs {
+    const double* uLast;
+    const double* delta;
+    double* u;
+    double lambda;
+    int64_t M;
+    ReduceScratch scratch;
+    double* shiftOut;
+};
+struct NormArgs {
+    const double* x;
+    int64_t M;
+    ReduceScratch scratch;
+    double* out;
+};
+// elementwise helpers of the mixed-precision solve
+struct ToFloatArgs {
+    const double* src;
+    float* dst;
+    int64_t n;
+};
+struct AccumArgs {
+    double* y;                // y += x
+    const float* x;
+    int64_t n;
+};
+struct DefectArgs {
+    const double* A;
+    const uint8_t* nbmask;
+    const double* x;          // accumulated update
+    const double* rhs;
+    double* y;                // rhs - A x
+    int64_t N;
+    int64_t off[7];
 };
 
 int reduceBlocks(int64_t M);
@@ -61,5 +111,31 @@ void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st);
 void launchNewtonUpdate(const double* uLast, const double* delta, double* u, double lambda, int64_t M,
                         const ReduceScratch& sc, double* shiftOut, cudaStream_t st);
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st);
+void launchToFloat(const ToFloatArgs& a, cudaStream_t st);
+void launchToDouble(const ToDoubleArgs& a, cudaStream_t st);
+void launchToDoubleBatch(const ToDoubleArgs* batch, int count, int64_t maxN, cudaStream_t st);
+void launchAccum(const AccumArgs& a, cudaStream_t st);
+void launchDefect(const DefectArgs& a, int b, int dim, cudaStream_t st);
+
+// Batched forms: one launch over `count` problems, problem p reading batch[p] (device
+// array, blockIdx.y = p for the grid-stride kernels).  maxM / maxN: the largest vector
+// length / cell count of the batch.  Each problem reduces over its own block count,
+// the one its single-problem launch uses, so batched and single results are identical.
+template <class MT, class VT>
+void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, int count, int64_t maxN, int b, int dim, int mode,
+                     cudaStream_t st);
+template <class VT>
+void launchBicgInitBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+template <class VT>
+void launchBicgRhoBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+template <class VT>
+void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+template <class VT>
+void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, int stage, cudaStream_t st);
+void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, int count, int64_t maxM, cudaStream_t st);
+void launchNorm2Batch(const NormArgs* batch, int count, int64_t maxM, cudaStream_t st);
+void launchToFloatBatch(const ToFloatArgs* batch, int count, int64_t maxN, cudaStream_t st);
+void launchAccumBatch(const AccumArgs* batch, int count, int64_t maxN, cudaStream_t st);
+void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, int dim, cudaStream_t st);
 
 }  // namespace dxg

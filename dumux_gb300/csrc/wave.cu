@@ -24,7 +24,9 @@
 //
 // The arithmetic per cell is the one of the level-scheduled kernels in linalg.cu (same
 // operand order), so both give the same factors and sweeps.
+#include <algorithm>
 #include <climits>
+#include <vector>
 
 #include <cooperative_groups.h>
 
@@ -228,8 +230,12 @@ struct LineState {
 
 // MODE 0: solve (forward DIR=+1 with L, backward DIR=-1 with U=A_upper and Dinv)
 // MODE 1: factorisation (DIR=+1): writes L and Dinv
+//
+// Batched launch (batch != nullptr): cluster k of the grid sweeps problem k; CTAs whose
+// rank is at or beyond that problem's slab count only take part in the two cluster
+// barriers.
 template <int B, class T, int DIM, int DIR, int MODE, int PF>
-__global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a)
+__global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArgs<T>* batch)
 {
     constexpr int PB = MODE == 1 ? B * B : B;
     constexpr int BB = B * B;
@@ -243,6 +249,13 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a)
 
     cg::cluster_group cluster = cg::this_cluster();
     const int cta = (int)cluster.block_rank();
+    const WaveArgs<T> a = batch ? batch[blockIdx.x / cluster.num_blocks()] : a0;
+    if (cta >= a.ctas) {
+        // idle CTA of a batched launch: nothing to sweep, no hand-off partner
+        cluster.sync();
+        cluster.sync();
+        return;
+    }
     const int C = a.ctas;
     const int LPC = a.linesPerCta;
     const int H = a.haloLines;
@@ -558,16 +571,23 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a)
 
 // ---------------------------------------------------------------- host side
 template <int B, class T, int DIR, int MODE>
-static size_t waveSmem(const WavePlan& p, int dim, int pfDepth)
+static size_t waveSmemFor(int dim, int linesPerCta, int haloLines, int threads, int pfDepth)
 {
     constexpr int PB = MODE == 1 ? B * B : B;
     const int rec = dim == 3 ? Rec<B, T, 3, DIR, MODE>::n : Rec<B, T, 2, DIR, MODE>::n;
-    return pfOffset(p.linesPerCta, p.haloLines, PB * (int)sizeof(T)) +
-           (size_t)pfDepth * p.threads * p.lpt * rec * sizeof(T);
+    const int lpt = (linesPerCta + threads - 1) / threads;
+    return pfOffset(linesPerCta, haloLines, PB * (int)sizeof(T)) + (size_t)pfDepth * threads * lpt * rec * sizeof(T);
 }
 
+// Uniform shape of one launch: `clusters` clusters of `ctas` CTAs.
+struct WaveLaunch {
+    int clusters, ctas, threads, pf;
+    size_t smem;
+};
+
 template <int B, class T, int DIM, int DIR, int MODE, int PF>
-static cudaError_t launchOne(const WavePlan& plan, const WaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
+static cudaError_t launchOne(const WaveLaunch& L, const WaveArgs<T>& a, const WaveArgs<T>* batch, cudaStream_t st,
+                             bool query, int* fits)
 {
     auto kern = waveKernel<B, T, DIM, DIR, MODE, PF>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -575,13 +595,13 @@ static cudaError_t launchOne(const WavePlan& plan, const WaveArgs<T>& a, cudaStr
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWaveSmemLimit);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(plan.ctas);
-    cfg.blockDim = dim3(plan.threads);
-    cfg.dynamicSmemBytes = waveSmem<B, T, DIR, MODE>(plan, DIM, PF);
+    cfg.gridDim = dim3(L.clusters * L.ctas);
+    cfg.blockDim = dim3(L.threads);
+    cfg.dynamicSmemBytes = L.smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = plan.ctas;
+    attr[0].val.clusterDim.x = L.ctas;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -589,30 +609,22 @@ static cudaError_t launchOne(const WavePlan& plan, const WaveArgs<T>& a, cudaStr
     if (query) {
         int n = 0;
         e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
-        *fits = (e == cudaSuccess && n > 0);
+        *fits = (e == cudaSuccess && n > 0) ? n : 0;
         if (e != cudaSuccess) cudaGetLastError();
         return cudaSuccess;
     }
-    return cudaLaunchKernelEx(&cfg, kern, a);
-}
-
-// prefetch depth: the deepest of {8, 4, 2, 1} within the shared-memory budget
-template <int B, class T, int DIR, int MODE>
-static int pickDepth(const WavePlan& p, int dim)
-{
-    for (int d : {8, 4, 2, 1})
-        if (waveSmem<B, T, DIR, MODE>(p, dim, d) <= kWaveSmemLimit) return d;
-    return 0;
+    return cudaLaunchKernelEx(&cfg, kern, a, batch);
 }
 
 template <int B, class T, int DIM, int DIR, int MODE>
-static cudaError_t dispatchPF(const WavePlan& plan, const WaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
+static cudaError_t dispatchPF(const WaveLaunch& L, const WaveArgs<T>& a, const WaveArgs<T>* batch, cudaStream_t st,
+                              bool query, int* fits)
 {
-    switch (pickDepth<B, T, DIR, MODE>(plan, DIM)) {
-        case 8: return launchOne<B, T, DIM, DIR, MODE, 8>(plan, a, st, query, fits);
-        case 4: return launchOne<B, T, DIM, DIR, MODE, 4>(plan, a, st, query, fits);
-        case 2: return launchOne<B, T, DIM, DIR, MODE, 2>(plan, a, st, query, fits);
-        case 1: return launchOne<B, T, DIM, DIR, MODE, 1>(plan, a, st, query, fits);
+    switch (L.pf) {
+        case 8: return launchOne<B, T, DIM, DIR, MODE, 8>(L, a, batch, st, query, fits);
+        case 4: return launchOne<B, T, DIM, DIR, MODE, 4>(L, a, batch, st, query, fits);
+        case 2: return launchOne<B, T, DIM, DIR, MODE, 2>(L, a, batch, st, query, fits);
+        case 1: return launchOne<B, T, DIM, DIR, MODE, 1>(L, a, batch, st, query, fits);
         default:
             if (fits) *fits = 0;
             return query ? cudaSuccess : cudaErrorInvalidConfiguration;
@@ -620,11 +632,28 @@ static cudaError_t dispatchPF(const WavePlan& plan, const WaveArgs<T>& a, cudaSt
 }
 
 template <int B, class T, int DIR, int MODE>
-static cudaError_t dispatch(const WavePlan& plan, int dim, const WaveArgs<T>& a, cudaStream_t st, bool query,
-                            int* fits)
+static cudaError_t dispatch(const WaveLaunch& L, int dim, const WaveArgs<T>& a, const WaveArgs<T>* batch,
+                            cudaStream_t st, bool query, int* fits)
 {
-    return dim == 3 ? dispatchPF<B, T, 3, DIR, MODE>(plan, a, st, query, fits)
-                    : dispatchPF<B, T, 2, DIR, MODE>(plan, a, st, query, fits);
+    return dim == 3 ? dispatchPF<B, T, 3, DIR, MODE>(L, a, batch, st, query, fits)
+                    : dispatchPF<B, T, 2, DIR, MODE>(L, a, batch, st, query, fits);
+}
+
+// prefetch depth of a single-problem launch: the deepest of {8, 4, 2, 1} within the
+// shared-memory budget
+template <int B, class T, int DIR, int MODE>
+static WaveLaunch singleLaunch(const WavePlan& p, int dim)
+{
+    WaveLaunch L{1, p.ctas, p.threads, 0, 0};
+    for (int d : {8, 4, 2, 1}) {
+        const size_t sm = waveSmemFor<B, T, DIR, MODE>(dim, p.linesPerCta, p.haloLines, p.threads, d);
+        if (sm <= kWaveSmemLimit) {
+            L.pf = d;
+            L.smem = sm;
+            break;
+        }
+    }
+    return L;
 }
 
 template <int B, class T>
@@ -632,28 +661,39 @@ static bool planFits(const WavePlan& p, int dim)
 {
     WaveArgs<T> dummy{};
     int f1 = 0, f2 = 0, f3 = 0;
-    dispatch<B, T, 1, 0>(p, dim, dummy, 0, true, &f1);
-    dispatch<B, T, -1, 0>(p, dim, dummy, 0, true, &f2);
-    dispatch<B, T, 1, 1>(p, dim, dummy, 0, true, &f3);
+    dispatch<B, T, 1, 0>(singleLaunch<B, T, 1, 0>(p, dim), dim, dummy, nullptr, 0, true, &f1);
+    dispatch<B, T, -1, 0>(singleLaunch<B, T, -1, 0>(p, dim), dim, dummy, nullptr, 0, true, &f2);
+    dispatch<B, T, 1, 1>(singleLaunch<B, T, 1, 1>(p, dim), dim, dummy, nullptr, 0, true, &f3);
     return f1 && f2 && f3;
+}
+
+WaveGeom waveGeom(int dim, int nx, int ny, int nz, int maxCtas)
+{
+    WaveGeom g{};
+    const int unit = dim == 3 ? ny : 1;                 // lines per plane of the slab axis
+    const int units = dim == 3 ? nz : ny;
+    if (units <= 0 || nx <= 0 || maxCtas <= 0) return g;
+    int ctas = std::min(maxCtas, units);
+    const int per = (units + ctas - 1) / ctas;
+    ctas = (units + per - 1) / per;
+    g.ctas = ctas;
+    g.linesPerCta = per * unit;
+    g.haloLines = dim == 3 ? ny : 1;
+    return g;
 }
 
 static WavePlan planFor(int dim, int nx, int ny, int nz, int maxCtas)
 {
     WavePlan p{};
-    const int nLines = ny * nz;
-    const int unit = dim == 3 ? ny : 1;                 // lines per plane of the slab axis
-    const int units = dim == 3 ? nz : ny;
-    int ctas = std::min(maxCtas, units);
-    const int per = (units + ctas - 1) / ctas;
-    ctas = (units + per - 1) / per;
-    p.ctas = ctas;
-    p.linesPerCta = per * unit;
-    p.haloLines = dim == 3 ? ny : 1;
+    const WaveGeom g = waveGeom(dim, nx, ny, nz, maxCtas);
+    if (g.ctas == 0) return p;
+    p.ctas = g.ctas;
+    p.linesPerCta = g.linesPerCta;
+    p.haloLines = g.haloLines;
     const int threads = std::min(1024, ((p.linesPerCta + 31) / 32) * 32);
     p.lpt = (p.linesPerCta + threads - 1) / threads;
     p.threads = threads;
-    p.ok = p.lpt <= 2 && nLines > 0 && nx > 0;
+    p.ok = p.lpt <= 2;
     return p;
 }
 
@@ -673,19 +713,87 @@ WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64)
 template <class T>
 void launchWaveFactor(const WavePlan& plan, const WaveArgs<T>& a, int b, cudaStream_t st)
 {
-    const cudaError_t e = b == 1 ? dispatch<1, T, 1, 1>(plan, a.dim, a, st, false, nullptr)
-                                 : dispatch<2, T, 1, 1>(plan, a.dim, a, st, false, nullptr);
+    const cudaError_t e = b == 1 ? dispatch<1, T, 1, 1>(singleLaunch<1, T, 1, 1>(plan, a.dim), a.dim, a, nullptr, st,
+                                                        false, nullptr)
+                                 : dispatch<2, T, 1, 1>(singleLaunch<2, T, 1, 1>(plan, a.dim), a.dim, a, nullptr, st,
+                                                        false, nullptr);
     DXG_CUDA(e);
 }
 template <class T>
 void launchWaveApply(const WavePlan& plan, const WaveArgs<T>& fwd, const WaveArgs<T>& bwd, int b, cudaStream_t st)
 {
+    const int dim = fwd.dim;
     if (b == 1) {
-        DXG_CUDA((dispatch<1, T, 1, 0>(plan, fwd.dim, fwd, st, false, nullptr)));
-        DXG_CUDA((dispatch<1, T, -1, 0>(plan, bwd.dim, bwd, st, false, nullptr)));
+        DXG_CUDA((dispatch<1, T, 1, 0>(singleLaunch<1, T, 1, 0>(plan, dim), dim, fwd, nullptr, st, false, nullptr)));
+        DXG_CUDA((dispatch<1, T, -1, 0>(singleLaunch<1, T, -1, 0>(plan, dim), dim, bwd, nullptr, st, false, nullptr)));
     } else {
-        DXG_CUDA((dispatch<2, T, 1, 0>(plan, fwd.dim, fwd, st, false, nullptr)));
-        DXG_CUDA((dispatch<2, T, -1, 0>(plan, bwd.dim, bwd, st, false, nullptr)));
+        DXG_CUDA((dispatch<2, T, 1, 0>(singleLaunch<2, T, 1, 0>(plan, dim), dim, fwd, nullptr, st, false, nullptr)));
+        DXG_CUDA((dispatch<2, T, -1, 0>(singleLaunch<2, T, -1, 0>(plan, dim), dim, bwd, nullptr, st, false, nullptr)));
+    }
+}
+
+// ---------------------------------------------------------------- batched launches
+// Shared memory of a batched launch of kernel (DIR, MODE): the largest problem's need.
+template <int B, class T, int DIR, int MODE>
+static size_t batchSmem(const WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim)
+{
+    size_t mx = 0;
+    for (const WaveGeom& g : geoms)
+        mx = std::max(mx, waveSmemFor<B, T, DIR, MODE>(dim, g.linesPerCta, g.haloLines, p.threads, p.pf));
+    return mx;
+}
+
+template <int B, class T>
+static int batchFits(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim, int count)
+{
+    p.smemFwd = batchSmem<B, T, 1, 0>(p, geoms, dim);
+    p.smemBwd = batchSmem<B, T, -1, 0>(p, geoms, dim);
+    p.smemFactor = batchSmem<B, T, 1, 1>(p, geoms, dim);
+    if (std::max(p.smemFwd, std::max(p.smemBwd, p.smemFactor)) > kWaveSmemLimit) return 0;
+    WaveArgs<T> dummy{};
+    int f1 = 0, f2 = 0, f3 = 0;
+    dispatch<B, T, 1, 0>(WaveLaunch{count, p.ctas, p.threads, p.pf, p.smemFwd}, dim, dummy, nullptr, 0, true, &f1);
+    dispatch<B, T, -1, 0>(WaveLaunch{count, p.ctas, p.threads, p.pf, p.smemBwd}, dim, dummy, nullptr, 0, true, &f2);
+    dispatch<B, T, 1, 1>(WaveLaunch{count, p.ctas, p.threads, p.pf, p.smemFactor}, dim, dummy, nullptr, 0, true, &f3);
+    return std::min(f1, std::min(f2, f3));
+}
+
+// Completes p (smem sizes) for problems of the given geometries under p.ctas CTAs per
+// cluster; returns the number of clusters that can be resident at once (0: invalid).
+int completeWaveBatchPlan(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim, int b, bool fp64)
+{
+    if (p.ctas < 1 || p.ctas > 16 || p.threads < 32 || p.threads > 1024 || p.threads % 32) return 0;
+    if (p.pf != 1 && p.pf != 2 && p.pf != 4 && p.pf != 8) return 0;
+    for (const WaveGeom& g : geoms) {
+        if (g.ctas < 1 || g.ctas > p.ctas) return 0;
+        if ((g.linesPerCta + p.threads - 1) / p.threads > 2) return 0;
+    }
+    const int count = (int)geoms.size();
+    if (b == 1) return fp64 ? batchFits<1, double>(p, geoms, dim, count) : batchFits<1, float>(p, geoms, dim, count);
+    return fp64 ? batchFits<2, double>(p, geoms, dim, count) : batchFits<2, float>(p, geoms, dim, count);
+}
+
+template <class T>
+void launchWaveFactorBatch(const WaveBatchPlan& p, const WaveArgs<T>* batch, int count, int dim, int b,
+                           cudaStream_t st)
+{
+    const WaveLaunch L{count, p.ctas, p.threads, p.pf, p.smemFactor};
+    const cudaError_t e = b == 1 ? dispatch<1, T, 1, 1>(L, dim, WaveArgs<T>{}, batch, st, false, nullptr)
+                                 : dispatch<2, T, 1, 1>(L, dim, WaveArgs<T>{}, batch, st, false, nullptr);
+    DXG_CUDA(e);
+}
+template <class T>
+void launchWaveApplyBatch(const WaveBatchPlan& p, const WaveArgs<T>* fwd, const WaveArgs<T>* bwd, int count, int dim,
+                          int b, cudaStream_t st)
+{
+    const WaveLaunch Lf{count, p.ctas, p.threads, p.pf, p.smemFwd};
+    const WaveLaunch Lb{count, p.ctas, p.threads, p.pf, p.smemBwd};
+    if (b == 1) {
+        DXG_CUDA((dispatch<1, T, 1, 0>(Lf, dim, WaveArgs<T>{}, fwd, st, false, nullptr)));
+        DXG_CUDA((dispatch<1, T, -1, 0>(Lb, dim, WaveArgs<T>{}, bwd, st, false, nullptr)));
+    } else {
+        DXG_CUDA((dispatch<2, T, 1, 0>(Lf, dim, WaveArgs<T>{}, fwd, st, false, nullptr)));
+        DXG_CUDA((dispatch<2, T, -1, 0>(Lb, dim, WaveArgs<T>{}, bwd, st, false, nullptr)));
     }
 }
 
@@ -695,5 +803,12 @@ template void launchWaveApply<double>(const WavePlan&, const WaveArgs<double>&, 
                                       cudaStream_t);
 template void launchWaveApply<float>(const WavePlan&, const WaveArgs<float>&, const WaveArgs<float>&, int,
                                      cudaStream_t);
+template void launchWaveFactorBatch<double>(const WaveBatchPlan&, const WaveArgs<double>*, int, int, int,
+                                            cudaStream_t);
+template void launchWaveFactorBatch<float>(const WaveBatchPlan&, const WaveArgs<float>*, int, int, int, cudaStream_t);
+template void launchWaveApplyBatch<double>(const WaveBatchPlan&, const WaveArgs<double>*, const WaveArgs<double>*, int,
+                                           int, int, cudaStream_t);
+template void launchWaveApplyBatch<float>(const WaveBatchPlan&, const WaveArgs<float>*, const WaveArgs<float>*, int,
+                                          int, int, cudaStream_t);
 
 }  // namespace dxg

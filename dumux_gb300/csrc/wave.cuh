@@ -1,6 +1,8 @@
 // wave.cuh -- cluster wavefront ILU(0) kernels (see wave.cu).
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 #include "linalg.cuh"
 
@@ -27,7 +29,27 @@ struct WavePlan {
     bool ok = false;
 };
 
+// Slab split of one problem under at most maxCtas CTAs.
+struct WaveGeom {
+    int ctas = 0, linesPerCta = 0, haloLines = 0;
+};
+
+// Launch shape shared by all problems of a batched sweep: clusters of `ctas` CTAs
+// (one cluster per problem), `threads` per CTA, prefetch depth `pf`.
+struct WaveBatchPlan {
+    int ctas = 0, threads = 0, pf = 0;
+    size_t smemFwd = 0, smemBwd = 0, smemFactor = 0;
+};
+
 WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64);
+WaveGeom waveGeom(int dim, int nx, int ny, int nz, int maxCtas);
+int completeWaveBatchPlan(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim, int b, bool fp64);
+template <class T>
+void launchWaveFactorBatch(const WaveBatchPlan& p, const WaveArgs<T>* batch, int count, int dim, int b,
+                           cudaStream_t st);
+template <class T>
+void launchWaveApplyBatch(const WaveBatchPlan& p, const WaveArgs<T>* fwd, const WaveArgs<T>* bwd, int count, int dim,
+                          int b, cudaStream_t st);
 template <class T>
 void launchWaveFactor(const WavePlan& plan, const WaveArgs<T>& a, int b, cudaStream_t st);
 template <class T>

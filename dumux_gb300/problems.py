@@ -2,8 +2,7 @@
 
 Each builder evaluates the problem's ``*AtPos`` callbacks at cell and face centres and
 returns a :class:`dumux_gb300.abi.ProblemDesc` (the input of ``dxg_problem_upload``)
-plus the initial solution.  This is the Python counterpart of the C++ tabulation in
-``include/dumux_gb300/tabulate.hh``.
+plus the initial solution.
 """
 import numpy as np
 
@@ -137,3 +136,55 @@ def dnapl_2p(cells=(64, 64, 32), extent=(6.0, 4.0, 1.0), seed=2, sigma=1.0, corr
                        density=(WATER_DENSITY, DNAPL_DENSITY), viscosity=(WATER_VISCOSITY, DNAPL_VISCOSITY),
                        material_params=np.array([[pe, lam, swr, snr, pc_low_swe]]))
     return desc, u0.reshape(-1)
+
+
+def ensemble_2p(count=256, seed=4, n_min=16, n_max=64, extent=(6.0, 4.0, 1.0)):
+    """Batched ensemble workload: `count` independent 2p DNAPL problems (dnapl_2p) with
+    uneven grids, each axis drawn uniformly from the integers n_min..n_max, and per
+    problem sigma ~ U[0.5, 2.0], correlation length ~ U[3, 10] cells and inflow
+    ~ U[0.01, 0.08] kg/m^2/s; problem i draws from PCG64(seed + i).
+    Returns a list of (desc, u0, meta)."""
+    out = []
+    for i in range(count):
+        rng = np.random.Generator(np.random.PCG64(seed + i))
+        cells = tuple(int(v) for v in rng.integers(n_min, n_max + 1, size=3))
+        sigma = float(rng.uniform(0.5, 2.0))
+        corr = float(rng.uniform(3.0, 10.0))
+        inflow = float(rng.uniform(0.01, 0.08))
+        desc, u0 = dnapl_2p(cells=cells, extent=extent, seed=1000 + seed + i, sigma=sigma, corr_len=corr,
+                            inflow=inflow)
+        out.append((desc, u0, {"cells": cells, "sigma": sigma, "corr_len": corr, "inflow": inflow}))
+    return out
+
+
+def served_requests(count, rate=200.0, seed=5, frac_1p=0.3, n_min=1e3, n_max=1e6, steps=(1, 20), dt=250.0):
+    """Served-stream workload: `count` requests with Poisson arrivals (mean `rate` per s),
+    a frac_1p / (1 - frac_1p) mix of 1p (darcy_1p) and 2p (dnapl_2p) problems, cell
+    counts log-uniform in [n_min, n_max] on cube-like 3D grids (round(N^(1/3)) cells per
+    axis, at least 10), seeded ln K fields (sigma ~ U[0.5, 2], correlation length
+    ~ U[3, 10] cells), 1..20 implicit-Euler steps of `dt` each.
+    Returns a list of dicts with arrival time, kind, desc, u0, dt and t_end (sorted by
+    arrival).  Problems are built lazily by make() so that a long stream stays cheap."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    reqs = []
+    for i in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        kind = "1p" if rng.uniform() < frac_1p else "2p"
+        n_cells = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        n = max(10, int(round(n_cells ** (1.0 / 3.0))))
+        sigma = float(rng.uniform(0.5, 2.0))
+        corr = float(rng.uniform(3.0, 10.0))
+        nsteps = int(rng.integers(steps[0], steps[1] + 1))
+        inflow = float(rng.uniform(0.01, 0.08))
+        reqs.append({"index": i, "arrival": t, "kind": kind, "cells": (n, n, n), "sigma": sigma, "corr_len": corr,
+                     "steps": nsteps, "dt": dt, "t_end": nsteps * dt, "inflow": inflow, "seed": 5000 + seed + i})
+    return reqs
+
+
+def make_request_problem(req):
+    """(desc, u0) of one served request from served_requests()."""
+    if req["kind"] == "1p":
+        return darcy_1p(cells=req["cells"], seed=req["seed"], sigma=req["sigma"], corr_len=req["corr_len"])
+    return dnapl_2p(cells=req["cells"], seed=req["seed"], sigma=req["sigma"], corr_len=req["corr_len"],
+                    inflow=req["inflow"])

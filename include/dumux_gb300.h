@@ -34,7 +34,8 @@ enum {
     DXG_ERR_NEWTON_NOT_CONVERGED = 8, /* Newton failed after all dt divisions         */
     DXG_ERR_TIMEOUT = 9,         /* a bounded device-side wait gave up                */
     DXG_ERR_NO_DEVICE = 10,      /* no CUDA device / extension built without GPU      */
-    DXG_ERR_SIZE = 11            /* input larger than a fixed capacity                */
+    DXG_ERR_SIZE = 11,           /* input larger than a fixed capacity                */
+    DXG_ERR_BUDGET = 12          /* admission would exceed the device-memory budget   */
 };
 
 /* ---- problem description (tabulated Problem + SpatialParams) ------------------
@@ -95,9 +96,12 @@ int dxg_ctx_destroy(dxg_ctx* ctx);
  * failed dxg_ctx_create when ctx == NULL). */
 const char* dxg_last_error(const dxg_ctx* ctx);
 
-/* Precision of the linear system: FP64 everywhere (the plain drop-in), or the
- * mixed form (FP32 Jacobian / ILU(0) / inner BiCGSTAB inside an FP64 residual,
- * FP64 numeric differentiation, update and norms).  Must be set before upload. */
+/* Precision of the linear solve: FP64 everywhere (the plain drop-in), or the mixed
+ * form: an FP32 copy of the Jacobian, FP32 ILU(0) factors and FP32 triangular sweeps
+ * as the preconditioner of a BiCGSTAB whose vectors, dots and SpMV stay FP64 on the
+ * FP64 Jacobian (the preconditioner is applied to FP32 copies of p and r and its
+ * result widened back), inside the FP64 residual, numeric differentiation, Newton
+ * update and norms.  Must be set before upload. */
 enum { DXG_PRECISION_FP64 = 0, DXG_PRECISION_MIXED = 1 };
 int dxg_set_precision(dxg_ctx* ctx, int precision);
 
@@ -252,6 +256,79 @@ int dxg_norm2_noalloc(const double* x, int64_t n, double* result, void* stream);
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */
 int dxg_sync(dxg_ctx* ctx);
+
+/* ---- batched and served forms -----------------------------------------------------------
+ * A dxg_batch advances many independent problems together.  Each admitted problem
+ * keeps its whole state (tables, solution, Jacobian, factors, Krylov vectors) in
+ * device memory until it is removed.  One call of dxg_batch_iterate is one tick:
+ * problems that start a Newton iteration are assembled and their ILU(0) factors
+ * computed, every active problem then runs 8 BiCGSTAB iterations, and problems whose
+ * linear solve ended take the Newton update and convergence test.  Problems of the
+ * same kind (num_eq, dim, difference method, gravity, transient) share each kernel
+ * launch, one launch per kernel for all of them, with one thread-block cluster per
+ * problem in the ILU(0) sweeps; a slow problem does not hold up the others.  Between
+ * iterations each problem follows its own time loop: a converged time step advances
+ * it (TimeLoop::advanceTimeStep + NewtonSolver::suggestTimeStepSize, capped at the
+ * problem's dt), a failed one restarts from the previous time level with dt times
+ * retry_time_step_reduction (NewtonSolver::solve, dumux/nonlinear/newtonsolver.hh:
+ * 309-382).  Problems may be added between iterations (continuous batching); the
+ * arithmetic of a problem does not depend on what else is in the batch.
+ * The reference runs such ensembles as separate processes; these entry points have
+ * no counterpart there.                                                                   */
+typedef struct dxg_batch dxg_batch;
+
+typedef struct dxg_batch_problem_info {
+    int32_t state;               /* 0 active, 1 finished, 2 failed                     */
+    int32_t status;              /* DXG_OK or the status that ended a failed problem   */
+    int32_t time_steps;          /* accepted time steps                                */
+    int32_t time_step_divisions; /* dt reductions after failed Newton solves           */
+    int64_t newton_iterations;   /* all Newton iterations, including wasted ones       */
+    int64_t linear_iterations;   /* BiCGSTAB iterations                                */
+    int64_t cells;
+    double time;                 /* simulated time reached                             */
+    double seconds_admitted;     /* engine clock (s since dxg_batch_create) at admission */
+    double seconds_finished;     /* engine clock when it finished or failed, else -1   */
+} dxg_batch_problem_info;
+
+enum { DXG_BATCH_OPT_GRAPHS = 0, DXG_BATCH_OPT_AUTOTUNE = 1 };
+
+int dxg_batch_create(dxg_batch** out, int device, int precision);
+int dxg_batch_destroy(dxg_batch* batch);
+const char* dxg_batch_last_error(const dxg_batch* batch);
+/* DXG_BATCH_OPT_GRAPHS: replay the BiCGSTAB iterations of a solve from one captured
+ * CUDA graph (default 1).  DXG_BATCH_OPT_AUTOTUNE: choose the cluster size, threads
+ * and prefetch depth of the batched ILU(0) sweeps by timing candidates on the first
+ * solve of each batch shape (default 1; 0 uses a fixed rule). */
+int dxg_batch_set_option(dxg_batch* batch, int option, int value);
+/* Device memory that admitting this problem takes (tables and all solver state). */
+int64_t dxg_problem_device_bytes(const dxg_problem_desc* desc, int precision);
+/* Admission limit on the device memory of all admitted problems (0: unlimited).
+ * dxg_batch_add refuses with DXG_ERR_BUDGET a problem that would exceed it. */
+int dxg_batch_set_memory_budget(dxg_batch* batch, int64_t bytes);
+int64_t dxg_batch_device_bytes(const dxg_batch* batch);
+/* Admit a problem: initial solution u0 (N*num_eq values, also the first previous
+ * time level), time step dt and end time t_end (t_end <= 0: one stationary Newton
+ * solve), Newton and linear-solver parameters (NULL: defaults).  *id receives its
+ * handle. */
+int dxg_batch_add(dxg_batch* batch, const dxg_problem_desc* desc, const double* u0, double dt, double t_end,
+                  const dxg_newton_params* params, int64_t* id);
+/* One tick (see above); *active receives the number of problems still active. */
+int dxg_batch_iterate(dxg_batch* batch, int32_t* active);
+/* Iterates until no problem is active. */
+int dxg_batch_run(dxg_batch* batch);
+int dxg_batch_info(const dxg_batch* batch, int64_t id, dxg_batch_problem_info* info);
+int dxg_batch_get_solution(dxg_batch* batch, int64_t id, double* u);
+/* Frees the device memory of a problem (any state). */
+int dxg_batch_remove(dxg_batch* batch, int64_t id);
+/* Kernel launches issued by the batch (graph replays count each kernel node). */
+int64_t dxg_batch_launch_count(const dxg_batch* batch);
+/* Per-kernel-class event timing of the batched launches (as dxg_set_kernel_timing;
+ * bytes summed over the problems of each launch).  While it is on, BiCGSTAB
+ * iterations are launched directly instead of from a captured graph. */
+int dxg_batch_set_kernel_timing(dxg_batch* batch, int enable);
+int dxg_batch_get_kernel_timing(dxg_batch* batch, int kernel_class, int64_t* launches, double* total_ms,
+                                double* bytes);
+void* dxg_batch_stream(const dxg_batch* batch);
 
 #ifdef __cplusplus
 }

@@ -42,3 +42,34 @@ def test_boundary_face_count(gpu_lib):
     d = desc.c
     gpu_lib.dxg_num_boundary_faces.restype = C.c_int64
     assert gpu_lib.dxg_num_boundary_faces(C.byref(d)) == num_boundary_faces(3, [5, 4, 3]) == 2 * (12 + 15 + 20)
+
+
+def test_batch_creation_fails_loudly_without_gpu(gpu_lib):
+    import dumux_gb300
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = os.path.exists("/dev/nvidia0")
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(dumux_gb300.DxgError) as e:
+        dumux_gb300.Batch()
+    assert e.value.status == 10   # DXG_ERR_NO_DEVICE
+
+
+def test_problem_device_bytes_scales_with_cells(gpu_lib):
+    """Admission sizes: host-only arithmetic, ~linear in cells; the mixed form holds FP32
+    copies of the Jacobian and factors beside the FP64 Jacobian and Krylov vectors."""
+    from dumux_gb300 import problem_device_bytes, problems
+    small, _ = problems.dnapl_2p(cells=(8, 8, 8))
+    large, _ = problems.dnapl_2p(cells=(16, 16, 16))
+    one_p, _ = problems.darcy_1p(cells=(20, 20))
+    s_mixed = problem_device_bytes(small, "mixed")
+    l_mixed = problem_device_bytes(large, "mixed")
+    assert s_mixed > problem_device_bytes(small, "fp64") > 0
+    assert 6.0 < (l_mixed - 64 * 1024) / (s_mixed - 64 * 1024) < 8.5
+    # 2p cells need more state than 1p cells
+    assert problem_device_bytes(one_p, "mixed") < s_mixed
+    # at least the Jacobian (7 blocks of 2x2 doubles) per cell
+    assert s_mixed > 512 * 7 * 4 * 8
