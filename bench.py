@@ -50,6 +50,7 @@ def parse():
                          "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching")
     ap.add_argument("--problems", type=int, default=256, help="ensemble size")
     ap.add_argument("--requests", type=int, default=48, help="served-stream length")
+    ap.add_argument("--ticks-per-step", type=int, default=25, help="ensemble: engine ticks per timed step")
     ap.add_argument("--plain-sample", type=int, default=8,
                     help="problems / requests of the workload also run alone on the plain FP64 path")
     return ap.parse_args()
@@ -282,7 +283,11 @@ def batch_roofline(batch):
 
 def run_ensemble(args):
     """Batched ensemble: `--problems` independent 2p problems (uneven grids 16..64 per
-    axis, own ln K fields and inflow rates) advanced together by one dxg_batch."""
+    axis, own ln K fields and inflow rates) resident together in one dxg_batch.
+    Steady-state throughput: every problem keeps time-stepping (no end time inside the
+    run), a step is `--ticks-per-step` engine ticks (each: one chunk of 8 BiCGSTAB
+    iterations for every problem, plus the assemblies and updates of the problems whose
+    Newton iteration starts or ends in it)."""
     rank, world, local = dist_info()
     import torch
     if world > 1:
@@ -294,6 +299,8 @@ def run_ensemble(args):
     from dumux_gb300.abi import newton_params
     params = newton_params()
     dt = args.dt
+    T = args.ticks_per_step
+    t_end = 1e12                   # problems keep stepping through the whole run
     probs = problems.ensemble_2p(count=args.problems, seed=4 + 100003 * rank)
     cells_total = sum(d.num_cells for d, _, _ in probs)
 
@@ -301,16 +308,17 @@ def run_ensemble(args):
         if world > 1:
             torch.distributed.barrier()
 
+    def ticks(b, n):
+        for _ in range(n):
+            b.iterate()
+
     batch = dumux_gb300.Batch(device=local, precision=args.precision)
-    t_end = (args.warmup + args.steps + 1) * dt
     ids = [batch.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
     cells_of = {pid: d.num_cells for pid, (d, _, _) in zip(ids, probs)}
-    # warm-up: every problem completes `warmup` time steps (includes the sweep autotuning)
-    while min(batch.info(i)["time_steps"] for i in ids) < args.warmup:
-        batch.iterate()
-    # kernel-class timing: one Newton iteration with events around the batched launches
+    ticks(batch, args.warmup * T)            # includes the sweep autotuning
+    # kernel-class timing over one step's ticks (events around the batched launches)
     batch.set_kernel_timing(True)
-    batch.iterate()
+    ticks(batch, T)
     kernels, roofline = batch_roofline(batch)
     batch.set_kernel_timing(False)
 
@@ -324,9 +332,7 @@ def run_ensemble(args):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    iterations = 0
-    while batch.iterate() > 0:
-        iterations += 1
+    ticks(batch, args.steps * T)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -334,9 +340,11 @@ def run_ensemble(args):
     sec = ev0.elapsed_time(ev1) / 1e3
     launches = batch.kernel_launches() - launches0
     after = {i: batch.info(i) for i in ids}
-    failed = sum(1 for i in ids if after[i]["state"] != "finished")
+    failed = sum(1 for i in ids if after[i]["state"] == "failed")
     work = sum(cells_of[i] * (after[i]["newton_iterations"] - before[i]["newton_iterations"]) for i in ids)
     solves = sum(after[i]["time_steps"] - before[i]["time_steps"] for i in ids)
+    lin = sum(after[i]["linear_iterations"] - before[i]["linear_iterations"] for i in ids)
+    newton = sum(after[i]["newton_iterations"] - before[i]["newton_iterations"] for i in ids)
     if world > 1:
         t = torch.tensor([sec, float(work), float(solves)], device=f"cuda:{local}", dtype=torch.float64)
         mx = t.clone()
@@ -345,19 +353,22 @@ def run_ensemble(args):
         sec, work, solves = float(mx[0]), float(t[1]), float(t[2])
     batch.close()
 
-    # ---- end to end through the C ABI: admit (tabulate + h2d), solve K steps, read back
+    # ---- end to end through the C ABI: admit (tabulation + h2d), then per step T ticks
+    # and the read-back of every problem's solution
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b2 = dumux_gb300.Batch(device=local, precision=args.precision)
-    ids2 = [b2.add(d, u0, dt=dt, t_end=args.steps * dt, params=params) for d, u0, _ in probs]
-    b2.run()
-    sols = [b2.solution(i) for i in ids2]
+    ids2 = [b2.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
+    d2h = 0
+    for _ in range(args.steps):
+        ticks(b2, T)
+        for i in ids2:
+            d2h += b2.solution(i).size * 8
     e2e_sec = time.perf_counter() - t0
     e2e_work = sum(d.num_cells * b2.info(i)["newton_iterations"] for i, (d, _, _) in zip(ids2, probs))
     b2.close()
     h2d = sum(d.num_dofs * 8 + d.num_cells * 16 + d.bc_type.size + d.bc_values.size * 8 for d, _, _ in probs)
-    d2h = sum(s.size * 8 for s in sols)
     if world > 1:
         t = torch.tensor([e2e_sec, float(e2e_work)], device=f"cuda:{local}", dtype=torch.float64)
         mx = t.clone()
@@ -366,7 +377,8 @@ def run_ensemble(args):
         e2e_sec, e2e_work = float(mx[0]), float(t[1])
     e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(d2h / args.steps),
-           "note": "fresh batch: admission (tabulation + upload) + all time steps + solution read-back"}
+           "note": "fresh batch: admission of every problem (tabulation + upload) and, per step, "
+                   f"{T} ticks and the read-back of all solutions"}
 
     value = work / sec
     line = {
@@ -378,10 +390,11 @@ def run_ensemble(args):
                                f"16..64 cells per axis (uniform integers), sigma U[0.5,2], corr. length U[3,10] "
                                f"cells, inflow U[0.01,0.08] kg/m^2/s, dt=250 s, {args.precision} precision",
                    "problems": args.problems, "cells_total": int(cells_total), "global_batch": world,
-                   "engine_iterations": iterations, "failed_problems": failed,
+                   "ticks_per_step": T, "newton_iterations": newton, "linear_iterations": lin,
+                   "failed_problems": failed,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, one batched launch per kernel",
-                   "l2": f"inputs larger than L2 (device working set {cells_total * 0.9e-6:.0f} MB+)",
-                   "step": "each problem's next implicit-Euler time step (problems advance independently)"},
+                   "l2": "inputs larger than L2 (all problems resident, GBs of state)",
+                   "step": f"{T} engine ticks with every problem resident and time-stepping"},
         "ensemble_solves_per_s": solves / sec,
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
