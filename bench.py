@@ -399,18 +399,20 @@ def run_ensemble(args):
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
     if rank == 0:
-        sample = probs[::max(1, len(probs) // max(1, args.plain_sample))][:args.plain_sample]
-        plain, _ = plain_fp64_alone([(d, u0, dt, dt) for d, u0, _ in sample], params, local)
-        line["plain_fp64_same_problems"] = {
-            "value": plain, "unit": UNIT, "sample": f"{len(sample)} of the problems, first time step each, "
-                                                     "alone through one FP64 context",
-            "speedup_of_batched": value / plain}
-        desc0, u00, _ = probs[0]
-        rate, sec_cpu, n_cpu = cpu_sample(desc0, u00, dt, args.cpu_sample_iters)
-        import oracle
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
-                                "sample": f"problem 0 ({desc0.num_cells} cells): first {n_cpu} Newton iterations "
-                                          f"of its first time step ({sec_cpu:.1f} s)"}
+        if args.plain_sample > 0:
+            sample = probs[::max(1, len(probs) // args.plain_sample)][:args.plain_sample]
+            plain, _ = plain_fp64_alone([(d, u0, dt, dt) for d, u0, _ in sample], params, local)
+            line["plain_fp64_same_problems"] = {
+                "value": plain, "unit": UNIT, "sample": f"{len(sample)} of the problems, first time step each, "
+                                                         "alone through one FP64 context",
+                "speedup_of_batched": value / plain}
+        if args.cpu_sample_iters > 0:
+            desc0, u00, _ = probs[0]
+            rate, sec_cpu, n_cpu = cpu_sample(desc0, u00, dt, args.cpu_sample_iters)
+            import oracle
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
+                                    "sample": f"problem 0 ({desc0.num_cells} cells): first {n_cpu} Newton "
+                                              f"iterations of its first time step ({sec_cpu:.1f} s)"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -467,8 +469,8 @@ def run_serve(args):
                         "solve, release"},
         "gpu_launches": int(launches), "clocks": clocks,
     }
-    if rank == 0:
-        sample = reqs[::max(1, len(reqs) // max(1, args.plain_sample))][:args.plain_sample]
+    if rank == 0 and args.plain_sample > 0:
+        sample = reqs[::max(1, len(reqs) // args.plain_sample)][:args.plain_sample]
         items = [(built[r["index"]][0], built[r["index"]][1], r["dt"], r["t_end"]) for r in sample]
         plain, service = plain_fp64_alone(items, params, local)
         served_lat = {r["index"]: rec["latency"] for rec in records for r in sample if rec["index"] == r["index"]}
@@ -478,6 +480,7 @@ def run_serve(args):
             "service_s": stats_of(service), "solves_per_s_sequential": len(service) / sum(service),
             "served_latency_of_same_requests_s": stats_of(list(served_lat.values())),
             "speedup_of_served": st["cell_newton_steps_per_s"] / plain}
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -542,6 +542,7 @@ struct GroupState {
     const void* dFwR = nullptr;
     const void* dBw = nullptr;
     const ToDoubleArgs* dTd = nullptr;
+    BlockMap mapM, mapN;     // vector kernels over N*b entries, SpMV over N cells
     int64_t maxN = 1, maxM = 1;
     double sweepBytes = 0, spmvBytes = 0;
     cudaGraphExec_t exec = nullptr;
@@ -613,9 +614,18 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
                                c->ks.get());
         td[k] = {c->fy.get(), c->ky.get(), c->M};
     }
+    std::vector<int64_t> lenM, lenN;
+    for (Slot* s : S) {
+        lenM.push_back(s->c->M);
+        lenN.push_back(s->c->N);
+    }
+    std::vector<uint2> mM, mN;
+    buildBlockMap(lenM, false, mM);
+    buildBlockMap(lenN, true, mN);
     std::vector<unsigned char> host;
     const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oP = pack(host, fwP),
-                 oR = pack(host, fwR), oW = pack(host, bw), oT = pack(host, td);
+                 oR = pack(host, fwR), oW = pack(host, bw), oT = pack(host, td), oM = pack(host, mM),
+                 oN = pack(host, mN);
     G.args.alloc(host.size());
     DXG_CUDA(cudaMemcpy(G.args.get(), host.data(), host.size(), cudaMemcpyHostToDevice));
     unsigned char* d = G.args.get();
@@ -626,6 +636,8 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.dFwR = d + oR;
     G.dBw = d + oW;
     G.dTd = reinterpret_cast<const ToDoubleArgs*>(d + oT);
+    G.mapM = {reinterpret_cast<const uint2*>(d + oM), (unsigned)mM.size()};
+    G.mapN = {reinterpret_cast<const uint2*>(d + oN), (unsigned)mN.size()};
     return G;
 }
 
@@ -643,23 +655,23 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
             TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
             launchWaveApplyBatch<PT>(G.plan, fw, bw, n, dim, b, st);
         }
-        if (mixed) launchToDoubleBatch(G.dTd, n, G.maxM, st);
+        if (mixed) launchToDoubleBatch(G.dTd, G.mapM, st);
     };
     for (int it = 0; it < kChunk; ++it) {
-        launchBicgRhoBatch<double>(G.dBicg, n, G.maxM, st);
-        launchBicgUpdatePBatch<double>(G.dBicg, n, G.maxM, st);
+        launchBicgRhoBatch<double>(G.dBicg, G.mapM, st);
+        launchBicgUpdatePBatch<double>(G.dBicg, G.mapM, st);
         precondition(fwP);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<double, double>(G.dSv1, n, G.maxN, b, dim, 1, st);
+            launchSpmvBatch<double, double>(G.dSv1, G.mapN, b, dim, 1, st);
         }
-        launchBicgAxpyNormBatch<double>(G.dBicg, n, G.maxM, 0, st);
+        launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 0, st);
         precondition(fwR);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<double, double>(G.dSv2, n, G.maxN, b, dim, 2, st);
+            launchSpmvBatch<double, double>(G.dSv2, G.mapN, b, dim, 2, st);
         }
-        launchBicgAxpyNormBatch<double>(G.dBicg, n, G.maxM, 1, st);
+        launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 1, st);
     }
 }
 
@@ -798,7 +810,11 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
     clearFlagsKernel<<<(n + 127) / 128, 128, 0, st>>>(B->arena.put(fl, st), n);
     DXG_CUDA(cudaGetLastError());
     launchWaveFactorBatch<PT>(G.plan, B->arena.put(fa, st), n, dim, b, st);
-    launchBicgInitBatch<double>(B->arena.put(bi, st), n, maxM, st);
+    std::vector<int64_t> lenM;
+    for (Slot* s : A) lenM.push_back(s->c->M);
+    std::vector<uint2> mM;
+    buildBlockMap(lenM, false, mM);
+    launchBicgInitBatch<double>(B->arena.put(bi, st), BlockMap{B->arena.put(mM, st), (unsigned)mM.size()}, st);
     B->launches += 5;
     for (Slot* s : A) {
         s->solving = true;
@@ -845,7 +861,11 @@ void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
         for (Slot* s : U)
             ua.push_back({s->c->u.get(), s->c->kx.get(), s->c->u.get(), 1.0, s->c->M, s->c->scratch(),
                           s->c->scal.get()});
-        launchNewtonUpdateBatch(B->arena.put(ua, st), (int)U.size(), maxDofs(U), st);
+        std::vector<int64_t> lenM;
+        for (Slot* s : U) lenM.push_back(s->c->M);
+        std::vector<uint2> mM;
+        buildBlockMap(lenM, false, mM);
+        launchNewtonUpdateBatch(B->arena.put(ua, st), BlockMap{B->arena.put(mM, st), (unsigned)mM.size()}, st);
         B->launches += 1;
         gather(B, U);
     }

@@ -59,26 +59,50 @@ __device__ __forceinline__ void blockSum(double (&v)[NV])
     }
 }
 
-// Blocks a reduction over M entries uses (host: reduceBlocks).
+// Blocks a vector kernel over M entries uses (host: reduceBlocks): kReducePerThread
+// entries per thread, at most kMaxReduceBlocks blocks.
 __host__ __device__ __forceinline__ int reduceBlocksFor(int64_t M)
 {
-    int64_t b = (M + kReduceThreads - 1) / kReduceThreads;
+    int64_t b = (M + kReduceThreads * kReducePerThread - 1) / (kReduceThreads * kReducePerThread);
     if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
     if (b < 1) b = 1;
     return (int)b;
+}
+// Blocks of the SpMV over N cells: one cell per thread, at most kMaxReduceBlocks blocks.
+__host__ __device__ __forceinline__ int cellBlocksFor(int64_t N)
+{
+    int64_t b = (N + kReduceThreads - 1) / kReduceThreads;
+    if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// The problem and problem-local block of this block: single launch (a0), batched
+// launch with blockIdx.y = problem, or batched launch through a block map.
+template <class ARGT>
+__device__ __forceinline__ ARGT problemOf(const ARGT& a0, const ARGT* batch, const uint2* map, unsigned& lb)
+{
+    if (map) {
+        const uint2 m = map[blockIdx.x];
+        lb = m.y;
+        return batch[m.x];
+    }
+    lb = blockIdx.x;
+    return batch ? batch[blockIdx.y] : a0;
 }
 
 // Writes this block's partials; returns true in thread 0 of the last of the nblk
 // participating blocks to finish, which then holds the totals (summed in block
 // order) in v.
 template <int NV>
-__device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsigned* counter, unsigned nblk)
+__device__ __forceinline__ bool gridSum(double (&v)[NV], double* partials, unsigned* counter, unsigned nblk,
+                                        unsigned lb)
 {
     blockSum<NV>(v);
     __shared__ bool amLast;
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) partials[k * kMaxReduceBlocks + blockIdx.x] = v[k];
+        for (int k = 0; k < NV; ++k) partials[k * kMaxReduceBlocks + lb] = v[k];
         __threadfence();
         const unsigned t = atomicAdd(counter, 1u);
         amLast = (t == nblk - 1);
@@ -144,16 +168,18 @@ __device__ __forceinline__ bool slotValid(unsigned mask, int dim, int s)
 // ---------------------------------------------------------------- SpMV
 // y = A x; MODE 0: plain; MODE 1: also dot(w, y) -> h, alpha; MODE 2: dots (y,w),(y,y) -> omega
 template <int B, int DIM, class MT, class VT, int MODE>
-__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0, const SpmvArgs<MT, VT>* batch)
+__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0, const SpmvArgs<MT, VT>* batch,
+                                                              const uint2* map)
 {
-    const SpmvArgs<MT, VT> a = batch ? batch[blockIdx.y] : a0;
-    const unsigned nblk = reduceBlocksFor(a.N);
-    if (blockIdx.x >= nblk) return;
+    unsigned lb;
+    const SpmvArgs<MT, VT> a = problemOf(a0, batch, map, lb);
+    const unsigned nblk = cellBlocksFor(a.N);
+    if (lb >= nblk) return;
     if (a.ks && a.ks->status != KS_RUNNING) return;
     constexpr int S = 2 * DIM + 1;
     constexpr int BB = B * B;
     double part[2] = {0.0, 0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
+    for (int64_t i = lb * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
         const unsigned m = a.nbmask[i];
         VT acc[B];
 #pragma unroll
@@ -183,7 +209,7 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0
         }
     }
     if (MODE == 0) return;
-    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE, nblk)) {
+    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE, nblk, lb)) {
         KrylovState& ks = *a.ks;
         if (MODE == 1) {
             ks.h = part[0];
@@ -335,20 +361,23 @@ __global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
 }
 
 // ---------------------------------------------------------------- BiCGSTAB vector kernels
-// Each kernel takes a single argument block, or (batch != nullptr) one per problem
-// selected by blockIdx.y; a problem's blocks are the first reduceBlocksFor(M) of the row.
-#define DXG_PROBLEM_BLOCKS(ARGT)                                  \
-    const ARGT a = batch ? batch[blockIdx.y] : a0;                \
-    const unsigned nblk = reduceBlocksFor(a.M);                   \
-    if (blockIdx.x >= nblk) return;                               \
-    const int64_t stride = (int64_t)nblk * blockDim.x;
+// Each kernel takes a single argument block, or (batch != nullptr) one per problem,
+// selected by blockIdx.y or by a block map; a problem always works with its own
+// reduceBlocksFor(M) blocks, as in a single launch.
+#define DXG_PROBLEM_BLOCKS(ARGT, LEN)                             \
+    unsigned lb;                                                  \
+    const ARGT a = problemOf(a0, batch, map, lb);                 \
+    const unsigned nblk = reduceBlocksFor(a.LEN);                 \
+    if (lb >= nblk) return;                                       \
+    const int64_t stride = (int64_t)nblk * blockDim.x;            \
+    const int64_t k0 = lb * (int64_t)blockDim.x + threadIdx.x;
 
 template <class VT>
-__global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
+__global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>, M)
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+    for (int64_t k = k0; k < a.M; k += stride) {
         const VT rv = (VT)a.rhs[k];
         a.r[k] = rv;
         a.rt[k] = rv;
@@ -357,7 +386,7 @@ __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, cons
         a.v[k] = 0;
         part[0] += (double)rv * (double)rv;
     }
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 4, nblk)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 4, nblk, lb)) {
         KrylovState& ks = *a.ks;
         if (a.maxHalf > 0) {
             ks.reduction = a.reduction;
@@ -374,14 +403,14 @@ __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, cons
 
 // rho_new = <rt, r>, breakdown checks and beta (first half of an iteration)
 template <class VT>
-__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
+__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>, M)
     if (a.ks->status != KS_RUNNING) return;
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride)
+    for (int64_t k = k0; k < a.M; k += stride)
         part[0] += (double)a.rt[k] * (double)a.r[k];
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5, nblk)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5, nblk, lb)) {
         KrylovState& ks = *a.ks;
         if (ks.halfsteps + 1 >= ks.maxHalf) { ks.status = KS_MAXIT; return; }
         ks.rho_new = part[0];
@@ -392,14 +421,14 @@ __global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a0, const
 
 // p = r (first iteration) or p = (p - omega v) * beta + r
 template <class VT>
-__global__ void bicgUpdateP(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
+__global__ void bicgUpdateP(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>, M)
     const KrylovState& ks = *a.ks;
     if (ks.status != KS_RUNNING) return;
     const bool first = ks.halfsteps == 0;
     const VT omega = (VT)ks.omega, beta = (VT)ks.beta;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+    for (int64_t k = k0; k < a.M; k += stride) {
         VT pk;
         if (first) pk = a.r[k];
         else {
@@ -415,9 +444,9 @@ __global__ void bicgUpdateP(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
 
 // x += s*y; r -= s*q; def = ||r||; STAGE 0: s = alpha, q = v; STAGE 1: s = omega, q = t
 template <class VT, int STAGE>
-__global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, const BicgArgs<VT>* batch)
+__global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(BicgArgs<VT>)
+    DXG_PROBLEM_BLOCKS(BicgArgs<VT>, M)
     const KrylovState& ksr = *a.ks;
     if (ksr.status != KS_RUNNING) return;
     const double sd = STAGE == 0 ? ksr.alpha : ksr.omega;
@@ -425,14 +454,14 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, 
     const VT* q = STAGE == 0 ? a.v : a.t;
     double part[1] = {0.0};
     float* rLow = STAGE == 0 ? a.rLow : nullptr;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+    for (int64_t k = k0; k < a.M; k += stride) {
         a.x[k] += s * a.y[k];
         const VT rk = a.r[k] + (-s) * q[k];
         a.r[k] = rk;
         if (rLow) rLow[k] = (float)rk;
         part[0] += (double)rk * (double)rk;
     }
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6, nblk)) {
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6, nblk, lb)) {
         KrylovState& ks = *a.ks;
         ks.def = sqrt(part[0]);
         ks.halfsteps += 1;
@@ -445,11 +474,11 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, 
 // ---------------------------------------------------------------- Newton helpers
 // u = uLast - lambda*delta (uLast keeps the iterate), shift = max relative shift
 // (maxRelativeShift, dumux/nonlinear/newtonsolver.hh:110-128)
-__global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(NewtonUpdArgs a0, const NewtonUpdArgs* batch)
+__global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(NewtonUpdArgs a0, const NewtonUpdArgs* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(NewtonUpdArgs)
+    DXG_PROBLEM_BLOCKS(NewtonUpdArgs, M)
     double mx = 0.0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride) {
+    for (int64_t k = k0; k < a.M; k += stride) {
         const double x = a.uLast[k];
         const double y = x + (-a.lambda) * a.delta[k];
         a.u[k] = y;
@@ -468,7 +497,7 @@ __global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(NewtonUpdAr
     if (threadIdx.x == 0) {
         double bm = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) bm = fmax(bm, sh[k]);
-        partials[blockIdx.x] = bm;
+        partials[lb] = bm;
         __threadfence();
         amLast = atomicAdd(counter, 1u) == nblk - 1;
     }
@@ -482,13 +511,13 @@ __global__ void __launch_bounds__(kReduceThreads) newtonUpdateKernel(NewtonUpdAr
     }
 }
 
-__global__ void __launch_bounds__(kReduceThreads) norm2Kernel(NormArgs a0, const NormArgs* batch)
+__global__ void __launch_bounds__(kReduceThreads) norm2Kernel(NormArgs a0, const NormArgs* batch, const uint2* map)
 {
-    DXG_PROBLEM_BLOCKS(NormArgs)
+    DXG_PROBLEM_BLOCKS(NormArgs, M)
     double part[1] = {0.0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.M; k += stride)
+    for (int64_t k = k0; k < a.M; k += stride)
         part[0] += a.x[k] * a.x[k];
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 3, nblk)) *a.out = sqrt(part[0]);
+    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 3, nblk, lb)) *a.out = sqrt(part[0]);
 }
 
 template <class VT>
@@ -505,11 +534,10 @@ __global__ void toFloatKernel(ToFloatArgs a0, const ToFloatArgs* batch)
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
         a.dst[k] = (float)a.src[k];
 }
-__global__ void toDoubleKernel(ToDoubleArgs a0, const ToDoubleArgs* batch)
+__global__ void toDoubleKernel(ToDoubleArgs a0, const ToDoubleArgs* batch, const uint2* map)
 {
-    const ToDoubleArgs a = batch ? batch[blockIdx.y] : a0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x)
-        a.dst[k] = (double)a.src[k];
+    DXG_PROBLEM_BLOCKS(ToDoubleArgs, n)
+    for (int64_t k = k0; k < a.n; k += stride) a.dst[k] = (double)a.src[k];
 }
 __global__ void accumKernel(AccumArgs a0, const AccumArgs* batch)
 {
@@ -545,6 +573,16 @@ __global__ void defectKernel(DefectArgs a0, const DefectArgs* batch)
 
 // ---------------------------------------------------------------- host launchers
 int reduceBlocks(int64_t M) { return reduceBlocksFor(M); }
+int cellBlocks(int64_t N) { return cellBlocksFor(N); }
+
+void buildBlockMap(const std::vector<int64_t>& lengths, bool cells, std::vector<uint2>& out)
+{
+    out.clear();
+    for (size_t p = 0; p < lengths.size(); ++p) {
+        const int nb = cells ? cellBlocksFor(lengths[p]) : reduceBlocksFor(lengths[p]);
+        for (int j = 0; j < nb; ++j) out.push_back(make_uint2((unsigned)p, (unsigned)j));
+    }
+}
 
 // grid of a batched grid-stride launch: x covers the largest problem (capped), y = problems
 static dim3 batchGrid(int64_t maxN, int count, int threads, int cap)
@@ -554,34 +592,39 @@ static dim3 batchGrid(int64_t maxN, int count, int threads, int cap)
     if (gx < 1) gx = 1;
     return dim3((unsigned)gx, (unsigned)count);
 }
-static dim3 reduceGrid(int64_t maxM, int count) { return dim3((unsigned)reduceBlocksFor(maxM), (unsigned)count); }
 
 template <int B, int DIM, class MT, class VT>
-static void spmvT(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, dim3 g, int mode, cudaStream_t st)
+static void spmvT(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, const uint2* map, dim3 g, int mode,
+                  cudaStream_t st)
 {
-    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a, batch);
-    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a, batch);
-    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a, batch);
+    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a, batch, map);
 }
 template <class MT, class VT>
-static void spmvDispatch(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, dim3 g, int b, int dim, int mode,
-                         cudaStream_t st)
+static void spmvDispatch(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, const uint2* map, dim3 g, int b,
+                         int dim, int mode, cudaStream_t st)
 {
-    if (b == 1) { if (dim == 2) spmvT<1, 2>(a, batch, g, mode, st); else spmvT<1, 3>(a, batch, g, mode, st); }
-    else { if (dim == 2) spmvT<2, 2>(a, batch, g, mode, st); else spmvT<2, 3>(a, batch, g, mode, st); }
+    if (b == 1) {
+        if (dim == 2) spmvT<1, 2>(a, batch, map, g, mode, st);
+        else spmvT<1, 3>(a, batch, map, g, mode, st);
+    } else {
+        if (dim == 2) spmvT<2, 2>(a, batch, map, g, mode, st);
+        else spmvT<2, 3>(a, batch, map, g, mode, st);
+    }
     DXG_CUDA(cudaGetLastError());
 }
 
 template <class MT, class VT>
 void launchSpmv(const SpmvArgs<MT, VT>& a, int b, int dim, int mode, cudaStream_t st)
 {
-    spmvDispatch<MT, VT>(a, nullptr, dim3(reduceBlocks(a.N)), b, dim, mode, st);
+    spmvDispatch<MT, VT>(a, nullptr, nullptr, dim3(cellBlocksFor(a.N)), b, dim, mode, st);
 }
 template <class MT, class VT>
-void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, int count, int64_t maxN, int b, int dim, int mode,
+void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
                      cudaStream_t st)
 {
-    spmvDispatch<MT, VT>(SpmvArgs<MT, VT>{}, batch, reduceGrid(maxN, count), b, dim, mode, st);
+    spmvDispatch<MT, VT>(SpmvArgs<MT, VT>{}, batch, cellMap.map, dim3(cellMap.blocks), b, dim, mode, st);
 }
 
 template <class MT>
@@ -634,46 +677,46 @@ void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st)
 {
     BicgArgs<VT> aa = a;
     aa.rhs = rhs;
-    bicgInit<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(aa, nullptr);
+    bicgInit<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(aa, nullptr, nullptr);
     DXG_CUDA(cudaGetLastError());
 }
 template <class VT>
 void launchBicgRho(const BicgArgs<VT>& a, cudaStream_t st)
 {
-    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
+    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
 }
 template <class VT>
 void launchBicgUpdateP(const BicgArgs<VT>& a, cudaStream_t st)
 {
-    bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
+    bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
 }
 template <class VT>
 void launchBicgAxpyNorm(const BicgArgs<VT>& a, int stage, cudaStream_t st)
 {
-    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
-    else bicgAxpyNorm<VT, 1><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr);
+    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
+    else bicgAxpyNorm<VT, 1><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
 }
 template <class VT>
-void launchBicgInitBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+void launchBicgInitBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStream_t st)
 {
-    bicgInit<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    bicgInit<VT><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
     DXG_CUDA(cudaGetLastError());
 }
 template <class VT>
-void launchBicgRhoBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+void launchBicgRhoBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStream_t st)
 {
-    bicgRho<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    bicgRho<VT><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
 }
 template <class VT>
-void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st)
+void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStream_t st)
 {
-    bicgUpdateP<VT><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    bicgUpdateP<VT><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
 }
 template <class VT>
-void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, int stage, cudaStream_t st)
+void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, const BlockMap& m, int stage, cudaStream_t st)
 {
-    if (stage == 0) bicgAxpyNorm<VT, 0><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
-    else bicgAxpyNorm<VT, 1><<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch);
+    if (stage == 0) bicgAxpyNorm<VT, 0><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
+    else bicgAxpyNorm<VT, 1><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
 }
 template <class VT>
 void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st)
@@ -685,23 +728,23 @@ void launchNewtonUpdate(const double* uLast, const double* delta, double* u, dou
                         const ReduceScratch& sc, double* shiftOut, cudaStream_t st)
 {
     const NewtonUpdArgs a{uLast, delta, u, lambda, M, sc, shiftOut};
-    newtonUpdateKernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr);
+    newtonUpdateKernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
     DXG_CUDA(cudaGetLastError());
 }
-void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, int count, int64_t maxM, cudaStream_t st)
+void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, const BlockMap& m, cudaStream_t st)
 {
-    newtonUpdateKernel<<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(NewtonUpdArgs{}, batch);
+    newtonUpdateKernel<<<m.blocks, kReduceThreads, 0, st>>>(NewtonUpdArgs{}, batch, m.map);
     DXG_CUDA(cudaGetLastError());
 }
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st)
 {
     const NormArgs a{x, M, sc, out};
-    norm2Kernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr);
+    norm2Kernel<<<reduceBlocks(M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
     DXG_CUDA(cudaGetLastError());
 }
-void launchNorm2Batch(const NormArgs* batch, int count, int64_t maxM, cudaStream_t st)
+void launchNorm2Batch(const NormArgs* batch, const BlockMap& m, cudaStream_t st)
 {
-    norm2Kernel<<<reduceGrid(maxM, count), kReduceThreads, 0, st>>>(NormArgs{}, batch);
+    norm2Kernel<<<m.blocks, kReduceThreads, 0, st>>>(NormArgs{}, batch, m.map);
     DXG_CUDA(cudaGetLastError());
 }
 void launchToFloat(const ToFloatArgs& a, cudaStream_t st)
@@ -716,12 +759,12 @@ void launchToFloatBatch(const ToFloatArgs* batch, int count, int64_t maxN, cudaS
 }
 void launchToDouble(const ToDoubleArgs& a, cudaStream_t st)
 {
-    toDoubleKernel<<<reduceBlocks(a.n), kReduceThreads, 0, st>>>(a, nullptr);
+    toDoubleKernel<<<reduceBlocks(a.n), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
     DXG_CUDA(cudaGetLastError());
 }
-void launchToDoubleBatch(const ToDoubleArgs* batch, int count, int64_t maxN, cudaStream_t st)
+void launchToDoubleBatch(const ToDoubleArgs* batch, const BlockMap& m, cudaStream_t st)
 {
-    toDoubleKernel<<<batchGrid(maxN, count, kReduceThreads, 1184), kReduceThreads, 0, st>>>(ToDoubleArgs{}, batch);
+    toDoubleKernel<<<m.blocks, kReduceThreads, 0, st>>>(ToDoubleArgs{}, batch, m.map);
     DXG_CUDA(cudaGetLastError());
 }
 void launchAccum(const AccumArgs& a, cudaStream_t st)
@@ -757,17 +800,18 @@ void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, 
 // explicit instantiations
 template void launchSpmv<double, double>(const SpmvArgs<double, double>&, int, int, int, cudaStream_t);
 template void launchSpmv<float, float>(const SpmvArgs<float, float>&, int, int, int, cudaStream_t);
-template void launchSpmvBatch<double, double>(const SpmvArgs<double, double>*, int, int64_t, int, int, int,
+template void launchSpmvBatch<double, double>(const SpmvArgs<double, double>*, const BlockMap&, int, int, int,
                                               cudaStream_t);
-template void launchSpmvBatch<float, float>(const SpmvArgs<float, float>*, int, int64_t, int, int, int, cudaStream_t);
-template void launchBicgInitBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
-template void launchBicgInitBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
-template void launchBicgRhoBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
-template void launchBicgRhoBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
-template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, int, int64_t, cudaStream_t);
-template void launchBicgUpdatePBatch<float>(const BicgArgs<float>*, int, int64_t, cudaStream_t);
-template void launchBicgAxpyNormBatch<double>(const BicgArgs<double>*, int, int64_t, int, cudaStream_t);
-template void launchBicgAxpyNormBatch<float>(const BicgArgs<float>*, int, int64_t, int, cudaStream_t);
+template void launchSpmvBatch<float, float>(const SpmvArgs<float, float>*, const BlockMap&, int, int, int,
+                                            cudaStream_t);
+template void launchBicgInitBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
+template void launchBicgInitBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
+template void launchBicgRhoBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
+template void launchBicgRhoBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
+template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
+template void launchBicgUpdatePBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
+template void launchBicgAxpyNormBatch<double>(const BicgArgs<double>*, const BlockMap&, int, cudaStream_t);
+template void launchBicgAxpyNormBatch<float>(const BicgArgs<float>*, const BlockMap&, int, cudaStream_t);
 template int64_t launchIluFactor<double>(const IluArgs<double, double>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluFactor<float>(const IluArgs<float, float>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluApply<double, double>(const IluArgs<double, double>&, const LevelSchedule&, int, int,

@@ -54,6 +54,7 @@ struct ReduceScratch {
     unsigned* counter;      // [8]
 };
 constexpr int kReduceThreads = 256;
+constexpr int kReducePerThread = 4;
 constexpr int kMaxReduceBlocks = 1024;
 
 }  // namespace dxg

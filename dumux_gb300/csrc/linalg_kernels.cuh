@@ -1,6 +1,8 @@
 // linalg_kernels.cuh -- argument blocks and launchers of the linear-algebra kernels.
 #pragma once
 
+#include <vector>
+
 #include "linalg.cuh"
 
 namespace dxg {
@@ -113,29 +115,39 @@ void launchNewtonUpdate(const double* uLast, const double* delta, double* u, dou
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st);
 void launchToFloat(const ToFloatArgs& a, cudaStream_t st);
 void launchToDouble(const ToDoubleArgs& a, cudaStream_t st);
-void launchToDoubleBatch(const ToDoubleArgs* batch, int count, int64_t maxN, cudaStream_t st);
 void launchAccum(const AccumArgs& a, cudaStream_t st);
 void launchDefect(const DefectArgs& a, int b, int dim, cudaStream_t st);
 
-// Batched forms: one launch over `count` problems, problem p reading batch[p] (device
-// array, blockIdx.y = p for the grid-stride kernels).  maxM / maxN: the largest vector
-// length / cell count of the batch.  Each problem reduces over its own block count,
-// the one its single-problem launch uses, so batched and single results are identical.
+// Batched forms: one launch over several problems, problem p reading batch[p] (device
+// array).  The vector kernels and the SpMV run through a block map: block k of the
+// grid works on problem map[k].x as that problem's block map[k].y, each problem with
+// exactly the blocks of its single launch (vector kernels: reduceBlocks(M); SpMV:
+// cellBlocks(N)), so batched and single results are identical and no block idles.
+struct BlockMap {
+    const uint2* map = nullptr;   // device array of `blocks` entries
+    unsigned blocks = 0;
+};
+int cellBlocks(int64_t N);
+// Host side of a block map: the entries for problems of the given lengths, blocks
+// per problem from reduceBlocks (cells == false) or cellBlocks (cells == true).
+void buildBlockMap(const std::vector<int64_t>& lengths, bool cells, std::vector<uint2>& out);
+
 template <class MT, class VT>
-void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, int count, int64_t maxN, int b, int dim, int mode,
+void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
                      cudaStream_t st);
 template <class VT>
-void launchBicgInitBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+void launchBicgInitBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
 template <class VT>
-void launchBicgRhoBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+void launchBicgRhoBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
 template <class VT>
-void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, cudaStream_t st);
+void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
 template <class VT>
-void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, int count, int64_t maxM, int stage, cudaStream_t st);
-void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, int count, int64_t maxM, cudaStream_t st);
-void launchNorm2Batch(const NormArgs* batch, int count, int64_t maxM, cudaStream_t st);
+void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, const BlockMap& map, int stage, cudaStream_t st);
+void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, const BlockMap& map, cudaStream_t st);
+void launchNorm2Batch(const NormArgs* batch, const BlockMap& map, cudaStream_t st);
+void launchToDoubleBatch(const ToDoubleArgs* batch, const BlockMap& map, cudaStream_t st);
+// grid-stride elementwise kernels, blockIdx.y = problem (maxN: the longest)
 void launchToFloatBatch(const ToFloatArgs* batch, int count, int64_t maxN, cudaStream_t st);
 void launchAccumBatch(const AccumArgs* batch, int count, int64_t maxN, cudaStream_t st);
 void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, int dim, cudaStream_t st);
-
 }  // namespace dxg
