@@ -151,6 +151,10 @@ def measured_peaks():
 # of the 64x64x32 FP64 system, from the ncu capture summarised in
 # profiles/ilu_sweep_64x64x32_fp64.md (cold-cache, serialised launches).
 ILU_TRAFFIC_PER_APPLY_64x64x32 = 14511616 + 18709760
+# DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from the ncu capture
+# of the 32-problem ensemble (2,379,154 cells) in profiles/ilu_sweep_batched_ensemble32_mixed.md;
+# traffic scales with the cells swept (each block and vector entry is moved once)
+ENSEMBLE_SWEEP_TRAFFIC_PER_CELL = (136113408 + 9772544 + 174257152 + 10788608) / 2379154
 
 
 def cpu_sample(desc, u0, dt, iters):
@@ -321,6 +325,10 @@ def run_ensemble(args):
     ticks(batch, T)
     kernels, roofline = batch_roofline(batch)
     batch.set_kernel_timing(False)
+    if roofline["kernel"].startswith("waveKernel") and args.precision == "mixed":
+        roofline["traffic"] = ENSEMBLE_SWEEP_TRAFFIC_PER_CELL * cells_total
+        roofline["traffic_note"] = ("ncu dram bytes of the 32-problem ensemble apply, scaled by cells "
+                                    "(profiles/ilu_sweep_batched_ensemble32_mixed.md)")
 
     before = {i: batch.info(i) for i in ids}
     stream = torch.cuda.ExternalStream(batch.stream_handle(), device=local)
