@@ -66,6 +66,21 @@ def dist_info():
 WORKLOAD = "2p"
 
 
+def reduce_over_ranks(seconds, sums, device):
+    """Across the torchrun ranks (replicas): the maximum of the timed seconds and the
+    sums of the work counters; identity on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(seconds), [float(v) for v in sums]
+    t = torch.tensor([float(seconds)] + [float(v) for v in sums], device=device, dtype=torch.float64)
+    mx = t[:1].clone()
+    rest = t[1:].clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(rest, op=dist.ReduceOp.SUM)
+    return float(mx[0]), [float(v) for v in rest]
+
+
 def workload(cells, seed=2):
     from dumux_gb300 import problems
     if WORKLOAD == "1p":
@@ -353,12 +368,7 @@ def run_ensemble(args):
     solves = sum(after[i]["time_steps"] - before[i]["time_steps"] for i in ids)
     lin = sum(after[i]["linear_iterations"] - before[i]["linear_iterations"] for i in ids)
     newton = sum(after[i]["newton_iterations"] - before[i]["newton_iterations"] for i in ids)
-    if world > 1:
-        t = torch.tensor([sec, float(work), float(solves)], device=f"cuda:{local}", dtype=torch.float64)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        sec, work, solves = float(mx[0]), float(t[1]), float(t[2])
+    sec, (work, solves) = reduce_over_ranks(sec, [work, solves], f"cuda:{local}")
     batch.close()
 
     # ---- end to end through the C ABI: admit (tabulation + h2d), then per step T ticks
@@ -377,12 +387,7 @@ def run_ensemble(args):
     e2e_work = sum(d.num_cells * b2.info(i)["newton_iterations"] for i, (d, _, _) in zip(ids2, probs))
     b2.close()
     h2d = sum(d.num_dofs * 8 + d.num_cells * 16 + d.bc_type.size + d.bc_values.size * 8 for d, _, _ in probs)
-    if world > 1:
-        t = torch.tensor([e2e_sec, float(e2e_work)], device=f"cuda:{local}", dtype=torch.float64)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        e2e_sec, e2e_work = float(mx[0]), float(t[1])
+    e2e_sec, (e2e_work,) = reduce_over_ranks(e2e_sec, [e2e_work], f"cuda:{local}")
     e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(d2h / args.steps),
            "note": "fresh batch: admission of every problem (tabulation + upload) and, per step, "
@@ -569,12 +574,7 @@ def main():
     launches = ctx.kernel_launches() - launches0
     sec = ms / 1e3
     u_after = ctx.solution()
-    if world > 1:
-        t = torch.tensor([sec, float(work)], device=f"cuda:{local}", dtype=torch.float64)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        sec, work = float(mx[0]), float(t[1])
+    sec, (work,) = reduce_over_ranks(sec, [work], f"cuda:{local}")
     value = work / sec
 
     # ---- end to end through the C ABI with host buffers (h2d + d2h inside the region)
@@ -593,12 +593,7 @@ def main():
         e2e_work += ctx.num_cells * (rep["iterations"] + rep["wasted_iterations"])
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_sec, float(e2e_work)], device=f"cuda:{local}", dtype=torch.float64)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        e2e_sec, e2e_work = float(mx[0]), float(t[1])
+    e2e_sec, (e2e_work,) = reduce_over_ranks(e2e_sec, [e2e_work], f"cuda:{local}")
     e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(ctx.num_dofs * 8),
            "d2h_bytes_per_step": int(ctx.num_dofs * 8)}
 

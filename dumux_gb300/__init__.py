@@ -100,6 +100,8 @@ def lib():
         L.dxg_batch_set_kernel_timing.argtypes = [vp, C.c_int]
         L.dxg_batch_get_kernel_timing.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                                   C.POINTER(C.c_double)]
+        L.dxg_selftest_bounded_wait.argtypes = [C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
+                                                C.POINTER(C.c_double)]
         L.dxg_batch_stream.argtypes = [vp]
         L.dxg_batch_stream.restype = C.c_void_p
         _lib = L
@@ -349,6 +351,18 @@ class NewtonSolver:
     suggestTimeStepSize = suggest_time_step_size
 
 
+def selftest_bounded_wait(kind="mbarrier", limit_ms=2.0, device=0):
+    """Runs the sweeps' bounded wait on a condition nothing satisfies (dxg_selftest_bounded_wait);
+    returns (kernel status name, milliseconds waited).  The expected status is DXG_ERR_TIMEOUT."""
+    k = {"mbarrier": 0, "flag": 1}[kind]
+    st = C.c_int32(-1)
+    ms = C.c_double(0.0)
+    rc = lib().dxg_selftest_bounded_wait(int(device), k, int(limit_ms * 1e6), C.byref(st), C.byref(ms))
+    if rc != 0:
+        raise DxgError(rc, "bounded-wait self-test did not run")
+    return STATUS_NAMES.get(st.value, st.value), ms.value
+
+
 def problem_device_bytes(desc, precision="mixed"):
     """Device memory a problem takes once admitted (dxg_problem_device_bytes)."""
     prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
@@ -455,4 +469,5 @@ class Batch:
 
 
 __all__ = ["Context", "FVAssembler", "ILUBiCGSTABIstlSolver", "NewtonSolver", "ProblemDesc", "newton_params",
-           "DxgError", "NumericalProblem", "lib", "LIB_PATH", "Batch", "problem_device_bytes"]
+           "DxgError", "NumericalProblem", "lib", "LIB_PATH", "Batch", "problem_device_bytes",
+           "selftest_bounded_wait"]

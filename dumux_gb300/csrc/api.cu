@@ -1275,6 +1275,22 @@ int dxg_get_kernel_timing(dxg_ctx* c, int kc, int64_t* launches, double* ms, dou
     });
 }
 
+int dxg_selftest_bounded_wait(int device, int32_t kind, int64_t limit_ns, int32_t* kernel_status,
+                              double* waited_ms)
+{
+    if (!kernel_status || (kind != 0 && kind != 1) || limit_ns <= 0 || limit_ns > 1000000000LL) return DXG_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return DXG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count || cudaSetDevice(device) != cudaSuccess) return DXG_ERR_ARG;
+    int ks = -1;
+    const int rc = runBoundedWaitSelfTest(kind, limit_ns, &ks, waited_ms);
+    *kernel_status = ks;
+    return rc;
+}
+
 int dxg_sync(dxg_ctx* c)
 {
     if (!c) return DXG_ERR_ARG;

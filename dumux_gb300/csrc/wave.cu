@@ -569,6 +569,61 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
     }
 }
 
+// ---------------------------------------------------------------- bounded-wait self-test
+// The waits of the sweeps, on conditions nothing ever satisfies: an mbarrier phase that
+// never completes (KIND 0) or a global flag nobody sets (KIND 1).  Each waits at most
+// limitNs, then records DXG_ERR_TIMEOUT and the time it waited, and returns.
+__global__ void boundedWaitSelfTest(int kind, unsigned long long limitNs, const int* flag, int* status,
+                                    unsigned long long* waitedNs)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbarInit(smemAddr(&bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const unsigned long long t0 = globalTimer();
+    const unsigned long long deadline = t0 + limitNs;
+    bool done = false;
+    while (!done) {
+        if (kind == 0) done = mbarTryWait(smemAddr(&bar), 0);
+        else done = *(volatile const int*)flag != 0;
+        if (!done && globalTimer() > deadline) break;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *status = done ? DXG_OK : DXG_ERR_TIMEOUT;
+        *waitedNs = globalTimer() - t0;
+    }
+}
+
+int runBoundedWaitSelfTest(int kind, long long limitNs, int* kernelStatus, double* waitedMs)
+{
+    int* dStatus = nullptr;
+    int* dFlag = nullptr;
+    unsigned long long* dWaited = nullptr;
+    int rc = DXG_OK;
+    if (cudaMalloc(&dStatus, sizeof(int)) != cudaSuccess || cudaMalloc(&dFlag, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&dWaited, sizeof(unsigned long long)) != cudaSuccess)
+        rc = DXG_ERR_OOM;
+    if (rc == DXG_OK && cudaMemset(dFlag, 0, sizeof(int)) != cudaSuccess) rc = DXG_ERR_CUDA;
+    if (rc == DXG_OK && cudaMemset(dStatus, 0xff, sizeof(int)) != cudaSuccess) rc = DXG_ERR_CUDA;
+    if (rc == DXG_OK) {
+        boundedWaitSelfTest<<<1, 32>>>(kind, (unsigned long long)limitNs, dFlag, dStatus, dWaited);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = DXG_ERR_CUDA;
+    }
+    unsigned long long waited = 0;
+    if (rc == DXG_OK &&
+        (cudaMemcpy(kernelStatus, dStatus, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(&waited, dWaited, sizeof(waited), cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = DXG_ERR_CUDA;
+    if (waitedMs) *waitedMs = waited / 1e6;
+    cudaFree(dStatus);
+    cudaFree(dFlag);
+    cudaFree(dWaited);
+    return rc;
+}
+
 // ---------------------------------------------------------------- host side
 template <int B, class T, int DIR, int MODE>
 static size_t waveSmemFor(int dim, int linesPerCta, int haloLines, int threads, int pfDepth)

@@ -50,6 +50,9 @@ void launchWaveFactorBatch(const WaveBatchPlan& p, const WaveArgs<T>* batch, int
 template <class T>
 void launchWaveApplyBatch(const WaveBatchPlan& p, const WaveArgs<T>* fwd, const WaveArgs<T>* bwd, int count, int dim,
                           int b, cudaStream_t st);
+// Runs the bounded-wait self-test kernel (kind 0: mbarrier, 1: global flag) on the
+// current device; *kernelStatus receives the kernel's verdict (DXG_ERR_TIMEOUT expected).
+int runBoundedWaitSelfTest(int kind, long long limitNs, int* kernelStatus, double* waitedMs);
 template <class T>
 void launchWaveFactor(const WavePlan& plan, const WaveArgs<T>& a, int b, cudaStream_t st);
 template <class T>

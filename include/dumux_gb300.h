@@ -252,6 +252,15 @@ int dxg_get_kernel_timing(dxg_ctx* ctx, int kernel_class, int64_t* launches, dou
  * reference (dune-istl's norms run on the host). */
 int dxg_norm2_noalloc(const double* x, int64_t n, double* result, void* stream);
 
+/* Failure-detection self-test: runs, on `device`, the bounded wait the ILU(0) sweeps use
+ * on a condition nothing satisfies -- kind 0: an mbarrier phase that never completes,
+ * kind 1: a global flag nobody sets -- with a limit of limit_ns (at most 1 s).  The
+ * kernel gives up, writes *kernel_status = DXG_ERR_TIMEOUT (the expected verdict) and
+ * returns; *waited_ms receives how long it waited.  The call returns DXG_OK when the
+ * test ran and the device stayed usable.  No counterpart in the reference. */
+int dxg_selftest_bounded_wait(int device, int32_t kind, int64_t limit_ns, int32_t* kernel_status,
+                              double* waited_ms);
+
 /* Kernel launches issued by this context since creation (all of them ours). */
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */
