@@ -1,0 +1,424 @@
+// dumux_gb300.hh -- C++ adapter over the C ABI of dumux_gb300.h (header only, C++17).
+//
+// What a DuMux application keeps: its Problem and SpatialParams classes, called through
+// the reference's *AtPos interface, and the call pattern of the Assembler / LinearSolver /
+// NewtonSolver concepts.  What changes: the classes below replace FVAssembler,
+// ILUBiCGSTABIstlSolver and NewtonSolver; they tabulate the problem once
+// (dxg_problem_upload) and run assembly, the linear solve and the Newton loop on the GPU.
+//
+//   reference                                              here
+//   Dumux::FVAssembler          (assembly/fvassembler.hh)   GpuFVAssembler
+//   Dumux::ILUBiCGSTABIstlSolver (linear/istlsolvers.hh)    GpuILUBiCGSTABSolver
+//   Dumux::NewtonSolver         (nonlinear/newtonsolver.hh) GpuNewtonSolver
+//
+// Problem interface used (dumux/common/fvproblem.hh:99-524; the reference's 2p test
+// problem, test/porousmediumflow/2p/incompressible/problem.hh:59-139, has this shape):
+//   BoundaryTypes boundaryTypesAtPos(const GlobalPosition&)   -- all Dirichlet or all Neumann
+//   PrimaryVariables dirichletAtPos(const GlobalPosition&)
+//   NumEqVector neumannAtPos(const GlobalPosition&)           -- mass flux, positive = outflow
+//   NumEqVector sourceAtPos(const GlobalPosition&)
+//   PrimaryVariables initialAtPos(const GlobalPosition&)
+// SpatialParams interface used (dumux/porousmediumflow/fvspatialparams*.hh):
+//   double permeabilityAtPos(const GlobalPosition&)           -- isotropic
+//   double porosityAtPos(const GlobalPosition&)
+//   double extrusionFactorAtPos(const GlobalPosition&)
+//   BrooksCoreyParams fluidMatrixInteractionAtPos(const GlobalPosition&)   (2p only)
+// Values are indexed with operator[] (FieldVector-like); GlobalPosition here is a
+// std::array<double, 3> (DUNE's FieldVector is not required).  Solution vectors are flat
+// std::vector<double> in the BlockVector<FieldVector<double, numEq>> order (cell major).
+#ifndef DUMUX_GB300_HH
+#define DUMUX_GB300_HH
+
+#include <array>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "dumux_gb300.h"
+
+namespace dumux_gb300 {
+
+using GlobalPosition = std::array<double, 3>;
+
+// Dumux::NumericalProblem: the recoverable failure of a linear or Newton solve.
+struct NumericalProblem : std::runtime_error {
+    int status;
+    NumericalProblem(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline bool recoverable(int st)
+{
+    return st == DXG_ERR_LINEAR_BREAKDOWN || st == DXG_ERR_LINEAR_NOT_CONVERGED || st == DXG_ERR_NAN ||
+           st == DXG_ERR_NEWTON_NOT_CONVERGED;
+}
+
+// Dumux::BoundaryTypes restricted to what the device path supports: every equation of a
+// boundary face Dirichlet, or every equation Neumann (mixed faces are rejected, as the
+// reference's cc-TPFA local residual does, cclocalresidual.hh:49-105).
+struct BoundaryTypes {
+    bool dirichlet = false;
+    void setAllDirichlet() { dirichlet = true; }
+    void setAllNeumann() { dirichlet = false; }
+    bool hasDirichlet() const { return dirichlet; }
+    bool hasNeumann() const { return !dirichlet; }
+};
+
+// Parameters of Dumux's regularised Brooks-Corey law (BrooksCoreyDefault):
+// pcEntry, lambda, Swr, Snr and the pc regularisation threshold pcLowSwe.
+struct BrooksCoreyParams {
+    double pcEntry = 0.0, lambda = 2.0, swr = 0.0, snr = 0.0, pcLowSwe = 0.01;
+};
+
+// A structured tensor-product grid (YaspGrid with tensor-product coordinates).
+struct StructuredGrid {
+    int dim = 3;
+    std::array<std::vector<double>, 3> coords;   // vertex coordinates per axis
+
+    static StructuredGrid equidistant(const std::array<double, 3>& lower, const std::array<double, 3>& upper,
+                                      const std::array<int, 3>& cells, int dim)
+    {
+        StructuredGrid g;
+        g.dim = dim;
+        for (int a = 0; a < dim; ++a) {
+            g.coords[a].resize(cells[a] + 1);
+            const double h = (upper[a] - lower[a]) / cells[a];
+            for (int i = 0; i <= cells[a]; ++i) g.coords[a][i] = lower[a] + i * h;
+        }
+        return g;
+    }
+    int cells(int a) const { return a < dim ? (int)coords[a].size() - 1 : 1; }
+    long long numCells() const { return (long long)cells(0) * cells(1) * cells(2); }
+    double center(int a, int i) const { return 0.5 * (coords[a][i] + coords[a][i + 1]); }
+};
+
+// Fluid constants of the immiscible phases (constant liquids, fluidsystems/2pimmiscible.hh).
+struct FluidProperties {
+    std::array<double, 2> density{1000.0, 1000.0};
+    std::array<double, 2> viscosity{1e-3, 1e-3};
+};
+
+// Numeric differentiation and upwinding parameters (Assembly.NumericDifference*,
+// Flux.UpwindWeight) and gravity (Problem.EnableGravity).
+struct AssemblyParams {
+    double baseEpsilon = 1e-10;
+    std::array<double, 2> priVarMagnitude{-1.0, -1.0};
+    int numericDifferenceMethod = 1;
+    double upwindWeight = 1.0;
+    bool enableGravity = true;
+};
+
+// The tables of dxg_problem_desc filled from a problem / spatial-params pair.
+struct Tabulation {
+    StructuredGrid grid;
+    int numEq = 1;
+    std::vector<double> permeability, porosity, extrusion, source, materialParams, bcValues, initial;
+    std::vector<int32_t> material;
+    std::vector<int8_t> bcType;
+    FluidProperties fluids;
+    AssemblyParams assembly;
+    dxg_problem_desc desc{};
+
+    // Points dxg_problem_desc at the tables (valid while this object lives unchanged).
+    const dxg_problem_desc& descriptor()
+    {
+        desc = dxg_problem_desc{};
+        desc.dim = grid.dim;
+        for (int a = 0; a < 3; ++a) {
+            desc.cells[a] = grid.cells(a);
+            desc.coords[a] = a < grid.dim ? grid.coords[a].data() : nullptr;
+        }
+        desc.num_eq = numEq;
+        desc.enable_gravity = assembly.enableGravity ? 1 : 0;
+        desc.gravity[0] = desc.gravity[1] = desc.gravity[2] = 0.0;
+        desc.gravity[grid.dim - 1] = -9.81;
+        for (int p = 0; p < 2; ++p) {
+            desc.density[p] = fluids.density[p];
+            desc.viscosity[p] = fluids.viscosity[p];
+            desc.privar_magnitude[p] = assembly.priVarMagnitude[p];
+        }
+        desc.permeability = permeability.data();
+        desc.porosity = porosity.data();
+        desc.extrusion = extrusion.data();
+        desc.material = material.data();
+        desc.source = source.data();
+        desc.num_materials = (int32_t)(materialParams.size() / 5);
+        desc.material_params = materialParams.data();
+        desc.bc_type = bcType.data();
+        desc.bc_values = bcValues.data();
+        desc.base_epsilon = assembly.baseEpsilon;
+        desc.numeric_difference_method = assembly.numericDifferenceMethod;
+        desc.upwind_weight = assembly.upwindWeight;
+        return desc;
+    }
+};
+
+namespace detail {
+// SpatialParams without extrusionFactorAtPos use 1 (the reference's default).
+template <class S>
+auto extrusionOf(const S& s, const GlobalPosition& x, int) -> decltype(s.extrusionFactorAtPos(x))
+{
+    return s.extrusionFactorAtPos(x);
+}
+template <class S>
+double extrusionOf(const S&, const GlobalPosition&, long)
+{
+    return 1.0;
+}
+template <class S>
+auto materialOf(const S& s, const GlobalPosition& x, int) -> decltype(s.fluidMatrixInteractionAtPos(x))
+{
+    return s.fluidMatrixInteractionAtPos(x);
+}
+template <class S>
+BrooksCoreyParams materialOf(const S&, const GlobalPosition&, long)
+{
+    return BrooksCoreyParams{};
+}
+}  // namespace detail
+
+// Evaluates the problem's and spatial parameters' *AtPos callbacks at the cell centres
+// and boundary-face centres (fvgridgeometry / fvproblem semantics), in the orderings
+// documented in dumux_gb300.h.
+template <int NumEq, class Problem, class SpatialParams>
+Tabulation tabulate(const StructuredGrid& grid, const Problem& problem, const SpatialParams& params,
+                    const FluidProperties& fluids, const AssemblyParams& assembly)
+{
+    static_assert(NumEq == 1 || NumEq == 2, "1p or 2p immiscible");
+    Tabulation t;
+    t.grid = grid;
+    t.numEq = NumEq;
+    t.fluids = fluids;
+    t.assembly = assembly;
+    const int dim = grid.dim;
+    const int n0 = grid.cells(0), n1 = grid.cells(1), n2 = grid.cells(2);
+    const long long N = grid.numCells();
+    t.permeability.resize(N);
+    t.porosity.resize(N);
+    t.extrusion.resize(N);
+    t.material.resize(N);
+    t.source.resize(N * NumEq);
+    t.initial.resize(N * NumEq);
+    std::vector<BrooksCoreyParams> laws;
+    for (int k = 0; k < n2; ++k)
+        for (int j = 0; j < n1; ++j)
+            for (int i = 0; i < n0; ++i) {
+                const long long c = i + (long long)n0 * (j + (long long)n1 * k);
+                GlobalPosition x{grid.center(0, i), dim > 1 ? grid.center(1, j) : 0.0,
+                                 dim > 2 ? grid.center(2, k) : 0.0};
+                t.permeability[c] = params.permeabilityAtPos(x);
+                t.porosity[c] = params.porosityAtPos(x);
+                t.extrusion[c] = detail::extrusionOf(params, x, 0);
+                const auto q = problem.sourceAtPos(x);
+                const auto u0 = problem.initialAtPos(x);
+                for (int e = 0; e < NumEq; ++e) {
+                    t.source[c * NumEq + e] = q[e];
+                    t.initial[c * NumEq + e] = u0[e];
+                }
+                int m = 0;
+                if (NumEq == 2) {
+                    const BrooksCoreyParams law = detail::materialOf(params, x, 0);
+                    for (m = 0; m < (int)laws.size(); ++m) {
+                        const auto& l = laws[m];
+                        if (l.pcEntry == law.pcEntry && l.lambda == law.lambda && l.swr == law.swr &&
+                            l.snr == law.snr && l.pcLowSwe == law.pcLowSwe)
+                            break;
+                    }
+                    if (m == (int)laws.size()) laws.push_back(law);
+                }
+                t.material[c] = m;
+            }
+    if (laws.empty()) laws.push_back(BrooksCoreyParams{});
+    for (const auto& l : laws)
+        t.materialParams.insert(t.materialParams.end(), {l.pcEntry, l.lambda, l.swr, l.snr, l.pcLowSwe});
+    // boundary faces: sides -x,+x,-y,+y,-z,+z, each lexicographic over the other axes
+    for (int f = 0; f < 2 * dim; ++f) {
+        const int a = f / 2, side = f % 2;
+        int o[2] = {-1, -1}, no = 0;
+        for (int q = 0; q < dim; ++q)
+            if (q != a) o[no++] = q;
+        const int m0 = no > 0 ? grid.cells(o[0]) : 1, m1 = no > 1 ? grid.cells(o[1]) : 1;
+        for (int jj = 0; jj < m1; ++jj)
+            for (int ii = 0; ii < m0; ++ii) {
+                GlobalPosition x{0.0, 0.0, 0.0};
+                x[a] = side == 0 ? grid.coords[a].front() : grid.coords[a].back();
+                if (no > 0) x[o[0]] = grid.center(o[0], ii);
+                if (no > 1) x[o[1]] = grid.center(o[1], jj);
+                const auto bt = problem.boundaryTypesAtPos(x);
+                const bool dir = bt.hasDirichlet();
+                t.bcType.push_back(dir ? 1 : 2);
+                if (dir) {
+                    const auto v = problem.dirichletAtPos(x);
+                    for (int e = 0; e < NumEq; ++e) t.bcValues.push_back(v[e]);
+                } else {
+                    const auto v = problem.neumannAtPos(x);
+                    for (int e = 0; e < NumEq; ++e) t.bcValues.push_back(v[e]);
+                }
+            }
+    }
+    return t;
+}
+
+// Owning handle of one device context.
+class Context {
+public:
+    explicit Context(int device = 0, int precision = DXG_PRECISION_FP64)
+    {
+        const int st = dxg_ctx_create(&ctx_, device);
+        if (st != DXG_OK) throw Error(st, dxg_last_error(nullptr));
+        check(dxg_set_precision(ctx_, precision));
+    }
+    ~Context()
+    {
+        if (ctx_) dxg_ctx_destroy(ctx_);
+    }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    dxg_ctx* get() const { return ctx_; }
+    void check(int st) const
+    {
+        if (st == DXG_OK) return;
+        if (recoverable(st)) throw NumericalProblem(st, dxg_last_error(ctx_));
+        throw Error(st, dxg_last_error(ctx_));
+    }
+
+private:
+    dxg_ctx* ctx_ = nullptr;
+};
+
+// Dumux::FVAssembler over the device: the same method names and meanings
+// (fvassembler.hh:101-390); jacobian() / residual() copy the device system to the host.
+class GpuFVAssembler {
+public:
+    using Scalar = double;
+    using SolutionVector = std::vector<double>;
+    using ResidualType = std::vector<double>;
+
+    // Stationary (no previous solution) or transient (prevSol set, time step dt).
+    GpuFVAssembler(Tabulation tab, int device = 0, int precision = DXG_PRECISION_FP64)
+        : tab_(std::move(tab)), ctx_(device, precision)
+    {
+        ctx_.check(dxg_problem_upload(ctx_.get(), &tab_.descriptor()));
+        int32_t b = 0;
+        ctx_.check(dxg_sizes(ctx_.get(), &numCells_, &b, &numBlocks_));
+        numEq_ = b;
+    }
+    void setPreviousSolution(const SolutionVector& u)
+    {
+        ctx_.check(dxg_set_prev_solution(ctx_.get(), u.data()));
+        stationary_ = false;
+    }
+    void setTimeStepSize(double dt) { ctx_.check(dxg_set_time_step(ctx_.get(), dt)); }
+    bool isStationaryProblem() const { return stationary_; }
+    void assembleJacobianAndResidual(const SolutionVector& u)
+    {
+        ctx_.check(dxg_set_solution(ctx_.get(), u.data()));
+        ctx_.check(dxg_assemble_jacobian_and_residual(ctx_.get()));
+    }
+    void assembleResidual(const SolutionVector& u)
+    {
+        ctx_.check(dxg_set_solution(ctx_.get(), u.data()));
+        ctx_.check(dxg_assemble_residual(ctx_.get()));
+    }
+    ResidualType residual() const
+    {
+        ResidualType r(numDofs());
+        ctx_.check(dxg_get_residual(ctx_.get(), r.data()));
+        return r;
+    }
+    // BCRS of FieldMatrix<double, numEq, numEq> blocks: row pointers, block columns, values
+    void jacobian(std::vector<int64_t>& rowPtr, std::vector<int32_t>& col, std::vector<double>& values) const
+    {
+        rowPtr.resize(numCells_ + 1);
+        col.resize(numBlocks_);
+        values.resize(numBlocks_ * numEq_ * numEq_);
+        ctx_.check(dxg_get_jacobian(ctx_.get(), rowPtr.data(), col.data(), values.data()));
+    }
+    double residualNorm() const
+    {
+        double n = 0.0;
+        ctx_.check(dxg_residual_norm(ctx_.get(), &n));
+        return n;
+    }
+    SolutionVector initialSolution() const { return tab_.initial; }
+    int64_t numCells() const { return numCells_; }
+    int numEq() const { return numEq_; }
+    int64_t numDofs() const { return numCells_ * numEq_; }
+    dxg_ctx* context() const { return ctx_.get(); }
+    const Context& handle() const { return ctx_; }
+
+private:
+    Tabulation tab_;
+    Context ctx_;
+    int64_t numCells_ = 0, numBlocks_ = 0;
+    int numEq_ = 1;
+    bool stationary_ = true;
+};
+
+// Dumux::ILUBiCGSTABIstlSolver over the device (istlsolvers.hh:635-642): ILU(0)-
+// preconditioned BiCGSTAB on the system last assembled by the GpuFVAssembler.
+class GpuILUBiCGSTABSolver {
+public:
+    void setResidualReduction(double r) { reduction_ = r; }
+    void setMaxIter(int n) { maxIter_ = n; }
+    // solve(A, x, b): A and b are the assembler's device system; x receives the update
+    bool solve(const GpuFVAssembler& A, std::vector<double>& x, const std::vector<double>& /*b*/)
+    {
+        dxg_linear_result res{};
+        const int st = dxg_linear_solve(A.context(), reduction_, maxIter_, &res);
+        if (st != DXG_OK && !recoverable(st)) A.handle().check(st);
+        last_ = res;
+        x.resize(A.numDofs());
+        A.handle().check(dxg_get_update(A.context(), x.data()));
+        return st == DXG_OK && res.converged;
+    }
+    double norm(const GpuFVAssembler& A) const { return A.residualNorm(); }
+    const dxg_linear_result& result() const { return last_; }
+
+private:
+    double reduction_ = 1e-13;
+    int maxIter_ = 250;
+    dxg_linear_result last_{};
+};
+
+// Dumux::NewtonSolver over the device (newtonsolver.hh:179-852): the loop, the update,
+// the shift criterion, the dt retries and the time-step suggestion run in the library.
+class GpuNewtonSolver {
+public:
+    explicit GpuNewtonSolver(GpuFVAssembler& assembler) : assembler_(assembler)
+    {
+        dxg_newton_default_params(&params_);
+    }
+    dxg_newton_params& params() { return params_; }
+    // solve(x, dt): one implicit Euler step from the assembler's previous solution (dt > 0),
+    // or the stationary solve (dt == 0); x is the initial guess and receives the solution.
+    // Throws NumericalProblem when all time-step divisions fail (NewtonSolver::solve).
+    void solve(std::vector<double>& x, double dt)
+    {
+        dxg_ctx* c = assembler_.context();
+        assembler_.handle().check(dxg_set_solution(c, x.data()));
+        const int st = dxg_newton_solve(c, dt, &params_, &report_);
+        assembler_.handle().check(st);
+        assembler_.handle().check(dxg_get_solution(c, x.data()));
+    }
+    // TimeLoop::advanceTimeStep: the converged solution becomes the previous time level
+    void advanceTimeStep() { assembler_.handle().check(dxg_advance_time_step(assembler_.context())); }
+    double suggestTimeStepSize(double oldDt) const
+    {
+        return dxg_suggest_time_step(assembler_.context(), oldDt, &params_);
+    }
+    const dxg_newton_report& report() const { return report_; }
+
+private:
+    GpuFVAssembler& assembler_;
+    dxg_newton_params params_{};
+    dxg_newton_report report_{};
+};
+
+}  // namespace dumux_gb300
+
+#endif  // DUMUX_GB300_HH

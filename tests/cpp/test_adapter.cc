@@ -1,0 +1,134 @@
+// Drop-in check of the C++ adapter (include/dumux_gb300.hh): a DuMux-style 2p problem and
+// spatial-params class, written against the reference's *AtPos interface (the shape of
+// test/porousmediumflow/2p/incompressible/problem.hh and spatialparams.hh), driven through
+// GpuFVAssembler / GpuILUBiCGSTABSolver / GpuNewtonSolver.
+//
+//   test_adapter NX NY NZ STEPS OUT.bin
+// writes the solution after STEPS implicit Euler steps of 250 s as raw doubles; exits 3
+// with "no-device" when no GPU is present.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "dumux_gb300.hh"
+
+using namespace dumux_gb300;
+
+struct Vec2 {
+    double v[2];
+    double operator[](int i) const { return v[i]; }
+};
+
+// Water-DNAPL problem: hydrostatic Dirichlet left/right (alpha-scaled depth), DNAPL inflow
+// on the top strip 0.5 < (xmax - x)/width < 2/3, no flow elsewhere (problem.hh:74-168).
+class DnaplProblem {
+public:
+    DnaplProblem(double xmax, double zmax, int vertical) : xmax_(xmax), zmax_(zmax), v_(vertical) {}
+    BoundaryTypes boundaryTypesAtPos(const GlobalPosition& x) const
+    {
+        BoundaryTypes bt;
+        if (x[0] < eps_ || x[0] > xmax_ - eps_) bt.setAllDirichlet();
+        else bt.setAllNeumann();
+        return bt;
+    }
+    Vec2 dirichletAtPos(const GlobalPosition& x) const
+    {
+        const double height = zmax_;
+        const double depth = zmax_ - x[v_];
+        const double alpha = 1 + 1.5 / height;
+        const double width = xmax_;
+        const double factor = (width * alpha + (1.0 - alpha) * x[0]) / width;
+        return Vec2{{1e5 - factor * 1000.0 * (-9.81) * depth, 0.0}};
+    }
+    Vec2 neumannAtPos(const GlobalPosition& x) const
+    {
+        const double lambda = (xmax_ - x[0]) / xmax_;
+        if (x[v_] > zmax_ - eps_ && 0.5 < lambda && lambda < 2.0 / 3.0) return Vec2{{0.0, -0.04}};
+        return Vec2{{0.0, 0.0}};
+    }
+    Vec2 sourceAtPos(const GlobalPosition&) const { return Vec2{{0.0, 0.0}}; }
+    Vec2 initialAtPos(const GlobalPosition& x) const
+    {
+        return Vec2{{1e5 - 1000.0 * (-9.81) * (zmax_ - x[v_]), 0.0}};
+    }
+
+private:
+    double xmax_, zmax_;
+    int v_;
+    double eps_ = 1e-6;
+};
+
+// Smoothly varying permeability, porosity 0.4, BrooksCoreyDefault (pe 500, lambda 2).
+class DnaplSpatialParams {
+public:
+    double permeabilityAtPos(const GlobalPosition& x) const
+    {
+        return 1e-11 * (1.0 + 0.3 * x[0] + 0.2 * x[1] * x[1] + 0.1 * x[2]);
+    }
+    double porosityAtPos(const GlobalPosition&) const { return 0.4; }
+    BrooksCoreyParams fluidMatrixInteractionAtPos(const GlobalPosition&) const
+    {
+        return BrooksCoreyParams{500.0, 2.0, 0.05, 0.0, 0.01};
+    }
+};
+
+int main(int argc, char** argv)
+{
+    if (argc < 6) {
+        std::fprintf(stderr, "usage: %s NX NY NZ STEPS OUT.bin\n", argv[0]);
+        return 2;
+    }
+    const int nx = std::atoi(argv[1]), ny = std::atoi(argv[2]), nz = std::atoi(argv[3]), steps = std::atoi(argv[4]);
+    const StructuredGrid grid = StructuredGrid::equidistant({0.0, 0.0, 0.0}, {6.0, 4.0, 1.0}, {nx, ny, nz}, 3);
+    FluidProperties fluids;
+    fluids.density = {1000.0, 1460.0};
+    fluids.viscosity = {1e-3, 5.7e-4};
+    const DnaplProblem problem(6.0, 1.0, 2);
+    const DnaplSpatialParams params;
+    try {
+        GpuFVAssembler assembler(tabulate<2>(grid, problem, params, fluids, AssemblyParams{}));
+        std::vector<double> u = assembler.initialSolution();
+        assembler.setPreviousSolution(u);
+        assembler.setTimeStepSize(250.0);
+
+        // assembler + linear solver as a LinearPDESolver would use them
+        assembler.assembleJacobianAndResidual(u);
+        std::vector<int64_t> rowPtr;
+        std::vector<int32_t> col;
+        std::vector<double> vals;
+        assembler.jacobian(rowPtr, col, vals);
+        GpuILUBiCGSTABSolver linear;
+        linear.setResidualReduction(1e-10);
+        std::vector<double> du;
+        if (!linear.solve(assembler, du, assembler.residual())) {
+            std::fprintf(stderr, "linear solve did not converge\n");
+            return 1;
+        }
+        if ((int64_t)rowPtr.back() != (int64_t)col.size()) return 1;
+
+        // the Newton loop with the time loop of the reference's 2p test
+        GpuNewtonSolver newton(assembler);
+        double dt = 250.0;
+        for (int s = 0; s < steps; ++s) {
+            newton.solve(u, dt);
+            newton.advanceTimeStep();
+        }
+        std::FILE* f = std::fopen(argv[5], "wb");
+        if (!f) return 1;
+        std::fwrite(u.data(), sizeof(double), u.size(), f);
+        std::fclose(f);
+        std::printf("ok cells=%lld newton_last=%d linear_first=%d\n", (long long)assembler.numCells(),
+                    newton.report().iterations, linear.result().iterations);
+        return 0;
+    } catch (const Error& e) {
+        if (e.status == DXG_ERR_NO_DEVICE) {
+            std::printf("no-device\n");
+            return 3;
+        }
+        std::fprintf(stderr, "error %d: %s\n", e.status, e.what());
+        return 1;
+    } catch (const NumericalProblem& e) {
+        std::fprintf(stderr, "numerical problem %d: %s\n", e.status, e.what());
+        return 1;
+    }
+}
