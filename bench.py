@@ -345,6 +345,7 @@ def run_ensemble(args):
         roofline["traffic_note"] = ("ncu dram bytes of the 32-problem ensemble apply, scaled by cells "
                                     "(profiles/ilu_sweep_batched_ensemble32_mixed.md)")
 
+    sweep_shapes = batch.describe().strip()
     before = {i: batch.info(i) for i in ids}
     stream = torch.cuda.ExternalStream(batch.stream_handle(), device=local)
     launches0 = batch.kernel_launches()
@@ -408,7 +409,7 @@ def run_ensemble(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, one batched launch per kernel",
                    "l2": "inputs larger than L2 (all problems resident, GBs of state)",
                    "step": f"{T} engine ticks with every problem resident and time-stepping"},
-        "ensemble_solves_per_s": solves / sec,
+        "ensemble_solves_per_s": solves / sec, "sweep_shapes": sweep_shapes,
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
     if rank == 0:

@@ -102,6 +102,7 @@ def lib():
                                                   C.POINTER(C.c_double)]
         L.dxg_selftest_bounded_wait.argtypes = [C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
                                                 C.POINTER(C.c_double)]
+        L.dxg_batch_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_batch_stream.argtypes = [vp]
         L.dxg_batch_stream.restype = C.c_void_p
         _lib = L
@@ -456,6 +457,12 @@ class Batch:
 
     def stream_handle(self):
         return self._L.dxg_batch_stream(self._h)
+
+    def describe(self):
+        """The groups of problems and their ILU(0) sweep launch shapes."""
+        buf = C.create_string_buffer(8192)
+        self._check(self._L.dxg_batch_describe(self._h, buf, len(buf)))
+        return buf.value.decode()
 
     def set_kernel_timing(self, enable=True):
         self._check(self._L.dxg_batch_set_kernel_timing(self._h, int(bool(enable))))

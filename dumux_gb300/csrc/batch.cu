@@ -22,6 +22,7 @@
 // :428-446, 657-701; suggestTimeStepSize :784-798; TimeLoop::setTimeStepSize capped by
 // the maximum, common/timeloop.hh:323).
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -178,6 +179,9 @@ struct dxg_batch {
     int device = 0;
     int precision = DXG_PRECISION_MIXED;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};   // forked streams of the sweep classes
+    cudaEvent_t forkEv = nullptr;
+    cudaEvent_t joinEv[3] = {nullptr, nullptr, nullptr};
     std::string err;
     bool graphs = true, autotune = true;
     int64_t budget = 0, bytesInUse = 0;
@@ -191,6 +195,7 @@ struct dxg_batch {
     size_t reportsCap = 0;
     std::map<std::tuple<int, int, int, int, int>, WaveBatchPlan> plans;   // autotuned sweep shapes
     std::map<GroupKey, std::unique_ptr<GroupState>> groups;              // per kind: chunk arguments, graph
+    std::map<std::vector<int>, std::vector<WaveBatchPlan>> jointPlans;   // class shapes refined together
     std::chrono::steady_clock::time_point epoch = std::chrono::steady_clock::now();
 
     // optional event timing per kernel class (direct launches while it is on)
@@ -499,8 +504,9 @@ WaveBatchPlan tunePlan(dxg_batch* B, const Members& S, int dim, int b)
     return best;
 }
 
-template <class PT>
-WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
+// Batch shape of a set of problems: kind, member count (next power of two), largest
+// extents (in multiples of 16 cells); sweep shapes are cached per batch shape.
+std::tuple<int, int, int, int, int> shapeKey(const Members& S, int dim, int b, int typeSize)
 {
     int mx[3] = {0, 0, 0};
     for (Slot* s : S) {
@@ -510,9 +516,14 @@ WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
     }
     int cnt = 1;
     while (cnt < (int)S.size()) cnt *= 2;
-    // batch shape: kind, member count (next power of two), largest extents (multiples of 16)
-    const auto key = std::make_tuple(b * 100 + dim * 10 + (int)sizeof(PT), cnt, (mx[0] + 15) / 16,
-                                     (mx[1] + 15) / 16, (mx[2] + 15) / 16);
+    return std::make_tuple(b * 100 + dim * 10 + typeSize, cnt, (mx[0] + 15) / 16, (mx[1] + 15) / 16,
+                           (mx[2] + 15) / 16);
+}
+
+template <class PT>
+WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
+{
+    const auto key = shapeKey(S, dim, b, (int)sizeof(PT));
     auto it = B->plans.find(key);
     if (it != B->plans.end()) {
         WaveBatchPlan p = it->second;
@@ -530,17 +541,33 @@ WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
 // ended (Krylov status not running) skip inside every kernel of the chunk.
 constexpr int kChunk = 8;    // BiCGSTAB iterations per tick
 
+// Sweep size classes: one block size serves every problem of a sweep launch, so problems
+// are split by their number of lines (ny*nz in 3D, ny in 2D) into classes with their own
+// autotuned launch shape; the classes' sweeps run concurrently on forked streams.
+constexpr int kMaxSweepClasses = 4;
+inline int sweepClassOf(const dxg_ctx* c)
+{
+    const int lines = c->dim == 3 ? c->pcHost.ny * c->pcHost.nz : c->pcHost.ny;
+    return lines <= 512 ? 0 : lines <= 1024 ? 1 : lines <= 2048 ? 2 : 3;
+}
+
+struct SweepClass {
+    std::vector<int> members;       // indices into the group
+    WaveBatchPlan plan;
+    const void* dFwP = nullptr;
+    const void* dFwR = nullptr;
+    const void* dBw = nullptr;
+};
+
 struct GroupState {
     std::vector<int64_t> ids;
-    WaveBatchPlan plan;
-    std::vector<WaveGeom> geo;
+    std::vector<SweepClass> classes;
+    std::vector<int> classOf;       // per member: index into classes
+    std::vector<WaveGeom> geo;      // per member, from its class's launch shape
     DevBuf<unsigned char> args;
     const BicgArgs<double>* dBicg = nullptr;
     const SpmvArgs<double, double>* dSv1 = nullptr;
     const SpmvArgs<double, double>* dSv2 = nullptr;
-    const void* dFwP = nullptr;
-    const void* dFwR = nullptr;
-    const void* dBw = nullptr;
     const ToDoubleArgs* dTd = nullptr;
     BlockMap mapM, mapN;     // vector kernels over N*b entries, SpMV over N cells
     int64_t maxN = 1, maxM = 1;
@@ -562,6 +589,103 @@ size_t pack(std::vector<unsigned char>& buf, const std::vector<T>& v)
     return off;
 }
 
+// The classes' sweeps run concurrently, so shapes tuned class by class (each alone on
+// an idle GPU) are not the best together.  One pass of coordinate descent re-chooses each
+// class's shape, the others fixed, by timing the whole concurrent apply on the members'
+// own factors (Krylov state detached; expired waits go to the batch's tuning flags).
+template <class PT>
+void refineClassPlans(dxg_batch* B, std::vector<SweepClass>& classes, const Members& S, int dim, int b)
+{
+    const int nc = (int)classes.size();
+    if (nc < 2 || !B->autotune) return;
+    std::vector<int> jkey;
+    std::vector<Members> subs(nc);
+    for (int q = 0; q < nc; ++q) {
+        for (int k : classes[q].members) subs[q].push_back(S[k]);
+        const auto k = shapeKey(subs[q], dim, b, (int)sizeof(PT));
+        jkey.insert(jkey.end(), {std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k)});
+    }
+    auto cached = B->jointPlans.find(jkey);
+    if (cached != B->jointPlans.end()) {
+        bool ok = true;
+        std::vector<WaveBatchPlan> plans = cached->second;
+        for (int q = 0; q < nc && ok; ++q)
+            ok = completeWaveBatchPlan(plans[q], geomsFor(subs[q], plans[q].ctas), dim, b, sizeof(PT) == 8) > 0;
+        if (ok) {
+            for (int q = 0; q < nc; ++q) classes[q].plan = plans[q];
+            return;
+        }
+    }
+    cudaStream_t st = B->stream;
+    if (!B->tuneFlags.get()) B->tuneFlags.alloc(2);
+    DXG_CUDA(cudaMemsetAsync(B->tuneFlags.get(), 0, 2 * sizeof(int), st));
+    cudaEvent_t e0, e1;
+    DXG_CUDA(cudaEventCreate(&e0));
+    DXG_CUDA(cudaEventCreate(&e1));
+    auto timeAll = [&](const std::vector<WaveBatchPlan>& plans) {
+        std::vector<const WaveArgs<PT>*> dfw(nc), dbw(nc);
+        for (int q = 0; q < nc; ++q) {
+            const std::vector<WaveGeom> g = geomsFor(subs[q], plans[q].ctas);
+            std::vector<WaveArgs<PT>> fw, bw;
+            for (size_t j = 0; j < subs[q].size(); ++j) {
+                dxg_ctx* c = subs[q][j]->c;
+                WaveArgs<PT> f = waveArgsOf<PT>(c, g[j], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c),
+                                                Pre<PT>::rIn(c), Pre<PT>::yOut(c), nullptr);
+                f.singular = B->tuneFlags.get();
+                f.err = B->tuneFlags.get() + 1;
+                WaveArgs<PT> w = f;
+                w.rhs = nullptr;
+                fw.push_back(f);
+                bw.push_back(w);
+            }
+            dfw[q] = B->arena.put(fw, st);
+            dbw[q] = B->arena.put(bw, st);
+        }
+        auto apply = [&] {
+            DXG_CUDA(cudaEventRecord(B->forkEv, st));
+            for (int q = 0; q < nc; ++q) {
+                cudaStream_t sq = q == 0 ? st : B->aux[q - 1];
+                if (q > 0) DXG_CUDA(cudaStreamWaitEvent(sq, B->forkEv, 0));
+                launchWaveApplyBatch<PT>(plans[q], dfw[q], dbw[q], (int)subs[q].size(), dim, b, sq);
+                if (q > 0) DXG_CUDA(cudaEventRecord(B->joinEv[q - 1], sq));
+            }
+            for (int q = 1; q < nc; ++q) DXG_CUDA(cudaStreamWaitEvent(st, B->joinEv[q - 1], 0));
+            B->launches += 2 * nc;
+        };
+        apply();   // warm-up
+        DXG_CUDA(cudaEventRecord(e0, st));
+        apply();
+        apply();
+        DXG_CUDA(cudaEventRecord(e1, st));
+        DXG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+    };
+    std::vector<WaveBatchPlan> plans(nc);
+    for (int q = 0; q < nc; ++q) plans[q] = classes[q].plan;
+    float best = timeAll(plans);
+    for (int q = 0; q < nc; ++q) {
+        for (const WaveBatchPlan& c : candidates(subs[q], dim, b, sizeof(PT) == 8)) {
+            if (c.ctas == plans[q].ctas && c.threads == plans[q].threads && c.pf == plans[q].pf) continue;
+            std::vector<WaveBatchPlan> trial = plans;
+            trial[q] = c;
+            const float t = timeAll(trial);
+            if (t < best) {
+                best = t;
+                plans = trial;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int flags[2] = {0, 0};
+    DXG_CUDA(cudaMemcpy(flags, B->tuneFlags.get(), sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[1]) throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out while tuning");
+    B->jointPlans[jkey] = plans;
+    for (int q = 0; q < nc; ++q) classes[q].plan = plans[q];
+}
+
 // (Re)builds the group's chunk arguments when its membership changed.
 template <class PT>
 GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
@@ -578,15 +702,39 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.ids = ids;
     const int n = (int)S.size();
     const int dim = S[0]->c->dim, b = S[0]->c->b;
-    G.plan = planFor<PT>(B, S, dim, b);
-    G.geo = geomsFor(S, G.plan.ctas);
+    {
+        int cls[kMaxSweepClasses] = {-1, -1, -1, -1};
+        G.classOf.resize(n);
+        for (int k = 0; k < n; ++k) {
+            const int q = sweepClassOf(S[k]->c);
+            if (cls[q] < 0) {
+                cls[q] = (int)G.classes.size();
+                G.classes.emplace_back();
+            }
+            G.classOf[k] = cls[q];
+            G.classes[cls[q]].members.push_back(k);
+        }
+        G.geo.resize(n);
+        for (SweepClass& sc : G.classes) {
+            Members sub;
+            for (int k : sc.members) sub.push_back(S[k]);
+            sc.plan = planFor<PT>(B, sub, dim, b);
+        }
+        refineClassPlans<PT>(B, G.classes, S, dim, b);
+        for (SweepClass& sc : G.classes) {
+            Members sub;
+            for (int k : sc.members) sub.push_back(S[k]);
+            const std::vector<WaveGeom> g = geomsFor(sub, sc.plan.ctas);
+            for (size_t j = 0; j < sc.members.size(); ++j) G.geo[sc.members[j]] = g[j];
+        }
+    }
     G.maxN = maxCells(S);
     G.maxM = maxDofs(S);
     G.sweepBytes = bytesOf(S, &dxg_ctx::bytesSweep, sizeof(PT) / 8.0);
     G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, 1.0);
     std::vector<BicgArgs<double>> ba(n);
     std::vector<SpmvArgs<double, double>> sv1(n), sv2(n);
-    std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);
+    std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);   // member order; repacked per class below
     std::vector<ToDoubleArgs> td(n);
     for (int k = 0; k < n; ++k) {
         dxg_ctx* c = S[k]->c;
@@ -623,18 +771,29 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     buildBlockMap(lenM, false, mM);
     buildBlockMap(lenN, true, mN);
     std::vector<unsigned char> host;
-    const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oP = pack(host, fwP),
-                 oR = pack(host, fwR), oW = pack(host, bw), oT = pack(host, td), oM = pack(host, mM),
-                 oN = pack(host, mN);
+    const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oT = pack(host, td),
+                 oM = pack(host, mM), oN = pack(host, mN);
+    std::vector<std::array<size_t, 3>> oc;
+    for (const SweepClass& sc : G.classes) {
+        std::vector<WaveArgs<PT>> cP, cR, cW;
+        for (int k : sc.members) {
+            cP.push_back(fwP[k]);
+            cR.push_back(fwR[k]);
+            cW.push_back(bw[k]);
+        }
+        oc.push_back({pack(host, cP), pack(host, cR), pack(host, cW)});
+    }
     G.args.alloc(host.size());
     DXG_CUDA(cudaMemcpy(G.args.get(), host.data(), host.size(), cudaMemcpyHostToDevice));
     unsigned char* d = G.args.get();
     G.dBicg = reinterpret_cast<const BicgArgs<double>*>(d + oB);
     G.dSv1 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o1);
     G.dSv2 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o2);
-    G.dFwP = d + oP;
-    G.dFwR = d + oR;
-    G.dBw = d + oW;
+    for (size_t q = 0; q < G.classes.size(); ++q) {
+        G.classes[q].dFwP = d + oc[q][0];
+        G.classes[q].dFwR = d + oc[q][1];
+        G.classes[q].dBw = d + oc[q][2];
+    }
     G.dTd = reinterpret_cast<const ToDoubleArgs*>(d + oT);
     G.mapM = {reinterpret_cast<const uint2*>(d + oM), (unsigned)mM.size()};
     G.mapN = {reinterpret_cast<const uint2*>(d + oN), (unsigned)mN.size()};
@@ -647,26 +806,35 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 {
     constexpr bool mixed = sizeof(PT) == 4;
     cudaStream_t st = B->stream;
-    const auto* fwP = static_cast<const WaveArgs<PT>*>(G.dFwP);
-    const auto* fwR = static_cast<const WaveArgs<PT>*>(G.dFwR);
-    const auto* bw = static_cast<const WaveArgs<PT>*>(G.dBw);
-    auto precondition = [&](const WaveArgs<PT>* fw) {
+    const int nc = (int)G.classes.size();
+    // forward + backward sweep of every class; classes after the first on forked streams
+    auto precondition = [&](bool onP) {
         {
             TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
-            launchWaveApplyBatch<PT>(G.plan, fw, bw, n, dim, b, st);
+            if (nc > 1) DXG_CUDA(cudaEventRecord(B->forkEv, st));
+            for (int q = 0; q < nc; ++q) {
+                const SweepClass& sc = G.classes[q];
+                cudaStream_t sq = q == 0 ? st : B->aux[q - 1];
+                if (q > 0) DXG_CUDA(cudaStreamWaitEvent(sq, B->forkEv, 0));
+                launchWaveApplyBatch<PT>(sc.plan, static_cast<const WaveArgs<PT>*>(onP ? sc.dFwP : sc.dFwR),
+                                         static_cast<const WaveArgs<PT>*>(sc.dBw), (int)sc.members.size(), dim, b,
+                                         sq);
+                if (q > 0) DXG_CUDA(cudaEventRecord(B->joinEv[q - 1], sq));
+            }
+            for (int q = 1; q < nc; ++q) DXG_CUDA(cudaStreamWaitEvent(st, B->joinEv[q - 1], 0));
         }
         if (mixed) launchToDoubleBatch(G.dTd, G.mapM, st);
     };
     for (int it = 0; it < kChunk; ++it) {
         launchBicgRhoBatch<double>(G.dBicg, G.mapM, st);
         launchBicgUpdatePBatch<double>(G.dBicg, G.mapM, st);
-        precondition(fwP);
+        precondition(true);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
             launchSpmvBatch<double, double>(G.dSv1, G.mapN, b, dim, 1, st);
         }
         launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 0, st);
-        precondition(fwR);
+        precondition(false);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
             launchSpmvBatch<double, double>(G.dSv2, G.mapN, b, dim, 2, st);
@@ -678,7 +846,7 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 template <class PT>
 void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
 {
-    constexpr int launchesPerIt = sizeof(PT) == 4 ? 12 : 10;
+    const int launchesPerIt = (sizeof(PT) == 4 ? 8 : 6) + 4 * (int)G.classes.size();
     cudaStream_t st = B->stream;
     if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
         G.graphTried = true;
@@ -809,13 +977,20 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
     }
     clearFlagsKernel<<<(n + 127) / 128, 128, 0, st>>>(B->arena.put(fl, st), n);
     DXG_CUDA(cudaGetLastError());
-    launchWaveFactorBatch<PT>(G.plan, B->arena.put(fa, st), n, dim, b, st);
+    for (size_t q = 0; q < G.classes.size(); ++q) {
+        std::vector<WaveArgs<PT>> fq;
+        for (int k = 0; k < n; ++k)
+            if (G.classOf[idx[k]] == (int)q) fq.push_back(fa[k]);
+        if (fq.empty()) continue;
+        launchWaveFactorBatch<PT>(G.classes[q].plan, B->arena.put(fq, st), (int)fq.size(), dim, b, st);
+        B->launches += 1;
+    }
     std::vector<int64_t> lenM;
     for (Slot* s : A) lenM.push_back(s->c->M);
     std::vector<uint2> mM;
     buildBlockMap(lenM, false, mM);
     launchBicgInitBatch<double>(B->arena.put(bi, st), BlockMap{B->arena.put(mM, st), (unsigned)mM.size()}, st);
-    B->launches += 5;
+    B->launches += 4;
     for (Slot* s : A) {
         s->solving = true;
         s->chunks = 0;
@@ -933,6 +1108,8 @@ void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
     batchCopy(B, advance);
 }
 
+std::string graphsNote(const GroupState& G) { return G.exec ? " graph" : ""; }
+
 GroupKey keyOf(const Slot* s)
 {
     const dxg_ctx* c = s->c;
@@ -978,6 +1155,9 @@ int dxg_batch_create(dxg_batch** out, int device, int precision)
     const int st = guardedB(b, [&] {
         DXG_CUDA(cudaSetDevice(device));
         DXG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        for (auto& a : b->aux) DXG_CUDA(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+        DXG_CUDA(cudaEventCreateWithFlags(&b->forkEv, cudaEventDisableTiming));
+        for (auto& e : b->joinEv) DXG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         return DXG_OK;
     });
     if (st != DXG_OK) {
@@ -1003,6 +1183,14 @@ int dxg_batch_destroy(dxg_batch* b)
     b->slots.clear();
     if (b->reportsHost) cudaFreeHost(b->reportsHost);
     b->reports.release();
+    for (auto a : b->aux)
+        if (a) {
+            cudaStreamSynchronize(a);
+            cudaStreamDestroy(a);
+        }
+    if (b->forkEv) cudaEventDestroy(b->forkEv);
+    for (auto e : b->joinEv)
+        if (e) cudaEventDestroy(e);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return DXG_OK;
@@ -1170,6 +1358,26 @@ int dxg_batch_remove(dxg_batch* b, int64_t id)
 }
 
 int64_t dxg_batch_launch_count(const dxg_batch* b) { return b ? b->launches : -1; }
+
+int dxg_batch_describe(const dxg_batch* b, char* buf, int64_t len)
+{
+    if (!b || !buf || len <= 0) return DXG_ERR_ARG;
+    std::string out;
+    for (const auto& kv : b->groups) {
+        const GroupKey& k = kv.first;
+        const GroupState& G = *kv.second;
+        out += "group num_eq=" + std::to_string(std::get<0>(k)) + " dim=" + std::to_string(std::get<1>(k)) +
+               " problems=" + std::to_string(G.ids.size()) + ":";
+        for (const SweepClass& sc : G.classes)
+            out += " [" + std::to_string(sc.members.size()) + " problems: cluster " + std::to_string(sc.plan.ctas) +
+                   " x " + std::to_string(sc.plan.threads) + " threads, prefetch " + std::to_string(sc.plan.pf) +
+                   "]";
+        out += graphsNote(G) + "\n";
+    }
+    std::strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+    return DXG_OK;
+}
 
 int dxg_batch_set_kernel_timing(dxg_batch* b, int enable)
 {

@@ -331,6 +331,8 @@ int dxg_batch_get_solution(dxg_batch* batch, int64_t id, double* u);
 int dxg_batch_remove(dxg_batch* batch, int64_t id);
 /* Kernel launches issued by the batch (graph replays count each kernel node). */
 int64_t dxg_batch_launch_count(const dxg_batch* batch);
+/* Text description of the current groups and their ILU(0) sweep launch shapes. */
+int dxg_batch_describe(const dxg_batch* batch, char* buf, int64_t len);
 /* Per-kernel-class event timing of the batched launches (as dxg_set_kernel_timing;
  * bytes summed over the problems of each launch).  While it is on, BiCGSTAB
  * iterations are launched directly instead of from a captured graph. */
