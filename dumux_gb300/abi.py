@@ -47,6 +47,7 @@ class ProblemDescC(C.Structure):
         ("privar_magnitude", C.c_double * 2),
         ("numeric_difference_method", C.c_int32),
         ("upwind_weight", C.c_double),
+        ("diff_method", C.c_int32),
     ]
 
 
@@ -185,7 +186,7 @@ class ProblemDesc:
                  enable_gravity=True, gravity=None, density=(1000.0, 1000.0),
                  viscosity=(1e-3, 1e-3), extrusion=None, material=None, source=None,
                  material_params=None, base_epsilon=1e-10, privar_magnitude=(-1.0, -1.0),
-                 numeric_difference_method=1, upwind_weight=1.0):
+                 numeric_difference_method=1, upwind_weight=1.0, analytic=False):
         self.coords = [np.ascontiguousarray(c, dtype=np.float64) for c in coords]
         self.dim = len(self.coords)
         self.cells = [len(c) - 1 for c in self.coords] + [1] * (3 - self.dim)
@@ -214,6 +215,7 @@ class ProblemDesc:
         self.privar_magnitude = tuple(privar_magnitude)
         self.numeric_difference_method = numeric_difference_method
         self.upwind_weight = upwind_weight
+        self.analytic = bool(analytic)
         self._c = None
 
     @property
@@ -243,6 +245,7 @@ class ProblemDesc:
         d.base_epsilon = self.base_epsilon
         d.numeric_difference_method = self.numeric_difference_method
         d.upwind_weight = self.upwind_weight
+        d.diff_method = 1 if self.analytic else 0
         self._c = d          # keep alive while the caller uses it
         return d
 

@@ -98,6 +98,13 @@ MaterialLaw makeLaw(const double* prm)
     m.pcDerivativeLowSw = dpc_dswe(swToSwe(lowSw)) * dswe_dsw * dsw_dswe;
     m.pcDerivativeHighSwEnd = dpc_dswe(swToSwe(highSw)) * dswe_dsw * dsw_dswe;
     m.pcLowSwePcValue = m.pe * std::pow(clamp01(swToSwe(lowSw)), -1.0 / m.lambda);
+    m.dsweDsw = 1.0 / (1.0 - m.swr - m.snr);
+    m.dpcCoef = -m.pe / m.lambda;
+    m.dpcExp = -1.0 / m.lambda - 1.0;
+    m.dkrwCoef = 2.0 / m.lambda + 3.0;
+    m.dkrwExp = 2.0 / m.lambda + 2.0;
+    m.lambdaInv = 1.0 / m.lambda;
+    m.dkrnExp = 2 * m.lambdaInv;
     return m;
 }
 double hostPc(const MaterialLaw& m, double sw)
@@ -234,6 +241,7 @@ dxg::AssemblyArgs dxg_ctx::asmArgs() const
     a.vvU = vvU.get();
     a.vvS = vvS.get();
     a.eps = eps.get();
+    a.dvv = dvv.get();
     a.stPrev = stPrev.get();
     a.A = A.get();
     a.r = r.get();
@@ -252,8 +260,10 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     for (int a = 0; a < d->dim; ++a)
         if (d->cells[a] < 1 || !d->coords[a]) throw Error(DXG_ERR_ARG, "invalid cells/coords");
     if (!d->permeability || !d->porosity || !d->bc_type || !d->bc_values) throw Error(DXG_ERR_ARG, "missing tables");
-    const int method = d->numeric_difference_method;
-    if (method != 1 && method != 0 && method != -1)
+    if (d->diff_method != 0 && d->diff_method != 1) throw Error(DXG_ERR_ARG, "diff_method must be 0 or 1");
+    // internal method code: 1 / 0 / -1 numeric differences, 3 analytic derivatives
+    const int method = d->diff_method == 1 ? 3 : d->numeric_difference_method;
+    if (method != 1 && method != 0 && method != -1 && method != 3)
         throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0 or -1 on the device");
     if (d->num_eq == 2 && (d->num_materials < 1 || d->num_materials > kMaxMaterials || !d->material_params))
         throw Error(DXG_ERR_ARG, "2p needs 1..16 Brooks-Corey parameter sets");
@@ -506,7 +516,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
         c->bytesSpmv = nnzb * bb8 + N * 1.0 + 2.0 * N * v8;
         // assembly: u read, volume variables written and read back, coefficients,
         // Jacobian rows and residual written
-        const int NS = 1 + (method == 0 ? 2 * b : b);
+        const int NS = method == 3 ? 1 : 1 + (method == 0 ? 2 * b : b);
         c->bytesAssembly = N * v8 + 3.0 * N * NS * v8 + N * b * 8.0 /*eps*/ + N * (8.0 * dim + 2.0 * 2 * b * 8.0) +
                            N * (3 * 8.0 + 1 + b * 8.0) + (double)c->slots * N * bb8 + N * v8;
     }
@@ -532,7 +542,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     upload(c->perm, perm, st);
     DXG_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
 
-    const int NS = 1 + (method == 0 ? 2 * b : b);
+    const int NS = method == 3 ? 1 : 1 + (method == 0 ? 2 * b : b);
     const int64_t M = N * b;
     c->u.alloc(M);
     c->uprev.alloc(M);
@@ -542,6 +552,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->vvU.alloc((size_t)NS * b * N);
     c->vvS.alloc((size_t)NS * b * N);
     c->eps.alloc((size_t)b * N);
+    if (method == 3 && b == 2) c->dvv.alloc((size_t)3 * N);   // d(krw, krn, pc)/dSn per cell
     c->A.alloc((size_t)c->slots * N * c->bb);
     c->r.alloc(M);
     c->delta.alloc(M);

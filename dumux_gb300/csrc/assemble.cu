@@ -54,6 +54,34 @@ __device__ __forceinline__ double bcKrn(const MaterialLaw& m, double sw)
     return sne * sne * (1.0 - pow(s, m.expKrn));
 }
 
+// Derivatives w.r.t. the absolute wetting saturation (TwoPMaterialLaw::dpc_dsw, dkrw_dsw,
+// dkrn_dsw, materiallaw.hh:121-239): regularised slopes outside the regularisation
+// thresholds, else the Brooks-Corey derivative (brookscorey.hh:166-174, 241-249, 295-305),
+// times dswe/dsw.
+__device__ __forceinline__ double bcDpcDsw(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= m.pcLowSwe) return m.pcDerivativeLowSw * m.dsweDsw;
+    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * m.dsweDsw;
+    const double s = fmin(fmax(swe, 0.0), 1.0);
+    return m.dpcCoef * pow(s, m.dpcExp) * m.dsweDsw;
+}
+__device__ __forceinline__ double bcDkrwDsw(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
+    const double s = fmin(fmax(swe, 0.0), 1.0);
+    return m.dkrwCoef * pow(s, m.dkrwExp) * m.dsweDsw;
+}
+__device__ __forceinline__ double bcDkrnDsw(const MaterialLaw& m, double sw)
+{
+    const double swe = (sw - m.swr) / m.denom;
+    if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
+    const double s = fmin(fmax(swe, 0.0), 1.0);
+    const double swePow = pow(s, m.dkrnExp);
+    return 2.0 * (s - 1.0) * (1.0 + (0.5 + m.lambdaInv) * swePow - (1.5 + m.lambdaInv) * swePow * s) * m.dsweDsw;
+}
+
 // Volume variables needed by the residual: phase pressure, upwind term rho*lambda and
 // the storage term (phi*rho*S)*extrusion (immiscible/localresidual.hh:64-86,
 // fvlocalresidual.hh:293-297).
@@ -98,7 +126,7 @@ __device__ __forceinline__ double numericEps(const ProblemConsts& pc, double x, 
 template <int B, int METHOD>
 __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ batch)
 {
-    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : (METHOD == 2 ? 0 : B));
+    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : ((METHOD == 2 || METHOD == 3) ? 0 : B));
     const AssemblyArgs a = batch ? batch[blockIdx.y] : a0;
     const ProblemConsts& pc = *a.pc;
     const int64_t N = a.N;
@@ -128,6 +156,15 @@ __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ 
                 a.vvU[(s * B + k) * N + i] = up[k];
                 a.vvS[(s * B + k) * N + i] = st[k];
             }
+        }
+        if (METHOD == 3 && B == 2) {
+            // derivatives w.r.t. S_n are the negatives of those w.r.t. S_w
+            // (2p/incompressiblelocalresidual.hh:198-205)
+            const MaterialLaw& law = pc.law[m];
+            const double Sw = 1 - x[B - 1];
+            a.dvv[i] = -1.0 * bcDkrwDsw(law, Sw);
+            a.dvv[N + i] = -1.0 * bcDkrnDsw(law, Sw);
+            a.dvv[2 * N + i] = -1.0 * bcDpcDsw(law, Sw);
         }
     }
 }
@@ -168,13 +205,35 @@ __device__ __forceinline__ double phaseFlux(double tij, double pin, double pout,
 template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP, bool WANT_JAC>
 __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
 {
-    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : B);
+    constexpr bool ANALYTIC = METHOD == 3;
+    constexpr int NS = ANALYTIC ? 1 : 1 + (METHOD == 0 ? 2 * B : B);
     constexpr int BB = B * B;
     constexpr int NF = 2 * DIM;
     constexpr int VA = DIM - 1;                 // vertical axis (gravity)
     const int64_t N = a.N;
     const ProblemConsts& pc = *a.pc;
     const double w = pc.upwindWeight;
+
+    // analytic path: diagonal block accumulated in the reference's order -- storage
+    // derivatives first (addStorageDerivatives), then each face in turn
+    double dII[BB];
+    double rhoMu[B], dI[3] = {0.0, 0.0, 0.0};
+    if (ANALYTIC && WANT_JAC) {
+#pragma unroll
+        for (int e = 0; e < BB; ++e) dII[e] = 0.0;
+#pragma unroll
+        for (int k = 0; k < B; ++k) rhoMu[k] = pc.density[k] / pc.viscosity[k];
+        if constexpr (B == 2) {
+            dI[0] = a.dvv[I];
+            dI[1] = a.dvv[N + I];
+            dI[2] = a.dvv[2 * N + I];
+            if (TRANSIENT) {
+                const double poreVolume = a.vol[I] * a.phi[I];
+                dII[0 * B + 1] -= poreVolume * pc.density[0] / a.dt;
+                dII[1 * B + 1] += poreVolume * pc.density[1] / a.dt;
+            }
+        }
+    }
 
     // own states
     double pI[NS][B], uI[NS][B];
@@ -235,7 +294,52 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
                     if (s == 0) F0[k] = F;
                     r[s][k] += F;
                 }
-            if (WANT_JAC) {
+            if (ANALYTIC && WANT_JAC) {
+                // addFluxDerivatives (1p: incompressiblelocalresidual.hh:117-123;
+                // 2p: incompressiblelocalresidual.hh:169-252)
+                double blk[BB];
+                if constexpr (B == 1) {
+                    const double deriv = tij * rhoMu[0];
+                    dII[0] += deriv;
+                    blk[0] = 0.0 - deriv;
+                } else {
+                    double flux[B];
+#pragma unroll
+                    for (int k = 0; k < B; ++k) {
+                        double fl = tij * (pI[0][k] - pJ[k]);
+                        if (GRAV && ax == VA) {
+                            fl = fl + g1[k];
+                            fl = fl - g2[k];
+                        }
+                        flux[k] = fl;
+                    }
+                    const double dJ0 = a.dvv[J], dJ1 = a.dvv[N + J], dJ2 = a.dvv[2 * N + J];
+                    const double iw_w = signbit(flux[0]) ? (1.0 - w) : w, ow_w = 1.0 - iw_w;
+                    const double iw_n = signbit(flux[1]) ? (1.0 - w) : w, ow_n = 1.0 - iw_n;
+                    const double up_w = uI[0][0] * iw_w + uJ[0] * ow_w;
+                    const double up_n = uI[0][1] * iw_n + uJ[1] * ow_n;
+                    const double rho_mu_flux_w = rhoMu[0] * flux[0];
+                    const double rho_mu_flux_n = rhoMu[1] * flux[1];
+                    const double tij_up_w = tij * up_w;
+                    const double tij_up_n = tij * up_n;
+                    double bJ[BB] = {0.0, 0.0, 0.0, 0.0};
+                    dII[0] += tij_up_w;
+                    bJ[0] -= tij_up_w;
+                    dII[1] += rho_mu_flux_w * dI[0] * iw_w;
+                    bJ[1] += rho_mu_flux_w * dJ0 * ow_w;
+                    dII[2] += tij_up_n;
+                    bJ[2] -= tij_up_n;
+                    dII[3] += rho_mu_flux_n * dI[1] * iw_n;
+                    bJ[3] += rho_mu_flux_n * dJ1 * ow_n;
+                    dII[3] += tij_up_n * dI[2];
+                    bJ[3] -= tij_up_n * dJ2;
+#pragma unroll
+                    for (int e = 0; e < BB; ++e) blk[e] = bJ[e];
+                }
+                double* dst = a.A + ((int64_t)slot * N + I) * BB;
+#pragma unroll
+                for (int e = 0; e < BB; ++e) dst[e] = blk[e];
+            } else if (WANT_JAC) {
                 double blk[BB];
 #pragma unroll
                 for (int pv = 0; pv < B; ++pv) {
@@ -282,17 +386,42 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
             const int8_t type = a.btype[bidx];
             if (type == 1) {
                 const double tij = a.bTij[bidx];
+                double flux[B], gU[B];
 #pragma unroll
                 for (int k = 0; k < B; ++k) {
                     const double gp = a.bP[k * a.nb + bidx];
                     const double gu = a.bU[k * a.nb + bidx];
                     const double g1 = a.bG1[k * a.nb + bidx];
+                    gU[k] = gu;
+                    double fl = tij * (pI[0][k] - gp);
+                    if (GRAV && ax == VA) {
+                        fl = fl + g1;
+                        fl = fl - 0.0;
+                    }
+                    flux[k] = fl;
 #pragma unroll
                     for (int s = 0; s < NR; ++s) {
                         const double F = (GRAV && ax == VA)
                                              ? phaseFlux<true, FULLUP>(tij, pI[s][k], gp, uI[s][k], gu, g1, 0.0, w)
                                              : phaseFlux<false, FULLUP>(tij, pI[s][k], gp, uI[s][k], gu, 0.0, 0.0, w);
                         r[s][k] += F;
+                    }
+                }
+                if (ANALYTIC && WANT_JAC) {
+                    // addCCDirichletFluxDerivatives (1p: incompressiblelocalresidual.hh:212-219;
+                    // 2p: incompressiblelocalresidual.hh:427-484)
+                    if constexpr (B == 1) {
+                        dII[0] += tij * rhoMu[0];
+                    } else {
+                        const double iw_w = signbit(flux[0]) ? (1.0 - w) : w, ow_w = 1.0 - iw_w;
+                        const double iw_n = signbit(flux[1]) ? (1.0 - w) : w, ow_n = 1.0 - iw_n;
+                        const double up_w = uI[0][0] * iw_w + gU[0] * ow_w;
+                        dII[0] += tij * up_w;
+                        dII[1] += rhoMu[0] * flux[0] * dI[0] * iw_w;
+                        const double up_n = uI[0][1] * iw_n + gU[1] * ow_n;
+                        dII[2] += tij * up_n;
+                        dII[3] += rhoMu[1] * flux[1] * dI[1] * iw_n;
+                        dII[3] += tij * dI[2] * up_n;
                     }
                 }
             } else {
@@ -330,7 +459,11 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
 #pragma unroll
     for (int e = 0; e < B; ++e) a.r[I * B + e] = r[0][e];
 
-    if (WANT_JAC) {
+    if (ANALYTIC && WANT_JAC) {
+        double* dst = a.A + ((int64_t)DIM * N + I) * BB;
+#pragma unroll
+        for (int e = 0; e < BB; ++e) dst[e] = dII[e];
+    } else if (WANT_JAC) {
         double blk[BB];
 #pragma unroll
         for (int pv = 0; pv < B; ++pv) {
@@ -384,11 +517,13 @@ static void volvarsDispatch(const AssemblyArgs& a, const Geo& g, int b, int meth
 {
     if (b == 1) {
         if (method == 2) volvarsT<1, 2>(a, g, st);
+        else if (method == 3) volvarsT<1, 3>(a, g, st);
         else if (method == 1) volvarsT<1, 1>(a, g, st);
         else if (method == -1) volvarsT<1, -1>(a, g, st);
         else volvarsT<1, 0>(a, g, st);
     } else {
         if (method == 2) volvarsT<2, 2>(a, g, st);
+        else if (method == 3) volvarsT<2, 3>(a, g, st);
         else if (method == 1) volvarsT<2, 1>(a, g, st);
         else if (method == -1) volvarsT<2, -1>(a, g, st);
         else volvarsT<2, 0>(a, g, st);
@@ -457,6 +592,7 @@ static void launchRow1(const AssemblyArgs& a, const Geo& g, int method, bool jac
                        bool fullup, cudaStream_t st)
 {
     if (method == 1) launchRow2<B, DIM, 1>(a, g, jac, grav, transient, fullup, st);
+    else if (method == 3) launchRow2<B, DIM, 3>(a, g, jac, grav, transient, fullup, st);
     else if (method == -1) launchRow2<B, DIM, -1>(a, g, jac, grav, transient, fullup, st);
     else launchRow2<B, DIM, 0>(a, g, jac, grav, transient, fullup, st);
 }

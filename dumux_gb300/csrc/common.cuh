@@ -63,6 +63,11 @@ struct MaterialLaw {
     double expKrw;                 // 2.0/lambda + 3.0
     double expKrn;                 // 2.0/lambda + 1.0
     double pcLowSwePcValue, pcDerivativeLowSw, pcDerivativeHighSwEnd, entryPressure;
+    // derivative constants (brookscorey.hh:166-174, 241-249, 295-305; efftoabsdefaultpolicy.hh:135)
+    double dsweDsw;                // 1.0/(1.0 - swr - snr)
+    double dpcCoef, dpcExp;        // -pe/lambda, -1.0/lambda - 1.0
+    double dkrwCoef, dkrwExp;      // 2.0/lambda + 3.0, 2.0/lambda + 2.0
+    double lambdaInv, dkrnExp;     // 1.0/lambda, 2*lambdaInv
 };
 
 // Problem constants visible to the kernels.
@@ -77,7 +82,7 @@ struct ProblemConsts {
     double mobility1p;             // 1.0/viscosity (1p)
     double upwindWeight;
     int upwindFull;                // upwind weight != 1
-    int method;                    // numeric difference method
+    int method;                    // numeric difference method (3: analytic derivatives)
     double baseEps;
     double magnitude[2];
     int numMaterials;

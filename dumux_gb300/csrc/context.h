@@ -36,6 +36,7 @@ struct dxg_ctx {
     // state
     dxg::DevBuf<double> u, uprev, uLast, stPrev;
     dxg::DevBuf<double> vvP, vvU, vvS, eps;
+    dxg::DevBuf<double> dvv;          // analytic derivatives: [dkrw/dSn, dkrn/dSn, dpc/dSn][N]
     dxg::DevBuf<double> A, r;
     double dt = 0.0;
     bool havePrev = false, stPrevValid = false, haveJac = false, haveRes = false, haveFactor = false;

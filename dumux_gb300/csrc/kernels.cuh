@@ -30,6 +30,7 @@ struct AssemblyArgs {
     double* vvU;
     double* vvS;
     double* eps;                // [b][N]
+    double* dvv;                // analytic path: [3][N] dkrw/dSn, dkrn/dSn, dpc/dSn
     double* stPrev;             // [b][N]
     // outputs
     double* A;                  // [slots][N][b*b]

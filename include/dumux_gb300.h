@@ -78,6 +78,11 @@ typedef struct dxg_problem_desc {
     double privar_magnitude[2];  /* Assembly.NumericDifference.PriVarMagnitude (<=0: |x|+1) */
     int32_t numeric_difference_method; /* Assembly.NumericDifferenceMethod: 1 forward, 0 central, -1 backward */
     double upwind_weight;        /* Flux.UpwindWeight (1.0)                         */
+    /* Jacobian differentiation (the assembler's DiffMethod): 0 numeric (default), 1
+     * analytic -- CCLocalAssembler<DiffMethod::analytic>, dumux/assembly/cclocalassembler.hh:
+     * 488-604, with the flux, Dirichlet and storage derivatives of the incompressible 1p / 2p
+     * local residuals (porousmediumflow/{1p,2p}/incompressiblelocalresidual.hh)         */
+    int32_t diff_method;
 } dxg_problem_desc;
 
 /* Number of boundary faces implied by the grid of desc. */

@@ -106,6 +106,33 @@ struct BrooksCoreyDefault {
         const double sne = 1.0 - s;
         return sne * sne * (1.0 - std::pow(s, exponent));
     }
+    // TwoPMaterialLaw::dpc_dsw / dkrw_dsw / dkrn_dsw (materiallaw.hh:121-239): the
+    // regularised slope (BrooksCoreyRegularization::dpc_dswe, dkrw_dswe, dkrn_dswe,
+    // brookscorey.hh:385-475) or the Brooks-Corey derivative (brookscorey.hh:166-305),
+    // times dswe/dsw (efftoabsdefaultpolicy.hh:135-138)
+    double dpc_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= pcLowSwe) return pcDerivativeLowSw * dswe_dsw();
+        else if (swe >= 1.0) return pcDerivativeHighSwEnd * dswe_dsw();
+        return base_dpc_dswe(swe) * dswe_dsw();
+    }
+    double dkrw_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
+        const double s = clamp01(swe);
+        return (2.0 / lambda + 3.0) * std::pow(s, 2.0 / lambda + 2.0) * dswe_dsw();
+    }
+    double dkrn_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
+        const double s = clamp01(swe);
+        const double lambdaInv = 1.0 / lambda;
+        const double swePow = std::pow(s, 2 * lambdaInv);
+        return 2.0 * (s - 1.0) * (1.0 + (0.5 + lambdaInv) * swePow - (1.5 + lambdaInv) * swePow * s) * dswe_dsw();
+    }
 };
 
 // ---------------------------------------------------------------- grid / geometry
@@ -284,6 +311,33 @@ static void computeFlux(const Problem& P, int64_t inside, const Face& f,
     }
 }
 
+// PorousMediumFluxVariables advective Darcy flux of phase ph without the upwinded
+// mobility (AdvectionType::flux, darcyslaw.hh:153-213) and the face transmissibility
+static double darcyFlux(const Problem& P, int64_t inside, const Face& f, const VolVars& vin, const VolVars& vout,
+                        int ph, double* tijOut)
+{
+    const double ti = tpfaT(P, f, inside, vin.K, vin.extr);
+    double tij;
+    if (f.boundary)
+        tij = f.area * ti;
+    else {
+        const double tj = -1.0 * tpfaT(P, f, f.outside, vout.K, vout.extr);
+        if (ti * tj <= 0.0) tij = 0;
+        else tij = f.area * (ti * tj) / (ti + tj);
+    }
+    *tijOut = tij;
+    if (!P.d.enable_gravity) return tij * (vin.p[ph] - vout.p[ph]);
+    const double rho = f.boundary ? vout.rho[ph] : (vin.rho[ph] + vout.rho[ph]) * 0.5;
+    const double alpha_inside = vin.K * nDotG(P, f) * vin.extr;
+    double flux = tij * (vin.p[ph] - vout.p[ph]) + rho * f.area * alpha_inside;
+    if (!f.boundary) {
+        const double outsideTi = -1.0 * tpfaT(P, f, f.outside, vout.K, vout.extr);
+        const double alpha_outside = vout.K * nDotG(P, f) * vout.extr;
+        flux -= rho * tij / outsideTi * (alpha_inside - alpha_outside);
+    }
+    return flux;
+}
+
 // element-local view: volume variables of the element, its neighbours and the
 // Dirichlet ghosts, bound at the current solution
 struct ElemView {
@@ -399,6 +453,7 @@ struct Pattern {
     std::vector<int32_t> col;
     std::vector<int64_t> diag;               // block index of (I,I)
     std::vector<int64_t> colBlock;           // per cell I, per face f: block index of (J,I), -1 if none
+    std::vector<int64_t> rowBlock;           // per cell I, per face f: block index of (I,J), -1 if none
 };
 
 static Pattern buildPattern(const Problem& P)
@@ -429,11 +484,15 @@ static Pattern buildPattern(const Problem& P)
     };
     pt.diag.resize(P.N);
     pt.colBlock.assign(P.N * nf, -1);
+    pt.rowBlock.assign(P.N * nf, -1);
     for (int64_t I = 0; I < P.N; ++I) {
         pt.diag[I] = find(I, I);
         for (int f = 0; f < nf; ++f) {
             const Face fc = P.face(I, f);
-            if (!fc.boundary) pt.colBlock[I * nf + f] = find(fc.outside, I);
+            if (!fc.boundary) {
+                pt.colBlock[I * nf + f] = find(fc.outside, I);
+                pt.rowBlock[I * nf + f] = find(I, fc.outside);
+            }
         }
     }
     return pt;
@@ -515,15 +574,102 @@ static void assembleElement(const Problem& P, const Pattern& pt, int64_t I, cons
     for (int e = 0; e < b; ++e) r[I * b + e] = orig0[e];
 }
 
+// CCLocalAssembler<analytic, implicit>::assembleJacobianAndResidualImpl
+// (cclocalassembler.hh:510-573) for element I: residual, then block row I from the
+// storage derivatives and each face's flux derivatives, in that order
+// (porousmediumflow/1p/incompressiblelocalresidual.hh:55-123, 204-219;
+//  porousmediumflow/2p/incompressiblelocalresidual.hh:80-252, 427-484)
+static void assembleElementAnalytic(const Problem& P, const Pattern& pt, int64_t I, const double* u,
+                                    const double* uprev, double dt, double* values, double* r)
+{
+    const int b = P.b, nf = 2 * P.dim;
+    ElemView ev;
+    bindElement(P, I, u, uprev, dt, ev);
+    double res[2];
+    localResidual(P, ev, ev.vI, res);
+    for (int e = 0; e < b; ++e) r[I * b + e] = res[e];
+    if (!values) return;
+    double* dII = values + pt.diag[I] * b * b;
+    const VolVars& vI = ev.vI;
+    if (b == 2 && ev.transient) {
+        const double poreVolume = P.volume(I) * vI.phi;
+        dII[0 * 2 + 1] -= poreVolume * vI.rho[0] / dt;
+        dII[1 * 2 + 1] += poreVolume * vI.rho[1] / dt;
+    }
+    const double w = P.d.upwind_weight;
+    for (int f = 0; f < nf; ++f) {
+        const Face& fc = ev.faces[f];
+        const bool dirichlet = fc.boundary && P.d.bc_type[fc.bidx] == 1;
+        if (fc.boundary && !dirichlet) continue;        // Neumann: no derivative (Robin hook empty)
+        const VolVars& vO = ev.vOut[f];
+        double* dIJ = dirichlet ? nullptr : values + pt.rowBlock[I * nf + f] * b * b;
+        double tij;
+        if (b == 1) {
+            darcyFlux(P, I, fc, vI, vO, 0, &tij);
+            const double up = vI.rho[0] / P.d.viscosity[0];
+            const double deriv = tij * up;
+            dII[0] += deriv;
+            if (dIJ) dIJ[0] -= deriv;
+            continue;
+        }
+        const double flux_w = darcyFlux(P, I, fc, vI, vO, 0, &tij);
+        const double flux_n = darcyFlux(P, I, fc, vI, vO, 1, &tij);
+        const double iw_w = std::signbit(flux_w) ? (1.0 - w) : w, ow_w = 1.0 - iw_w;
+        const double iw_n = std::signbit(flux_n) ? (1.0 - w) : w, ow_n = 1.0 - iw_n;
+        const double rhow_muw = vI.rho[0] / P.d.viscosity[0];
+        const double rhon_mun = vI.rho[1] / P.d.viscosity[1];
+        const double upW_in = vI.rho[0] * vI.mob[0], upN_in = vI.rho[1] * vI.mob[1];
+        const double upW_out = vO.rho[0] * vO.mob[0], upN_out = vO.rho[1] * vO.mob[1];
+        const auto& lawI = P.law(I);
+        const double dKrw_in = -1.0 * lawI.dkrw_dsw(vI.S[0]);
+        const double dKrn_in = -1.0 * lawI.dkrn_dsw(vI.S[0]);
+        const double dpc_in = -1.0 * lawI.dpc_dsw(vI.S[0]);
+        if (dirichlet) {
+            const double up_w = upW_in * iw_w + upW_out * ow_w;
+            dII[0] += tij * up_w;
+            dII[1] += rhow_muw * flux_w * dKrw_in * iw_w;
+            const double up_n = upN_in * iw_n + upN_out * ow_n;
+            dII[2] += tij * up_n;
+            dII[3] += rhon_mun * flux_n * dKrn_in * iw_n;
+            dII[3] += tij * dpc_in * up_n;
+        } else {
+            const auto& lawJ = P.law(fc.outside);
+            const double dKrw_out = -1.0 * lawJ.dkrw_dsw(vO.S[0]);
+            const double dKrn_out = -1.0 * lawJ.dkrn_dsw(vO.S[0]);
+            const double dpc_out = -1.0 * lawJ.dpc_dsw(vO.S[0]);
+            const double up_w = upW_in * iw_w + upW_out * ow_w;
+            const double up_n = upN_in * iw_n + upN_out * ow_n;
+            const double rho_mu_flux_w = rhow_muw * flux_w;
+            const double rho_mu_flux_n = rhon_mun * flux_n;
+            const double tij_up_w = tij * up_w;
+            const double tij_up_n = tij * up_n;
+            dII[0] += tij_up_w;
+            dIJ[0] -= tij_up_w;
+            dII[1] += rho_mu_flux_w * dKrw_in * iw_w;
+            dIJ[1] += rho_mu_flux_w * dKrw_out * ow_w;
+            dII[2] += tij_up_n;
+            dIJ[2] -= tij_up_n;
+            dII[3] += rho_mu_flux_n * dKrn_in * iw_n;
+            dIJ[3] += rho_mu_flux_n * dKrn_out * ow_n;
+            dII[3] += tij_up_n * dpc_in;
+            dIJ[3] -= tij_up_n * dpc_out;
+        }
+    }
+}
+
 static void assemble(const Problem& P, const Pattern& pt, const double* u, const double* uprev, double dt,
                      double* values, double* r)
 {
     const int b = P.b;
     if (values) std::fill(values, values + pt.rowPtr[P.N] * b * b, 0.0);
-    // Column-wise scatter: element I writes only block column I and r[I], so the
-    // element loop is race free without colouring.
+    // Numeric: column-wise scatter, element I writes only block column I and r[I];
+    // analytic: element I writes only block row I and r[I]; both race free.
+    const bool analytic = P.d.diff_method == 1;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
-    for (int64_t I = 0; I < P.N; ++I) assembleElement(P, pt, I, u, uprev, dt, values, r);
+    for (int64_t I = 0; I < P.N; ++I) {
+        if (analytic) assembleElementAnalytic(P, pt, I, u, uprev, dt, values, r);
+        else assembleElement(P, pt, I, u, uprev, dt, values, r);
+    }
 }
 
 // ---------------------------------------------------------------- dune-istl restatement
