@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--workload", default="2p", choices=["2p", "1p", "ensemble", "serve"],
                     help="2p: transient water-DNAPL (default); 1p: stationary Darcy, 100x100, one Newton step; "
                          "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching")
+    ap.add_argument("--diff", default="numeric", choices=["numeric", "analytic"],
+                    help="Jacobian by numeric differentiation (default, the reference's default) or analytic")
     ap.add_argument("--problems", type=int, default=256, help="ensemble size")
     ap.add_argument("--requests", type=int, default=48, help="served-stream length")
     ap.add_argument("--ticks-per-step", type=int, default=25, help="ensemble: engine ticks per timed step")
@@ -64,6 +66,7 @@ def dist_info():
 
 
 WORKLOAD = "2p"
+DIFF = "numeric"
 
 
 def reduce_over_ranks(seconds, sums, device):
@@ -93,7 +96,8 @@ def workload_name(cells, precision):
         return (f"1p incompressible Darcy cc-TPFA {'x'.join(map(str, cells[:2]))} cells on [0,1]^2, stationary, "
                 f"one Newton step, ILU0-BiCGSTAB reduction 1e-12, {precision.upper()} linear system")
     return (f"2p water-DNAPL cc-TPFA {'x'.join(map(str, cells))} cells, implicit Euler dt=250 s, "
-            f"Newton shift 1e-8, ILU0-BiCGSTAB reduction 1e-6, {precision.upper()} linear system")
+            f"Newton shift 1e-8, ILU0-BiCGSTAB reduction 1e-6, {precision.upper()} linear system"
+            + (", analytic Jacobian" if DIFF == "analytic" else ""))
 
 
 def step_params():
@@ -321,6 +325,8 @@ def run_ensemble(args):
     T = args.ticks_per_step
     t_end = 1e12                   # problems keep stepping through the whole run
     probs = problems.ensemble_2p(count=args.problems, seed=4 + 100003 * rank)
+    for d, _, _ in probs:
+        d.analytic = args.diff == "analytic"
     cells_total = sum(d.num_cells for d, _, _ in probs)
 
     def barrier():
@@ -502,9 +508,10 @@ def run_serve(args):
 
 
 def main():
-    global WORKLOAD
+    global WORKLOAD, DIFF
     args = parse()
     WORKLOAD = args.workload
+    DIFF = args.diff
     if args.workload in ("ensemble", "serve") and args.impl == "gb300":
         if args.precision == "fp64" and "--precision" not in sys.argv:
             args.precision = "mixed"
@@ -527,6 +534,7 @@ def main():
 
     import dumux_gb300
     desc, u0 = workload(cells, seed=2 + rank)
+    desc.analytic = args.diff == "analytic"
     ctx = dumux_gb300.Context(desc, device=local, precision=args.precision)
     params = step_params()
     stationary = args.workload == "1p"
