@@ -48,6 +48,7 @@ class ProblemDescC(C.Structure):
         ("numeric_difference_method", C.c_int32),
         ("upwind_weight", C.c_double),
         ("diff_method", C.c_int32),
+        ("material_law", C.c_int32),
     ]
 
 
@@ -186,7 +187,7 @@ class ProblemDesc:
                  enable_gravity=True, gravity=None, density=(1000.0, 1000.0),
                  viscosity=(1e-3, 1e-3), extrusion=None, material=None, source=None,
                  material_params=None, base_epsilon=1e-10, privar_magnitude=(-1.0, -1.0),
-                 numeric_difference_method=1, upwind_weight=1.0, analytic=False):
+                 numeric_difference_method=1, upwind_weight=1.0, analytic=False, material_law="brooks-corey"):
         self.coords = [np.ascontiguousarray(c, dtype=np.float64) for c in coords]
         self.dim = len(self.coords)
         self.cells = [len(c) - 1 for c in self.coords] + [1] * (3 - self.dim)
@@ -198,9 +199,11 @@ class ProblemDesc:
         self.extrusion = None if extrusion is None else np.ascontiguousarray(extrusion, dtype=np.float64).reshape(n)
         self.material = None if material is None else np.ascontiguousarray(material, dtype=np.int32).reshape(n)
         self.source = None if source is None else np.ascontiguousarray(source, dtype=np.float64).reshape(n * self.num_eq)
+        self.material_law = {"brooks-corey": 0, "van-genuchten": 1}[material_law]
+        width = 5 if self.material_law == 0 else 9
         if material_params is None:
-            material_params = np.zeros((1, 5))
-        self.material_params = np.ascontiguousarray(material_params, dtype=np.float64).reshape(-1, 5)
+            material_params = np.zeros((1, width))
+        self.material_params = np.ascontiguousarray(material_params, dtype=np.float64).reshape(-1, width)
         nb = num_boundary_faces(self.dim, self.cells)
         self.bc_type = np.ascontiguousarray(bc_type, dtype=np.int8).reshape(nb)
         self.bc_values = np.ascontiguousarray(bc_values, dtype=np.float64).reshape(nb * self.num_eq)
@@ -246,6 +249,7 @@ class ProblemDesc:
         d.numeric_difference_method = self.numeric_difference_method
         d.upwind_weight = self.upwind_weight
         d.diff_method = 1 if self.analytic else 0
+        d.material_law = self.material_law
         self._c = d          # keep alive while the caller uses it
         return d
 

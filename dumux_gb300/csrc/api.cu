@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "context.h"
+#include "materiallaw.cuh"
 
 using namespace dxg;
 
@@ -74,63 +75,6 @@ double dotN(int dim, const double* n, const double* g)
 }
 
 // BrooksCoreyDefault evaluated on the host (Dirichlet ghost states, law constants)
-MaterialLaw makeLaw(const double* prm)
-{
-    MaterialLaw m{};
-    m.pe = prm[0];
-    m.lambda = prm[1];
-    m.swr = prm[2];
-    m.snr = prm[3];
-    m.pcLowSwe = prm[4];
-    m.denom = 1.0 - m.swr - m.snr;
-    m.expPc = -1.0 / m.lambda;
-    m.expKrw = 2.0 / m.lambda + 3.0;
-    m.expKrn = 2.0 / m.lambda + 1.0;
-    auto swToSwe = [&](double sw) { return (sw - m.swr) / (1.0 - m.swr - m.snr); };
-    auto sweToSw = [&](double swe) { return swe * (1.0 - m.swr - m.snr) + m.swr; };
-    auto clamp01 = [](double v) { return std::clamp(v, 0.0, 1.0); };
-    auto dpc_dswe = [&](double swe) { swe = clamp01(swe); return -m.pe / m.lambda * std::pow(swe, -1.0 / m.lambda - 1.0); };
-    const double dswe_dsw = 1.0 / (1.0 - m.swr - m.snr);
-    const double dsw_dswe = 1.0 - m.swr - m.snr;
-    const double lowSw = sweToSw(m.pcLowSwe);
-    const double highSw = sweToSw(1.0);
-    m.entryPressure = m.pe;
-    m.pcDerivativeLowSw = dpc_dswe(swToSwe(lowSw)) * dswe_dsw * dsw_dswe;
-    m.pcDerivativeHighSwEnd = dpc_dswe(swToSwe(highSw)) * dswe_dsw * dsw_dswe;
-    m.pcLowSwePcValue = m.pe * std::pow(clamp01(swToSwe(lowSw)), -1.0 / m.lambda);
-    m.dsweDsw = 1.0 / (1.0 - m.swr - m.snr);
-    m.dpcCoef = -m.pe / m.lambda;
-    m.dpcExp = -1.0 / m.lambda - 1.0;
-    m.dkrwCoef = 2.0 / m.lambda + 3.0;
-    m.dkrwExp = 2.0 / m.lambda + 2.0;
-    m.lambdaInv = 1.0 / m.lambda;
-    m.dkrnExp = 2 * m.lambdaInv;
-    return m;
-}
-double hostPc(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
-    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0) + m.entryPressure;
-    return m.pe * std::pow(std::clamp(swe, 0.0, 1.0), m.expPc);
-}
-double hostKrw(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0) return 0.0;
-    else if (swe >= 1.0) return 1.0;
-    return std::pow(std::clamp(swe, 0.0, 1.0), m.expKrw);
-}
-double hostKrn(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0) return 1.0;
-    else if (swe >= 1.0) return 0.0;
-    const double s = std::clamp(swe, 0.0, 1.0);
-    const double sne = 1.0 - s;
-    return sne * sne * (1.0 - std::pow(s, m.expKrn));
-}
-
 template <class T>
 void upload(DevBuf<T>& buf, const std::vector<T>& h, cudaStream_t st)
 {
@@ -265,6 +209,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     const int method = d->diff_method == 1 ? 3 : d->numeric_difference_method;
     if (method != 1 && method != 0 && method != -1 && method != 3)
         throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0 or -1 on the device");
+    if (d->num_eq == 2 && d->material_law != 0 && d->material_law != 1)
+        throw Error(DXG_ERR_ARG, "material_law must be 0 (Brooks-Corey) or 1 (Van Genuchten)");
     if (d->num_eq == 2 && (d->num_materials < 1 || d->num_materials > kMaxMaterials || !d->material_params))
         throw Error(DXG_ERR_ARG, "2p needs 1..16 Brooks-Corey parameter sets");
 
@@ -326,7 +272,9 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     pc.baseEps = d->base_epsilon > 0 ? d->base_epsilon : 1e-10;
     pc.numMaterials = b == 2 ? d->num_materials : 0;
     pc.hasSource = d->source != nullptr;
-    for (int m = 0; m < pc.numMaterials; ++m) pc.law[m] = makeLaw(d->material_params + 5 * m);
+    const int lawWidth = d->material_law == 1 ? 9 : 5;
+    for (int m = 0; m < pc.numMaterials; ++m)
+        pc.law[m] = makeMaterialLaw(d->material_law, d->material_params + lawWidth * m);
 
     const int64_t strides[3] = {1, g.n[0], g.n[0] * g.n[1]};
     for (int s = 0; s < c->slots; ++s) c->off[s] = 0;
@@ -461,11 +409,11 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
                         const MaterialLaw& m = pc.law[mat[i]];
                         const double Sn = bv[1];
                         const double Sw = 1 - Sn;
-                        const double pcap = hostPc(m, Sw);
+                        const double pcap = lawPc(m, Sw);
                         bP[0 * nb + bidx] = bv[0];
                         bP[1 * nb + bidx] = bv[0] + pcap;
-                        bU[0 * nb + bidx] = d->density[0] * (hostKrw(m, Sw) / d->viscosity[0]);
-                        bU[1 * nb + bidx] = d->density[1] * (hostKrn(m, Sw) / d->viscosity[1]);
+                        bU[0 * nb + bidx] = d->density[0] * (lawKrw(m, Sw) / d->viscosity[0]);
+                        bU[1 * nb + bidx] = d->density[1] * (lawKrn(m, Sw) / d->viscosity[1]);
                     }
                     if (c->gravity && a == va && grav[va] != 0.0) {
                         const double ng = dotN(dim, n, grav);

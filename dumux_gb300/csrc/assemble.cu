@@ -24,63 +24,13 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "materiallaw.cuh"
 
 namespace dxg {
 
 // ---------------------------------------------------------------- constitutive laws
-// Regularised Brooks-Corey (brookscorey.hh:99-503 with TwoPEffToAbsDefaultPolicy).
-__device__ __forceinline__ double bcPc(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
-    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0) + m.entryPressure;
-    const double s = fmin(fmax(swe, 0.0), 1.0);
-    return m.pe * pow(s, m.expPc);
-}
-__device__ __forceinline__ double bcKrw(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0) return 0.0;
-    else if (swe >= 1.0) return 1.0;
-    return pow(fmin(fmax(swe, 0.0), 1.0), m.expKrw);
-}
-__device__ __forceinline__ double bcKrn(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0) return 1.0;
-    else if (swe >= 1.0) return 0.0;
-    const double s = fmin(fmax(swe, 0.0), 1.0);
-    const double sne = 1.0 - s;
-    return sne * sne * (1.0 - pow(s, m.expKrn));
-}
-
-// Derivatives w.r.t. the absolute wetting saturation (TwoPMaterialLaw::dpc_dsw, dkrw_dsw,
-// dkrn_dsw, materiallaw.hh:121-239): regularised slopes outside the regularisation
-// thresholds, else the Brooks-Corey derivative (brookscorey.hh:166-174, 241-249, 295-305),
-// times dswe/dsw.
-__device__ __forceinline__ double bcDpcDsw(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= m.pcLowSwe) return m.pcDerivativeLowSw * m.dsweDsw;
-    else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * m.dsweDsw;
-    const double s = fmin(fmax(swe, 0.0), 1.0);
-    return m.dpcCoef * pow(s, m.dpcExp) * m.dsweDsw;
-}
-__device__ __forceinline__ double bcDkrwDsw(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
-    const double s = fmin(fmax(swe, 0.0), 1.0);
-    return m.dkrwCoef * pow(s, m.dkrwExp) * m.dsweDsw;
-}
-__device__ __forceinline__ double bcDkrnDsw(const MaterialLaw& m, double sw)
-{
-    const double swe = (sw - m.swr) / m.denom;
-    if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
-    const double s = fmin(fmax(swe, 0.0), 1.0);
-    const double swePow = pow(s, m.dkrnExp);
-    return 2.0 * (s - 1.0) * (1.0 + (0.5 + m.lambdaInv) * swePow - (1.5 + m.lambdaInv) * swePow * s) * m.dsweDsw;
-}
+// Regularised Brooks-Corey / Van Genuchten: materiallaw.cuh (lawPc, lawKrw, lawKrn and
+// their derivatives w.r.t. sw).
 
 // Volume variables needed by the residual: phase pressure, upwind term rho*lambda and
 // the storage term (phi*rho*S)*extrusion (immiscible/localresidual.hh:64-86,
@@ -100,11 +50,11 @@ __device__ __forceinline__ void volVars(const ProblemConsts& pc, const double* p
         const MaterialLaw& m = pc.law[mat];
         const double Sn = pv[1];
         const double Sw = 1 - Sn;
-        const double pcap = bcPc(m, Sw);
+        const double pcap = lawPc(m, Sw);
         p[0] = pv[0];
         p[1] = pv[0] + pcap;
-        const double mobW = bcKrw(m, Sw) / pc.viscosity[0];
-        const double mobN = bcKrn(m, Sw) / pc.viscosity[1];
+        const double mobW = lawKrw(m, Sw) / pc.viscosity[0];
+        const double mobN = lawKrn(m, Sw) / pc.viscosity[1];
         up[0] = pc.density[0] * mobW;
         up[1] = pc.density[1] * mobN;
         double sW = phi * pc.density[0] * Sw;
@@ -162,9 +112,9 @@ __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ 
             // (2p/incompressiblelocalresidual.hh:198-205)
             const MaterialLaw& law = pc.law[m];
             const double Sw = 1 - x[B - 1];
-            a.dvv[i] = -1.0 * bcDkrwDsw(law, Sw);
-            a.dvv[N + i] = -1.0 * bcDkrnDsw(law, Sw);
-            a.dvv[2 * N + i] = -1.0 * bcDpcDsw(law, Sw);
+            a.dvv[i] = -1.0 * lawDkrwDsw(law, Sw);
+            a.dvv[N + i] = -1.0 * lawDkrnDsw(law, Sw);
+            a.dvv[2 * N + i] = -1.0 * lawDpcDsw(law, Sw);
         }
     }
 }

@@ -56,7 +56,15 @@ constexpr int kMaxMaterials = 16;
 
 // Derived constants of one regularised Brooks-Corey parameter set
 // (BrooksCoreyRegularization::initPcParameters_, brookscorey.hh:477-486).
+// Two-point cubic spline of the Van Genuchten regularisation (Spline<Scalar, 2>,
+// dumux/common/spline.hh:310-345): end points, values and the moments of the clamped
+// spline (dumux/common/splinecommon_.hh:419-440).
+struct Spline2 {
+    double x0, x1, y0, y1, M0, M1;
+};
+
 struct MaterialLaw {
+    int kind;                      // 0 regularised Brooks-Corey, 1 regularised Van Genuchten
     double pe, lambda, swr, snr, pcLowSwe;
     double denom;                  // 1.0 - swr - snr
     double expPc;                  // -1.0/lambda
@@ -68,6 +76,12 @@ struct MaterialLaw {
     double dpcCoef, dpcExp;        // -pe/lambda, -1.0/lambda - 1.0
     double dkrwCoef, dkrwExp;      // 2.0/lambda + 3.0, 2.0/lambda + 2.0
     double lambdaInv, dkrnExp;     // 1.0/lambda, 2*lambdaInv
+    // Van Genuchten (vangenuchten.hh:30-300): alpha, n, m = 1 - 1/n, l and the exponents
+    // the reference forms at run time; regularisation thresholds and splines
+    double vgAlpha, vgN, vgM, vgL;
+    double vgNegInvM, vgInvN, vgInvM;       // -1.0/m, 1.0/n, 1.0/m
+    double pcHighSwe, krnLowSwe, krwHighSwe;
+    Spline2 pcSpline, krwSpline, krnSpline;
 };
 
 // Problem constants visible to the kernels.

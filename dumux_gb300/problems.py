@@ -188,3 +188,36 @@ def make_request_problem(req):
         return darcy_1p(cells=req["cells"], seed=req["seed"], sigma=req["sigma"], corr_len=req["corr_len"])
     return dnapl_2p(cells=req["cells"], seed=req["seed"], sigma=req["sigma"], corr_len=req["corr_len"],
                     inflow=req["inflow"])
+
+
+# Van Genuchten parameter sets of the reference's 2p lens test (SpatialParams.Lens /
+# SpatialParams.Outer of test/porousmediumflow/2p/incompressible/params.input; l, Snr and
+# the regularisation thresholds at their defaults): alpha, n, l, Swr, Snr, pcLowSwe,
+# pcHighSwe, krnLowSwe, krwHighSwe
+LENS_VG = (0.00045, 7.3, 0.5, 0.18, 0.0, 0.01, 0.99, 0.1, 0.9)
+OUTER_VG = (0.0037, 4.7, 0.5, 0.05, 0.0, 0.01, 0.99, 0.1, 0.9)
+
+
+def twop_lens_problem(cells=(48, 32), analytic=False):
+    """The reference's 2p incompressible cc-TPFA test (test/porousmediumflow/2p/
+    incompressible: problem.hh, spatialparams.hh, params.input): [0,6]x[0,4] m, DNAPL
+    lens [1,4]x[2,3] with K 9.05e-12 in 4.6e-10 m^2, regularised Van Genuchten laws,
+    porosity 0.4, gravity, hydrostatic Dirichlet left/right, DNAPL inflow -0.04 kg/m^2/s on
+    the top strip, p_w hydrostatic and S_n = 0 initially.  Run with dt 250 s and end time
+    3000 s it is the case of test_2p_incompressible_tpfa(_analytic)."""
+    base, u0 = dnapl_2p(cells=cells, extent=(6.0, 4.0), lnk=np.zeros(int(np.prod(cells))))
+    coords = base.coords
+    cc = cell_centers(coords)
+    eps = 1.5e-7
+    lo, hi = (1.0, 2.0), (4.0, 3.0)
+    in_lens = np.ones(len(cc), dtype=bool)
+    for a in range(2):
+        in_lens &= ~((cc[:, a] < lo[a] + eps) | (cc[:, a] > hi[a] - eps))
+    K = np.where(in_lens, 9.05e-12, 4.6e-10)
+    desc = ProblemDesc(coords=coords, num_eq=2, permeability=K, porosity=np.full(len(cc), 0.4),
+                       bc_type=base.bc_type, bc_values=base.bc_values, enable_gravity=True,
+                       density=(WATER_DENSITY, DNAPL_DENSITY), viscosity=(WATER_VISCOSITY, DNAPL_VISCOSITY),
+                       material=np.where(in_lens, 0, 1).astype(np.int32),
+                       material_params=np.array([LENS_VG, OUTER_VG]), material_law="van-genuchten",
+                       analytic=analytic)
+    return desc, u0

@@ -83,6 +83,12 @@ typedef struct dxg_problem_desc {
      * 488-604, with the flux, Dirichlet and storage derivatives of the incompressible 1p / 2p
      * local residuals (porousmediumflow/{1p,2p}/incompressiblelocalresidual.hh)         */
     int32_t diff_method;
+    /* Material law of the 2p parameter sets: 0 regularised Brooks-Corey (5 doubles per set,
+     * see above), 1 regularised Van Genuchten (VanGenuchtenDefault, material/
+     * fluidmatrixinteractions/2p/vangenuchten.hh; 9 doubles per set: alpha [1/Pa], n, l,
+     * Swr, Snr, pcLowSwe, pcHighSwe, krnLowSwe, krwHighSwe -- the reference's defaults
+     * for the last four are 0.01, 0.99, 0.1, 0.9)                                        */
+    int32_t material_law;
 } dxg_problem_desc;
 
 /* Number of boundary faces implied by the grid of desc. */

@@ -35,6 +35,7 @@ def lib():
         L.orc_suggest_time_step.argtypes = [C.c_int32, C.c_double, C.POINTER(NewtonParamsC)]
         L.orc_suggest_time_step.restype = C.c_double
         L.orc_brooks_corey.argtypes = [dp, C.c_int32, C.c_int64, dp, dp]
+        L.orc_van_genuchten.argtypes = [dp, C.c_int32, C.c_int64, dp, dp]
         L.orc_numdiff_poly.argtypes = [C.c_int32, C.c_double, C.c_double]
         L.orc_numdiff_poly.restype = C.c_double
         L.orc_newton_scalar.argtypes = [C.c_double, C.POINTER(NewtonParamsC), dp, i32p]
@@ -114,6 +115,16 @@ def brooks_corey(params5, what, sw):
     out = np.zeros_like(sw)
     prm = np.ascontiguousarray(params5, dtype=np.float64)
     lib().orc_brooks_corey(_dp(prm), {"pc": 0, "krw": 1, "krn": 2}[what], len(sw), _dp(sw), _dp(out))
+    return out
+
+
+def van_genuchten(params9, what, sw):
+    """Regularised Van Genuchten: what in pc, krw, krn, dpc_dsw, dkrw_dsw, dkrn_dsw."""
+    sw = np.ascontiguousarray(sw, dtype=np.float64)
+    prm = np.ascontiguousarray(params9, dtype=np.float64)
+    out = np.zeros_like(sw)
+    k = ["pc", "krw", "krn", "dpc_dsw", "dkrw_dsw", "dkrn_dsw"].index(what)
+    assert lib().orc_van_genuchten(_dp(prm), k, sw.size, _dp(sw), _dp(out)) == 0
     return out
 
 

@@ -136,6 +136,172 @@ struct BrooksCoreyDefault {
 };
 
 // ---------------------------------------------------------------- grid / geometry
+// VanGenuchtenDefault = TwoPMaterialLaw<VanGenuchten, VanGenuchtenRegularization,
+// TwoPEffToAbsDefaultPolicy> (material/fluidmatrixinteractions/2p/vangenuchten.hh:30-620,
+// materiallaw.hh:103-239): base law on the clamped effective saturation; regularisation by
+// linear extensions and clamped two-point cubic splines (common/spline.hh:310-345,
+// common/splinecommon_.hh:419-523) outside [pcLowSwe, pcHighSwe] for pc, above krwHighSwe
+// for krw and below krnLowSwe for krn.
+struct Spline2Point {
+    double x0 = 0, x1 = 1, y0 = 0, y1 = 0, M0 = 0, M1 = 0;
+    Spline2Point() = default;
+    Spline2Point(double a0, double a1, double b0, double b1, double m0, double m1)
+        : x0(a0), x1(a1), y0(b0), y1(b1)
+    {
+        // moments of the clamped spline: [[2,1],[1,2]] M = d, closed-form 2x2 solve
+        const double h = x1 - x0;
+        const double d0 = 6 / h * ((y1 - y0) / h - m0);
+        const double d1 = 6 / h * (m1 - (y1 - y0) / h);
+        double detinv = 2.0 * 2.0 - 1.0 * 1.0;
+        detinv = 1.0 / detinv;
+        M0 = detinv * (2.0 * d0 - 1.0 * d1);
+        M1 = detinv * (2.0 * d1 - 1.0 * d0);
+    }
+    double eval(double x) const
+    {
+        const double h = x1 - x0, xi = x - x0, xi1 = x1 - x;
+        const double A = (y1 - y0) / h - h / 6 * (M1 - M0);
+        const double B = y0 - M0 * (h * h) / 6;
+        return M0 * xi1 * xi1 * xi1 / (6 * h) + M1 * xi * xi * xi / (6 * h) + A * xi + B;
+    }
+    double derivative(double x) const
+    {
+        const double h = x1 - x0, xi = x - x0, xi1 = x1 - x;
+        const double A = (y1 - y0) / h - h / 6 * (M1 - M0);
+        return -M0 * xi1 * xi1 / (2 * h) + M1 * xi * xi / (2 * h) + A;
+    }
+};
+
+struct VanGenuchtenDefault {
+    double alpha, n, m, l, swr, snr;
+    double pcLowSwe, pcHighSwe, krnLowSwe, krwHighSwe;
+    double pcLowSwePcValue = 0, pcDerivativeLowSw = 0, pcDerivativeHighSweEnd = 0;
+    Spline2Point pcSpline, krwSpline, krnSpline;
+
+    explicit VanGenuchtenDefault(const double* prm)
+        : alpha(prm[0]), n(prm[1]), m(1.0 - 1.0 / prm[1]), l(prm[2]), swr(prm[3]), snr(prm[4]),
+          pcLowSwe(prm[5]), pcHighSwe(prm[6]), krnLowSwe(prm[7]), krwHighSwe(prm[8])
+    {
+        const double dsw_dswe = 1.0 - swr - snr;
+        // initPcParameters_ (vangenuchten.hh:553-574)
+        const double lowSw = sweToSw(pcLowSwe), highSw = sweToSw(pcHighSwe);
+        pcDerivativeLowSw = base_dpc_dswe(swToSwe(lowSw)) * dswe_dsw() * dsw_dswe;
+        const double pcDerivativeHighSweThreshold = base_dpc_dswe(swToSwe(highSw)) * dswe_dsw() * dsw_dswe;
+        pcDerivativeHighSweEnd = 2.0 * (0.0 - base_pc(swToSwe(highSw))) / (1.0 - pcHighSwe);
+        pcLowSwePcValue = base_pc(swToSwe(lowSw));
+        const double pcHighSwePcValue = base_pc(swToSwe(highSw));
+        if (pcHighSwe < 1.0)
+            pcSpline = Spline2Point(pcHighSwe, 1.0, pcHighSwePcValue, 0, pcDerivativeHighSweThreshold,
+                                    pcDerivativeHighSweEnd);
+        // initKrParameters_ (vangenuchten.hh:576-598)
+        const double krLowSw = sweToSw(krnLowSwe), krHighSw = sweToSw(krwHighSwe);
+        const double krwHighSw = base_krw(swToSwe(krHighSw));
+        const double dkrwHighSw = base_dkrw_dswe(swToSwe(krHighSw)) * dswe_dsw() * dsw_dswe;
+        const double krnLowSw = base_krn(swToSwe(krLowSw));
+        const double dkrnLowSw = base_dkrn_dswe(swToSwe(krLowSw)) * dswe_dsw() * dsw_dswe;
+        if (krwHighSwe < 1.0) krwSpline = Spline2Point(krwHighSwe, 1.0, krwHighSw, 1.0, dkrwHighSw, 0.0);
+        if (krnLowSwe > 0.0) krnSpline = Spline2Point(0.0, krnLowSwe, 1.0, krnLowSw, 0.0, dkrnLowSw);
+    }
+    double swToSwe(double sw) const { return (sw - swr) / (1.0 - swr - snr); }
+    double sweToSw(double swe) const { return swe * (1.0 - swr - snr) + swr; }
+    double dswe_dsw() const { return 1.0 / (1.0 - swr - snr); }
+    static double c01(double x) { return std::clamp(x, 0.0, 1.0); }
+    double base_pc(double swe) const { swe = c01(swe); return std::pow(std::pow(swe, -1.0 / m) - 1, 1.0 / n) / alpha; }
+    double base_dpc_dswe(double swe) const
+    {
+        swe = c01(swe);
+        const double powSwe = std::pow(swe, -1 / m);
+        return -1.0 / alpha * std::pow(powSwe - 1, 1.0 / n - 1) / n * powSwe / swe / m;
+    }
+    double base_krw(double swe) const
+    {
+        swe = c01(swe);
+        const double r = 1.0 - std::pow(1.0 - std::pow(swe, 1.0 / m), m);
+        return std::pow(swe, l) * r * r;
+    }
+    double base_dkrw_dswe(double swe) const
+    {
+        swe = c01(swe);
+        const double x = 1.0 - std::pow(swe, 1.0 / m);
+        const double xToM = std::pow(x, m);
+        return (1.0 - xToM) * std::pow(swe, l - 1) * ((1.0 - xToM) * l + 2 * xToM * (1.0 - x) / x);
+    }
+    double base_krn(double swe) const
+    {
+        swe = c01(swe);
+        return std::pow(1 - swe, l) * std::pow(1 - std::pow(swe, 1.0 / m), 2 * m);
+    }
+    double base_dkrn_dswe(double swe) const
+    {
+        swe = c01(swe);
+        const double sne = 1.0 - swe;
+        const double x = 1.0 - std::pow(swe, 1.0 / m);
+        return -std::pow(sne, l - 1.0) * std::pow(x, 2 * m - 1.0) * (l * x + 2.0 * sne / swe * (1.0 - x));
+    }
+    double pc(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= pcLowSwe) return pcLowSwePcValue + pcDerivativeLowSw * (swe - pcLowSwe);
+        else if (swe >= 1.0) return pcDerivativeHighSweEnd * (swe - 1.0);
+        else if (swe > pcHighSwe) return pcSpline.eval(swe);
+        return base_pc(swe);
+    }
+    double krw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0) return 0.0;
+        else if (swe >= 1.0) return 1.0;
+        else if (swe >= krwHighSwe) return krwSpline.eval(swe);
+        return base_krw(swe);
+    }
+    double krn(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0) return 1.0;
+        else if (swe >= 1.0) return 0.0;
+        else if (swe <= krnLowSwe) return krnSpline.eval(swe);
+        return base_krn(swe);
+    }
+    double dpc_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= pcLowSwe) return pcDerivativeLowSw * dswe_dsw();
+        else if (swe >= 1.0) return pcDerivativeHighSweEnd * dswe_dsw();
+        else if (swe > pcHighSwe) return pcSpline.derivative(swe) * dswe_dsw();
+        return base_dpc_dswe(swe) * dswe_dsw();
+    }
+    double dkrw_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
+        else if (swe >= krwHighSwe) return krwSpline.derivative(swe) * dswe_dsw();
+        return base_dkrw_dswe(swe) * dswe_dsw();
+    }
+    double dkrn_dsw(double sw) const
+    {
+        const double swe = swToSwe(sw);
+        if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
+        else if (swe <= krnLowSwe) return krnSpline.derivative(swe) * dswe_dsw();
+        return base_dkrn_dswe(swe) * dswe_dsw();
+    }
+};
+
+// The 2p material law of one parameter set: Brooks-Corey or Van Genuchten.
+struct TwoPLaw {
+    int kind;
+    BrooksCoreyDefault bc;
+    VanGenuchtenDefault vg;
+    static const double* zeros() { static const double z[9] = {1, 2, 0, 0, 0, 0.01, 0.99, 0.1, 0.9}; return z; }
+    TwoPLaw(int k, const double* prm)
+        : kind(k), bc(k == 0 ? prm : zeros()), vg(k == 1 ? prm : zeros()) {}
+    double pc(double sw) const { return kind == 0 ? bc.pc(sw) : vg.pc(sw); }
+    double krw(double sw) const { return kind == 0 ? bc.krw(sw) : vg.krw(sw); }
+    double krn(double sw) const { return kind == 0 ? bc.krn(sw) : vg.krn(sw); }
+    double dpc_dsw(double sw) const { return kind == 0 ? bc.dpc_dsw(sw) : vg.dpc_dsw(sw); }
+    double dkrw_dsw(double sw) const { return kind == 0 ? bc.dkrw_dsw(sw) : vg.dkrw_dsw(sw); }
+    double dkrn_dsw(double sw) const { return kind == 0 ? bc.dkrn_dsw(sw) : vg.dkrn_dsw(sw); }
+};
+
 struct Face {
     int axis, side;            // local face f = 2*axis + side
     bool boundary;
@@ -149,7 +315,7 @@ struct Problem {
     int dim, b;
     int64_t n[3], N;
     int64_t side_offset[7];
-    std::vector<BrooksCoreyDefault> laws;
+    std::vector<TwoPLaw> laws;
     double g[3] = {0, 0, 0};
 
     explicit Problem(const dxg_problem_desc& desc) : d(desc)
@@ -166,7 +332,10 @@ struct Problem {
             for (int c = 0; c < dim; ++c) if (c != a) cnt *= n[c];
             side_offset[f + 1] = side_offset[f] + cnt;
         }
-        if (b == 2) for (int m = 0; m < d.num_materials; ++m) laws.emplace_back(d.material_params + 5 * m);
+        if (b == 2) {
+            const int width = d.material_law == 1 ? 9 : 5;
+            for (int m = 0; m < d.num_materials; ++m) laws.emplace_back(d.material_law, d.material_params + width * m);
+        }
         if (d.enable_gravity) for (int a = 0; a < dim; ++a) g[a] = d.gravity[a];
     }
     void ijk(int64_t c, int64_t* id) const { id[0] = c % n[0]; id[1] = (c / n[0]) % n[1]; id[2] = c / (n[0] * n[1]); }
@@ -215,7 +384,7 @@ struct Problem {
     double perm(int64_t c) const { return d.permeability[c]; }
     double poro(int64_t c) const { return d.porosity[c]; }
     double extr(int64_t c) const { return d.extrusion ? d.extrusion[c] : 1.0; }
-    const BrooksCoreyDefault& law(int64_t c) const { return laws[d.material ? d.material[c] : 0]; }
+    const TwoPLaw& law(int64_t c) const { return laws[d.material ? d.material[c] : 0]; }
 };
 
 struct VolVars {
@@ -1128,6 +1297,20 @@ int orc_brooks_corey(const double* params, int32_t what, int64_t n, const double
         if (what == 0) out[i] = law.pc(sw[i]);
         else if (what == 1) out[i] = law.krw(sw[i]);
         else out[i] = law.krn(sw[i]);
+    }
+    return 0;
+}
+
+int orc_van_genuchten(const double* params, int32_t what, int64_t n, const double* sw, double* out)
+{
+    VanGenuchtenDefault law(params);
+    for (int64_t i = 0; i < n; ++i) {
+        if (what == 0) out[i] = law.pc(sw[i]);
+        else if (what == 1) out[i] = law.krw(sw[i]);
+        else if (what == 2) out[i] = law.krn(sw[i]);
+        else if (what == 3) out[i] = law.dpc_dsw(sw[i]);
+        else if (what == 4) out[i] = law.dkrw_dsw(sw[i]);
+        else out[i] = law.dkrn_dsw(sw[i]);
     }
     return 0;
 }

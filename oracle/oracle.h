@@ -53,6 +53,9 @@ double orc_suggest_time_step(int32_t newton_iterations, double old_dt, const dxg
 /* Regularised Brooks-Corey law (BrooksCoreyDefault); params = pcEntry, lambda, Swr,
  * Snr, pcLowSwe.  what: 0 pc, 1 krw, 2 krn. */
 int orc_brooks_corey(const double* params, int32_t what, int64_t n, const double* sw, double* out);
+/* Regularised Van Genuchten (VanGenuchtenDefault); params: alpha, n, l, Swr, Snr, pcLowSwe,
+ * pcHighSwe, krnLowSwe, krwHighSwe; what: 0 pc, 1 krw, 2 krn, 3 dpc/dsw, 4 dkrw/dsw, 5 dkrn/dsw. */
+int orc_van_genuchten(const double* params, int32_t what, int64_t n, const double* sw, double* out);
 
 /* Numeric differentiation of the reference polynomial test function
  * f(x) = x^4/24 + x^3/6 + x^2/2 + x at x0 with the given method and eps. */

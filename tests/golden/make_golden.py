@@ -7,6 +7,14 @@ Run in a container that has the DuMux source tree at REFERENCE (default
   pcsw_brookscorey.txt     test/references/test_pcsw_brookscorey-reference.dat
                            (regularised Brooks-Corey pc(sw) at linspace(0,1,100),
                            pe=1e4, lambda=2, Swr=Snr=0.1, pcLowSwe=0.01)
+  pcsw_vangenuchten.txt    test/references/test_pcsw_vangenuchten-reference.dat
+                           (regularised Van Genuchten pc(sw) at linspace(0,1,100), alpha=6.66e-5,
+                           n=3.652, l=0.5, Swr=Snr=0.1, thresholds 0.01/0.99/0.1/0.9;
+                           test/material/fluidmatrixinteractions/2p/test_material_2p_vangenuchten.cc)
+  twop_lens_tpfa.txt       cell fields S_napl, p_aq, p_napl, pc of
+                           test/references/test_2p_incompressible_cc-reference.vtu (48x32 2p
+                           Van Genuchten lens, output 7 = t 3000 s; the reference's
+                           test_2p_incompressible_tpfa and _tpfa_analytic compare with it)
 """
 import os
 import re
@@ -29,6 +37,24 @@ def main():
     with open(os.path.join(HERE, "pcsw_brookscorey.txt"), "w") as f:
         f.write("# test/references/test_pcsw_brookscorey-reference.dat\n")
         f.write("\n".join(dat) + "\n")
+    dat = open(os.path.join(REFERENCE, "test/references/test_pcsw_vangenuchten-reference.dat")).read().split()
+    assert len(dat) == 100
+    with open(os.path.join(HERE, "pcsw_vangenuchten.txt"), "w") as f:
+        f.write("# test/references/test_pcsw_vangenuchten-reference.dat\n")
+        f.write("\n".join(dat) + "\n")
+    vtu = open(os.path.join(REFERENCE, "test/references/test_2p_incompressible_cc-reference.vtu")).read()
+    fields = ["S_napl", "p_aq", "p_napl", "pc"]
+    cols = []
+    for name in fields:
+        m = re.search(r'Name="%s"[^>]*>(.*?)</DataArray>' % name, vtu, re.S)
+        vals = m.group(1).split()
+        assert len(vals) == 1536, (name, len(vals))
+        cols.append(vals)
+    with open(os.path.join(HERE, "twop_lens_tpfa.txt"), "w") as f:
+        f.write("# cell fields of test/references/test_2p_incompressible_cc-reference.vtu (Float32, ascii)\n")
+        f.write("# " + " ".join(fields) + "\n")
+        for row in zip(*cols):
+            f.write(" ".join(row) + "\n")
     print("wrote fixtures to", HERE)
 
 
