@@ -88,7 +88,7 @@ def lib():
         L.dxg_batch_set_memory_budget.argtypes = [vp, C.c_int64]
         L.dxg_batch_device_bytes.argtypes = [vp]
         L.dxg_batch_device_bytes.restype = C.c_int64
-        L.dxg_batch_add.argtypes = [vp, C.POINTER(ProblemDescC), dp, C.c_double, C.c_double,
+        L.dxg_batch_add.argtypes = [vp, C.POINTER(ProblemDescC), dp, C.c_double, C.c_double, C.c_double,
                                     C.POINTER(NewtonParamsC), C.POINTER(C.c_int64)]
         L.dxg_batch_iterate.argtypes = [vp, C.POINTER(C.c_int32)]
         L.dxg_batch_run.argtypes = [vp]
@@ -409,14 +409,17 @@ class Batch:
         except Exception:
             pass
 
-    def add(self, desc, u0, dt=0.0, t_end=0.0, params=None):
-        """Admits a problem; returns its id, or None when the memory budget refuses it."""
+    def add(self, desc, u0, dt=0.0, t_end=0.0, params=None, max_dt=None):
+        """Admits a problem; returns its id, or None when the memory budget refuses it.
+        dt: initial time step; max_dt: TimeLoop.MaxTimeStepSize (default: dt, i.e. fixed
+        steps unless Newton asks for smaller ones; 0: unlimited)."""
         u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
         if u0.size != desc.num_dofs:
             raise ValueError(f"u0 has {u0.size} entries, expected {desc.num_dofs}")
         p = params if params is not None else newton_params()
         pid = C.c_int64()
-        st = self._L.dxg_batch_add(self._h, C.byref(desc.c), _dp(u0), float(dt), float(t_end), C.byref(p),
+        mdt = float(dt) if max_dt is None else float(max_dt)
+        st = self._L.dxg_batch_add(self._h, C.byref(desc.c), _dp(u0), float(dt), mdt, float(t_end), C.byref(p),
                                    C.byref(pid))
         if st == DXG_ERR_BUDGET:
             return None

@@ -1230,8 +1230,8 @@ int dxg_batch_set_memory_budget(dxg_batch* b, int64_t bytes)
 
 int64_t dxg_batch_device_bytes(const dxg_batch* b) { return b ? b->bytesInUse : -1; }
 
-int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, double dt, double t_end,
-                  const dxg_newton_params* params, int64_t* id)
+int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, double dt, double max_dt,
+                  double t_end, const dxg_newton_params* params, int64_t* id)
 {
     if (!b || !d || !u0 || !id) return DXG_ERR_ARG;
     const int64_t need = dxg_problem_device_bytes(d, b->precision);
@@ -1266,7 +1266,8 @@ int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, dou
     }
     s->transient = t_end > 0.0 && dt > 0.0;
     s->tEnd = s->transient ? t_end : 0.0;
-    s->dtMax = s->dt = s->transient ? std::min(dt, t_end) : 0.0;
+    s->dt = s->transient ? std::min(dt, t_end) : 0.0;
+    s->dtMax = max_dt > 0.0 ? max_dt : 1e300;
     s->bytes = need;
     s->tAdmit = b->clock();
     s->id = b->nextId++;

@@ -327,11 +327,11 @@ int64_t dxg_problem_device_bytes(const dxg_problem_desc* desc, int precision);
 int dxg_batch_set_memory_budget(dxg_batch* batch, int64_t bytes);
 int64_t dxg_batch_device_bytes(const dxg_batch* batch);
 /* Admit a problem: initial solution u0 (N*num_eq values, also the first previous
- * time level), time step dt and end time t_end (t_end <= 0: one stationary Newton
- * solve), Newton and linear-solver parameters (NULL: defaults).  *id receives its
- * handle. */
-int dxg_batch_add(dxg_batch* batch, const dxg_problem_desc* desc, const double* u0, double dt, double t_end,
-                  const dxg_newton_params* params, int64_t* id);
+ * time level), initial time step dt, maximum time step max_dt (TimeLoop.MaxTimeStepSize;
+ * <= 0: unlimited) and end time t_end (t_end <= 0: one stationary Newton solve), Newton
+ * and linear-solver parameters (NULL: defaults).  *id receives its handle. */
+int dxg_batch_add(dxg_batch* batch, const dxg_problem_desc* desc, const double* u0, double dt, double max_dt,
+                  double t_end, const dxg_newton_params* params, int64_t* id);
 /* One tick (see above); *active receives the number of problems still active. */
 int dxg_batch_iterate(dxg_batch* batch, int32_t* active);
 /* Iterates until no problem is active. */

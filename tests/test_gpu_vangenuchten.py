@@ -83,7 +83,7 @@ def test_lens_case_end_to_end(analytic, precision):
 def test_lens_case_in_a_batch_equals_alone():
     desc, u0 = problems.twop_lens_problem(analytic=True)
     batch = Batch(precision="mixed")
-    pid = batch.add(desc, u0, dt=250.0, t_end=3000.0, params=newton_params())
+    pid = batch.add(desc, u0, dt=250.0, t_end=3000.0, params=newton_params(), max_dt=0.0)
     batch.run()
     u, _, _ = _gpu_time_loop(desc, u0, "mixed")
     assert batch.info(pid)["time_steps"] == 7
