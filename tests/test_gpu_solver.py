@@ -121,3 +121,20 @@ def test_wavefront_ilu_equals_level_scheduled(dims, precision):
     assert abs(rl["iterations"] - rw["iterations"]) <= 2
     tol = 1e-7 if precision == "fp64" else 1e-3
     assert np.max(np.abs(xl - xw)) <= tol * np.max(np.abs(xl))
+
+
+@pytest.mark.parametrize("criterion", ["line_search", "residual"])
+def test_newton_line_search_and_residual_criterion_match_oracle(criterion):
+    """NewtonSolver with UseLineSearch (newtonsolver.hh:1154-1178) or the residual
+    criterion (EnableResidualCriterion, :657-701) on: the per-iteration residual norms
+    drive the control flow, so iteration counts and fields must follow the oracle's."""
+    desc, u0 = problems.twop_lens_problem(cells=(24, 16), analytic=True)
+    kw = dict(use_line_search=1) if criterion == "line_search" else dict(enable_residual_criterion=1)
+    p = newton_params(linear_reduction=1e-13, linear_max_iter=500, record_residual_norms=1, **kw)
+    u_gpu, reps = _run_time_loop_gpu(desc, u0, 500.0, 3, p)
+    u_orc, oreps = oracle.time_loop(desc, u0, 500.0, 3, params=p, max_dt=500.0)
+    for rg, ro in zip(reps, oreps):
+        assert rg["iterations"] == ro["iterations"]
+        rn_g, rn_o = np.array(rg["residual_norm"]), np.array(ro["residual_norm"])
+        assert np.all(np.abs(rn_g - rn_o) <= 1e-9 * rg["initial_residual"])
+    assert np.max(np.abs(u_gpu - u_orc)) <= 1e-9 * np.max(np.abs(u_orc))
