@@ -77,6 +77,10 @@ class NewtonParamsC(C.Structure):
         ("linear_reduction", C.c_double),
         ("linear_max_iter", C.c_int32),
         ("record_residual_norms", C.c_int32),
+        ("enable_partial_reassembly", C.c_int32),
+        ("reassembly_min_threshold", C.c_double),
+        ("reassembly_max_threshold", C.c_double),
+        ("reassembly_shift_weight", C.c_double),
     ]
 
 
@@ -164,6 +168,10 @@ def newton_params(**kw):
     p.linear_reduction = 1e-6
     p.linear_max_iter = 250
     p.record_residual_norms = 0
+    p.enable_partial_reassembly = 0
+    p.reassembly_min_threshold = 0.0
+    p.reassembly_max_threshold = 0.0
+    p.reassembly_shift_weight = 1e-3
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)

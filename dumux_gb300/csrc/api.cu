@@ -186,6 +186,7 @@ dxg::AssemblyArgs dxg_ctx::asmArgs() const
     a.vvS = vvS.get();
     a.eps = eps.get();
     a.dvv = dvv.get();
+    a.color = partialActive ? partialColor.get() : nullptr;
     a.stPrev = stPrev.get();
     a.A = A.get();
     a.r = r.get();
@@ -788,12 +789,36 @@ struct NewtonRun {
         residualNorm = deviceNorm(c, c->r.get());
         reduction = residualNorm / initialResidual;
     }
+    // partial reassembly: colors from the accumulated shifts (newtonsolver.hh:565-603)
+    void updateColors()
+    {
+        const double tol = p.max_relative_shift;
+        const double minEps = p.reassembly_min_threshold > 0 ? p.reassembly_min_threshold : 1e-1 * tol;
+        const double maxEps = p.reassembly_max_threshold > 0 ? p.reassembly_max_threshold : 1e2 * tol;
+        const double threshold = std::max(minEps, std::min(maxEps, shift * p.reassembly_shift_weight));
+        launchPartialColors(c->uLast.get(), c->u.get(), c->partialDist.get(), c->partialColor.get(), c->N, c->b,
+                            threshold, c->stream);
+        c->launches += 1;
+    }
+
     // NewtonSolver::solveImpl_ (newtonsolver.hh:976-1072); false on NumericalProblem
     bool run()
     {
         using clk = std::chrono::steady_clock;
         numSteps = 0;
         bool conv = false;
+        // newtonBegin: all colors red (resetColors); numeric differentiation only
+        c->partialActive = p.enable_partial_reassembly != 0 && c->method != 3;
+        if (c->partialActive) {
+            c->partialDist.alloc(c->N);
+            c->partialColor.alloc(c->N);
+            DXG_CUDA(cudaMemsetAsync(c->partialDist.get(), 0, c->N * sizeof(double), c->stream));
+            DXG_CUDA(cudaMemsetAsync(c->partialColor.get(), 1, c->N, c->stream));
+        }
+        struct Deactivate {
+            dxg_ctx* c;
+            ~Deactivate() { c->partialActive = false; }
+        } deactivate{c};
         DXG_CUDA(cudaMemcpyAsync(c->uLast.get(), c->u.get(), c->M * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
         try {
             while (proceed(conv)) {
@@ -829,6 +854,7 @@ struct NewtonRun {
                     shift = update(1.0);
                     if (p.enable_residual_criterion) residualReduction();
                 }
+                if (c->partialActive) updateColors();
                 auto t3 = clk::now();
                 if (numSteps < DXG_MAX_NEWTON_RECORD) {
                     rep->shift[numSteps] = shift;
@@ -1117,6 +1143,10 @@ void dxg_newton_default_params(dxg_newton_params* p)
     p->linear_reduction = 1e-6;
     p->linear_max_iter = 250;
     p->record_residual_norms = 0;
+    p->enable_partial_reassembly = 0;
+    p->reassembly_min_threshold = 0.0;
+    p->reassembly_max_threshold = 0.0;
+    p->reassembly_shift_weight = 1e-3;
 }
 
 int dxg_newton_solve(dxg_ctx* c, double dt, const dxg_newton_params* params, dxg_newton_report* report)

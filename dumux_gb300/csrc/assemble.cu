@@ -86,8 +86,11 @@ __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ 
         for (int e = 0; e < B; ++e) x[e] = a.u[i * B + e];
         const double ph = a.phi[i], ex = a.extr[i];
         const int m = (B == 2) ? a.mat[i] : 0;
+        // a green cell keeps its Jacobian column: its perturbed states are not needed
+        const int ns = (a.color && !a.color[i]) ? 1 : NS;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
+            if (s >= ns) break;
             double q[B];
 #pragma unroll
             for (int e = 0; e < B; ++e) q[e] = x[e];
@@ -185,14 +188,17 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
         }
     }
 
+    // partial reassembly: the column of a green cell keeps its values
+    const bool jacI = WANT_JAC && !(a.color && !a.color[I]);
     // own states
     double pI[NS][B], uI[NS][B];
 #pragma unroll
     for (int s = 0; s < (WANT_JAC ? NS : 1); ++s)
 #pragma unroll
         for (int k = 0; k < B; ++k) {
-            pI[s][k] = a.vvP[(s * B + k) * N + I];
-            uI[s][k] = a.vvU[(s * B + k) * N + I];
+            const bool have = s == 0 || jacI;
+            pI[s][k] = have ? a.vvP[(s * B + k) * N + I] : 0.0;
+            uI[s][k] = have ? a.vvU[(s * B + k) * N + I] : 0.0;
         }
     constexpr int NR = WANT_JAC ? NS : 1;
     double r[NS][B];
@@ -244,6 +250,7 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
                     if (s == 0) F0[k] = F;
                     r[s][k] += F;
                 }
+            const bool jacJ = !(a.color && !a.color[J]);
             if (ANALYTIC && WANT_JAC) {
                 // addFluxDerivatives (1p: incompressiblelocalresidual.hh:117-123;
                 // 2p: incompressiblelocalresidual.hh:169-252)
@@ -289,7 +296,7 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
                 double* dst = a.A + ((int64_t)slot * N + I) * BB;
 #pragma unroll
                 for (int e = 0; e < BB; ++e) dst[e] = blk[e];
-            } else if (WANT_JAC) {
+            } else if (WANT_JAC && jacJ) {
                 double blk[BB];
 #pragma unroll
                 for (int pv = 0; pv < B; ++pv) {
@@ -413,7 +420,7 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
         double* dst = a.A + ((int64_t)DIM * N + I) * BB;
 #pragma unroll
         for (int e = 0; e < BB; ++e) dst[e] = dII[e];
-    } else if (WANT_JAC) {
+    } else if (WANT_JAC && jacI) {
         double blk[BB];
 #pragma unroll
         for (int pv = 0; pv < B; ++pv) {

@@ -1260,8 +1260,8 @@ int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, dou
     if ((st = step(dxg_set_prev_solution(s->c, u0))) != DXG_OK) return st;
     if (params) s->p = *params;
     else dxg_newton_default_params(&s->p);
-    if (s->p.use_line_search || s->p.enable_residual_criterion) {
-        b->err = "batched problems use the shift criterion without line search";
+    if (s->p.use_line_search || s->p.enable_residual_criterion || s->p.enable_partial_reassembly) {
+        b->err = "batched problems use the shift criterion, full reassembly and no line search";
         return DXG_ERR_ARG;
     }
     s->transient = t_end > 0.0 && dt > 0.0;

@@ -58,6 +58,11 @@ struct dxg_ctx {
 
     int lastNewtonSteps = 0;
 
+    // partial reassembly (active during a Newton solve that asks for it)
+    bool partialActive = false;
+    dxg::DevBuf<double> partialDist;
+    dxg::DevBuf<uint8_t> partialColor;
+
     // ILU(0) kernels: cluster wavefront (default) or level-scheduled launches
     int iluKernel = DXG_ILU_AUTO;
     dxg::WavePlan wavePlan;

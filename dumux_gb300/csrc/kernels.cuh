@@ -39,6 +39,9 @@ struct AssemblyArgs {
     // state read by the volume-variable kernels
     const double* u;            // current solution [N][b]
     const double* uprev;        // previous time level [N][b]
+    // partial reassembly: per-cell color, 1 red (reassemble the cell's Jacobian column),
+    // 0 green (keep it); nullptr: everything red
+    const uint8_t* color;
 };
 
 void launchVolvars(const AssemblyArgs& a, int b, int method, const double* u, cudaStream_t st);

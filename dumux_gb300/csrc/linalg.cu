@@ -527,6 +527,27 @@ __global__ void copyToDouble(const VT* __restrict__ x, double* y, int64_t M)
         y[k] = (double)x[k];
 }
 
+// ---------------------------------------------------------------- partial reassembly
+// newtonUpdate's partial-reassembly block (newtonsolver.hh:590-602, 1257-1280) and
+// PartialReassemblerEngine<CCTpfa>::computeColors (partialreassembler.hh:313-343): add the
+// cell's relative shift to its distance from the last linearisation, color it red when
+// the distance exceeds the threshold, and reset the distance of red cells.
+__global__ void partialColorKernel(const double* __restrict__ uLast, const double* __restrict__ u, double* dist,
+                                   uint8_t* color, int64_t N, int b, double threshold)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int e = 0; e < b; ++e) {
+            const double x = uLast[i * b + e], y = u[i * b + e];
+            s = fmax(s, fabs(x - y) / fmax(1.0, fabs(x + y) * 0.5));
+        }
+        const double d = dist[i] + s;
+        const bool red = d > threshold;
+        color[i] = red ? 1 : 0;
+        dist[i] = red ? 0.0 : d;
+    }
+}
+
 // ---------------------------------------------------------------- mixed-precision helpers
 __global__ void toFloatKernel(ToFloatArgs a0, const ToFloatArgs* batch)
 {
@@ -745,6 +766,12 @@ void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* ou
 void launchNorm2Batch(const NormArgs* batch, const BlockMap& m, cudaStream_t st)
 {
     norm2Kernel<<<m.blocks, kReduceThreads, 0, st>>>(NormArgs{}, batch, m.map);
+    DXG_CUDA(cudaGetLastError());
+}
+void launchPartialColors(const double* uLast, const double* u, double* dist, uint8_t* color, int64_t N, int b,
+                         double threshold, cudaStream_t st)
+{
+    partialColorKernel<<<reduceBlocks(N), kReduceThreads, 0, st>>>(uLast, u, dist, color, N, b, threshold);
     DXG_CUDA(cudaGetLastError());
 }
 void launchToFloat(const ToFloatArgs& a, cudaStream_t st)

@@ -113,6 +113,8 @@ void launchCopyToDouble(const VT* x, double* y, int64_t M, cudaStream_t st);
 void launchNewtonUpdate(const double* uLast, const double* delta, double* u, double lambda, int64_t M,
                         const ReduceScratch& sc, double* shiftOut, cudaStream_t st);
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st);
+void launchPartialColors(const double* uLast, const double* u, double* dist, uint8_t* color, int64_t N, int b,
+                         double threshold, cudaStream_t st);
 void launchToFloat(const ToFloatArgs& a, cudaStream_t st);
 void launchToDouble(const ToDoubleArgs& a, cudaStream_t st);
 void launchAccum(const AccumArgs& a, cudaStream_t st);

@@ -192,6 +192,15 @@ typedef struct dxg_newton_params {
     double linear_reduction;     /* LinearSolver.ResidualReduction used in Newton (1e-6) */
     int32_t linear_max_iter;     /* LinearSolver.MaxIterations (250)                 */
     int32_t record_residual_norms; /* compute ||r|| after each update as a diagnostic */
+    /* Partial reassembly (Newton.EnablePartialReassembly, newtonsolver.hh:565-603 with
+     * PartialReassemblerEngine<CCTpfa>, assembly/partialreassembler.hh:300-391): only the
+     * Jacobian columns of cells whose relative shift accumulated since their last
+     * linearisation exceeds max(min, min(max, weight*shift)) are reassembled; the others
+     * keep their values.  Numeric differentiation only; single contexts only.          */
+    int32_t enable_partial_reassembly;     /* (false)                                    */
+    double reassembly_min_threshold;       /* Newton.ReassemblyMinThreshold (<= 0: 1e-1*max_relative_shift) */
+    double reassembly_max_threshold;       /* Newton.ReassemblyMaxThreshold (<= 0: 1e2*max_relative_shift)  */
+    double reassembly_shift_weight;        /* Newton.ReassemblyShiftWeight (1e-3)        */
 } dxg_newton_params;
 
 /* Fills p with the reference defaults (newtonsolver.hh:1213-1247). */

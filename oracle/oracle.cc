@@ -826,10 +826,28 @@ static void assembleElementAnalytic(const Problem& P, const Pattern& pt, int64_t
     }
 }
 
+// colors (partial reassembly): 1 red -- reassemble the element's Jacobian column, 0 green --
+// keep it (FVAssembler::assemble_ with PartialReassembler::resetJacobian, fvassembler.hh:461-510,
+// partialreassembler.hh:360-376, and CCLocalAssemblerBase::assembleJacobianAndResidual)
 static void assemble(const Problem& P, const Pattern& pt, const double* u, const double* uprev, double dt,
-                     double* values, double* r)
+                     double* values, double* r, const uint8_t* colors = nullptr)
 {
-    const int b = P.b;
+    const int b = P.b, bb = b * b, nf = 2 * P.dim;
+    if (values && colors && P.d.diff_method != 1) {
+        // reset the columns of the non-green elements only
+        for (int64_t I = 0; I < P.N; ++I) {
+            if (!colors[I]) continue;
+            std::fill(values + pt.diag[I] * bb, values + (pt.diag[I] + 1) * bb, 0.0);
+            for (int f = 0; f < nf; ++f) {
+                const int64_t blk = pt.colBlock[I * nf + f];
+                if (blk >= 0) std::fill(values + blk * bb, values + (blk + 1) * bb, 0.0);
+            }
+        }
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+        for (int64_t I = 0; I < P.N; ++I)
+            assembleElement(P, pt, I, u, uprev, dt, colors[I] ? values : nullptr, r);
+        return;
+    }
     if (values) std::fill(values, values + pt.rowPtr[P.N] * b * b, 0.0);
     // Numeric: column-wise scatter, element I writes only block column I and r[I];
     // analytic: element I writes only block row I and r[I]; both race free.
@@ -1031,6 +1049,9 @@ static dxg_linear_result bicgstab(int64_t n, int b, const int64_t* rowPtr, const
 struct NewtonAssembler {
     virtual ~NewtonAssembler() = default;
     virtual int64_t size() const = 0;                         // scalar entries of u
+    virtual int blockSize() const { return 1; }
+    // element colors for partial reassembly (nullptr: assemble everything)
+    virtual void setColors(const uint8_t*) {}
     virtual void assembleJacobianAndResidual(const std::vector<double>& u) = 0;
     virtual void assembleResidual(const std::vector<double>& u) = 0;
     virtual double residualNorm() const = 0;
@@ -1072,11 +1093,47 @@ struct Newton {
         residualNorm = A.residualNorm();
         reduction = residualNorm / initialResidual;
     }
+    // partial reassembly state: distance from the last linearisation and element colors
+    std::vector<double> distance;
+    std::vector<uint8_t> colors;
+
+    // newtonUpdate's partial-reassembly block (newtonsolver.hh:565-603): threshold from
+    // the achieved shift, accumulated per-cell shift, colors, reset of the red distances
+    void updateColors(NewtonAssembler& A, const std::vector<double>& u)
+    {
+        const double tol = prm.max_relative_shift;
+        const double minEps = prm.reassembly_min_threshold > 0 ? prm.reassembly_min_threshold : 1e-1 * tol;
+        const double maxEps = prm.reassembly_max_threshold > 0 ? prm.reassembly_max_threshold : 1e2 * tol;
+        const double threshold = std::max(minEps, std::min(maxEps, shift * prm.reassembly_shift_weight));
+        const int b = A.blockSize();
+        const size_t n = distance.size();
+        for (size_t i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int e = 0; e < b; ++e) {
+                const double x = uLastIter[i * b + e], y = u[i * b + e];
+                s = std::max(s, std::abs(x - y) / std::max<double>(1.0, std::abs(x + y) * 0.5));
+            }
+            distance[i] += s;
+        }
+        // PartialReassemblerEngine<CCTpfa>::computeColors: red above the threshold
+        for (size_t i = 0; i < n; ++i) colors[i] = distance[i] > threshold ? 1 : 0;
+        for (size_t i = 0; i < n; ++i)
+            if (colors[i]) distance[i] = 0;
+    }
+
     // solveImpl_ (newtonsolver.hh:976-1072); throws NumericalProblem
     bool solveImpl(NewtonAssembler& A, std::vector<double>& u)
     {
         numSteps = 0;
         uLastIter = u;
+        const bool partial = prm.enable_partial_reassembly != 0;
+        if (partial) {
+            // newtonBegin: resetColors -- everything red
+            const size_t n = u.size() / A.blockSize();
+            distance.assign(n, 0.0);
+            colors.assign(n, 1);
+            A.setColors(colors.data());
+        }
         std::vector<double> deltaU(u.size(), 0.0);
         bool conv = false;
         using clk = std::chrono::steady_clock;
@@ -1113,6 +1170,7 @@ struct Newton {
                 if (prm.enable_residual_criterion) computeResidualReduction(A, u);
             }
             shift = maxRelShift(uLastIter, u);
+            if (partial) updateColors(A, u);
             auto t3 = clk::now();
             if (rep && numSteps < DXG_MAX_NEWTON_RECORD) {
                 rep->shift[numSteps] = shift;
@@ -1154,8 +1212,14 @@ struct FVAssembler final : NewtonAssembler {
     std::vector<double> J, r;
     FVAssembler(const Problem& p, const Pattern& pat, const double* up, double dt_)
         : P(p), pt(pat), uprev(up), dt(dt_), J(pat.rowPtr[p.N] * p.b * p.b), r(p.N * p.b) {}
+    const uint8_t* colors = nullptr;
     int64_t size() const override { return P.N * P.b; }
-    void assembleJacobianAndResidual(const std::vector<double>& u) override { assemble(P, pt, u.data(), uprev, dt, J.data(), r.data()); }
+    int blockSize() const override { return P.b; }
+    void setColors(const uint8_t* c) override { colors = c; }
+    void assembleJacobianAndResidual(const std::vector<double>& u) override
+    {
+        assemble(P, pt, u.data(), uprev, dt, J.data(), r.data(), colors);
+    }
     void assembleResidual(const std::vector<double>& u) override { assemble(P, pt, u.data(), uprev, dt, nullptr, r.data()); }
     double residualNorm() const override { return std::sqrt(dot((int64_t)r.size(), r.data(), r.data())); }
     bool solveLinear(std::vector<double>& delta, double reduction, int maxit, int* iters) override

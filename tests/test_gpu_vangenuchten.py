@@ -88,3 +88,26 @@ def test_lens_case_in_a_batch_equals_alone():
     u, _, _ = _gpu_time_loop(desc, u0, "mixed")
     assert batch.info(pid)["time_steps"] == 7
     assert np.array_equal(batch.solution(pid), u)
+
+
+def test_partial_reassembly_matches_oracle():
+    """Newton.EnablePartialReassembly on the device follows the oracle (same colors, same
+    iteration counts) and still reproduces the reference's golden VTU."""
+    desc, u0 = problems.twop_lens_problem(analytic=False)
+    p = newton_params(enable_partial_reassembly=1)
+    ctx = Context(desc)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    t, dt, iters = 0.0, 250.0, []
+    while True:
+        rep = ctx.newton_solve(dt, p)
+        t += rep["dt_used"]
+        ctx.advance_time_step()
+        iters.append(rep["iterations"])
+        if 3000.0 - t <= 3e-6:
+            break
+        dt = min(ctx.suggest_time_step(rep["dt_used"], p), 3000.0 - t)
+    uo, reps = oracle.time_loop(desc, u0, 250.0, 100, p, t_end=3000.0)
+    assert iters == [r["iterations"] for r in reps]
+    u = ctx.solution()
+    assert np.max(np.abs(u - uo)) <= 1e-9 * np.max(np.abs(uo))

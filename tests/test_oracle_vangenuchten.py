@@ -67,3 +67,28 @@ def test_lens_case_matches_reference_vtu(analytic):
     # the reference's own check is fuzzy at 1e-2; the golden file prints 6 significant
     # digits (Float32), which is the level reached here
     assert err_p <= 2e-5 and err_s <= 1e-4 and small <= 1e-6, (err_p, err_s, small)
+
+
+def test_lens_case_with_partial_reassembly_matches_reference_vtu():
+    """test_2p_incompressible_tpfa itself: numeric Jacobian with Newton.EnablePartialReassembly."""
+    desc, u0 = problems.twop_lens_problem(analytic=False)
+    p = newton_params(enable_partial_reassembly=1)
+    u, reps = oracle.time_loop(desc, u0, 250.0, 100, p, t_end=3000.0)
+    times = [r["time"] for r in reps]
+    assert len(times) == 7 and abs(times[-1] - 3000.0) < 1e-6 and abs(times[4] - 2054.01) < 5e-3
+    err_p, err_s, small = _compare_with_golden(u)
+    assert err_p <= 2e-5 and err_s <= 1e-4 and small <= 1e-6, (err_p, err_s, small)
+
+
+def test_partial_reassembly_keeps_green_columns():
+    """The second Newton iteration's Jacobian differs from a full reassembly exactly in
+    the columns of cells whose accumulated shift stayed below the threshold."""
+    desc, u0 = problems.twop_lens_problem(cells=(12, 8), analytic=False)
+    full = newton_params(min_steps=3, max_steps=3, max_relative_shift=1e-30, linear_reduction=1e-12)
+    part = newton_params(min_steps=3, max_steps=3, max_relative_shift=1e-30, linear_reduction=1e-12,
+                         enable_partial_reassembly=1, reassembly_min_threshold=1e-3, reassembly_max_threshold=1e-3)
+    st1, u_full, _ = oracle.newton_solve(desc, u0, u0, 250.0, full)
+    st2, u_part, _ = oracle.newton_solve(desc, u0, u0, 250.0, part)
+    # a coarse threshold keeps many columns: the iterates differ, yet both stay close
+    assert not np.array_equal(u_full, u_part)
+    assert np.max(np.abs(u_full - u_part)) <= 1e-2 * np.max(np.abs(u_full))
