@@ -635,7 +635,6 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
 {
     constexpr bool mixed = sizeof(PT) == 4;
     cudaStream_t st = c->stream;
-    const double* A = c->A.get();
     const PT* PA = mixed ? (const PT*)c->Af.get() : (const PT*)c->A.get();
     PT* PL = mixed ? (PT*)c->Lf.get() : (PT*)c->L.get();
     PT* PD = mixed ? (PT*)c->Dinvf.get() : (PT*)c->Dinv.get();
@@ -659,7 +658,8 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     }
     double *x = c->kx.get(), *r = c->kr.get(), *rt = c->krt.get(), *p = c->kp.get(), *v = c->kv.get(),
            *t = c->kt.get(), *y = c->ky.get();
-    BicgArgs<double> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr};
+    BicgArgs<double> ba{x, r, rt, p, v, t, y, c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr,
+                        nullptr};
     // preconditioner operands: FP32 copies of p / r and an FP32 result, or the FP64 vectors
     const PT* pIn = mixed ? (const PT*)c->fp.get() : (const PT*)p;
     const PT* rIn = mixed ? (const PT*)c->fr.get() : (const PT*)r;
@@ -667,6 +667,7 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     if (mixed) {
         ba.pLow = c->fp.get();
         ba.rLow = c->fr.get();
+        ba.yLow = c->fy.get();
     }
     KrylovState init{};
     init.reduction = reduction;
@@ -674,20 +675,16 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     DXG_CUDA(cudaMemcpyAsync(c->ks.get(), &init, sizeof(KrylovState), cudaMemcpyHostToDevice, st));
     launchBicgInit<double>(ba, rhs, st);
     c->launches += 1;
-    SpmvArgs<double, double> sv{};
-    sv.A = A;
+    // SpMV: the FP64 Jacobian times the FP64 preconditioner output, or (mixed) the FP32
+    // Jacobian copy times the FP32 preconditioner output, FP64 result and dots
+    SpmvArgs<PT, double, PT> sv{};
+    sv.A = PA;
     sv.nbmask = c->nbmask.get();
     sv.N = c->N;
     for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
     sv.ks = c->ks.get();
     sv.scratch = c->scratch();
-    auto precondition = [&](const PT* in) {
-        c->launches += iluApply<PT>(c, ia, PA, PL, PD, in, yOut);
-        if (mixed) {
-            launchToDouble(ToDoubleArgs{c->fy.get(), y, c->M}, st);
-            c->launches += 1;
-        }
-    };
+    auto precondition = [&](const PT* in) { c->launches += iluApply<PT>(c, ia, PA, PL, PD, in, yOut); };
     const int chunk = 4;
     int done = 0;
     while (true) {
@@ -696,18 +693,18 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
             launchBicgUpdateP<double>(ba, st);
             c->launches += 2;
             precondition(pIn);
-            sv.x = y; sv.y = v; sv.w = rt;
+            sv.x = yOut; sv.y = v; sv.w = rt;
             {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv);
-                launchSpmv<double, double>(sv, c->b, c->dim, 1, st);
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
+                launchSpmv<PT, double, PT>(sv, c->b, c->dim, 1, st);
             }
             launchBicgAxpyNorm<double>(ba, 0, st);
             c->launches += 2;
             precondition(rIn);
-            sv.x = y; sv.y = t; sv.w = r;
+            sv.x = yOut; sv.y = t; sv.w = r;
             {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv);
-                launchSpmv<double, double>(sv, c->b, c->dim, 2, st);
+                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
+                launchSpmv<PT, double, PT>(sv, c->b, c->dim, 2, st);
             }
             launchBicgAxpyNorm<double>(ba, 1, st);
             c->launches += 2;

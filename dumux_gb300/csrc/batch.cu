@@ -433,10 +433,11 @@ struct Pre<float> {
 BicgArgs<double> krylovArgs(dxg_ctx* c, bool mixed)
 {
     BicgArgs<double> a{c->kx.get(), c->kr.get(), c->krt.get(), c->kp.get(), c->kv.get(), c->kt.get(), c->ky.get(),
-                       c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr};
+                       c->M, c->ks.get(), c->scratch(), nullptr, 0.0, 0, nullptr, nullptr, nullptr};
     if (mixed) {
         a.pLow = c->fp.get();
         a.rLow = c->fr.get();
+        a.yLow = c->fy.get();
     }
     return a;
 }
@@ -566,8 +567,8 @@ struct GroupState {
     std::vector<WaveGeom> geo;      // per member, from its class's launch shape
     DevBuf<unsigned char> args;
     const BicgArgs<double>* dBicg = nullptr;
-    const SpmvArgs<double, double>* dSv1 = nullptr;
-    const SpmvArgs<double, double>* dSv2 = nullptr;
+    const void* dSv1 = nullptr;      // SpmvArgs<PT, double, PT>
+    const void* dSv2 = nullptr;
     const ToDoubleArgs* dTd = nullptr;
     BlockMap mapM, mapN;     // vector kernels over N*b entries, SpMV over N cells
     int64_t maxN = 1, maxM = 1;
@@ -731,22 +732,22 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.maxN = maxCells(S);
     G.maxM = maxDofs(S);
     G.sweepBytes = bytesOf(S, &dxg_ctx::bytesSweep, sizeof(PT) / 8.0);
-    G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, 1.0);
+    G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, sizeof(PT) / 8.0);
     std::vector<BicgArgs<double>> ba(n);
-    std::vector<SpmvArgs<double, double>> sv1(n), sv2(n);
+    std::vector<SpmvArgs<PT, double, PT>> sv1(n), sv2(n);
     std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);   // member order; repacked per class below
     std::vector<ToDoubleArgs> td(n);
     for (int k = 0; k < n; ++k) {
         dxg_ctx* c = S[k]->c;
         ba[k] = krylovArgs(c, mixed);
-        SpmvArgs<double, double> sv{};
-        sv.A = c->A.get();
+        SpmvArgs<PT, double, PT> sv{};
+        sv.A = Pre<PT>::A(c);
         sv.nbmask = c->nbmask.get();
         sv.N = c->N;
         for (int q = 0; q < 7; ++q) sv.off[q] = c->off[q];
         sv.ks = c->ks.get();
         sv.scratch = c->scratch();
-        sv.x = ba[k].y;
+        sv.x = Pre<PT>::yOut(c);
         sv.y = ba[k].v;
         sv.w = ba[k].rt;
         sv1[k] = sv;
@@ -787,8 +788,8 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     DXG_CUDA(cudaMemcpy(G.args.get(), host.data(), host.size(), cudaMemcpyHostToDevice));
     unsigned char* d = G.args.get();
     G.dBicg = reinterpret_cast<const BicgArgs<double>*>(d + oB);
-    G.dSv1 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o1);
-    G.dSv2 = reinterpret_cast<const SpmvArgs<double, double>*>(d + o2);
+    G.dSv1 = d + o1;
+    G.dSv2 = d + o2;
     for (size_t q = 0; q < G.classes.size(); ++q) {
         G.classes[q].dFwP = d + oc[q][0];
         G.classes[q].dFwR = d + oc[q][1];
@@ -823,7 +824,6 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
             }
             for (int q = 1; q < nc; ++q) DXG_CUDA(cudaStreamWaitEvent(st, B->joinEv[q - 1], 0));
         }
-        if (mixed) launchToDoubleBatch(G.dTd, G.mapM, st);
     };
     for (int it = 0; it < kChunk; ++it) {
         launchBicgRhoBatch<double>(G.dBicg, G.mapM, st);
@@ -831,13 +831,15 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
         precondition(true);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<double, double>(G.dSv1, G.mapN, b, dim, 1, st);
+            launchSpmvBatch<PT, double, PT>(static_cast<const SpmvArgs<PT, double, PT>*>(G.dSv1), G.mapN, b, dim, 1,
+                                            st);
         }
         launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 0, st);
         precondition(false);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<double, double>(G.dSv2, G.mapN, b, dim, 2, st);
+            launchSpmvBatch<PT, double, PT>(static_cast<const SpmvArgs<PT, double, PT>*>(G.dSv2), G.mapN, b, dim, 2,
+                                            st);
         }
         launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 1, st);
     }
@@ -846,7 +848,7 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 template <class PT>
 void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
 {
-    const int launchesPerIt = (sizeof(PT) == 4 ? 8 : 6) + 4 * (int)G.classes.size();
+    const int launchesPerIt = 6 + 4 * (int)G.classes.size();
     cudaStream_t st = B->stream;
     if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
         G.graphTried = true;

@@ -16,6 +16,7 @@
 // captured without a host round trip per half step.  Reductions are deterministic:
 // per-block partial sums in a fixed grid, combined in block order by the last block.
 #include <cuda/atomic>
+#include <type_traits>
 
 #include "common.cuh"
 #include "linalg.cuh"
@@ -167,12 +168,14 @@ __device__ __forceinline__ bool slotValid(unsigned mask, int dim, int s)
 
 // ---------------------------------------------------------------- SpMV
 // y = A x; MODE 0: plain; MODE 1: also dot(w, y) -> h, alpha; MODE 2: dots (y,w),(y,y) -> omega
-template <int B, int DIM, class MT, class VT, int MODE>
-__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0, const SpmvArgs<MT, VT>* batch,
-                                                              const uint2* map)
+template <int B, int DIM, class MT, class VT, class XT, int MODE>
+__global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT> a0,
+                                                              const SpmvArgs<MT, VT, XT>* batch, const uint2* map)
 {
+    // accumulation: FP32 when both operands are FP32, else the output type
+    using AT = typename std::conditional<sizeof(MT) == 4 && sizeof(XT) == 4, float, VT>::type;
     unsigned lb;
-    const SpmvArgs<MT, VT> a = problemOf(a0, batch, map, lb);
+    const SpmvArgs<MT, VT, XT> a = problemOf(a0, batch, map, lb);
     const unsigned nblk = cellBlocksFor(a.N);
     if (lb >= nblk) return;
     if (a.ks && a.ks->status != KS_RUNNING) return;
@@ -181,17 +184,21 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT> a0
     double part[2] = {0.0, 0.0};
     for (int64_t i = lb * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
         const unsigned m = a.nbmask[i];
-        VT acc[B];
+        AT sum[B];
 #pragma unroll
-        for (int e = 0; e < B; ++e) acc[e] = 0;
+        for (int e = 0; e < B; ++e) sum[e] = 0;
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             if (!slotValid(m, DIM, s)) continue;
             const int64_t j = i + a.off[s];
-            VT xj[B];
-            loadVec<B>(a.x, j, xj);
-            blkMv<B>(a.A + ((int64_t)s * a.N + i) * BB, xj, acc);
+            AT xj[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) xj[e] = (AT)a.x[j * B + e];
+            blkMv<B>(a.A + ((int64_t)s * a.N + i) * BB, xj, sum);
         }
+        VT acc[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) acc[e] = (VT)sum[e];
         storeVec<B>(a.y, i, acc);
         if (MODE == 1) {
             VT w[B];
@@ -455,7 +462,8 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, 
     double part[1] = {0.0};
     float* rLow = STAGE == 0 ? a.rLow : nullptr;
     for (int64_t k = k0; k < a.M; k += stride) {
-        a.x[k] += s * a.y[k];
+        const VT yk = a.yLow ? (VT)a.yLow[k] : a.y[k];
+        a.x[k] += s * yk;
         const VT rk = a.r[k] + (-s) * q[k];
         a.r[k] = rk;
         if (rLow) rLow[k] = (float)rk;
@@ -614,17 +622,17 @@ static dim3 batchGrid(int64_t maxN, int count, int threads, int cap)
     return dim3((unsigned)gx, (unsigned)count);
 }
 
-template <int B, int DIM, class MT, class VT>
-static void spmvT(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, const uint2* map, dim3 g, int mode,
-                  cudaStream_t st)
+template <int B, int DIM, class MT, class VT, class XT>
+static void spmvT(const SpmvArgs<MT, VT, XT>& a, const SpmvArgs<MT, VT, XT>* batch, const uint2* map, dim3 g,
+                  int mode, cudaStream_t st)
 {
-    if (mode == 0) spmvKernel<B, DIM, MT, VT, 0><<<g, kReduceThreads, 0, st>>>(a, batch, map);
-    else if (mode == 1) spmvKernel<B, DIM, MT, VT, 1><<<g, kReduceThreads, 0, st>>>(a, batch, map);
-    else spmvKernel<B, DIM, MT, VT, 2><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    if (mode == 0) spmvKernel<B, DIM, MT, VT, XT, 0><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    else if (mode == 1) spmvKernel<B, DIM, MT, VT, XT, 1><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    else spmvKernel<B, DIM, MT, VT, XT, 2><<<g, kReduceThreads, 0, st>>>(a, batch, map);
 }
-template <class MT, class VT>
-static void spmvDispatch(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batch, const uint2* map, dim3 g, int b,
-                         int dim, int mode, cudaStream_t st)
+template <class MT, class VT, class XT>
+static void spmvDispatch(const SpmvArgs<MT, VT, XT>& a, const SpmvArgs<MT, VT, XT>* batch, const uint2* map, dim3 g,
+                         int b, int dim, int mode, cudaStream_t st)
 {
     if (b == 1) {
         if (dim == 2) spmvT<1, 2>(a, batch, map, g, mode, st);
@@ -636,16 +644,16 @@ static void spmvDispatch(const SpmvArgs<MT, VT>& a, const SpmvArgs<MT, VT>* batc
     DXG_CUDA(cudaGetLastError());
 }
 
-template <class MT, class VT>
-void launchSpmv(const SpmvArgs<MT, VT>& a, int b, int dim, int mode, cudaStream_t st)
+template <class MT, class VT, class XT>
+void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st)
 {
-    spmvDispatch<MT, VT>(a, nullptr, nullptr, dim3(cellBlocksFor(a.N)), b, dim, mode, st);
+    spmvDispatch<MT, VT, XT>(a, nullptr, nullptr, dim3(cellBlocksFor(a.N)), b, dim, mode, st);
 }
-template <class MT, class VT>
-void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
+template <class MT, class VT, class XT>
+void launchSpmvBatch(const SpmvArgs<MT, VT, XT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
                      cudaStream_t st)
 {
-    spmvDispatch<MT, VT>(SpmvArgs<MT, VT>{}, batch, cellMap.map, dim3(cellMap.blocks), b, dim, mode, st);
+    spmvDispatch<MT, VT, XT>(SpmvArgs<MT, VT, XT>{}, batch, cellMap.map, dim3(cellMap.blocks), b, dim, mode, st);
 }
 
 template <class MT>
@@ -825,12 +833,13 @@ void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, 
 }
 
 // explicit instantiations
-template void launchSpmv<double, double>(const SpmvArgs<double, double>&, int, int, int, cudaStream_t);
-template void launchSpmv<float, float>(const SpmvArgs<float, float>&, int, int, int, cudaStream_t);
-template void launchSpmvBatch<double, double>(const SpmvArgs<double, double>*, const BlockMap&, int, int, int,
-                                              cudaStream_t);
-template void launchSpmvBatch<float, float>(const SpmvArgs<float, float>*, const BlockMap&, int, int, int,
-                                            cudaStream_t);
+template void launchSpmv<double, double, double>(const SpmvArgs<double, double, double>&, int, int, int,
+                                                cudaStream_t);
+template void launchSpmv<float, double, float>(const SpmvArgs<float, double, float>&, int, int, int, cudaStream_t);
+template void launchSpmvBatch<double, double, double>(const SpmvArgs<double, double, double>*, const BlockMap&, int,
+                                                      int, int, cudaStream_t);
+template void launchSpmvBatch<float, double, float>(const SpmvArgs<float, double, float>*, const BlockMap&, int, int,
+                                                    int, cudaStream_t);
 template void launchBicgInitBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
 template void launchBicgInitBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
 template void launchBicgRhoBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);

@@ -7,11 +7,14 @@
 
 namespace dxg {
 
-template <class MT, class VT>
+// y = A x with matrix values MT, input XT and output / dot operands VT.  With MT = XT =
+// float (the mixed form's FP32 Jacobian times the FP32 preconditioner output) the block
+// products and row sums are FP32 and the result is widened to VT.
+template <class MT, class VT, class XT = VT>
 struct SpmvArgs {
     const MT* A;
     const uint8_t* nbmask;
-    const VT* x;
+    const XT* x;
     VT* y;
     const VT* w;              // second operand of the fused dot(s)
     int64_t N;
@@ -46,6 +49,8 @@ struct BicgArgs {
     // update): the inputs of an FP32 preconditioner inside an FP64 iteration
     float* pLow;
     float* rLow;
+    // FP32 preconditioner output read by the x updates in place of y (x += s*yLow)
+    const float* yLow;
 };
 
 struct ToDoubleArgs {
@@ -93,8 +98,8 @@ struct DefectArgs {
 
 int reduceBlocks(int64_t M);
 
-template <class MT, class VT>
-void launchSpmv(const SpmvArgs<MT, VT>& a, int b, int dim, int mode, cudaStream_t st);
+template <class MT, class VT, class XT = VT>
+void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);
 template <class MT>
 int64_t launchIluFactor(const IluArgs<MT, MT>& a, const LevelSchedule& ls, int b, int dim, cudaStream_t st);
 template <class MT, class VT>
@@ -134,8 +139,8 @@ int cellBlocks(int64_t N);
 // per problem from reduceBlocks (cells == false) or cellBlocks (cells == true).
 void buildBlockMap(const std::vector<int64_t>& lengths, bool cells, std::vector<uint2>& out);
 
-template <class MT, class VT>
-void launchSpmvBatch(const SpmvArgs<MT, VT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
+template <class MT, class VT, class XT = VT>
+void launchSpmvBatch(const SpmvArgs<MT, VT, XT>* batch, const BlockMap& cellMap, int b, int dim, int mode,
                      cudaStream_t st);
 template <class VT>
 void launchBicgInitBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);

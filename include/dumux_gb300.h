@@ -108,11 +108,11 @@ int dxg_ctx_destroy(dxg_ctx* ctx);
 const char* dxg_last_error(const dxg_ctx* ctx);
 
 /* Precision of the linear solve: FP64 everywhere (the plain drop-in), or the mixed
- * form: an FP32 copy of the Jacobian, FP32 ILU(0) factors and FP32 triangular sweeps
- * as the preconditioner of a BiCGSTAB whose vectors, dots and SpMV stay FP64 on the
- * FP64 Jacobian (the preconditioner is applied to FP32 copies of p and r and its
- * result widened back), inside the FP64 residual, numeric differentiation, Newton
- * update and norms.  Must be set before upload. */
+ * form: an FP32 copy of the Jacobian, FP32 ILU(0) factors and triangular sweeps, and
+ * the BiCGSTAB operator products on the FP32 Jacobian (FP32 block products and row sums
+ * of the FP32 preconditioner output), while the Krylov vectors, their updates and all dot
+ * products stay FP64 -- an inexact Newton step inside the FP64 residual, numeric
+ * differentiation, Newton update and norms.  Must be set before upload. */
 enum { DXG_PRECISION_FP64 = 0, DXG_PRECISION_MIXED = 1 };
 int dxg_set_precision(dxg_ctx* ctx, int precision);
 
