@@ -359,7 +359,8 @@ std::vector<WaveGeom> geomsFor(const Members& S, int ctas)
 }
 
 // Candidate launch shapes: cluster sizes 1..16, the fewest threads that keep every
-// problem at <= 2 lines per thread (and twice that), prefetch depths 1..8.
+// problem at <= 2 lines per thread (and twice that), prefetch depths 1..8 through the
+// shared-memory ring or 0 (direct loads behind L1 prefetches).
 std::vector<WaveBatchPlan> candidates(const Members& S, int dim, int b, bool fp64)
 {
     std::vector<WaveBatchPlan> out;
@@ -370,7 +371,7 @@ std::vector<WaveBatchPlan> candidates(const Members& S, int dim, int b, bool fp6
         const int t2 = ((maxLines + 1) / 2 + 31) / 32 * 32;
         for (int threads : {t2, 2 * t2}) {
             if (threads < 32 || threads > 1024) continue;
-            for (int pf : {1, 2, 4, 8}) {
+            for (int pf : {0, 1, 2, 4, 8}) {
                 WaveBatchPlan p;
                 p.ctas = ctas;
                 p.threads = threads;

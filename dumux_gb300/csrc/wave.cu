@@ -365,54 +365,79 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
 #pragma unroll
         for (int e = 0; e < PB; ++e) prev[k][e] = 0;
 
-    // prefetch this thread's cells of step s into ring slot s % PF
+    // The matrix blocks and vector entries of this thread's cell of step s on line k:
+    // visit(offset in the record, source, number of elements) -- blocks (BB) or vectors (B)
+    constexpr bool RING = PF > 0;      // PF == 0: no shared-memory ring (direct loads)
+    constexpr int PFR = RING ? PF : 1;
+    constexpr int PD = 8;              // direct loads: L1 prefetch distance in levels
+    auto forCell = [&](int s, int k, auto&& visitBlk, auto&& visitVec) {
+        if (s >= nSteps) return;
+        const LineState& st = ls[k];
+        if (st.ll < 0) return;
+        const int L = DIR > 0 ? Lfirst + s : Lfirst - s;
+        const int x = L - st.yz;
+        if ((unsigned)x >= (unsigned)nx) return;
+        const int64_t i = st.base + x;
+        const bool vx = DIR > 0 ? x > 0 : x < nx - 1;
+        const bool vy = st.nbY != kNone, vz = st.nbZ != kNone;
+        if (MODE == 1) {
+            if (DIM == 3 && vz) {
+                visitBlk(sMz * BB, a.A + ((int64_t)sMz * N + i) * BB);
+                visitBlk((DIM + 1 + sMz) * BB, a.A + ((int64_t)(2 * DIM - sMz) * N + i - planeStride) * BB);
+            }
+            if (vy) {
+                visitBlk(sMy * BB, a.A + ((int64_t)sMy * N + i) * BB);
+                visitBlk((DIM + 1 + sMy) * BB, a.A + ((int64_t)(2 * DIM - sMy) * N + i - nx) * BB);
+            }
+            if (vx) {
+                visitBlk(sMx * BB, a.A + ((int64_t)sMx * N + i) * BB);
+                visitBlk((DIM + 1 + sMx) * BB, a.A + ((int64_t)(2 * DIM - sMx) * N + i - 1) * BB);
+            }
+            visitBlk(DIM * BB, a.A + ((int64_t)sDiag * N + i) * BB);
+        } else if (DIR > 0) {
+            if (DIM == 3 && vz) visitBlk(sMz * BB, a.L + ((int64_t)sMz * N + i) * BB);
+            if (vy) visitBlk(sMy * BB, a.L + ((int64_t)sMy * N + i) * BB);
+            if (vx) visitBlk(sMx * BB, a.L + ((int64_t)sMx * N + i) * BB);
+            visitVec(DIM * BB, a.rhs + i * B);
+        } else {
+            if (vx) visitBlk(0 * BB, a.A + ((int64_t)sPx * N + i) * BB);
+            if (vy) visitBlk(1 * BB, a.A + ((int64_t)sPy * N + i) * BB);
+            if (DIM == 3 && vz) visitBlk(2 * BB, a.A + ((int64_t)sPz * N + i) * BB);
+            visitBlk(DIM * BB, a.Dinv + i * BB);
+            visitVec(DIM * BB + BB, a.v + i * B);
+        }
+    };
+    // ring: copy the cells of step s into ring slot s % PF with cp.async;
+    // direct: prefetch the cells PD levels ahead into L1
     auto issue = [&](int s) {
-        if (s < nSteps) {
-            const int L = DIR > 0 ? Lfirst + s : Lfirst - s;
+        if constexpr (RING) {
 #pragma unroll
             for (int k = 0; k < kMaxLpt; ++k) {
-                const LineState& st = ls[k];
-                if (st.ll < 0) continue;
-                const int x = L - st.yz;
-                if ((unsigned)x >= (unsigned)nx) continue;
-                const int64_t i = st.base + x;
-                T* rec = pf + ((size_t)(s & (PF - 1)) * nthr * lpt + k * nthr + threadIdx.x) * REC;
-                const bool vx = DIR > 0 ? x > 0 : x < nx - 1;
-                const bool vy = st.nbY != kNone, vz = st.nbZ != kNone;
-                if (MODE == 1) {
-                    if (DIM == 3 && vz) {
-                        copyElems<T, BB>(rec + sMz * BB, a.A + ((int64_t)sMz * N + i) * BB);
-                        copyElems<T, BB>(rec + (DIM + 1 + sMz) * BB, a.A + ((int64_t)(2 * DIM - sMz) * N + i - planeStride) * BB);
-                    }
-                    if (vy) {
-                        copyElems<T, BB>(rec + sMy * BB, a.A + ((int64_t)sMy * N + i) * BB);
-                        copyElems<T, BB>(rec + (DIM + 1 + sMy) * BB, a.A + ((int64_t)(2 * DIM - sMy) * N + i - nx) * BB);
-                    }
-                    if (vx) {
-                        copyElems<T, BB>(rec + sMx * BB, a.A + ((int64_t)sMx * N + i) * BB);
-                        copyElems<T, BB>(rec + (DIM + 1 + sMx) * BB, a.A + ((int64_t)(2 * DIM - sMx) * N + i - 1) * BB);
-                    }
-                    copyElems<T, BB>(rec + DIM * BB, a.A + ((int64_t)sDiag * N + i) * BB);
-                } else if (DIR > 0) {
-                    if (DIM == 3 && vz) copyElems<T, BB>(rec + sMz * BB, a.L + ((int64_t)sMz * N + i) * BB);
-                    if (vy) copyElems<T, BB>(rec + sMy * BB, a.L + ((int64_t)sMy * N + i) * BB);
-                    if (vx) copyElems<T, BB>(rec + sMx * BB, a.L + ((int64_t)sMx * N + i) * BB);
-                    copyElems<T, B>(rec + DIM * BB, a.rhs + i * B);
-                } else {
-                    if (vx) copyElems<T, BB>(rec + 0 * BB, a.A + ((int64_t)sPx * N + i) * BB);
-                    if (vy) copyElems<T, BB>(rec + 1 * BB, a.A + ((int64_t)sPy * N + i) * BB);
-                    if (DIM == 3 && vz) copyElems<T, BB>(rec + 2 * BB, a.A + ((int64_t)sPz * N + i) * BB);
-                    copyElems<T, BB>(rec + DIM * BB, a.Dinv + i * BB);
-                    copyElems<T, B>(rec + DIM * BB + BB, a.v + i * B);
-                }
+                T* rec = pf + ((size_t)(s & (PFR - 1)) * nthr * lpt + k * nthr + threadIdx.x) * REC;
+                forCell(
+                    s, k, [&](int off, const T* src) { copyElems<T, BB>(rec + off, src); },
+                    [&](int off, const T* src) { copyElems<T, B>(rec + off, src); });
             }
+            cpCommit();
+        } else {
+            // called with s = step + 1: the cells PD levels ahead of the current step
+            auto pre = [&](int, const T* src) { asm volatile("prefetch.global.L1 [%0];" ::"l"(src)); };
+#pragma unroll
+            for (int k = 0; k < kMaxLpt; ++k) forCell(s + PD - 1, k, pre, pre);
         }
-        cpCommit();
     };
 
     if (!skip) {
+        if constexpr (RING) {
 #pragma unroll
-        for (int s = 0; s < PF; ++s) issue(s);
+            for (int s = 0; s < PFR; ++s) issue(s);
+        } else {
+            // warm L1 with the first PD levels
+            auto pre = [&](int, const T* src) { asm volatile("prefetch.global.L1 [%0];" ::"l"(src)); };
+            for (int s = 0; s < PD; ++s)
+#pragma unroll
+                for (int k = 0; k < kMaxLpt; ++k) forCell(s, k, pre, pre);
+        }
     }
 
     for (int step = 0; step < nSteps && !skip; ++step) {
@@ -432,7 +457,7 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
         bool haveHalo = !needsHalo;
         bool roomChecked = false;
 
-        cpWait<PF - 1>();
+        if constexpr (RING) cpWait<PFR - 1>();
 #pragma unroll
         for (int k = 0; k < kMaxLpt; ++k) {
             const LineState& st = ls[k];
@@ -440,7 +465,25 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
             const int x = L - st.yz;
             if ((unsigned)x >= (unsigned)nx) continue;
             const int64_t i = st.base + x;
-            const T* rec = pf + ((size_t)(step & (PF - 1)) * nthr * lpt + k * nthr + threadIdx.x) * REC;
+            T recLocal[RING ? 1 : REC];
+            const T* rec;
+            if constexpr (RING) {
+                rec = pf + ((size_t)(step & (PFR - 1)) * nthr * lpt + k * nthr + threadIdx.x) * REC;
+            } else {
+                // direct loads (L1, filled by the prefetches); v is written in place by the
+                // backward sweep, by this thread only, after this read
+                forCell(
+                    step, k,
+                    [&](int off, const T* src) {
+#pragma unroll
+                        for (int e = 0; e < BB; ++e) recLocal[off + e] = src[e];
+                    },
+                    [&](int off, const T* src) {
+#pragma unroll
+                        for (int e = 0; e < B; ++e) recLocal[off + e] = src[e];
+                    });
+                rec = recLocal;
+            }
             const bool hx = DIR > 0 ? x > 0 : x < nx - 1;
             if (!haveHalo && ((st.nbY != kNone && st.nbY < 0) || (st.nbZ != kNone && st.nbZ < 0))) {
                 const uint32_t parity = (uint32_t)(((gIn - gInFirst) / kRing) & 1);
@@ -553,12 +596,13 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
             }
         }
         // prefetch the cells PF levels ahead into the slot consumed by this step
-        issue(step + PF);
+        // (direct: prefetch PD levels ahead into L1)
+        issue(step + PFR);
         __syncthreads();
         if (abortFlag) break;
         if (threadIdx.x == 0 && hasUp) stRelaxedCluster(upConsumed, gstep);
     }
-    cpWait<0>();
+    if constexpr (RING) cpWait<0>();
     // no CTA may leave while others can still write into its shared memory
     cluster.sync();
     if (abortFlag) {
@@ -680,6 +724,7 @@ static cudaError_t dispatchPF(const WaveLaunch& L, const WaveArgs<T>& a, const W
         case 4: return launchOne<B, T, DIM, DIR, MODE, 4>(L, a, batch, st, query, fits);
         case 2: return launchOne<B, T, DIM, DIR, MODE, 2>(L, a, batch, st, query, fits);
         case 1: return launchOne<B, T, DIM, DIR, MODE, 1>(L, a, batch, st, query, fits);
+        case 0: return launchOne<B, T, DIM, DIR, MODE, 0>(L, a, batch, st, query, fits);
         default:
             if (fits) *fits = 0;
             return query ? cudaSuccess : cudaErrorInvalidConfiguration;
@@ -818,7 +863,7 @@ static int batchFits(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int d
 int completeWaveBatchPlan(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim, int b, bool fp64)
 {
     if (p.ctas < 1 || p.ctas > 16 || p.threads < 32 || p.threads > 1024 || p.threads % 32) return 0;
-    if (p.pf != 1 && p.pf != 2 && p.pf != 4 && p.pf != 8) return 0;
+    if (p.pf != 0 && p.pf != 1 && p.pf != 2 && p.pf != 4 && p.pf != 8) return 0;
     for (const WaveGeom& g : geoms) {
         if (g.ctas < 1 || g.ctas > p.ctas) return 0;
         if ((g.linesPerCta + p.threads - 1) / p.threads > 2) return 0;
