@@ -689,9 +689,9 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     int done = 0;
     while (true) {
         for (int k = 0; k < chunk; ++k) {
-            launchBicgRho<double>(ba, st);
+            // the rho step ran in the kernel that closed the previous iteration
             launchBicgUpdateP<double>(ba, st);
-            c->launches += 2;
+            c->launches += 1;
             precondition(pIn);
             sv.x = yOut; sv.y = v; sv.w = rt;
             {

@@ -827,7 +827,7 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
         }
     };
     for (int it = 0; it < kChunk; ++it) {
-        launchBicgRhoBatch<double>(G.dBicg, G.mapM, st);
+        // the rho step ran in the kernel that closed the previous iteration
         launchBicgUpdatePBatch<double>(G.dBicg, G.mapM, st);
         precondition(true);
         {
@@ -849,7 +849,7 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 template <class PT>
 void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
 {
-    const int launchesPerIt = 6 + 4 * (int)G.classes.size();
+    const int launchesPerIt = 5 + 4 * (int)G.classes.size();
     cudaStream_t st = B->stream;
     if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
         G.graphTried = true;

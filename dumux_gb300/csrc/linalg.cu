@@ -159,6 +159,39 @@ __device__ __forceinline__ void storeVec(T* p, int64_t i, const T* v)
     for (int e = 0; e < B; ++e) p[i * B + e] = v[e];
 }
 
+// Read-only vector loads of one b x b block / one b-vector (16-byte loads for 2 x 2 FP32
+// blocks and FP64 pairs; every block and vector entry starts on a multiple of its size
+// from a cudaMalloc base).  Only for data no kernel writes while the reader runs.
+template <int B, class T>
+__device__ __forceinline__ void ldgBlock(const T* p, T* o)
+{
+    if constexpr (B == 2 && sizeof(T) == 4) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    } else if constexpr (B == 2 && sizeof(T) == 8) {
+        const double2 v0 = __ldg(reinterpret_cast<const double2*>(p));
+        const double2 v1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+        o[0] = v0.x; o[1] = v0.y; o[2] = v1.x; o[3] = v1.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) o[e] = __ldg(p + e);
+    }
+}
+template <int B, class T>
+__device__ __forceinline__ void ldgVec(const T* p, T* o)
+{
+    if constexpr (B == 2 && sizeof(T) == 4) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        o[0] = v.x; o[1] = v.y;
+    } else if constexpr (B == 2 && sizeof(T) == 8) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+        o[0] = v.x; o[1] = v.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < B; ++e) o[e] = __ldg(p + e);
+    }
+}
+
 __device__ __forceinline__ bool slotValid(unsigned mask, int dim, int s)
 {
     if (s == dim) return true;
@@ -183,18 +216,26 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT
     constexpr int BB = B * B;
     double part[2] = {0.0, 0.0};
     for (int64_t i = lb * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
-        const unsigned m = a.nbmask[i];
+        const unsigned m = __ldg(a.nbmask + i);
         AT sum[B];
 #pragma unroll
         for (int e = 0; e < B; ++e) sum[e] = 0;
+        // straight-line code: every slot's block (always allocated) and x entry (the
+        // cell's own for a missing neighbour) is loaded without a branch, so all loads of
+        // the row are in flight together; a missing neighbour's block enters as zero
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-            if (!slotValid(m, DIM, s)) continue;
-            const int64_t j = i + a.off[s];
+            const bool valid = slotValid(m, DIM, s);
+            MT blk[BB];
+            XT xs[B];
+            ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, blk);
+            ldgVec<B>(a.x + (i + (valid ? a.off[s] : 0)) * B, xs);
             AT xj[B];
 #pragma unroll
-            for (int e = 0; e < B; ++e) xj[e] = (AT)a.x[j * B + e];
-            blkMv<B>(a.A + ((int64_t)s * a.N + i) * BB, xj, sum);
+            for (int e = 0; e < B; ++e) xj[e] = valid ? (AT)xs[e] : (AT)0;
+#pragma unroll
+            for (int e = 0; e < BB; ++e) blk[e] = valid ? blk[e] : (MT)0;
+            blkMv<B>(blk, xj, sum);
         }
         VT acc[B];
 #pragma unroll
@@ -379,6 +420,17 @@ __global__ void iluBackwardLevel(IluArgs<MT, VT> a, VT* v, int begin, int count)
     const int64_t stride = (int64_t)nblk * blockDim.x;            \
     const int64_t k0 = lb * (int64_t)blockDim.x + threadIdx.x;
 
+// The rho step that opens an iteration, taken by the kernel that closed the previous one
+// (the last block of bicgInit or of the stage-1 update, with rhoNew = <rt, r>): iteration
+// limit, breakdown checks and beta.
+__device__ __forceinline__ void rhoStep(KrylovState& ks, double rhoNew)
+{
+    if (ks.halfsteps + 1 >= ks.maxHalf) { ks.status = KS_MAXIT; return; }
+    ks.rho_new = rhoNew;
+    if (fabs(ks.rho) <= 1e-80 || fabs(ks.omega) <= 1e-80) { ks.status = KS_BREAKDOWN; return; }
+    if (ks.halfsteps > 0) ks.beta = (ks.rho_new / ks.rho) * (ks.alpha / ks.omega);
+}
+
 template <class VT>
 __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
@@ -404,25 +456,11 @@ __global__ void __launch_bounds__(kReduceThreads) bicgInit(BicgArgs<VT> a0, cons
         ks.halfsteps = 0;
         if (!isfinite(ks.def)) ks.status = KS_NAN;
         else if (ks.def < 1e-30) ks.status = KS_CONVERGED;
-        else ks.status = KS_RUNNING;
-    }
-}
-
-// rho_new = <rt, r>, breakdown checks and beta (first half of an iteration)
-template <class VT>
-__global__ void __launch_bounds__(kReduceThreads) bicgRho(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
-{
-    DXG_PROBLEM_BLOCKS(BicgArgs<VT>, M)
-    if (a.ks->status != KS_RUNNING) return;
-    double part[1] = {0.0};
-    for (int64_t k = k0; k < a.M; k += stride)
-        part[0] += (double)a.rt[k] * (double)a.r[k];
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 5, nblk, lb)) {
-        KrylovState& ks = *a.ks;
-        if (ks.halfsteps + 1 >= ks.maxHalf) { ks.status = KS_MAXIT; return; }
-        ks.rho_new = part[0];
-        if (fabs(ks.rho) <= 1e-80 || fabs(ks.omega) <= 1e-80) { ks.status = KS_BREAKDOWN; return; }
-        if (ks.halfsteps > 0) ks.beta = (ks.rho_new / ks.rho) * (ks.alpha / ks.omega);
+        else {
+            ks.status = KS_RUNNING;
+            // first rho step: rt = r, so <rt, r> is the defect sum just formed
+            rhoStep(ks, part[0]);
+        }
     }
 }
 
@@ -449,7 +487,8 @@ __global__ void bicgUpdateP(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const ui
     }
 }
 
-// x += s*y; r -= s*q; def = ||r||; STAGE 0: s = alpha, q = v; STAGE 1: s = omega, q = t
+// x += s*y; r -= s*q; def = ||r||; STAGE 0: s = alpha, q = v; STAGE 1: s = omega, q = t,
+// and the next iteration's rho step on <rt, r>
 template <class VT, int STAGE>
 __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, const BicgArgs<VT>* batch, const uint2* map)
 {
@@ -459,7 +498,10 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, 
     const double sd = STAGE == 0 ? ksr.alpha : ksr.omega;
     const VT s = (VT)sd;
     const VT* q = STAGE == 0 ? a.v : a.t;
-    double part[1] = {0.0};
+    constexpr int NP = STAGE == 1 ? 2 : 1;
+    double part[NP];
+#pragma unroll
+    for (int e = 0; e < NP; ++e) part[e] = 0.0;
     float* rLow = STAGE == 0 ? a.rLow : nullptr;
     for (int64_t k = k0; k < a.M; k += stride) {
         const VT yk = a.yLow ? (VT)a.yLow[k] : a.y[k];
@@ -468,14 +510,16 @@ __global__ void __launch_bounds__(kReduceThreads) bicgAxpyNorm(BicgArgs<VT> a0, 
         a.r[k] = rk;
         if (rLow) rLow[k] = (float)rk;
         part[0] += (double)rk * (double)rk;
+        if (STAGE == 1) part[NP - 1] += (double)a.rt[k] * (double)rk;
     }
-    if (gridSum<1>(part, a.scratch.partials, a.scratch.counter + 6, nblk, lb)) {
+    if (gridSum<NP>(part, a.scratch.partials, a.scratch.counter + 6, nblk, lb)) {
         KrylovState& ks = *a.ks;
         ks.def = sqrt(part[0]);
         ks.halfsteps += 1;
         if (STAGE == 1) ks.rho = ks.rho_new;
         if (!isfinite(ks.def)) ks.status = KS_NAN;
         else if (ks.def < ks.def0 * ks.reduction || ks.def < 1e-30) ks.status = KS_CONVERGED;
+        else if (STAGE == 1) rhoStep(ks, part[NP - 1]);
     }
 }
 
@@ -710,11 +754,6 @@ void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st)
     DXG_CUDA(cudaGetLastError());
 }
 template <class VT>
-void launchBicgRho(const BicgArgs<VT>& a, cudaStream_t st)
-{
-    bicgRho<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
-}
-template <class VT>
 void launchBicgUpdateP(const BicgArgs<VT>& a, cudaStream_t st)
 {
     bicgUpdateP<VT><<<reduceBlocks(a.M), kReduceThreads, 0, st>>>(a, nullptr, nullptr);
@@ -730,11 +769,6 @@ void launchBicgInitBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStrea
 {
     bicgInit<VT><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
     DXG_CUDA(cudaGetLastError());
-}
-template <class VT>
-void launchBicgRhoBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStream_t st)
-{
-    bicgRho<VT><<<m.blocks, kReduceThreads, 0, st>>>(BicgArgs<VT>{}, batch, m.map);
 }
 template <class VT>
 void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, const BlockMap& m, cudaStream_t st)
@@ -842,8 +876,6 @@ template void launchSpmvBatch<float, double, float>(const SpmvArgs<float, double
                                                     int, cudaStream_t);
 template void launchBicgInitBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
 template void launchBicgInitBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
-template void launchBicgRhoBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
-template void launchBicgRhoBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
 template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
 template void launchBicgUpdatePBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
 template void launchBicgAxpyNormBatch<double>(const BicgArgs<double>*, const BlockMap&, int, cudaStream_t);
@@ -856,8 +888,6 @@ template int64_t launchIluApply<float, float>(const IluArgs<float, float>&, cons
                                               const float*, float*, cudaStream_t);
 template void launchBicgInit<double>(const BicgArgs<double>&, const double*, cudaStream_t);
 template void launchBicgInit<float>(const BicgArgs<float>&, const double*, cudaStream_t);
-template void launchBicgRho<double>(const BicgArgs<double>&, cudaStream_t);
-template void launchBicgRho<float>(const BicgArgs<float>&, cudaStream_t);
 template void launchBicgUpdateP<double>(const BicgArgs<double>&, cudaStream_t);
 template void launchBicgUpdateP<float>(const BicgArgs<float>&, cudaStream_t);
 template void launchBicgAxpyNorm<double>(const BicgArgs<double>&, int, cudaStream_t);

@@ -108,8 +108,6 @@ int64_t launchIluApply(const IluArgs<MT, VT>& a, const LevelSchedule& ls, int b,
 template <class VT>
 void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st);
 template <class VT>
-void launchBicgRho(const BicgArgs<VT>& a, cudaStream_t st);
-template <class VT>
 void launchBicgUpdateP(const BicgArgs<VT>& a, cudaStream_t st);
 template <class VT>
 void launchBicgAxpyNorm(const BicgArgs<VT>& a, int stage, cudaStream_t st);
@@ -144,8 +142,6 @@ void launchSpmvBatch(const SpmvArgs<MT, VT, XT>* batch, const BlockMap& cellMap,
                      cudaStream_t st);
 template <class VT>
 void launchBicgInitBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
-template <class VT>
-void launchBicgRhoBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
 template <class VT>
 void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, const BlockMap& map, cudaStream_t st);
 template <class VT>
