@@ -644,7 +644,8 @@ def main():
                    "unknowns": ctx.num_dofs, "newton_iterations": newton_iters, "global_batch": world,
                    "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)",
                    "step": "one stationary Newton step from the same initial state (includes its 80 KB h2d reset)"
-                           if stationary else "one implicit-Euler time step"},
+                           if stationary else "one implicit-Euler time step",
+                   "ilu_kernels": ctx.describe()},
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
     if rank == 0:

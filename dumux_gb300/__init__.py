@@ -103,6 +103,7 @@ def lib():
         L.dxg_selftest_bounded_wait.argtypes = [C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
                                                 C.POINTER(C.c_double)]
         L.dxg_batch_describe.argtypes = [vp, C.c_char_p, C.c_int64]
+        L.dxg_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_batch_stream.argtypes = [vp]
         L.dxg_batch_stream.restype = C.c_void_p
         _lib = L
@@ -263,6 +264,12 @@ class Context:
         n = C.c_int64(); ms = C.c_double(); by = C.c_double()
         self._check(self._L.dxg_get_kernel_timing(self._h, k, C.byref(n), C.byref(ms), C.byref(by)))
         return n.value, ms.value, by.value
+
+    def describe(self):
+        """The ILU(0) kernels in use and, once tuned, the time of every launch shape tried."""
+        buf = C.create_string_buffer(1024)
+        self._check(self._L.dxg_describe(self._h, buf, len(buf)))
+        return buf.value.decode()
 
     def kernel_launches(self):
         return int(self._L.dxg_kernel_launch_count(self._h))

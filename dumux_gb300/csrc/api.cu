@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -524,6 +525,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->scal.alloc(4);
     c->singular.alloc(2);
     c->wavePlan = makeWavePlan(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b, c->precision == DXG_PRECISION_FP64);
+    c->waveTuned = false;
+    c->waveTuneCount = 0;
     DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
     DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
     DXG_CUDA(cudaMemsetAsync(c->ks.get(), 0, sizeof(KrylovState), st));
@@ -597,6 +600,55 @@ WaveArgs<T> waveArgs(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* rhs, T* v)
 }
 
 bool useWave(const dxg_ctx* c) { return c->iluKernel != DXG_ILU_LEVELS && c->wavePlan.ok; }
+
+// Launch shape of the wavefront sweeps, chosen once per context by timing: every plan
+// that fits (cluster sizes 16..1) applies the preconditioner built by the first
+// factorisation to `in` (a scratch read) into `out` (overwritten by the solve that
+// follows); the fastest is kept.  Small grids run faster on fewer CTAs (fewer hand-offs
+// per level), large ones on more (more SMs per level).
+template <class T>
+void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
+{
+    c->waveTuned = true;
+    const std::vector<WavePlan> cand = wavePlanCandidates(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
+                                                          (int)c->pcHost.nz, c->b, sizeof(T) == 8);
+    if (cand.size() < 2) return;
+    cudaStream_t st = c->stream;
+    cudaEvent_t e0, e1;
+    DXG_CUDA(cudaEventCreate(&e0));
+    DXG_CUDA(cudaEventCreate(&e1));
+    const WavePlan chosen = c->wavePlan;
+    WavePlan best = chosen;
+    float bestMs = 0.f;
+    constexpr int kReps = 3;
+    c->waveTuneCount = 0;
+    for (const WavePlan& p : cand) {
+        c->wavePlan = p;
+        WaveArgs<T> w = waveArgs<T>(c, A, L, Dinv, in, out);
+        w.ks = nullptr;   // never skip while timing
+        launchWaveApply<T>(p, w, w, c->b, st);   // warm-up
+        DXG_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < kReps; ++r) launchWaveApply<T>(p, w, w, c->b, st);
+        DXG_CUDA(cudaEventRecord(e1, st));
+        DXG_CUDA(cudaEventSynchronize(e1));
+        c->launches += 2 * (1 + kReps);
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= kReps;
+        if (c->waveTuneCount < 5) {
+            c->waveTuneMs[c->waveTuneCount] = ms;
+            c->waveTuneCtas[c->waveTuneCount] = p.ctas;
+            ++c->waveTuneCount;
+        }
+        if (bestMs == 0.f || ms < bestMs) {
+            bestMs = ms;
+            best = p;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->wavePlan = best;
+}
 
 template <class T>
 int64_t iluApply(dxg_ctx* c, const IluArgs<T, T>& ia, const T* A, T* L, T* Dinv, const T* d, T* v)
@@ -684,6 +736,7 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
     sv.ks = c->ks.get();
     sv.scratch = c->scratch();
+    if (refactor && useWave(c) && !c->waveTuned) tuneWavePlan<PT>(c, PA, PL, PD, pIn, yOut);
     auto precondition = [&](const PT* in) { c->launches += iluApply<PT>(c, ia, PA, PL, PD, in, yOut); };
     const int chunk = 4;
     int done = 0;
@@ -1227,6 +1280,31 @@ int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
     }
     c->iluKernel = kind;
     c->haveFactor = false;
+    return DXG_OK;
+}
+
+int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
+{
+    if (!c || !buf || len <= 0) return DXG_ERR_ARG;
+    std::string out;
+    if (!c->uploaded) out = "no problem uploaded";
+    else if (!useWave(c)) out = "ILU(0): level-scheduled kernels";
+    else {
+        const WavePlan& p = c->wavePlan;
+        out = "ILU(0): wavefront, cluster " + std::to_string(p.ctas) + " x " + std::to_string(p.threads) +
+              " threads";
+        if (c->waveTuned && c->waveTuneCount > 0) {
+            out += ", tuned (ms per apply:";
+            char tmp[64];
+            for (int k = 0; k < c->waveTuneCount; ++k) {
+                std::snprintf(tmp, sizeof tmp, " %d CTAs %.3f", c->waveTuneCtas[k], c->waveTuneMs[k]);
+                out += tmp;
+            }
+            out += ")";
+        }
+    }
+    std::strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
     return DXG_OK;
 }
 

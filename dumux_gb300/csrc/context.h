@@ -66,6 +66,10 @@ struct dxg_ctx {
     // ILU(0) kernels: cluster wavefront (default) or level-scheduled launches
     int iluKernel = DXG_ILU_AUTO;
     dxg::WavePlan wavePlan;
+    bool waveTuned = false;           // launch shape chosen by timing (first factorisation)
+    double waveTuneMs[5] = {0, 0, 0, 0, 0};   // ms per apply of each candidate tried
+    int waveTuneCtas[5] = {0, 0, 0, 0, 0};
+    int waveTuneCount = 0;
 
     // optional event timing per kernel class (pairs resolved lazily)
     struct TimedLaunch {

@@ -440,6 +440,7 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
         }
     }
 
+    int roomSeen = INT_MIN;   // last consumer progress observed by this thread
     for (int step = 0; step < nSteps && !skip; ++step) {
         const int L = DIR > 0 ? Lfirst + step : Lfirst - step;
         const int gstep = gOfL(L);
@@ -572,12 +573,14 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
             // boundary lines feed the next CTA in sweep direction
             if (st.outIdx >= 0) {
                 if (!roomChecked) {
-                    // slot gstep%kRing was last read by the consumer at its step gstep-kRing+1
+                    // slot gstep%kRing was last read by the consumer at its step gstep-kRing+1;
+                    // the consumer's progress only grows, so a value seen earlier that
+                    // already covers the target needs no new load
                     const int target = gstep - kRing + 1;
-                    if (ldAcquireCluster(&consumerDone) < target) {
+                    if (roomSeen < target && (roomSeen = ldAcquireCluster(&consumerDone)) < target) {
                         const unsigned long long deadline = globalTimer() + kWaitNs;
                         bool ok = true;
-                        while (ldAcquireCluster(&consumerDone) < target) {
+                        while ((roomSeen = ldAcquireCluster(&consumerDone)) < target) {
                             if (*(volatile int*)&abortFlag) { ok = false; break; }
                             if (globalTimer() > deadline) {
                                 atomicExch(a.err, DXG_ERR_TIMEOUT);
@@ -740,12 +743,13 @@ static cudaError_t dispatch(const WaveLaunch& L, int dim, const WaveArgs<T>& a, 
 }
 
 // prefetch depth of a single-problem launch: the deepest of {8, 4, 2, 1} within the
-// shared-memory budget
+// shared-memory budget, else 0 (no ring); pf stays -1 (refused by the dispatch) when not
+// even the ring-free layout fits
 template <int B, class T, int DIR, int MODE>
 static WaveLaunch singleLaunch(const WavePlan& p, int dim)
 {
-    WaveLaunch L{1, p.ctas, p.threads, 0, 0};
-    for (int d : {8, 4, 2, 1}) {
+    WaveLaunch L{1, p.ctas, p.threads, -1, 0};
+    for (int d : {8, 4, 2, 1, 0}) {
         const size_t sm = waveSmemFor<B, T, DIR, MODE>(dim, p.linesPerCta, p.haloLines, p.threads, d);
         if (sm <= kWaveSmemLimit) {
             L.pf = d;
@@ -797,17 +801,27 @@ static WavePlan planFor(int dim, int nx, int ny, int nz, int maxCtas)
     return p;
 }
 
-WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64)
+std::vector<WavePlan> wavePlanCandidates(int dim, int nx, int ny, int nz, int b, bool fp64)
 {
+    std::vector<WavePlan> out;
     for (int maxCtas = 16; maxCtas >= 1; maxCtas /= 2) {
         WavePlan p = planFor(dim, nx, ny, nz, maxCtas);
         if (!p.ok) continue;
         bool fits;
         if (b == 1) fits = fp64 ? planFits<1, double>(p, dim) : planFits<1, float>(p, dim);
         else fits = fp64 ? planFits<2, double>(p, dim) : planFits<2, float>(p, dim);
-        if (fits) return p;
+        if (!fits) continue;
+        bool dup = false;
+        for (const WavePlan& q : out) dup = dup || q.ctas == p.ctas;
+        if (!dup) out.push_back(p);
     }
-    return WavePlan{};
+    return out;
+}
+
+WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64)
+{
+    const std::vector<WavePlan> c = wavePlanCandidates(dim, nx, ny, nz, b, fp64);
+    return c.empty() ? WavePlan{} : c.front();
 }
 
 template <class T>

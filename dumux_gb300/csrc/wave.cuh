@@ -42,6 +42,10 @@ struct WaveBatchPlan {
 };
 
 WavePlan makeWavePlan(int dim, int nx, int ny, int nz, int b, bool fp64);
+// Every plan that fits, one per cluster size (16, 8, 4, 2, 1 CTAs); the first is
+// makeWavePlan's.  The factors and sweeps do not depend on the plan (same arithmetic
+// per cell), so a context may switch between them at any time.
+std::vector<WavePlan> wavePlanCandidates(int dim, int nx, int ny, int nz, int b, bool fp64);
 WaveGeom waveGeom(int dim, int nx, int ny, int nz, int maxCtas);
 int completeWaveBatchPlan(WaveBatchPlan& p, const std::vector<WaveGeom>& geoms, int dim, int b, bool fp64);
 template <class T>

@@ -243,6 +243,10 @@ int dxg_advance_time_step(dxg_ctx* ctx);
  * reference (dune-istl's SeqILU is sequential). */
 enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2 };
 int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
+/* The ILU(0) kernels in use, as text: the wavefront launch shape (cluster size, threads,
+ * prefetch depth) and, once the first factorisation has chosen it by timing, the time per
+ * apply of every shape tried. */
+int dxg_describe(const dxg_ctx* ctx, char* buf, int64_t len);
 
 /* ---- diagnostics --------------------------------------------------------------------- */
 /* The CUDA stream (cudaStream_t) all work of this context runs on, for event timing
