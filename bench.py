@@ -50,6 +50,9 @@ def parse():
                          "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching")
     ap.add_argument("--diff", default="numeric", choices=["numeric", "analytic"],
                     help="Jacobian by numeric differentiation (default, the reference's default) or analytic")
+    ap.add_argument("--ilu", default="natural", choices=["natural", "redblack"],
+                    help="ILU(0) ordering of the single-problem workloads: natural (the reference's "
+                         "SeqILU, default) or red-black (two parallel passes per sweep, more iterations)")
     ap.add_argument("--problems", type=int, default=256, help="ensemble size")
     ap.add_argument("--requests", type=int, default=48, help="served-stream length")
     ap.add_argument("--ticks-per-step", type=int, default=25, help="ensemble: engine ticks per timed step")
@@ -67,6 +70,7 @@ def dist_info():
 
 WORKLOAD = "2p"
 DIFF = "numeric"
+ILU = "natural"
 
 
 def reduce_over_ranks(seconds, sums, device):
@@ -97,7 +101,8 @@ def workload_name(cells, precision):
                 f"one Newton step, ILU0-BiCGSTAB reduction 1e-12, {precision.upper()} linear system")
     return (f"2p water-DNAPL cc-TPFA {'x'.join(map(str, cells))} cells, implicit Euler dt=250 s, "
             f"Newton shift 1e-8, ILU0-BiCGSTAB reduction 1e-6, {precision.upper()} linear system"
-            + (", analytic Jacobian" if DIFF == "analytic" else ""))
+            + (", analytic Jacobian" if DIFF == "analytic" else "")
+            + (", red-black ordered ILU(0)" if ILU == "redblack" else ""))
 
 
 def step_params():
@@ -105,8 +110,9 @@ def step_params():
     if WORKLOAD == "1p":
         # LinearPDESolver semantics: one assembly, one solve, one update
         return newton_params(min_steps=1, max_steps=1, max_relative_shift=1e300, linear_reduction=1e-12,
-                             max_time_step_divisions=0)
-    return newton_params()
+                             max_time_step_divisions=0, linear_max_iter=1000 if ILU == "redblack" else 250)
+    # the red-black preconditioner needs about twice the BiCGSTAB iterations: a higher cap
+    return newton_params(linear_max_iter=1000) if ILU == "redblack" else newton_params()
 
 
 class ClockSampler:
@@ -508,10 +514,11 @@ def run_serve(args):
 
 
 def main():
-    global WORKLOAD, DIFF
+    global WORKLOAD, DIFF, ILU
     args = parse()
     WORKLOAD = args.workload
     DIFF = args.diff
+    ILU = args.ilu
     if args.workload in ("ensemble", "serve") and args.impl == "gb300":
         if args.precision == "fp64" and "--precision" not in sys.argv:
             args.precision = "mixed"
@@ -536,6 +543,8 @@ def main():
     desc, u0 = workload(cells, seed=2 + rank)
     desc.analytic = args.diff == "analytic"
     ctx = dumux_gb300.Context(desc, device=local, precision=args.precision)
+    if args.ilu == "redblack":
+        ctx.set_ilu_kernel("redblack")
     params = step_params()
     stationary = args.workload == "1p"
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=local)

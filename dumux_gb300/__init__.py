@@ -248,8 +248,11 @@ class Context:
         return self._L.dxg_suggest_time_step(self._h, float(old_dt), C.byref(p))
 
     def set_ilu_kernel(self, kind):
-        """'auto' / 'wavefront' (one cluster launch per sweep) or 'levels' (one launch per level)."""
-        self._check(self._L.dxg_set_ilu_kernel(self._h, {"auto": 0, "wavefront": 1, "levels": 2}[kind]))
+        """'auto' / 'wavefront' (one cluster launch per sweep) or 'levels' (one launch per
+        level): the natural-order ILU(0) of the reference; 'redblack': ILU(0) of the red-black
+        reordered matrix (a different preconditioner, two parallel passes per sweep)."""
+        self._check(self._L.dxg_set_ilu_kernel(self._h, {"auto": 0, "wavefront": 1, "levels": 2,
+                                                          "redblack": 3}[kind]))
 
     def stream_handle(self):
         """cudaStream_t of this context (as an int) for event timing by the caller."""

@@ -599,7 +599,27 @@ WaveArgs<T> waveArgs(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* rhs, T* v)
     return w;
 }
 
-bool useWave(const dxg_ctx* c) { return c->iluKernel != DXG_ILU_LEVELS && c->wavePlan.ok; }
+bool useWave(const dxg_ctx* c)
+{
+    return c->iluKernel != DXG_ILU_LEVELS && c->iluKernel != DXG_ILU_REDBLACK && c->wavePlan.ok;
+}
+
+template <class T>
+RbArgs<T> rbArgs(dxg_ctx* c, const T* A, T* Dinv)
+{
+    RbArgs<T> r{};
+    r.A = A;
+    r.Dinv = Dinv;
+    r.nbmask = c->nbmask.get();
+    r.N = c->N;
+    for (int s = 0; s < 7; ++s) r.off[s] = c->off[s];
+    r.nx = (int)c->pcHost.nx;
+    r.ny = (int)c->pcHost.ny;
+    r.nz = (int)c->pcHost.nz;
+    r.singular = c->singular.get();
+    r.ks = c->ks.get();
+    return r;
+}
 
 // Launch shape of the wavefront sweeps, chosen once per context by timing: every plan
 // that fits (cluster sizes 16..1) applies the preconditioner built by the first
@@ -654,6 +674,7 @@ template <class T>
 int64_t iluApply(dxg_ctx* c, const IluArgs<T, T>& ia, const T* A, T* L, T* Dinv, const T* d, T* v)
 {
     TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(T) / 8.0);
+    if (c->iluKernel == DXG_ILU_REDBLACK) return launchRbApply<T>(rbArgs<T>(c, A, Dinv), c->b, c->dim, d, v, c->stream);
     if (useWave(c)) {
         launchWaveApply<T>(c->wavePlan, waveArgs<T>(c, A, L, Dinv, d, v), waveArgs<T>(c, A, L, Dinv, d, v), c->b,
                            c->stream);
@@ -698,7 +719,9 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
             c->launches += 1;
         }
         DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
-        if (useWave(c)) {
+        if (c->iluKernel == DXG_ILU_REDBLACK) {
+            c->launches += launchRbFactor<PT>(rbArgs<PT>(c, PA, PD), c->b, c->dim, st);
+        } else if (useWave(c)) {
             // the factor kernel must not skip: give it no Krylov state
             WaveArgs<PT> w = waveArgs<PT>(c, PA, PL, PD, nullptr, nullptr);
             w.ks = nullptr;
@@ -1273,7 +1296,7 @@ int dxg_advance_time_step(dxg_ctx* c)
 
 int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
 {
-    if (!c || kind < DXG_ILU_AUTO || kind > DXG_ILU_LEVELS) return DXG_ERR_ARG;
+    if (!c || kind < DXG_ILU_AUTO || kind > DXG_ILU_REDBLACK) return DXG_ERR_ARG;
     if (kind == DXG_ILU_WAVEFRONT && c->uploaded && !c->wavePlan.ok) {
         c->err = "no wavefront plan fits this grid";
         return DXG_ERR_ARG;
@@ -1288,6 +1311,7 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
     if (!c || !buf || len <= 0) return DXG_ERR_ARG;
     std::string out;
     if (!c->uploaded) out = "no problem uploaded";
+    else if (c->iluKernel == DXG_ILU_REDBLACK) out = "ILU(0): red-black ordering, two parallel passes per sweep";
     else if (!useWave(c)) out = "ILU(0): level-scheduled kernels";
     else {
         const WavePlan& p = c->wavePlan;

@@ -353,6 +353,134 @@ __device__ __forceinline__ void blkFmaSub(const MT* __restrict__ blk, const VT* 
         for (int c = 0; c < B; ++c) acc[r] = fma(-(VT)blk[r * B + c], x[c], acc[r]);
 }
 
+// ---------------------------------------------------------------- red-black ILU(0)
+// Cell k of colour c (0 red: x+y+z even) in row-major order of the half rows; -1 past the end.
+__device__ __forceinline__ int64_t rbCell(int64_t k, int c, int nx, int ny, int64_t rows)
+{
+    const int h = (nx + 1) / 2;
+    const int64_t row = k / h;
+    if (row >= rows) return -1;
+    const int j = (int)(k - row * h);
+    const int y = (int)(row % ny), z = (int)(row / ny);
+    const int x = 2 * j + ((c + y + z) & 1);
+    return x < nx ? row * nx + x : -1;
+}
+
+// red cells: D_r^-1 = A_rr^-1
+template <int B, int DIM, class T>
+__global__ void rbFactorRed(RbArgs<T> a)
+{
+    constexpr int BB = B * B;
+    const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rbCell(k, 0, a.nx, a.ny, rows);
+        if (i < 0) continue;
+        T D[BB], inv[BB];
+        ldgBlock<B>(a.A + ((int64_t)DIM * a.N + i) * BB, D);
+        if (!blkInvert<B>(D, inv)) *a.singular = 1;
+#pragma unroll
+        for (int e = 0; e < BB; ++e) a.Dinv[i * BB + e] = inv[e];
+    }
+}
+
+// black cells: D_b^-1 = (A_bb - sum_r A_br D_r^-1 A_rb)^-1, neighbours in slot order
+template <int B, int DIM, class T>
+__global__ void rbFactorBlack(RbArgs<T> a)
+{
+    constexpr int BB = B * B, S = 2 * DIM + 1;
+    const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rbCell(k, 1, a.nx, a.ny, rows);
+        if (i < 0) continue;
+        const unsigned m = a.nbmask[i];
+        T D[BB];
+        ldgBlock<B>(a.A + ((int64_t)DIM * a.N + i) * BB, D);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (s == DIM || !slotValid(m, DIM, s)) continue;
+            const int64_t j = i + a.off[s];
+            T Aij[BB], Dj[BB], Aji[BB], Lij[BB], P[BB];
+            ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, Aij);
+            ldgBlock<B>(a.Dinv + j * BB, Dj);
+            ldgBlock<B>(a.A + ((int64_t)(2 * DIM - s) * a.N + j) * BB, Aji);
+            blkMul<B>(Aij, Dj, Lij);
+            blkMul<B>(Lij, Aji, P);
+#pragma unroll
+            for (int e = 0; e < BB; ++e) D[e] -= P[e];
+        }
+        T inv[BB];
+        if (!blkInvert<B>(D, inv)) *a.singular = 1;
+#pragma unroll
+        for (int e = 0; e < BB; ++e) a.Dinv[i * BB + e] = inv[e];
+    }
+}
+
+// black pass: v_b = D_b^-1 (d_b - sum_r A_br (D_r^-1 d_r))
+template <int B, int DIM, class T>
+__global__ void rbApplyBlack(RbArgs<T> a, const T* __restrict__ d, T* __restrict__ v)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    constexpr int BB = B * B, S = 2 * DIM + 1;
+    const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rbCell(k, 1, a.nx, a.ny, rows);
+        if (i < 0) continue;
+        const unsigned m = __ldg(a.nbmask + i);
+        T acc[B];
+        ldgVec<B>(d + i * B, acc);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (s == DIM || !slotValid(m, DIM, s)) continue;
+            const int64_t j = i + a.off[s];
+            T Aij[BB], Dj[BB], dj[B], w[B];
+            ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, Aij);
+            ldgBlock<B>(a.Dinv + j * BB, Dj);
+            ldgVec<B>(d + j * B, dj);
+#pragma unroll
+            for (int e = 0; e < B; ++e) w[e] = 0;
+            blkMv<B>(Dj, dj, w);
+            blkFmaSub<B>(Aij, w, acc);
+        }
+        T Di[BB], out[B];
+        ldgBlock<B>(a.Dinv + i * BB, Di);
+#pragma unroll
+        for (int e = 0; e < B; ++e) out[e] = 0;
+        blkMv<B>(Di, acc, out);
+        storeVec<B>(v, i, out);
+    }
+}
+
+// red pass: v_r = D_r^-1 (d_r - sum_b A_rb v_b)
+template <int B, int DIM, class T>
+__global__ void rbApplyRed(RbArgs<T> a, const T* __restrict__ d, T* v)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    constexpr int BB = B * B, S = 2 * DIM + 1;
+    const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rbCell(k, 0, a.nx, a.ny, rows);
+        if (i < 0) continue;
+        const unsigned m = __ldg(a.nbmask + i);
+        T acc[B];
+        ldgVec<B>(d + i * B, acc);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (s == DIM || !slotValid(m, DIM, s)) continue;
+            const int64_t j = i + a.off[s];
+            T Aij[BB], vj[B];
+            ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, Aij);
+            loadVec<B>(v, j, vj);   // written by the black pass (previous launch)
+            blkFmaSub<B>(Aij, vj, acc);
+        }
+        T Di[BB], out[B];
+        ldgBlock<B>(a.Dinv + i * BB, Di);
+#pragma unroll
+        for (int e = 0; e < B; ++e) out[e] = 0;
+        blkMv<B>(Di, acc, out);
+        storeVec<B>(v, i, out);
+    }
+}
+
 // forward sweep of one level: z_i = d_i - L_ix z_x - L_iy z_y - L_iz z_z
 template <int B, int DIM, class MT, class VT>
 __global__ void iluForwardLevel(IluArgs<MT, VT> a, const VT* __restrict__ d, VT* v, int begin, int count)
@@ -745,6 +873,43 @@ int64_t launchIluApply(const IluArgs<MT, VT>& a, const LevelSchedule& ls, int b,
     return n;
 }
 
+static unsigned rbBlocks(const int64_t half)
+{
+    int64_t g = (half + 255) / 256;
+    if (g > 4096) g = 4096;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <class T>
+int64_t launchRbFactor(const RbArgs<T>& a, int b, int dim, cudaStream_t st)
+{
+    const unsigned g = rbBlocks((int64_t)a.ny * a.nz * ((a.nx + 1) / 2));
+    if (b == 1) {
+        if (dim == 2) { rbFactorRed<1, 2, T><<<g, 256, 0, st>>>(a); rbFactorBlack<1, 2, T><<<g, 256, 0, st>>>(a); }
+        else { rbFactorRed<1, 3, T><<<g, 256, 0, st>>>(a); rbFactorBlack<1, 3, T><<<g, 256, 0, st>>>(a); }
+    } else {
+        if (dim == 2) { rbFactorRed<2, 2, T><<<g, 256, 0, st>>>(a); rbFactorBlack<2, 2, T><<<g, 256, 0, st>>>(a); }
+        else { rbFactorRed<2, 3, T><<<g, 256, 0, st>>>(a); rbFactorBlack<2, 3, T><<<g, 256, 0, st>>>(a); }
+    }
+    DXG_CUDA(cudaGetLastError());
+    return 2;
+}
+
+template <class T>
+int64_t launchRbApply(const RbArgs<T>& a, int b, int dim, const T* d, T* v, cudaStream_t st)
+{
+    const unsigned g = rbBlocks((int64_t)a.ny * a.nz * ((a.nx + 1) / 2));
+    if (b == 1) {
+        if (dim == 2) { rbApplyBlack<1, 2, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<1, 2, T><<<g, 256, 0, st>>>(a, d, v); }
+        else { rbApplyBlack<1, 3, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<1, 3, T><<<g, 256, 0, st>>>(a, d, v); }
+    } else {
+        if (dim == 2) { rbApplyBlack<2, 2, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<2, 2, T><<<g, 256, 0, st>>>(a, d, v); }
+        else { rbApplyBlack<2, 3, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<2, 3, T><<<g, 256, 0, st>>>(a, d, v); }
+    }
+    DXG_CUDA(cudaGetLastError());
+    return 2;
+}
+
 template <class VT>
 void launchBicgInit(const BicgArgs<VT>& a, const double* rhs, cudaStream_t st)
 {
@@ -880,6 +1045,10 @@ template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, const Bloc
 template void launchBicgUpdatePBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
 template void launchBicgAxpyNormBatch<double>(const BicgArgs<double>*, const BlockMap&, int, cudaStream_t);
 template void launchBicgAxpyNormBatch<float>(const BicgArgs<float>*, const BlockMap&, int, cudaStream_t);
+template int64_t launchRbFactor<double>(const RbArgs<double>&, int, int, cudaStream_t);
+template int64_t launchRbFactor<float>(const RbArgs<float>&, int, int, cudaStream_t);
+template int64_t launchRbApply<double>(const RbArgs<double>&, int, int, const double*, double*, cudaStream_t);
+template int64_t launchRbApply<float>(const RbArgs<float>&, int, int, const float*, float*, cudaStream_t);
 template int64_t launchIluFactor<double>(const IluArgs<double, double>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluFactor<float>(const IluArgs<float, float>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluApply<double, double>(const IluArgs<double, double>&, const LevelSchedule&, int, int,

@@ -36,6 +36,23 @@ struct IluArgs {
     const KrylovState* ks;    // apply kernels skip when the solve has stopped
 };
 
+// Red-black ordered block ILU(0): cells coloured by the parity of x+y+z (red even).
+// With no red-red or black-black couplings on the TPFA stencil, ILU(0) in this order
+// keeps D_r = A_rr and D_b = A_bb - sum_r A_br D_r^-1 A_rb, and a sweep pair is two
+// fully parallel passes: black v_b = D_b^-1 (d_b - sum_r A_br D_r^-1 d_r), then red
+// v_r = D_r^-1 (d_r - sum_b A_rb v_b).
+template <class T>
+struct RbArgs {
+    const T* A;
+    T* Dinv;
+    const uint8_t* nbmask;
+    int64_t N;
+    int64_t off[7];
+    int nx, ny, nz;
+    int* singular;
+    const KrylovState* ks;    // apply passes skip when the solve has stopped
+};
+
 template <class VT>
 struct BicgArgs {
     VT *x, *r, *rt, *p, *v, *t, *y;
@@ -118,6 +135,10 @@ void launchNewtonUpdate(const double* uLast, const double* delta, double* u, dou
 void launchNorm2(const double* x, int64_t M, const ReduceScratch& sc, double* out, cudaStream_t st);
 void launchPartialColors(const double* uLast, const double* u, double* dist, uint8_t* color, int64_t N, int b,
                          double threshold, cudaStream_t st);
+template <class T>
+int64_t launchRbFactor(const RbArgs<T>& a, int b, int dim, cudaStream_t st);
+template <class T>
+int64_t launchRbApply(const RbArgs<T>& a, int b, int dim, const T* d, T* v, cudaStream_t st);
 void launchToFloat(const ToFloatArgs& a, cudaStream_t st);
 void launchToDouble(const ToDoubleArgs& a, cudaStream_t st);
 void launchAccum(const AccumArgs& a, cudaStream_t st);

@@ -237,11 +237,16 @@ double dxg_suggest_time_step(const dxg_ctx* ctx, double old_dt, const dxg_newton
 int dxg_advance_time_step(dxg_ctx* ctx);
 
 /* ---- tuning --------------------------------------------------------------------------- */
-/* Kernels of the ILU(0) factorisation and sweeps (same factors, same sweeps):
- * DXG_ILU_AUTO / DXG_ILU_WAVEFRONT: one thread-block-cluster wavefront launch per
- * sweep; DXG_ILU_LEVELS: one launch per wavefront level.  No counterpart in the
- * reference (dune-istl's SeqILU is sequential). */
-enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2 };
+/* Kernels of the ILU(0) factorisation and sweeps.  DXG_ILU_AUTO / DXG_ILU_WAVEFRONT: one
+ * thread-block-cluster wavefront launch per sweep; DXG_ILU_LEVELS: one launch per
+ * wavefront level.  Both compute SeqILU's natural-order ILU(0) (the drop-in setting).
+ * DXG_ILU_REDBLACK: ILU(0) of the red-black reordered matrix (cells coloured by the parity
+ * of x+y+z) -- a different preconditioner, not the reference's: BiCGSTAB needs more
+ * iterations (about 1.6-2.2x on the 2p problems), but a sweep pair is two fully
+ * parallel passes instead of nx+ny+nz-2 dependent levels; the Newton solution is the
+ * same to the linear and Newton tolerances.  No counterpart in the reference (dune-istl's
+ * SeqILU is sequential, natural order). */
+enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2, DXG_ILU_REDBLACK = 3 };
 int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
 /* The ILU(0) kernels in use, as text: the wavefront launch shape (cluster size, threads,
  * prefetch depth) and, once the first factorisation has chosen it by timing, the time per
