@@ -527,6 +527,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->wavePlan = makeWavePlan(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b, c->precision == DXG_PRECISION_FP64);
     c->waveTuned = false;
     c->waveTuneCount = 0;
+    c->dropGraphs();   // the captured chunks hold the old buffers' addresses
     DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
     DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
     DXG_CUDA(cudaMemsetAsync(c->ks.get(), 0, sizeof(KrylovState), st));
@@ -760,30 +761,67 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     sv.ks = c->ks.get();
     sv.scratch = c->scratch();
     if (refactor && useWave(c) && !c->waveTuned) tuneWavePlan<PT>(c, PA, PL, PD, pIn, yOut);
-    auto precondition = [&](const PT* in) { c->launches += iluApply<PT>(c, ia, PA, PL, PD, in, yOut); };
-    const int chunk = 4;
+    // one BiCGSTAB iteration; returns the number of kernels it launched
+    auto iteration = [&]() -> int64_t {
+        int64_t n = 0;
+        // the rho step ran in the kernel that closed the previous iteration
+        launchBicgUpdateP<double>(ba, st);
+        n += 1 + iluApply<PT>(c, ia, PA, PL, PD, pIn, yOut);
+        sv.x = yOut; sv.y = v; sv.w = rt;
+        {
+            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
+            launchSpmv<PT, double, PT>(sv, c->b, c->dim, 1, st);
+        }
+        launchBicgAxpyNorm<double>(ba, 0, st);
+        n += 2 + iluApply<PT>(c, ia, PA, PL, PD, rIn, yOut);
+        sv.x = yOut; sv.y = t; sv.w = r;
+        {
+            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
+            launchSpmv<PT, double, PT>(sv, c->b, c->dim, 2, st);
+        }
+        launchBicgAxpyNorm<double>(ba, 1, st);
+        return n + 2;
+    };
+    // Chunks of iterations between host checks of the Krylov state: replayed from a CUDA
+    // graph (captured once per context, precision and preconditioner shape; every
+    // argument lives at a fixed device address), or launched one by one while per-kernel
+    // timing is on.  Kernels of iterations past the end of the solve return at once.
+    const bool graphs = !c->timing;
+    const int chunk = graphs ? 8 : 4;
+    dxg_ctx::ChunkGraph& G = c->chunkGraph[mixed ? 1 : 0];
+    if (graphs) {
+        const int key[4] = {c->iluKernel, useWave(c) ? c->wavePlan.ctas : 0, useWave(c) ? c->wavePlan.threads : 0,
+                            chunk};
+        if (G.exec && !std::equal(key, key + 4, G.key)) {
+            cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
+        }
+        if (!G.exec) {
+            cudaGraph_t graph = nullptr;
+            DXG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            int64_t n = 0;
+            try {
+                for (int k = 0; k < chunk; ++k) n += iteration();
+            } catch (...) {
+                cudaStreamEndCapture(st, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            DXG_CUDA(cudaStreamEndCapture(st, &graph));
+            const cudaError_t e = cudaGraphInstantiate(&G.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            DXG_CUDA(e);
+            std::copy(key, key + 4, G.key);
+            G.launches = n;
+        }
+    }
     int done = 0;
     while (true) {
-        for (int k = 0; k < chunk; ++k) {
-            // the rho step ran in the kernel that closed the previous iteration
-            launchBicgUpdateP<double>(ba, st);
-            c->launches += 1;
-            precondition(pIn);
-            sv.x = yOut; sv.y = v; sv.w = rt;
-            {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
-                launchSpmv<PT, double, PT>(sv, c->b, c->dim, 1, st);
-            }
-            launchBicgAxpyNorm<double>(ba, 0, st);
-            c->launches += 2;
-            precondition(rIn);
-            sv.x = yOut; sv.y = t; sv.w = r;
-            {
-                TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
-                launchSpmv<PT, double, PT>(sv, c->b, c->dim, 2, st);
-            }
-            launchBicgAxpyNorm<double>(ba, 1, st);
-            c->launches += 2;
+        if (graphs) {
+            DXG_CUDA(cudaGraphLaunch(G.exec, st));
+            c->launches += G.launches;
+        } else {
+            for (int k = 0; k < chunk; ++k) c->launches += iteration();
         }
         done += chunk;
         DXG_CUDA(cudaMemcpyAsync(c->ksHost, c->ks.get(), sizeof(KrylovState), cudaMemcpyDeviceToHost, st));
@@ -1016,6 +1054,7 @@ int dxg_ctx_destroy(dxg_ctx* c)
         cudaEventDestroy(t.stop);
     }
     for (auto e : c->eventPool) cudaEventDestroy(e);
+    c->dropGraphs();
     if (c->ksHost) cudaFreeHost(c->ksHost);
     if (c->scalHost) cudaFreeHost(c->scalHost);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -58,6 +58,21 @@ struct dxg_ctx {
 
     int lastNewtonSteps = 0;
 
+    // captured chunk of BiCGSTAB iterations per preconditioner precision ([0] FP64, [1] FP32)
+    struct ChunkGraph {
+        cudaGraphExec_t exec = nullptr;
+        int key[4] = {-1, -1, -1, -1};
+        int64_t launches = 0;
+    };
+    ChunkGraph chunkGraph[2];
+    void dropGraphs()
+    {
+        for (auto& g : chunkGraph) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    }
+
     // partial reassembly (active during a Newton solve that asks for it)
     bool partialActive = false;
     dxg::DevBuf<double> partialDist;
