@@ -326,7 +326,7 @@ def run_ensemble(args):
     import dumux_gb300
     from dumux_gb300 import problems
     from dumux_gb300.abi import newton_params
-    params = newton_params()
+    params = newton_params(linear_max_iter=1000) if args.ilu == "redblack" else newton_params()
     dt = args.dt
     T = args.ticks_per_step
     t_end = 1e12                   # problems keep stepping through the whole run
@@ -343,7 +343,7 @@ def run_ensemble(args):
         for _ in range(n):
             b.iterate()
 
-    batch = dumux_gb300.Batch(device=local, precision=args.precision)
+    batch = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu)
     ids = [batch.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
     cells_of = {pid: d.num_cells for pid, (d, _, _) in zip(ids, probs)}
     ticks(batch, args.warmup * T)            # includes the sweep autotuning
@@ -389,7 +389,7 @@ def run_ensemble(args):
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b2 = dumux_gb300.Batch(device=local, precision=args.precision)
+    b2 = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu)
     ids2 = [b2.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
     d2h = 0
     for _ in range(args.steps):
@@ -458,12 +458,12 @@ def run_serve(args):
     from dumux_gb300 import problems
     from dumux_gb300.abi import newton_params
     from dumux_gb300.serve import Server
-    params = newton_params()
+    params = newton_params(linear_max_iter=1000) if args.ilu == "redblack" else newton_params()
     reqs = problems.served_requests(args.requests, rate=200.0, seed=5 + 100003 * rank)
     built = {r["index"]: problems.make_request_problem(r) for r in reqs}
     free, _ = torch.cuda.mem_get_info(local)
     budget = int(0.8 * free)
-    server = Server(device=local, precision=args.precision, memory_budget=budget, params=params)
+    server = Server(device=local, precision=args.precision, memory_budget=budget, params=params, ilu=args.ilu)
     # warm-up: small requests of both kinds (kernel loading, sweep autotuning)
     warm = problems.served_requests(max(3, args.warmup), rate=1e6, seed=99, n_max=2e4)
     server.serve(warm, problems.make_request_problem)

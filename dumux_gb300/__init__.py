@@ -16,8 +16,8 @@ import os
 
 import numpy as np
 
-from .abi import (DXG_BATCH_OPT_AUTOTUNE, DXG_BATCH_OPT_GRAPHS, DXG_ERR_BUDGET, DXG_PRECISION_FP64,
-                  DXG_PRECISION_MIXED, STATUS_NAMES, BatchProblemInfoC, LinearResultC, NewtonParamsC, NewtonReportC,
+from .abi import (DXG_BATCH_OPT_AUTOTUNE, DXG_BATCH_OPT_GRAPHS, DXG_BATCH_OPT_ILU_REDBLACK, DXG_ERR_BUDGET,
+                  DXG_PRECISION_FP64, DXG_PRECISION_MIXED, STATUS_NAMES, BatchProblemInfoC, LinearResultC, NewtonParamsC, NewtonReportC,
                   ProblemDesc, ProblemDescC, newton_params)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -389,7 +389,7 @@ class Batch:
     depend on what else is in the batch.
     """
 
-    def __init__(self, device=0, precision="mixed", graphs=True, autotune=True, memory_budget=0):
+    def __init__(self, device=0, precision="mixed", graphs=True, autotune=True, memory_budget=0, ilu="natural"):
         L = lib()
         h = C.c_void_p()
         prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
@@ -402,6 +402,8 @@ class Batch:
         self._sizes = {}
         self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_GRAPHS, int(bool(graphs))))
         self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_AUTOTUNE, int(bool(autotune))))
+        self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_ILU_REDBLACK,
+                                           {"natural": 0, "redblack": 1}[ilu]))
         self._check(L.dxg_batch_set_memory_budget(h, int(memory_budget)))
 
     def _check(self, st):

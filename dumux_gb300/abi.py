@@ -17,6 +17,7 @@ STATUS_NAMES = {
 DXG_ERR_BUDGET = 12
 DXG_BATCH_OPT_GRAPHS = 0
 DXG_BATCH_OPT_AUTOTUNE = 1
+DXG_BATCH_OPT_ILU_REDBLACK = 2
 DXG_PRECISION_FP64 = 0
 DXG_PRECISION_MIXED = 1
 MAX_NEWTON_RECORD = 64

@@ -184,6 +184,7 @@ struct dxg_batch {
     cudaEvent_t joinEv[3] = {nullptr, nullptr, nullptr};
     std::string err;
     bool graphs = true, autotune = true;
+    bool redBlack = false;            // red-black ordered ILU(0) instead of the natural order
     int64_t budget = 0, bytesInUse = 0;
     int64_t nextId = 1;
     int64_t launches = 0;
@@ -431,6 +432,23 @@ struct Pre<float> {
     static float* yOut(dxg_ctx* c) { return c->fy.get(); }
 };
 
+template <class T>
+RbArgs<T> rbArgsOf(dxg_ctx* c, const KrylovState* ks)
+{
+    RbArgs<T> r{};
+    r.A = Pre<T>::A(c);
+    r.Dinv = Pre<T>::Dinv(c);
+    r.nbmask = c->nbmask.get();
+    r.N = c->N;
+    for (int s = 0; s < 7; ++s) r.off[s] = c->off[s];
+    r.nx = (int)c->pcHost.nx;
+    r.ny = (int)c->pcHost.ny;
+    r.nz = (int)c->pcHost.nz;
+    r.singular = c->singular.get();
+    r.ks = ks;
+    return r;
+}
+
 BicgArgs<double> krylovArgs(dxg_ctx* c, bool mixed)
 {
     BicgArgs<double> a{c->kx.get(), c->kr.get(), c->krt.get(), c->kp.get(), c->kv.get(), c->kt.get(), c->ky.get(),
@@ -571,7 +589,10 @@ struct GroupState {
     const void* dSv1 = nullptr;      // SpmvArgs<PT, double, PT>
     const void* dSv2 = nullptr;
     const ToDoubleArgs* dTd = nullptr;
+    const void* dRbP = nullptr;      // red-black order: RbArgs<PT> applied to p / to r
+    const void* dRbR = nullptr;
     BlockMap mapM, mapN;     // vector kernels over N*b entries, SpMV over N cells
+    BlockMap mapH;           // red-black passes over each problem's colour slots
     int64_t maxN = 1, maxM = 1;
     double sweepBytes = 0, spmvBytes = 0;
     cudaGraphExec_t exec = nullptr;
@@ -704,7 +725,7 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.ids = ids;
     const int n = (int)S.size();
     const int dim = S[0]->c->dim, b = S[0]->c->b;
-    {
+    if (!B->redBlack) {
         int cls[kMaxSweepClasses] = {-1, -1, -1, -1};
         G.classOf.resize(n);
         for (int k = 0; k < n; ++k) {
@@ -737,6 +758,7 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     std::vector<BicgArgs<double>> ba(n);
     std::vector<SpmvArgs<PT, double, PT>> sv1(n), sv2(n);
     std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);   // member order; repacked per class below
+    std::vector<RbArgs<PT>> rbP(n), rbR(n);
     std::vector<ToDoubleArgs> td(n);
     for (int k = 0; k < n; ++k) {
         dxg_ctx* c = S[k]->c;
@@ -756,25 +778,36 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
         sv.w = ba[k].r;
         sv2[k] = sv;
         const PT* PA = Pre<PT>::A(c);
-        fwP[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::pIn(c), Pre<PT>::yOut(c),
-                                c->ks.get());
-        fwR[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c), Pre<PT>::yOut(c),
-                                c->ks.get());
-        bw[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr, Pre<PT>::yOut(c),
-                               c->ks.get());
+        if (!B->redBlack) {
+            fwP[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::pIn(c),
+                                    Pre<PT>::yOut(c), c->ks.get());
+            fwR[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c),
+                                    Pre<PT>::yOut(c), c->ks.get());
+            bw[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr, Pre<PT>::yOut(c),
+                                   c->ks.get());
+        }
+        RbArgs<PT> rb = rbArgsOf<PT>(c, c->ks.get());
+        rb.v = Pre<PT>::yOut(c);
+        rb.d = Pre<PT>::pIn(c);
+        rbP[k] = rb;
+        rb.d = Pre<PT>::rIn(c);
+        rbR[k] = rb;
         td[k] = {c->fy.get(), c->ky.get(), c->M};
     }
-    std::vector<int64_t> lenM, lenN;
+    std::vector<int64_t> lenM, lenN, lenH;
     for (Slot* s : S) {
         lenM.push_back(s->c->M);
         lenN.push_back(s->c->N);
+        lenH.push_back(rbSlots((int)s->c->pcHost.nx, (int)s->c->pcHost.ny, (int)s->c->pcHost.nz));
     }
-    std::vector<uint2> mM, mN;
+    std::vector<uint2> mM, mN, mH;
     buildBlockMap(lenM, false, mM);
     buildBlockMap(lenN, true, mN);
+    buildBlockMap(lenH, true, mH);
     std::vector<unsigned char> host;
     const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oT = pack(host, td),
-                 oM = pack(host, mM), oN = pack(host, mN);
+                 oM = pack(host, mM), oN = pack(host, mN), oH = pack(host, mH), oRP = pack(host, rbP),
+                 oRR = pack(host, rbR);
     std::vector<std::array<size_t, 3>> oc;
     for (const SweepClass& sc : G.classes) {
         std::vector<WaveArgs<PT>> cP, cR, cW;
@@ -799,6 +832,9 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.dTd = reinterpret_cast<const ToDoubleArgs*>(d + oT);
     G.mapM = {reinterpret_cast<const uint2*>(d + oM), (unsigned)mM.size()};
     G.mapN = {reinterpret_cast<const uint2*>(d + oN), (unsigned)mN.size()};
+    G.mapH = {reinterpret_cast<const uint2*>(d + oH), (unsigned)mH.size()};
+    G.dRbP = d + oRP;
+    G.dRbR = d + oRR;
     return G;
 }
 
@@ -811,6 +847,11 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
     const int nc = (int)G.classes.size();
     // forward + backward sweep of every class; classes after the first on forked streams
     auto precondition = [&](bool onP) {
+        if (B->redBlack) {
+            TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
+            launchRbApplyBatch<PT>(static_cast<const RbArgs<PT>*>(onP ? G.dRbP : G.dRbR), G.mapH, b, dim, st);
+            return;
+        }
         {
             TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
             if (nc > 1) DXG_CUDA(cudaEventRecord(B->forkEv, st));
@@ -849,7 +890,7 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 template <class PT>
 void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
 {
-    const int launchesPerIt = 5 + 4 * (int)G.classes.size();
+    const int launchesPerIt = 5 + (B->redBlack ? 4 : 4 * (int)G.classes.size());
     cudaStream_t st = B->stream;
     if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
         G.graphTried = true;
@@ -948,6 +989,7 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
     std::vector<ToFloatArgs> tf(n);
     std::vector<GatherArgs> fl(n);
     std::vector<WaveArgs<PT>> fa(n);
+    std::vector<RbArgs<PT>> rf(n);
     std::vector<BicgArgs<double>> bi(n);
     int64_t maxA = 1;
     for (int k = 0; k < n; ++k) {
@@ -960,8 +1002,10 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
         tf[k] = {c->A.get(), c->Af.get(), nA};
         fl[k] = {c->ks.get(), c->scal.get(), c->singular.get()};
         // the factor must not skip: no Krylov state
-        fa[k] = waveArgsOf<PT>(c, G.geo[idx[k]], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr, nullptr,
-                               nullptr);
+        if (B->redBlack) rf[k] = rbArgsOf<PT>(c, nullptr);
+        else
+            fa[k] = waveArgsOf<PT>(c, G.geo[idx[k]], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr,
+                                   nullptr, nullptr);
         BicgArgs<double> a = krylovArgs(c, mixed);
         a.rhs = c->r.get();
         a.reduction = s->p.linear_reduction;
@@ -980,6 +1024,15 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
     }
     clearFlagsKernel<<<(n + 127) / 128, 128, 0, st>>>(B->arena.put(fl, st), n);
     DXG_CUDA(cudaGetLastError());
+    if (B->redBlack) {
+        std::vector<int64_t> lenH;
+        for (Slot* s : A) lenH.push_back(rbSlots((int)s->c->pcHost.nx, (int)s->c->pcHost.ny, (int)s->c->pcHost.nz));
+        std::vector<uint2> mH;
+        buildBlockMap(lenH, true, mH);
+        launchRbFactorBatch<PT>(B->arena.put(rf, st), BlockMap{B->arena.put(mH, st), (unsigned)mH.size()}, b, dim,
+                                st);
+        B->launches += 2;
+    }
     for (size_t q = 0; q < G.classes.size(); ++q) {
         std::vector<WaveArgs<PT>> fq;
         for (int k = 0; k < n; ++k)
@@ -1208,6 +1261,13 @@ int dxg_batch_set_option(dxg_batch* b, int option, int value)
     else if (option == DXG_BATCH_OPT_AUTOTUNE) {
         b->autotune = value != 0;
         b->plans.clear();
+    } else if (option == DXG_BATCH_OPT_ILU_REDBLACK) {
+        if (!b->slots.empty()) {
+            b->err = "the ILU(0) ordering is chosen before problems are added";
+            return DXG_ERR_STATE;
+        }
+        b->redBlack = value != 0;
+        b->groups.clear();
     } else return DXG_ERR_ARG;
     return DXG_OK;
 }
@@ -1372,6 +1432,7 @@ int dxg_batch_describe(const dxg_batch* b, char* buf, int64_t len)
         const GroupState& G = *kv.second;
         out += "group num_eq=" + std::to_string(std::get<0>(k)) + " dim=" + std::to_string(std::get<1>(k)) +
                " problems=" + std::to_string(G.ids.size()) + ":";
+        if (b->redBlack) out += " [red-black ILU(0): two parallel passes per sweep]";
         for (const SweepClass& sc : G.classes)
             out += " [" + std::to_string(sc.members.size()) + " problems: cluster " + std::to_string(sc.plan.ctas) +
                    " x " + std::to_string(sc.plan.threads) + " threads, prefetch " + std::to_string(sc.plan.pf) +

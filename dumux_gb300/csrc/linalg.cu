@@ -368,11 +368,15 @@ __device__ __forceinline__ int64_t rbCell(int64_t k, int c, int nx, int ny, int6
 
 // red cells: D_r^-1 = A_rr^-1
 template <int B, int DIM, class T>
-__global__ void rbFactorRed(RbArgs<T> a)
+__global__ void rbFactorRed(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* map)
 {
+    unsigned lb;
+    const RbArgs<T> a = problemOf(a0, batch, map, lb);
     constexpr int BB = B * B;
     const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned nblk = cellBlocksFor(total);
+    if (lb >= nblk) return;
+    for (int64_t k = lb * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)nblk * blockDim.x) {
         const int64_t i = rbCell(k, 0, a.nx, a.ny, rows);
         if (i < 0) continue;
         T D[BB], inv[BB];
@@ -385,11 +389,15 @@ __global__ void rbFactorRed(RbArgs<T> a)
 
 // black cells: D_b^-1 = (A_bb - sum_r A_br D_r^-1 A_rb)^-1, neighbours in slot order
 template <int B, int DIM, class T>
-__global__ void rbFactorBlack(RbArgs<T> a)
+__global__ void rbFactorBlack(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* map)
 {
+    unsigned lb;
+    const RbArgs<T> a = problemOf(a0, batch, map, lb);
     constexpr int BB = B * B, S = 2 * DIM + 1;
     const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned nblk = cellBlocksFor(total);
+    if (lb >= nblk) return;
+    for (int64_t k = lb * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)nblk * blockDim.x) {
         const int64_t i = rbCell(k, 1, a.nx, a.ny, rows);
         if (i < 0) continue;
         const unsigned m = a.nbmask[i];
@@ -417,12 +425,18 @@ __global__ void rbFactorBlack(RbArgs<T> a)
 
 // black pass: v_b = D_b^-1 (d_b - sum_r A_br (D_r^-1 d_r))
 template <int B, int DIM, class T>
-__global__ void rbApplyBlack(RbArgs<T> a, const T* __restrict__ d, T* __restrict__ v)
+__global__ void rbApplyBlack(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* map)
 {
+    unsigned lb;
+    const RbArgs<T> a = problemOf(a0, batch, map, lb);
     if (a.ks && a.ks->status != KS_RUNNING) return;
+    const T* __restrict__ d = a.d;
+    T* __restrict__ v = a.v;
     constexpr int BB = B * B, S = 2 * DIM + 1;
     const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned nblk = cellBlocksFor(total);
+    if (lb >= nblk) return;
+    for (int64_t k = lb * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)nblk * blockDim.x) {
         const int64_t i = rbCell(k, 1, a.nx, a.ny, rows);
         if (i < 0) continue;
         const unsigned m = __ldg(a.nbmask + i);
@@ -452,12 +466,18 @@ __global__ void rbApplyBlack(RbArgs<T> a, const T* __restrict__ d, T* __restrict
 
 // red pass: v_r = D_r^-1 (d_r - sum_b A_rb v_b)
 template <int B, int DIM, class T>
-__global__ void rbApplyRed(RbArgs<T> a, const T* __restrict__ d, T* v)
+__global__ void rbApplyRed(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* map)
 {
+    unsigned lb;
+    const RbArgs<T> a = problemOf(a0, batch, map, lb);
     if (a.ks && a.ks->status != KS_RUNNING) return;
+    const T* __restrict__ d = a.d;
+    T* v = a.v;
     constexpr int BB = B * B, S = 2 * DIM + 1;
     const int64_t rows = (int64_t)a.ny * a.nz, total = rows * ((a.nx + 1) / 2);
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned nblk = cellBlocksFor(total);
+    if (lb >= nblk) return;
+    for (int64_t k = lb * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)nblk * blockDim.x) {
         const int64_t i = rbCell(k, 0, a.nx, a.ny, rows);
         if (i < 0) continue;
         const unsigned m = __ldg(a.nbmask + i);
@@ -873,41 +893,58 @@ int64_t launchIluApply(const IluArgs<MT, VT>& a, const LevelSchedule& ls, int b,
     return n;
 }
 
-static unsigned rbBlocks(const int64_t half)
+template <class T, int B, int DIM>
+static void rbFactorPasses(const RbArgs<T>& a, const RbArgs<T>* batch, const uint2* map, unsigned g, cudaStream_t st)
 {
-    int64_t g = (half + 255) / 256;
-    if (g > 4096) g = 4096;
-    return (unsigned)(g < 1 ? 1 : g);
+    rbFactorRed<B, DIM, T><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    rbFactorBlack<B, DIM, T><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+}
+template <class T, int B, int DIM>
+static void rbApplyPasses(const RbArgs<T>& a, const RbArgs<T>* batch, const uint2* map, unsigned g, cudaStream_t st)
+{
+    rbApplyBlack<B, DIM, T><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+    rbApplyRed<B, DIM, T><<<g, kReduceThreads, 0, st>>>(a, batch, map);
+}
+template <class T>
+static void rbDispatch(bool factor, const RbArgs<T>& a, const RbArgs<T>* batch, const uint2* map, unsigned g, int b,
+                       int dim, cudaStream_t st)
+{
+    if (factor) {
+        if (b == 1) dim == 2 ? rbFactorPasses<T, 1, 2>(a, batch, map, g, st) : rbFactorPasses<T, 1, 3>(a, batch, map, g, st);
+        else dim == 2 ? rbFactorPasses<T, 2, 2>(a, batch, map, g, st) : rbFactorPasses<T, 2, 3>(a, batch, map, g, st);
+    } else {
+        if (b == 1) dim == 2 ? rbApplyPasses<T, 1, 2>(a, batch, map, g, st) : rbApplyPasses<T, 1, 3>(a, batch, map, g, st);
+        else dim == 2 ? rbApplyPasses<T, 2, 2>(a, batch, map, g, st) : rbApplyPasses<T, 2, 3>(a, batch, map, g, st);
+    }
+    DXG_CUDA(cudaGetLastError());
 }
 
 template <class T>
 int64_t launchRbFactor(const RbArgs<T>& a, int b, int dim, cudaStream_t st)
 {
-    const unsigned g = rbBlocks((int64_t)a.ny * a.nz * ((a.nx + 1) / 2));
-    if (b == 1) {
-        if (dim == 2) { rbFactorRed<1, 2, T><<<g, 256, 0, st>>>(a); rbFactorBlack<1, 2, T><<<g, 256, 0, st>>>(a); }
-        else { rbFactorRed<1, 3, T><<<g, 256, 0, st>>>(a); rbFactorBlack<1, 3, T><<<g, 256, 0, st>>>(a); }
-    } else {
-        if (dim == 2) { rbFactorRed<2, 2, T><<<g, 256, 0, st>>>(a); rbFactorBlack<2, 2, T><<<g, 256, 0, st>>>(a); }
-        else { rbFactorRed<2, 3, T><<<g, 256, 0, st>>>(a); rbFactorBlack<2, 3, T><<<g, 256, 0, st>>>(a); }
-    }
-    DXG_CUDA(cudaGetLastError());
+    rbDispatch<T>(true, a, nullptr, nullptr, (unsigned)cellBlocksFor(rbSlots(a.nx, a.ny, a.nz)), b, dim, st);
     return 2;
 }
 
 template <class T>
 int64_t launchRbApply(const RbArgs<T>& a, int b, int dim, const T* d, T* v, cudaStream_t st)
 {
-    const unsigned g = rbBlocks((int64_t)a.ny * a.nz * ((a.nx + 1) / 2));
-    if (b == 1) {
-        if (dim == 2) { rbApplyBlack<1, 2, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<1, 2, T><<<g, 256, 0, st>>>(a, d, v); }
-        else { rbApplyBlack<1, 3, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<1, 3, T><<<g, 256, 0, st>>>(a, d, v); }
-    } else {
-        if (dim == 2) { rbApplyBlack<2, 2, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<2, 2, T><<<g, 256, 0, st>>>(a, d, v); }
-        else { rbApplyBlack<2, 3, T><<<g, 256, 0, st>>>(a, d, v); rbApplyRed<2, 3, T><<<g, 256, 0, st>>>(a, d, v); }
-    }
-    DXG_CUDA(cudaGetLastError());
+    RbArgs<T> aa = a;
+    aa.d = d;
+    aa.v = v;
+    rbDispatch<T>(false, aa, nullptr, nullptr, (unsigned)cellBlocksFor(rbSlots(a.nx, a.ny, a.nz)), b, dim, st);
     return 2;
+}
+
+template <class T>
+void launchRbFactorBatch(const RbArgs<T>* batch, const BlockMap& m, int b, int dim, cudaStream_t st)
+{
+    rbDispatch<T>(true, RbArgs<T>{}, batch, m.map, m.blocks, b, dim, st);
+}
+template <class T>
+void launchRbApplyBatch(const RbArgs<T>* batch, const BlockMap& m, int b, int dim, cudaStream_t st)
+{
+    rbDispatch<T>(false, RbArgs<T>{}, batch, m.map, m.blocks, b, dim, st);
 }
 
 template <class VT>
@@ -1049,6 +1086,10 @@ template int64_t launchRbFactor<double>(const RbArgs<double>&, int, int, cudaStr
 template int64_t launchRbFactor<float>(const RbArgs<float>&, int, int, cudaStream_t);
 template int64_t launchRbApply<double>(const RbArgs<double>&, int, int, const double*, double*, cudaStream_t);
 template int64_t launchRbApply<float>(const RbArgs<float>&, int, int, const float*, float*, cudaStream_t);
+template void launchRbFactorBatch<double>(const RbArgs<double>*, const BlockMap&, int, int, cudaStream_t);
+template void launchRbFactorBatch<float>(const RbArgs<float>*, const BlockMap&, int, int, cudaStream_t);
+template void launchRbApplyBatch<double>(const RbArgs<double>*, const BlockMap&, int, int, cudaStream_t);
+template void launchRbApplyBatch<float>(const RbArgs<float>*, const BlockMap&, int, int, cudaStream_t);
 template int64_t launchIluFactor<double>(const IluArgs<double, double>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluFactor<float>(const IluArgs<float, float>&, const LevelSchedule&, int, int, cudaStream_t);
 template int64_t launchIluApply<double, double>(const IluArgs<double, double>&, const LevelSchedule&, int, int,

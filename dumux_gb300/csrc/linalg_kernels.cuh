@@ -51,7 +51,11 @@ struct RbArgs {
     int nx, ny, nz;
     int* singular;
     const KrylovState* ks;    // apply passes skip when the solve has stopped
+    const T* d;               // apply: input
+    T* v;                     // apply: output
 };
+// cells of one colour slot range: rows * ceil(nx / 2) (the red-black kernels' index space)
+inline int64_t rbSlots(int nx, int ny, int nz) { return (int64_t)ny * nz * ((nx + 1) / 2); }
 
 template <class VT>
 struct BicgArgs {
@@ -168,6 +172,11 @@ void launchBicgUpdatePBatch(const BicgArgs<VT>* batch, const BlockMap& map, cuda
 template <class VT>
 void launchBicgAxpyNormBatch(const BicgArgs<VT>* batch, const BlockMap& map, int stage, cudaStream_t st);
 void launchNewtonUpdateBatch(const NewtonUpdArgs* batch, const BlockMap& map, cudaStream_t st);
+// red-black ILU(0) over several problems: block map over rbSlots of each problem (cells == true)
+template <class T>
+void launchRbFactorBatch(const RbArgs<T>* batch, const BlockMap& map, int b, int dim, cudaStream_t st);
+template <class T>
+void launchRbApplyBatch(const RbArgs<T>* batch, const BlockMap& map, int b, int dim, cudaStream_t st);
 void launchNorm2Batch(const NormArgs* batch, const BlockMap& map, cudaStream_t st);
 void launchToDoubleBatch(const ToDoubleArgs* batch, const BlockMap& map, cudaStream_t st);
 // grid-stride elementwise kernels, blockIdx.y = problem (maxN: the longest)

@@ -31,10 +31,12 @@ class Server:
     memory_budget: bytes of device memory all admitted problems may hold (0: no limit).
     """
 
-    def __init__(self, device=0, precision="mixed", memory_budget=0, params=None, graphs=True, autotune=True):
+    def __init__(self, device=0, precision="mixed", memory_budget=0, params=None, graphs=True, autotune=True,
+                 ilu="natural"):
         self.batch = Batch(device=device, precision=precision, graphs=graphs, autotune=autotune,
-                           memory_budget=memory_budget)
-        self.params = params if params is not None else newton_params(linear_max_iter=500)
+                           memory_budget=memory_budget, ilu=ilu)
+        default_iter = 1000 if ilu == "redblack" else 500
+        self.params = params if params is not None else newton_params(linear_max_iter=default_iter)
 
     def serve(self, requests, problem_of, clock=time.perf_counter):
         """Serves `requests` (dicts with 'arrival' seconds from the start, 'dt', 't_end')
