@@ -442,16 +442,26 @@ __global__ void rbApplyBlack(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* 
         const unsigned m = __ldg(a.nbmask + i);
         T acc[B];
         ldgVec<B>(d + i * B, acc);
+        // FP32: straight-line loads of every neighbour slot (the cell's own entries stand in
+        // for a missing neighbour, whose block enters as zero), so all gathers are in flight
+        // together; FP64 skips missing neighbours (its zero products would cost FP64 issue)
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-            if (s == DIM || !slotValid(m, DIM, s)) continue;
-            const int64_t j = i + a.off[s];
+            if (s == DIM) continue;
+            const bool valid = slotValid(m, DIM, s);
+            if (sizeof(T) == 8 && !valid) continue;
+            const int64_t j = i + (valid ? a.off[s] : 0);
             T Aij[BB], Dj[BB], dj[B], w[B];
             ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, Aij);
             ldgBlock<B>(a.Dinv + j * BB, Dj);
             ldgVec<B>(d + j * B, dj);
 #pragma unroll
-            for (int e = 0; e < B; ++e) w[e] = 0;
+            for (int e = 0; e < BB; ++e) Aij[e] = valid ? Aij[e] : (T)0;
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                dj[e] = valid ? dj[e] : (T)0;
+                w[e] = 0;
+            }
             blkMv<B>(Dj, dj, w);
             blkFmaSub<B>(Aij, w, acc);
         }
@@ -485,11 +495,18 @@ __global__ void rbApplyRed(RbArgs<T> a0, const RbArgs<T>* batch, const uint2* ma
         ldgVec<B>(d + i * B, acc);
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-            if (s == DIM || !slotValid(m, DIM, s)) continue;
-            const int64_t j = i + a.off[s];
+            if (s == DIM) continue;
+            const bool valid = slotValid(m, DIM, s);
+            if (sizeof(T) == 8 && !valid) continue;   // as in the black pass
+            const int64_t j = i + (valid ? a.off[s] : 0);
             T Aij[BB], vj[B];
             ldgBlock<B>(a.A + ((int64_t)s * a.N + i) * BB, Aij);
             loadVec<B>(v, j, vj);   // written by the black pass (previous launch)
+#pragma unroll
+            for (int e = 0; e < BB; ++e) Aij[e] = valid ? Aij[e] : (T)0;
+            // a missing neighbour reads this cell's own (not yet written) entry: zero it
+#pragma unroll
+            for (int e = 0; e < B; ++e) vj[e] = valid ? vj[e] : (T)0;
             blkFmaSub<B>(Aij, vj, acc);
         }
         T Di[BB], out[B];
