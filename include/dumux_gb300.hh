@@ -365,6 +365,10 @@ class GpuILUBiCGSTABSolver {
 public:
     void setResidualReduction(double r) { reduction_ = r; }
     void setMaxIter(int n) { maxIter_ = n; }
+    // DXG_ILU_AUTO (natural order, the reference's SeqILU; default) or DXG_ILU_REDBLACK
+    // (red-black ordered ILU(0): not the reference's preconditioner, faster per time step);
+    // takes effect at the assembler's next factorisation
+    void setIluKernel(GpuFVAssembler& A, int kind) { A.handle().check(dxg_set_ilu_kernel(A.context(), kind)); }
     // solve(A, x, b): A and b are the assembler's device system; x receives the update
     bool solve(const GpuFVAssembler& A, std::vector<double>& x, const std::vector<double>& /*b*/)
     {
