@@ -70,6 +70,7 @@ def lib():
         L.dxg_suggest_time_step.restype = C.c_double
         L.dxg_advance_time_step.argtypes = [vp]
         L.dxg_set_ilu_kernel.argtypes = [vp, C.c_int]
+        L.dxg_set_linear_solver.argtypes = [vp, C.c_int]
         L.dxg_stream_handle.argtypes = [vp]
         L.dxg_stream_handle.restype = C.c_void_p
         L.dxg_set_kernel_timing.argtypes = [vp, C.c_int]
@@ -253,6 +254,11 @@ class Context:
         reordered matrix (a different preconditioner, two parallel passes per sweep)."""
         self._check(self._L.dxg_set_ilu_kernel(self._h, {"auto": 0, "wavefront": 1, "levels": 2,
                                                           "redblack": 3}[kind]))
+
+    def set_linear_solver(self, kind):
+        """'ilu' (ILU(0)-BiCGSTAB, the default) or 'amg' (BiCGSTAB preconditioned by one
+        V-cycle of the aggregation AMG, the reference's AMGBiCGSTAB solver type)."""
+        self._check(self._L.dxg_set_linear_solver(self._h, {"ilu": 0, "amg": 1}[kind]))
 
     def stream_handle(self):
         """cudaStream_t of this context (as an int) for event timing by the caller."""

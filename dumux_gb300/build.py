@@ -26,6 +26,7 @@ UNITS = {
     "api.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],
+    "amg.cu": [],
 }
 
 

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <vector>
 
+#include "amg.cuh"
 #include "context.h"
 #include "materiallaw.cuh"
 
@@ -622,6 +623,58 @@ RbArgs<T> rbArgs(dxg_ctx* c, const T* A, T* Dinv)
     return r;
 }
 
+// Levels of the aggregation AMG in value type T: level 0 is the Jacobian itself (A, the
+// inverted pivots in Dinv, the preconditioner's input `in` and output `out`), the coarse
+// levels live in one device allocation, made on first use.
+template <class T>
+std::vector<AmgLevel<T>> amgLevels(dxg_ctx* c, const T* A, T* Dinv, const T* in, T* out)
+{
+    const int dim = c->dim, b = c->b, bb = c->bb, S = 2 * dim + 1;
+    const auto dims = amgLevelDims(dim, (int)c->pcHost.nx, (int)c->pcHost.ny, (int)c->pcHost.nz);
+    auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    size_t bytes = 2 * align((size_t)c->M * sizeof(T));
+    for (const auto& d : dims) {
+        const size_t n = (size_t)d[0] * d[1] * d[2];
+        bytes += align((size_t)S * n * bb * sizeof(T)) + align(n * bb * sizeof(T)) + 4 * align(n * b * sizeof(T));
+    }
+    const size_t nLast = dims.empty() ? (size_t)c->N : (size_t)dims.back()[0] * dims.back()[1] * dims.back()[2];
+    bytes += align(nLast * b * nLast * b * sizeof(T));   // dense inverse of the last level
+    if (c->amgMem.bytes() < bytes) c->amgMem.alloc(bytes);
+    unsigned char* p = c->amgMem.get();
+    auto take = [&](size_t n) {
+        T* q = reinterpret_cast<T*>(p);
+        p += align(n * sizeof(T));
+        return q;
+    };
+    std::vector<AmgLevel<T>> L(1 + dims.size());
+    L[0].nx = (int)c->pcHost.nx;
+    L[0].ny = (int)c->pcHost.ny;
+    L[0].nz = dim == 3 ? (int)c->pcHost.nz : 1;
+    L[0].N = c->N;
+    L[0].A = A;
+    L[0].Dinv = Dinv;
+    L[0].b = const_cast<T*>(in);
+    L[0].x = out;
+    L[0].tmp = take((size_t)c->M);
+    L[0].r = take((size_t)c->M);
+    for (size_t k = 0; k < dims.size(); ++k) {
+        AmgLevel<T>& l = L[k + 1];
+        l.nx = dims[k][0];
+        l.ny = dims[k][1];
+        l.nz = dims[k][2];
+        l.N = (int64_t)l.nx * l.ny * l.nz;
+        l.A = take((size_t)S * l.N * bb);
+        l.Dinv = take((size_t)l.N * bb);
+        l.b = take((size_t)l.N * b);
+        l.x = take((size_t)l.N * b);
+        l.tmp = take((size_t)l.N * b);
+        l.r = take((size_t)l.N * b);
+    }
+    for (AmgLevel<T>& l : L) l.sweeps = l.N <= kAmgSmallLevel ? kAmgSmallSweeps : 1;
+    L.back().Ainv = take(nLast * b * nLast * b);
+    return L;
+}
+
 // Launch shape of the wavefront sweeps, chosen once per context by timing: every plan
 // that fits (cluster sizes 16..1) applies the preconditioner built by the first
 // factorisation to `in` (a scratch read) into `out` (overwritten by the solve that
@@ -720,7 +773,14 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
             c->launches += 1;
         }
         DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
-        if (c->iluKernel == DXG_ILU_REDBLACK) {
+        if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB) {
+            // AMG setup: fine pivots, then each coarse operator (with its pivots) from the one above
+            std::vector<AmgLevel<PT>> L = amgLevels<PT>(c, PA, PD, nullptr, nullptr);
+            launchAmgDiagInv<PT>(L[0], c->dim, c->b, c->singular.get(), st);
+            for (size_t k = 1; k < L.size(); ++k) launchAmgCoarsen<PT>(L[k - 1], L[k], c->dim, c->b, c->singular.get(), st);
+            launchAmgCoarseInvert<PT>(L.back(), c->dim, c->b, c->singular.get(), st);
+            c->launches += (int64_t)L.size() + 1;
+        } else if (c->iluKernel == DXG_ILU_REDBLACK) {
             c->launches += launchRbFactor<PT>(rbArgs<PT>(c, PA, PD), c->b, c->dim, st);
         } else if (useWave(c)) {
             // the factor kernel must not skip: give it no Krylov state
@@ -760,20 +820,33 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
     sv.ks = c->ks.get();
     sv.scratch = c->scratch();
-    if (refactor && useWave(c) && !c->waveTuned) tuneWavePlan<PT>(c, PA, PL, PD, pIn, yOut);
+    const bool amg = c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB;
+    if (refactor && !amg && useWave(c) && !c->waveTuned) tuneWavePlan<PT>(c, PA, PL, PD, pIn, yOut);
+    std::vector<AmgLevel<PT>> amgP, amgR;
+    if (amg) {
+        amgP = amgLevels<PT>(c, PA, PD, pIn, yOut);
+        amgR = amgLevels<PT>(c, PA, PD, rIn, yOut);
+    }
+    auto precondition = [&](const PT* in) -> int64_t {
+        if (amg) {
+            TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(PT) / 8.0);
+            return launchAmgVcycle<PT>(in == pIn ? amgP : amgR, c->dim, c->b, c->ks.get(), st);
+        }
+        return iluApply<PT>(c, ia, PA, PL, PD, in, yOut);
+    };
     // one BiCGSTAB iteration; returns the number of kernels it launched
     auto iteration = [&]() -> int64_t {
         int64_t n = 0;
         // the rho step ran in the kernel that closed the previous iteration
         launchBicgUpdateP<double>(ba, st);
-        n += 1 + iluApply<PT>(c, ia, PA, PL, PD, pIn, yOut);
+        n += 1 + precondition(pIn);
         sv.x = yOut; sv.y = v; sv.w = rt;
         {
             TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
             launchSpmv<PT, double, PT>(sv, c->b, c->dim, 1, st);
         }
         launchBicgAxpyNorm<double>(ba, 0, st);
-        n += 2 + iluApply<PT>(c, ia, PA, PL, PD, rIn, yOut);
+        n += 2 + precondition(rIn);
         sv.x = yOut; sv.y = t; sv.w = r;
         {
             TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
@@ -790,8 +863,8 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     const int chunk = graphs ? 8 : 4;
     dxg_ctx::ChunkGraph& G = c->chunkGraph[mixed ? 1 : 0];
     if (graphs) {
-        const int key[4] = {c->iluKernel, useWave(c) ? c->wavePlan.ctas : 0, useWave(c) ? c->wavePlan.threads : 0,
-                            chunk};
+        const int key[4] = {c->iluKernel + 16 * c->linearSolver, useWave(c) ? c->wavePlan.ctas : 0,
+                            useWave(c) ? c->wavePlan.threads : 0, chunk};
         if (G.exec && !std::equal(key, key + 4, G.key)) {
             cudaGraphExecDestroy(G.exec);
             G.exec = nullptr;
@@ -1345,11 +1418,23 @@ int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
     return DXG_OK;
 }
 
+int dxg_set_linear_solver(dxg_ctx* c, int kind)
+{
+    if (!c || (kind != DXG_LINEAR_SOLVER_ILU_BICGSTAB && kind != DXG_LINEAR_SOLVER_AMG_BICGSTAB)) return DXG_ERR_ARG;
+    c->linearSolver = kind;
+    c->haveFactor = false;
+    return DXG_OK;
+}
+
 int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
 {
     if (!c || !buf || len <= 0) return DXG_ERR_ARG;
     std::string out;
     if (!c->uploaded) out = "no problem uploaded";
+    else if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB)
+        out = "AMG-BiCGSTAB: " + std::to_string(amgLevelDims(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
+                                                               (int)c->pcHost.nz).size() + 1) +
+              " levels of 2x2(x2) aggregation, damped block-Jacobi smoothing";
     else if (c->iluKernel == DXG_ILU_REDBLACK) out = "ILU(0): red-black ordering, two parallel passes per sweep";
     else if (!useWave(c)) out = "ILU(0): level-scheduled kernels";
     else {

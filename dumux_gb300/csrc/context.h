@@ -78,6 +78,10 @@ struct dxg_ctx {
     dxg::DevBuf<double> partialDist;
     dxg::DevBuf<uint8_t> partialColor;
 
+    // preconditioner of the BiCGSTAB solve: ILU(0) (default) or aggregation AMG
+    int linearSolver = DXG_LINEAR_SOLVER_ILU_BICGSTAB;
+    dxg::DevBuf<unsigned char> amgMem;   // fine-level scratch, then every coarse level (one allocation)
+
     // ILU(0) kernels: cluster wavefront (default) or level-scheduled launches
     int iluKernel = DXG_ILU_AUTO;
     dxg::WavePlan wavePlan;

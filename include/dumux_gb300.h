@@ -248,6 +248,16 @@ int dxg_advance_time_step(dxg_ctx* ctx);
  * SeqILU is sequential, natural order). */
 enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2, DXG_ILU_REDBLACK = 3 };
 int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
+/* The linear solver of dxg_linear_solve / dxg_newton_solve, as the reference's solver
+ * types: DXG_LINEAR_SOLVER_ILU_BICGSTAB (ILUBiCGSTABIstlSolver, istlsolvers.hh:635-642;
+ * default) or DXG_LINEAR_SOLVER_AMG_BICGSTAB (AMGBiCGSTABIstlSolver, istlsolvers.hh:729-736):
+ * BiCGSTAB preconditioned by one V-cycle of aggregation AMG -- 2x2(x2) box aggregates of
+ * the structured grid down to one cell, Galerkin coarse operators, damped block-Jacobi
+ * smoothing (the parallel counterpart of dune-istl's SSOR smoother).  In the context's
+ * precision (FP32 in mixed precision).  Fewer iterations than ILU(0) and no level chain;
+ * not dune-istl's AMG iterate for iterate (its aggregation and smoother differ). */
+enum { DXG_LINEAR_SOLVER_ILU_BICGSTAB = 0, DXG_LINEAR_SOLVER_AMG_BICGSTAB = 1 };
+int dxg_set_linear_solver(dxg_ctx* ctx, int kind);
 /* The ILU(0) kernels in use, as text: the wavefront launch shape (cluster size, threads,
  * prefetch depth) and, once the first factorisation has chosen it by timing, the time per
  * apply of every shape tried. */
