@@ -1,6 +1,10 @@
 // amg.cu -- aggregation AMG kernels (setup and V-cycle) on the structured stencil.
 #include "amg.cuh"
 
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
+
 namespace dxg {
 
 namespace {
@@ -181,94 +185,182 @@ __device__ __forceinline__ bool stopped(const KrylovState* ks)
     return ks && ks->status != KS_RUNNING;
 }
 
+// ---- per-cell bodies of the V-cycle passes (shared by the per-level kernels and the
+// cluster kernel of the small levels)
+
 // out = omega D^-1 b
 template <int B, class T>
-__global__ void amgFirstKernel(AmgLevel<T> L, T* out, T omega, const KrylovState* ks)
+__device__ __forceinline__ void firstCell(const AmgLevel<T>& L, int64_t i, T* out, T omega)
 {
-    if (stopped<T>(ks)) return;
     constexpr int BB = B * B;
-    AMG_LOOP(L)
-    {
-        T D[BB], bi[B], y[B];
-        ldBlk<B>(L.Dinv + i * BB, D);
+    T D[BB], bi[B], y[B];
+    ldBlk<B>(L.Dinv + i * BB, D);
 #pragma unroll
-        for (int e = 0; e < B; ++e) bi[e] = L.b[i * B + e];
-        mv<B>(D, bi, y);
+    for (int e = 0; e < B; ++e) bi[e] = L.b[i * B + e];
+    mv<B>(D, bi, y);
 #pragma unroll
-        for (int e = 0; e < B; ++e) out[i * B + e] = omega * y[e];
-    }
+    for (int e = 0; e < B; ++e) out[i * B + e] = omega * y[e];
 }
 
 // out = x~ + omega D^-1 (b - A x~), x~ = xin (+ prolongated xc when given)
 template <int B, int DIM, class T>
-__global__ void amgJacobiKernel(AmgLevel<T> L, const T* xin, const T* xc, int cnx, int cny, T* out, T omega,
-                                const KrylovState* ks)
+__device__ __forceinline__ void jacobiCell(const AmgLevel<T>& L, int64_t i, const T* xin, const T* xc, int cnx, int cny,
+                                           T* out, T omega)
 {
-    if (stopped<T>(ks)) return;
     constexpr int BB = B * B;
-    AMG_LOOP(L)
-    {
-        T ax[B], res[B], D[BB], y[B];
-        rowTimes<B, DIM, T>(L, i, xin, xc, cnx, cny, ax);
+    T ax[B], res[B], D[BB], y[B];
+    rowTimes<B, DIM, T>(L, i, xin, xc, cnx, cny, ax);
 #pragma unroll
-        for (int e = 0; e < B; ++e) res[e] = L.b[i * B + e] - ax[e];
-        ldBlk<B>(L.Dinv + i * BB, D);
-        mv<B>(D, res, y);
-        int x, yy, z;
-        coordOf(i, L.nx, L.ny, x, yy, z);
-        const int64_t C = xc ? (x >> 1) + (int64_t)cnx * ((yy >> 1) + (int64_t)cny * (z >> 1)) : 0;
+    for (int e = 0; e < B; ++e) res[e] = L.b[i * B + e] - ax[e];
+    ldBlk<B>(L.Dinv + i * BB, D);
+    mv<B>(D, res, y);
+    int x, yy, z;
+    coordOf(i, L.nx, L.ny, x, yy, z);
+    const int64_t C = xc ? (x >> 1) + (int64_t)cnx * ((yy >> 1) + (int64_t)cny * (z >> 1)) : 0;
 #pragma unroll
-        for (int e = 0; e < B; ++e) {
-            T xi = xin[i * B + e];
-            if (xc) xi += xc[C * B + e];
-            out[i * B + e] = xi + omega * y[e];
-        }
+    for (int e = 0; e < B; ++e) {
+        T xi = xin[i * B + e];
+        if (xc) xi += xc[C * B + e];
+        out[i * B + e] = xi + omega * y[e];
     }
 }
 
 // r = b - A x
 template <int B, int DIM, class T>
-__global__ void amgResidualKernel(AmgLevel<T> L, const T* xin, const KrylovState* ks)
+__device__ __forceinline__ void residualCell(const AmgLevel<T>& L, int64_t i, const T* xin)
 {
-    if (stopped<T>(ks)) return;
-    AMG_LOOP(L)
-    {
-        T ax[B];
-        rowTimes<B, DIM, T>(L, i, xin, nullptr, 0, 0, ax);
+    T ax[B];
+    rowTimes<B, DIM, T>(L, i, xin, nullptr, 0, 0, ax);
 #pragma unroll
-        for (int e = 0; e < B; ++e) L.r[i * B + e] = L.b[i * B + e] - ax[e];
-    }
+    for (int e = 0; e < B; ++e) L.r[i * B + e] = L.b[i * B + e] - ax[e];
 }
 
 // coarse b = sum of the aggregate's fine residuals (fixed order)
 template <int B, int DIM, class T>
+__device__ __forceinline__ void restrictCell(const AmgLevel<T>& F, const AmgLevel<T>& C, int64_t i)
+{
+    int cx, cy, cz;
+    coordOf(i, C.nx, C.ny, cx, cy, cz);
+    T acc[B];
+#pragma unroll
+    for (int e = 0; e < B; ++e) acc[e] = 0;
+    for (int dz = 0; dz < (DIM == 3 ? 2 : 1); ++dz) {
+        const int z = 2 * cz + dz;
+        if (z >= F.nz) continue;
+        for (int dy = 0; dy < 2; ++dy) {
+            const int y = 2 * cy + dy;
+            if (y >= F.ny) continue;
+            for (int dx = 0; dx < 2; ++dx) {
+                const int x = 2 * cx + dx;
+                if (x >= F.nx) continue;
+                const int64_t f = x + (int64_t)F.nx * (y + (int64_t)F.ny * z);
+#pragma unroll
+                for (int e = 0; e < B; ++e) acc[e] += F.r[f * B + e];
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < B; ++e) C.b[i * B + e] = acc[e];
+}
+
+// row i of x = Ainv b on the last level
+template <class T>
+__device__ __forceinline__ void coarseRow(const AmgLevel<T>& L, int n, int i)
+{
+    T t = 0;
+    for (int j = 0; j < n; ++j) t = fma(L.Ainv[(int64_t)i * n + j], L.b[j], t);
+    L.x[i] = t;
+}
+
+template <int B, class T>
+__global__ void amgFirstKernel(AmgLevel<T> L, T* out, T omega, const KrylovState* ks)
+{
+    if (stopped<T>(ks)) return;
+    AMG_LOOP(L) firstCell<B, T>(L, i, out, omega);
+}
+
+template <int B, int DIM, class T>
+__global__ void amgJacobiKernel(AmgLevel<T> L, const T* xin, const T* xc, int cnx, int cny, T* out, T omega,
+                                const KrylovState* ks)
+{
+    if (stopped<T>(ks)) return;
+    AMG_LOOP(L) jacobiCell<B, DIM, T>(L, i, xin, xc, cnx, cny, out, omega);
+}
+
+template <int B, int DIM, class T>
+__global__ void amgResidualKernel(AmgLevel<T> L, const T* xin, const KrylovState* ks)
+{
+    if (stopped<T>(ks)) return;
+    AMG_LOOP(L) residualCell<B, DIM, T>(L, i, xin);
+}
+
+template <int B, int DIM, class T>
 __global__ void amgRestrictKernel(AmgLevel<T> F, AmgLevel<T> C, const KrylovState* ks)
 {
     if (stopped<T>(ks)) return;
-    AMG_LOOP(C)
-    {
-        int cx, cy, cz;
-        coordOf(i, C.nx, C.ny, cx, cy, cz);
-        T acc[B];
-#pragma unroll
-        for (int e = 0; e < B; ++e) acc[e] = 0;
-        for (int dz = 0; dz < (DIM == 3 ? 2 : 1); ++dz) {
-            const int z = 2 * cz + dz;
-            if (z >= F.nz) continue;
-            for (int dy = 0; dy < 2; ++dy) {
-                const int y = 2 * cy + dy;
-                if (y >= F.ny) continue;
-                for (int dx = 0; dx < 2; ++dx) {
-                    const int x = 2 * cx + dx;
-                    if (x >= F.nx) continue;
-                    const int64_t f = x + (int64_t)F.nx * (y + (int64_t)F.ny * z);
-#pragma unroll
-                    for (int e = 0; e < B; ++e) acc[e] += F.r[f * B + e];
-                }
-            }
+    AMG_LOOP(C) restrictCell<B, DIM, T>(F, C, i);
+}
+
+// The V-cycle below a level of at most kAmgClusterLevel cells as one launch of one thread
+// block cluster: every pass is a loop over the level's cells across the cluster's threads,
+// followed by a cluster barrier (release/acquire at cluster scope orders the passes' global
+// memory traffic).  Same per-cell arithmetic and pass order as the per-level kernels.
+constexpr int kAmgMaxClusterLevels = 12;
+constexpr int kAmgClusterCtas = 16;
+constexpr int kAmgClusterThreads = 512;
+template <class T>
+struct AmgCycle {
+    AmgLevel<T> lv[kAmgMaxClusterLevels];
+    int count;
+};
+
+template <int B, int DIM, class T>
+__global__ void __launch_bounds__(kAmgClusterThreads) amgClusterCycle(AmgCycle<T> cy, const KrylovState* ks)
+{
+    if (stopped<T>(ks)) return;   // uniform: the status does not change during the launch
+    cg::cluster_group cl = cg::this_cluster();
+    const int64_t gid = (int64_t)cl.block_rank() * blockDim.x + threadIdx.x;
+    const int64_t gstride = (int64_t)cl.num_blocks() * blockDim.x;
+    const T omega = (T)kAmgOmega;
+    const T* pre[kAmgMaxClusterLevels];
+    const int last = cy.count - 1;
+    for (int l = 0; l < last; ++l) {
+        const AmgLevel<T>& L = cy.lv[l];
+        T* buf[2] = {L.tmp, L.x};
+        int w = 0;
+        for (int64_t i = gid; i < L.N; i += gstride) firstCell<B, T>(L, i, buf[0], omega);
+        cl.sync();
+        for (int k = 1; k < L.sweeps; ++k, ++w) {
+            for (int64_t i = gid; i < L.N; i += gstride)
+                jacobiCell<B, DIM, T>(L, i, buf[w & 1], nullptr, 0, 0, buf[(w + 1) & 1], omega);
+            cl.sync();
         }
-#pragma unroll
-        for (int e = 0; e < B; ++e) C.b[i * B + e] = acc[e];
+        pre[l] = buf[w & 1];
+        for (int64_t i = gid; i < L.N; i += gstride) residualCell<B, DIM, T>(L, i, pre[l]);
+        cl.sync();
+        for (int64_t i = gid; i < cy.lv[l + 1].N; i += gstride) restrictCell<B, DIM, T>(L, cy.lv[l + 1], i);
+        cl.sync();
+    }
+    {
+        const AmgLevel<T>& L = cy.lv[last];
+        const int n = (int)L.N * B;
+        for (int64_t i = gid; i < n; i += gstride) coarseRow<T>(L, n, (int)i);
+        cl.sync();
+    }
+    for (int l = last - 1; l >= 0; --l) {
+        const AmgLevel<T>& L = cy.lv[l];
+        const AmgLevel<T>& C = cy.lv[l + 1];
+        T* buf[2] = {L.tmp, L.x};
+        int w = L.sweeps - 1;   // index of the last pre-smoothing write
+        for (int64_t i = gid; i < L.N; i += gstride)
+            jacobiCell<B, DIM, T>(L, i, pre[l], C.x, C.nx, C.ny, buf[(w + 1) & 1], omega);
+        ++w;
+        cl.sync();
+        for (int k = 1; k < L.sweeps; ++k, ++w) {
+            for (int64_t i = gid; i < L.N; i += gstride)
+                jacobiCell<B, DIM, T>(L, i, buf[w & 1], nullptr, 0, 0, buf[(w + 1) & 1], omega);
+            cl.sync();
+        }
     }
 }
 
@@ -366,11 +458,7 @@ template <class T>
 __global__ void amgCoarseSolveKernel(AmgLevel<T> L, int n, const KrylovState* ks)
 {
     if (stopped<T>(ks)) return;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        T t = 0;
-        for (int j = 0; j < n; ++j) t = fma(L.Ainv[(int64_t)i * n + j], L.b[j], t);
-        L.x[i] = t;
-    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) coarseRow<T>(L, n, i);
 }
 
 unsigned gridFor(int64_t n)
@@ -385,6 +473,27 @@ int64_t vcycle(const std::vector<AmgLevel<T>>& Ls, size_t l, const KrylovState* 
 {
     const AmgLevel<T>& L = Ls[l];
     const unsigned g = gridFor(L.N);
+    if (L.N <= kAmgClusterLevel && Ls.size() - l <= (size_t)kAmgMaxClusterLevels) {
+        // this level and all below: one cluster launch
+        AmgCycle<T> cy{};
+        cy.count = (int)(Ls.size() - l);
+        for (int k = 0; k < cy.count; ++k) cy.lv[k] = Ls[l + k];
+        auto kern = amgClusterCycle<B, DIM, T>;
+        DXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kAmgClusterCtas);
+        cfg.blockDim = dim3(kAmgClusterThreads);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kAmgClusterCtas;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        DXG_CUDA(cudaLaunchKernelEx(&cfg, kern, cy, ks));
+        return 1;
+    }
     if (l + 1 == Ls.size()) {
         amgCoarseSolveKernel<T><<<1, kAmgThreads, 0, st>>>(L, (int)L.N * B, ks);   // exact solve
         return 1;

@@ -14,7 +14,10 @@
 //   * the last level is solved exactly: its dense inverse (Gauss-Jordan elimination
 //     with partial pivoting in one CTA's shared memory) is formed at setup and applied
 //     as one dense matrix-vector product;
-//   * the V-cycle is a fixed linear operator, so it preconditions BiCGSTAB.
+//   * the V-cycle is a fixed linear operator, so it preconditions BiCGSTAB;
+//   * the levels of at most 4096 cells run as one launch of a 16-CTA thread block
+//     cluster (passes separated by cluster barriers) instead of a few-microsecond
+//     launch per pass.
 // Every kernel is a pass over one level's cells (bandwidth bound); the setup (pivot
 // inverses, coarse operators) runs once per Jacobian.
 #pragma once
@@ -46,6 +49,7 @@ constexpr double kAmgOmega = 0.8;
 constexpr int64_t kAmgSmallLevel = 4096;
 constexpr int kAmgSmallSweeps = 2;
 constexpr int64_t kAmgCoarsest = 64;   // cells of the directly solved last level (at most)
+constexpr int64_t kAmgClusterLevel = 4096;    // levels this small and below: one cluster launch
 
 // Grid extents of the levels below a fine grid (2D: nz = 1), the last one of at most
 // kAmgCoarsest cells (none when the fine grid is that small).
