@@ -372,6 +372,7 @@ public:
     // solve(A, x, b): A and b are the assembler's device system; x receives the update
     bool solve(const GpuFVAssembler& A, std::vector<double>& x, const std::vector<double>& /*b*/)
     {
+        A.handle().check(dxg_set_linear_solver(A.context(), kind_));
         dxg_linear_result res{};
         const int st = dxg_linear_solve(A.context(), reduction_, maxIter_, &res);
         if (st != DXG_OK && !recoverable(st)) A.handle().check(st);
@@ -383,10 +384,21 @@ public:
     double norm(const GpuFVAssembler& A) const { return A.residualNorm(); }
     const dxg_linear_result& result() const { return last_; }
 
+protected:
+    int kind_ = DXG_LINEAR_SOLVER_ILU_BICGSTAB;
+
 private:
     double reduction_ = 1e-13;
     int maxIter_ = 250;
     dxg_linear_result last_{};
+};
+
+// Dumux::AMGBiCGSTABIstlSolver over the device (istlsolvers.hh:729-736): BiCGSTAB
+// preconditioned by one V-cycle of the library's aggregation AMG (structured 2x2(x2)
+// aggregates, Galerkin coarse operators, damped block-Jacobi smoothing).
+class GpuAMGBiCGSTABSolver : public GpuILUBiCGSTABSolver {
+public:
+    GpuAMGBiCGSTABSolver() { kind_ = DXG_LINEAR_SOLVER_AMG_BICGSTAB; }
 };
 
 // Dumux::NewtonSolver over the device (newtonsolver.hh:179-852): the loop, the update,

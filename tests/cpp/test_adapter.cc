@@ -6,6 +6,8 @@
 //   test_adapter NX NY NZ STEPS OUT.bin
 // writes the solution after STEPS implicit Euler steps of 250 s as raw doubles; exits 3
 // with "no-device" when no GPU is present.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -105,6 +107,25 @@ int main(int argc, char** argv)
             return 1;
         }
         if ((int64_t)rowPtr.back() != (int64_t)col.size()) return 1;
+        // the AMGBiCGSTAB solver type on the same system: the same update to the tolerance
+        GpuAMGBiCGSTABSolver amg;
+        amg.setResidualReduction(1e-10);
+        std::vector<double> duAmg;
+        if (!amg.solve(assembler, duAmg, assembler.residual())) {
+            std::fprintf(stderr, "AMG linear solve did not converge\n");
+            return 1;
+        }
+        double dmax = 0, umax = 0;
+        for (size_t k = 0; k < du.size(); ++k) {
+            dmax = std::max(dmax, std::fabs(du[k] - duAmg[k]));
+            umax = std::max(umax, std::fabs(du[k]));
+        }
+        if (dmax > 1e-6 * umax) {
+            std::fprintf(stderr, "AMG and ILU updates differ: %g of %g\n", dmax, umax);
+            return 1;
+        }
+        // the Newton loop below uses the default ILU(0)-BiCGSTAB again
+        if (dxg_set_linear_solver(assembler.context(), DXG_LINEAR_SOLVER_ILU_BICGSTAB) != DXG_OK) return 1;
 
         // the Newton loop with the time loop of the reference's 2p test
         GpuNewtonSolver newton(assembler);
