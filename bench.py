@@ -54,8 +54,8 @@ def parse():
                     help="ILU(0) ordering of the single-problem workloads: natural (the reference's "
                          "SeqILU, default) or red-black (two parallel passes per sweep, more iterations)")
     ap.add_argument("--solver", default="ilu", choices=["ilu", "amg"],
-                    help="single-problem workloads: ILU(0)-BiCGSTAB (default, the reference's "
-                         "ILUBiCGSTABIstlSolver) or AMG-BiCGSTAB (AMGBiCGSTABIstlSolver)")
+                    help="ILU(0)-BiCGSTAB (default, the reference's ILUBiCGSTABIstlSolver) or "
+                         "AMG-BiCGSTAB (AMGBiCGSTABIstlSolver)")
     ap.add_argument("--problems", type=int, default=256, help="ensemble size")
     ap.add_argument("--requests", type=int, default=48, help="served-stream length")
     ap.add_argument("--ticks-per-step", type=int, default=25, help="ensemble: engine ticks per timed step")
@@ -353,7 +353,7 @@ def run_ensemble(args):
         for _ in range(n):
             b.iterate()
 
-    batch = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu)
+    batch = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu, solver=args.solver)
     ids = [batch.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
     cells_of = {pid: d.num_cells for pid, (d, _, _) in zip(ids, probs)}
     ticks(batch, args.warmup * T)            # includes the sweep autotuning
@@ -399,7 +399,7 @@ def run_ensemble(args):
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b2 = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu)
+    b2 = dumux_gb300.Batch(device=local, precision=args.precision, ilu=args.ilu, solver=args.solver)
     ids2 = [b2.add(d, u0, dt=dt, t_end=t_end, params=params) for d, u0, _ in probs]
     d2h = 0
     for _ in range(args.steps):
@@ -473,7 +473,8 @@ def run_serve(args):
     built = {r["index"]: problems.make_request_problem(r) for r in reqs}
     free, _ = torch.cuda.mem_get_info(local)
     budget = int(0.8 * free)
-    server = Server(device=local, precision=args.precision, memory_budget=budget, params=params, ilu=args.ilu)
+    server = Server(device=local, precision=args.precision, memory_budget=budget, params=params, ilu=args.ilu,
+                    solver=args.solver)
     # warm-up: small requests of both kinds (kernel loading, sweep autotuning)
     warm = problems.served_requests(max(3, args.warmup), rate=1e6, seed=99, n_max=2e4)
     server.serve(warm, problems.make_request_problem)

@@ -16,7 +16,8 @@ import os
 
 import numpy as np
 
-from .abi import (DXG_BATCH_OPT_AUTOTUNE, DXG_BATCH_OPT_GRAPHS, DXG_BATCH_OPT_ILU_REDBLACK, DXG_ERR_BUDGET,
+from .abi import (DXG_BATCH_OPT_AMG, DXG_BATCH_OPT_AUTOTUNE, DXG_BATCH_OPT_GRAPHS, DXG_BATCH_OPT_ILU_REDBLACK,
+                  DXG_ERR_BUDGET,
                   DXG_PRECISION_FP64, DXG_PRECISION_MIXED, STATUS_NAMES, BatchProblemInfoC, LinearResultC, NewtonParamsC, NewtonReportC,
                   ProblemDesc, ProblemDescC, newton_params)
 
@@ -395,7 +396,8 @@ class Batch:
     depend on what else is in the batch.
     """
 
-    def __init__(self, device=0, precision="mixed", graphs=True, autotune=True, memory_budget=0, ilu="natural"):
+    def __init__(self, device=0, precision="mixed", graphs=True, autotune=True, memory_budget=0, ilu="natural",
+                 solver="ilu"):
         L = lib()
         h = C.c_void_p()
         prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
@@ -410,6 +412,7 @@ class Batch:
         self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_AUTOTUNE, int(bool(autotune))))
         self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_ILU_REDBLACK,
                                            {"natural": 0, "redblack": 1}[ilu]))
+        self._check(L.dxg_batch_set_option(h, DXG_BATCH_OPT_AMG, {"ilu": 0, "amg": 1}[solver]))
         self._check(L.dxg_batch_set_memory_budget(h, int(memory_budget)))
 
     def _check(self, st):

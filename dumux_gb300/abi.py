@@ -18,6 +18,7 @@ DXG_ERR_BUDGET = 12
 DXG_BATCH_OPT_GRAPHS = 0
 DXG_BATCH_OPT_AUTOTUNE = 1
 DXG_BATCH_OPT_ILU_REDBLACK = 2
+DXG_BATCH_OPT_AMG = 3
 DXG_PRECISION_FP64 = 0
 DXG_PRECISION_MIXED = 1
 MAX_NEWTON_RECORD = 64

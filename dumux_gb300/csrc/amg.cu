@@ -73,25 +73,28 @@ __device__ __forceinline__ void coordOf(int64_t i, int nx, int ny, int& x, int& 
 }
 
 template <int B, class T>
-__global__ void amgDiagInvKernel(AmgLevel<T> L, int dim, int* singular)
+__device__ __forceinline__ void diagInvCell(const AmgLevel<T>& L, int64_t i, int dim, int* singular)
 {
     constexpr int BB = B * B;
-    AMG_LOOP(L)
-    {
-        T D[BB], inv[BB];
-        ldBlk<B>(L.A + ((int64_t)dim * L.N + i) * BB, D);
-        if (!invBlk<B>(D, inv)) *singular = 1;
+    T D[BB], inv[BB];
+    ldBlk<B>(L.A + ((int64_t)dim * L.N + i) * BB, D);
+    if (!invBlk<B>(D, inv)) *singular = 1;
 #pragma unroll
-        for (int e = 0; e < BB; ++e) L.Dinv[i * BB + e] = inv[e];
-    }
+    for (int e = 0; e < BB; ++e) L.Dinv[i * BB + e] = inv[e];
+}
+
+template <int B, class T>
+__global__ void amgDiagInvKernel(AmgLevel<T> L, int dim, int* singular)
+{
+    AMG_LOOP(L) diagInvCell<B, T>(L, i, dim, singular);
 }
 
 // coarse cell C = block sums over its aggregate's fine cells (fixed order: z, y, x, slot)
 template <int B, int DIM, class T>
-__global__ void amgCoarsenKernel(AmgLevel<T> F, AmgLevel<T> C, T* Ac, int* singular)
+__device__ __forceinline__ void coarsenCell(const AmgLevel<T>& F, const AmgLevel<T>& C, int64_t i, int* singular)
 {
     constexpr int BB = B * B, S = 2 * DIM + 1;
-    AMG_LOOP(C)
+    T* Ac = const_cast<T*>(C.A);
     {
         int cx, cy, cz;
         coordOf(i, C.nx, C.ny, cx, cy, cz);
@@ -138,6 +141,12 @@ __global__ void amgCoarsenKernel(AmgLevel<T> F, AmgLevel<T> C, T* Ac, int* singu
 #pragma unroll
         for (int e = 0; e < BB; ++e) C.Dinv[i * BB + e] = inv[e];
     }
+}
+
+template <int B, int DIM, class T>
+__global__ void amgCoarsenKernel(AmgLevel<T> F, AmgLevel<T> C, int* singular)
+{
+    AMG_LOOP(C) coarsenCell<B, DIM, T>(F, C, i, singular);
 }
 
 // sum_s A_is x_j over the existing neighbours and the diagonal
@@ -369,9 +378,8 @@ __global__ void __launch_bounds__(kAmgClusterThreads) amgClusterCycle(AmgCycle<T
 // elimination with partial pivoting (row exchanges, undone as column exchanges in reverse
 // order at the end); one CTA.
 template <int B, int DIM, class T>
-__global__ void amgCoarseInvertKernel(AmgLevel<T> L, int* singular)
+__device__ void coarseInvertCta(const AmgLevel<T>& L, int* singular, unsigned char* smemRaw)
 {
-    extern __shared__ __align__(16) unsigned char smemRaw[];
     constexpr int BB = B * B, S = 2 * DIM + 1;
     const int n = (int)L.N * B;
     T* a = reinterpret_cast<T*>(smemRaw);   // [n][n]
@@ -453,12 +461,56 @@ __global__ void amgCoarseInvertKernel(AmgLevel<T> L, int* singular)
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) L.Ainv[e] = a[e];
 }
 
+template <int B, int DIM, class T>
+__global__ void amgCoarseInvertKernel(AmgLevel<T> L, int* singular)
+{
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    coarseInvertCta<B, DIM, T>(L, singular, smemRaw);
+}
+
 // x = Ainv b on the last level (one row per thread, fixed order)
 template <class T>
 __global__ void amgCoarseSolveKernel(AmgLevel<T> L, int n, const KrylovState* ks)
 {
     if (stopped<T>(ks)) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) coarseRow<T>(L, n, i);
+}
+
+// ---- batched passes: one launch runs one pass for several problems, block k of the
+// grid working on problem map[k].x as its block map[k].y of amgPassBlocks(items)
+__host__ __device__ __forceinline__ int64_t passItems(int kind, int64_t LN, int64_t CN, int b)
+{
+    return (kind == AMG_RESTRICT || kind == AMG_COARSEN) ? CN : (kind == AMG_COARSE ? LN * b : LN);
+}
+
+template <int B, int DIM, class T, int KIND>
+__global__ void __launch_bounds__(kAmgThreads) amgPassBatch(const AmgPass<T>* passes, const uint2* map)
+{
+    const uint2 m = map[blockIdx.x];
+    const AmgPass<T>& P = passes[m.x];
+    if (stopped<T>(P.ks)) return;
+    const int64_t n = passItems(KIND, P.L.N, P.C.N, B);
+    const unsigned nblk = amgPassBlocks(n);
+    if (m.y >= nblk) return;
+    for (int64_t i = m.y * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)nblk * blockDim.x) {
+        if constexpr (KIND == AMG_FIRST) firstCell<B, T>(P.L, i, P.out, P.omega);
+        else if constexpr (KIND == AMG_JACOBI)
+            jacobiCell<B, DIM, T>(P.L, i, P.in, P.prolong ? P.C.x : nullptr, P.C.nx, P.C.ny, P.out, P.omega);
+        else if constexpr (KIND == AMG_RESIDUAL) residualCell<B, DIM, T>(P.L, i, P.in);
+        else if constexpr (KIND == AMG_RESTRICT) restrictCell<B, DIM, T>(P.L, P.C, i);
+        else if constexpr (KIND == AMG_COARSE) coarseRow<T>(P.L, (int)n, (int)i);
+        else if constexpr (KIND == AMG_DIAGINV) diagInvCell<B, T>(P.L, i, DIM, P.singular);
+        else coarsenCell<B, DIM, T>(P.L, P.C, i, P.singular);
+    }
+}
+
+// one CTA per problem: dense inverse of its last level
+template <int B, int DIM, class T>
+__global__ void amgInvertBatch(const AmgPass<T>* passes)
+{
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    const AmgPass<T>& P = passes[blockIdx.x];
+    coarseInvertCta<B, DIM, T>(P.L, P.singular, smemRaw);
 }
 
 unsigned gridFor(int64_t n)
@@ -550,13 +602,12 @@ template <class T>
 void launchAmgCoarsen(const AmgLevel<T>& fine, AmgLevel<T>& coarse, int dim, int b, int* singular, cudaStream_t st)
 {
     const unsigned g = gridFor(coarse.N);
-    T* Ac = const_cast<T*>(coarse.A);
     if (b == 1) {
-        if (dim == 2) amgCoarsenKernel<1, 2, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, Ac, singular);
-        else amgCoarsenKernel<1, 3, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, Ac, singular);
+        if (dim == 2) amgCoarsenKernel<1, 2, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, singular);
+        else amgCoarsenKernel<1, 3, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, singular);
     } else {
-        if (dim == 2) amgCoarsenKernel<2, 2, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, Ac, singular);
-        else amgCoarsenKernel<2, 3, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, Ac, singular);
+        if (dim == 2) amgCoarsenKernel<2, 2, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, singular);
+        else amgCoarsenKernel<2, 3, T><<<g, kAmgThreads, 0, st>>>(fine, coarse, singular);
     }
     DXG_CUDA(cudaGetLastError());
 }
@@ -586,6 +637,49 @@ int64_t launchAmgVcycle(const std::vector<AmgLevel<T>>& levels, int dim, int b, 
     return n;
 }
 
+template <class T, int B, int DIM>
+static void passDispatch(int kind, const AmgPass<T>* p, const uint2* map, unsigned blocks, cudaStream_t st)
+{
+    switch (kind) {
+        case AMG_FIRST: amgPassBatch<B, DIM, T, AMG_FIRST><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        case AMG_JACOBI: amgPassBatch<B, DIM, T, AMG_JACOBI><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        case AMG_RESIDUAL: amgPassBatch<B, DIM, T, AMG_RESIDUAL><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        case AMG_RESTRICT: amgPassBatch<B, DIM, T, AMG_RESTRICT><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        case AMG_COARSE: amgPassBatch<B, DIM, T, AMG_COARSE><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        case AMG_DIAGINV: amgPassBatch<B, DIM, T, AMG_DIAGINV><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+        default: amgPassBatch<B, DIM, T, AMG_COARSEN><<<blocks, kAmgThreads, 0, st>>>(p, map); break;
+    }
+}
+
+template <class T>
+void launchAmgPassBatch(int kind, const AmgPass<T>* passes, const uint2* map, unsigned blocks, int dim, int b,
+                        cudaStream_t st)
+{
+    if (b == 1) dim == 2 ? passDispatch<T, 1, 2>(kind, passes, map, blocks, st)
+                         : passDispatch<T, 1, 3>(kind, passes, map, blocks, st);
+    else dim == 2 ? passDispatch<T, 2, 2>(kind, passes, map, blocks, st)
+                  : passDispatch<T, 2, 3>(kind, passes, map, blocks, st);
+    DXG_CUDA(cudaGetLastError());
+}
+
+template <class T>
+void launchAmgInvertBatch(const AmgPass<T>* passes, int count, int maxN, int dim, int b, cudaStream_t st)
+{
+    const int n = maxN * b;
+    const size_t smem = (size_t)n * n * sizeof(T) + (size_t)n * sizeof(T) + (size_t)n * sizeof(int);
+    auto go = [&](auto kern) {
+        DXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<count, kAmgThreads, smem, st>>>(passes);
+    };
+    if (b == 1) dim == 2 ? go(amgInvertBatch<1, 2, T>) : go(amgInvertBatch<1, 3, T>);
+    else dim == 2 ? go(amgInvertBatch<2, 2, T>) : go(amgInvertBatch<2, 3, T>);
+    DXG_CUDA(cudaGetLastError());
+}
+
+template void launchAmgPassBatch<double>(int, const AmgPass<double>*, const uint2*, unsigned, int, int, cudaStream_t);
+template void launchAmgPassBatch<float>(int, const AmgPass<float>*, const uint2*, unsigned, int, int, cudaStream_t);
+template void launchAmgInvertBatch<double>(const AmgPass<double>*, int, int, int, int, cudaStream_t);
+template void launchAmgInvertBatch<float>(const AmgPass<float>*, int, int, int, int, cudaStream_t);
 template void launchAmgDiagInv<double>(const AmgLevel<double>&, int, int, int*, cudaStream_t);
 template void launchAmgDiagInv<float>(const AmgLevel<float>&, int, int, int*, cudaStream_t);
 template void launchAmgCoarseInvert<double>(const AmgLevel<double>&, int, int, int*, cudaStream_t);

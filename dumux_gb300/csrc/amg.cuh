@@ -51,6 +51,34 @@ constexpr int kAmgSmallSweeps = 2;
 constexpr int64_t kAmgCoarsest = 64;   // cells of the directly solved last level (at most)
 constexpr int64_t kAmgClusterLevel = 4096;    // levels this small and below: one cluster launch
 
+// One pass of a V-cycle or of the setup for one problem of a batch.
+enum { AMG_FIRST = 0, AMG_JACOBI = 1, AMG_RESIDUAL = 2, AMG_RESTRICT = 3, AMG_COARSE = 4, AMG_DIAGINV = 5,
+       AMG_COARSEN = 6 };
+template <class T>
+struct AmgPass {
+    AmgLevel<T> L;            // the level of the pass (restrict, coarsen: the finer level)
+    AmgLevel<T> C;            // the coarser level (restrict, coarsen, prolongation)
+    const T* in = nullptr;    // Jacobi / residual input
+    T* out = nullptr;         // first / Jacobi output
+    int prolong = 0;          // Jacobi: the input is in + the prolongated C.x
+    T omega = 0;
+    int* singular = nullptr;
+    const KrylovState* ks = nullptr;   // V-cycle passes skip once the solve has stopped
+};
+// blocks a batched pass gives one problem with `items` work items (256 threads each)
+__host__ __device__ inline unsigned amgPassBlocks(int64_t items)
+{
+    int64_t g = (items + 255) / 256;
+    if (g > 1024) g = 1024;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+template <class T>
+void launchAmgPassBatch(int kind, const AmgPass<T>* passes, const uint2* map, unsigned blocks, int dim, int b,
+                        cudaStream_t st);
+// one CTA per problem: the dense inverse of each problem's last level (maxN: its largest cell count)
+template <class T>
+void launchAmgInvertBatch(const AmgPass<T>* passes, int count, int maxN, int dim, int b, cudaStream_t st);
+
 // Grid extents of the levels below a fine grid (2D: nz = 1), the last one of at most
 // kAmgCoarsest cells (none when the fine grid is that small).
 std::vector<std::array<int, 3>> amgLevelDims(int dim, int nx, int ny, int nz);

@@ -1067,6 +1067,16 @@ struct NewtonRun {
 
 }  // namespace
 
+namespace dxg {
+template <class T>
+std::vector<AmgLevel<T>> amgLevelsOf(dxg_ctx* c, const T* A, T* Dinv, const T* in, T* out)
+{
+    return amgLevels<T>(c, A, Dinv, in, out);
+}
+template std::vector<AmgLevel<double>> amgLevelsOf<double>(dxg_ctx*, const double*, double*, const double*, double*);
+template std::vector<AmgLevel<float>> amgLevelsOf<float>(dxg_ctx*, const float*, float*, const float*, float*);
+}  // namespace dxg
+
 // ================================================================ C ABI
 extern "C" {
 

@@ -185,6 +185,7 @@ struct dxg_batch {
     std::string err;
     bool graphs = true, autotune = true;
     bool redBlack = false;            // red-black ordered ILU(0) instead of the natural order
+    bool amg = false;                 // AMG-BiCGSTAB instead of ILU(0)-BiCGSTAB
     int64_t budget = 0, bytesInUse = 0;
     int64_t nextId = 1;
     int64_t launches = 0;
@@ -593,6 +594,12 @@ struct GroupState {
     const void* dRbR = nullptr;
     BlockMap mapM, mapN;     // vector kernels over N*b entries, SpMV over N cells
     BlockMap mapH;           // red-black passes over each problem's colour slots
+    struct AmgLaunch {
+        int kind;
+        const void* passes;      // AmgPass<PT>[] of the problems taking part
+        BlockMap map;
+    };
+    std::vector<AmgLaunch> amgP, amgR;   // V-cycle passes applied to p / to r
     int64_t maxN = 1, maxM = 1;
     double sweepBytes = 0, spmvBytes = 0;
     cudaGraphExec_t exec = nullptr;
@@ -709,6 +716,101 @@ void refineClassPlans(dxg_batch* B, std::vector<SweepClass>& classes, const Memb
     for (int q = 0; q < nc; ++q) classes[q].plan = plans[q];
 }
 
+// The passes of one V-cycle for every member, aligned by (level, phase, sweep): a problem
+// takes part in a pass when it has that level (above its last) and that many sweeps.  The
+// per-problem sequence is the single context's (same passes, same buffers, same order).
+template <class PT>
+struct AmgPassList {
+    int kind;
+    std::vector<AmgPass<PT>> passes;
+    std::vector<uint2> map;
+};
+template <class PT>
+std::vector<AmgPassList<PT>> amgCycleSchedule(const std::vector<std::vector<AmgLevel<PT>>>& lv,
+                                              const std::vector<const KrylovState*>& ks, int b)
+{
+    size_t dmax = 0;
+    int smax = 1;
+    for (const auto& L : lv) {
+        dmax = std::max(dmax, L.size());
+        for (const auto& l : L) smax = std::max(smax, l.sweeps);
+    }
+    std::vector<AmgPassList<PT>> out;
+    const PT omega = (PT)kAmgOmega;
+    auto emit = [&](int kind, auto&& make) {
+        AmgPassList<PT> pl;
+        pl.kind = kind;
+        for (size_t k = 0; k < lv.size(); ++k) {
+            AmgPass<PT> p{};
+            if (!make(k, p)) continue;
+            p.ks = ks[k];
+            p.omega = omega;
+            const unsigned nb = amgPassBlocks(kind == AMG_RESTRICT ? p.C.N : (kind == AMG_COARSE ? p.L.N * b : p.L.N));
+            for (unsigned j = 0; j < nb; ++j) pl.map.push_back(make_uint2((unsigned)pl.passes.size(), j));
+            pl.passes.push_back(p);
+        }
+        if (!pl.passes.empty()) out.push_back(std::move(pl));
+    };
+    for (size_t l = 0; l + 1 < dmax; ++l) {
+        emit(AMG_FIRST, [&](size_t k, AmgPass<PT>& p) {
+            if (l + 1 >= lv[k].size()) return false;
+            p.L = lv[k][l];
+            p.out = p.L.tmp;
+            return true;
+        });
+        for (int kk = 1; kk < smax; ++kk)
+            emit(AMG_JACOBI, [&](size_t k, AmgPass<PT>& p) {
+                if (l + 1 >= lv[k].size() || kk >= lv[k][l].sweeps) return false;
+                p.L = lv[k][l];
+                PT* buf[2] = {p.L.tmp, p.L.x};
+                p.in = buf[(kk - 1) & 1];
+                p.out = buf[kk & 1];
+                return true;
+            });
+        emit(AMG_RESIDUAL, [&](size_t k, AmgPass<PT>& p) {
+            if (l + 1 >= lv[k].size()) return false;
+            p.L = lv[k][l];
+            PT* buf[2] = {p.L.tmp, p.L.x};
+            p.in = buf[(p.L.sweeps - 1) & 1];
+            return true;
+        });
+        emit(AMG_RESTRICT, [&](size_t k, AmgPass<PT>& p) {
+            if (l + 1 >= lv[k].size()) return false;
+            p.L = lv[k][l];
+            p.C = lv[k][l + 1];
+            return true;
+        });
+    }
+    emit(AMG_COARSE, [&](size_t k, AmgPass<PT>& p) {
+        p.L = lv[k].back();
+        return true;
+    });
+    for (size_t l = dmax - 1; l-- > 0;) {
+        emit(AMG_JACOBI, [&](size_t k, AmgPass<PT>& p) {
+            if (l + 1 >= lv[k].size()) return false;
+            p.L = lv[k][l];
+            p.C = lv[k][l + 1];
+            PT* buf[2] = {p.L.tmp, p.L.x};
+            const int sw = p.L.sweeps;
+            p.in = buf[(sw - 1) & 1];
+            p.out = buf[sw & 1];
+            p.prolong = 1;
+            return true;
+        });
+        for (int kk = 1; kk < smax; ++kk)
+            emit(AMG_JACOBI, [&](size_t k, AmgPass<PT>& p) {
+                if (l + 1 >= lv[k].size() || kk >= lv[k][l].sweeps) return false;
+                p.L = lv[k][l];
+                PT* buf[2] = {p.L.tmp, p.L.x};
+                const int sw = p.L.sweeps;
+                p.in = buf[(sw - 1 + kk) & 1];
+                p.out = buf[(sw + kk) & 1];
+                return true;
+            });
+    }
+    return out;
+}
+
 // (Re)builds the group's chunk arguments when its membership changed.
 template <class PT>
 GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
@@ -725,7 +827,7 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.ids = ids;
     const int n = (int)S.size();
     const int dim = S[0]->c->dim, b = S[0]->c->b;
-    if (!B->redBlack) {
+    if (!B->redBlack && !B->amg) {
         int cls[kMaxSweepClasses] = {-1, -1, -1, -1};
         G.classOf.resize(n);
         for (int k = 0; k < n; ++k) {
@@ -778,7 +880,7 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
         sv.w = ba[k].r;
         sv2[k] = sv;
         const PT* PA = Pre<PT>::A(c);
-        if (!B->redBlack) {
+        if (!B->redBlack && !B->amg) {
             fwP[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::pIn(c),
                                     Pre<PT>::yOut(c), c->ks.get());
             fwR[k] = waveArgsOf<PT>(c, G.geo[k], PA, Pre<PT>::L(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c),
@@ -808,6 +910,27 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     const size_t oB = pack(host, ba), o1 = pack(host, sv1), o2 = pack(host, sv2), oT = pack(host, td),
                  oM = pack(host, mM), oN = pack(host, mN), oH = pack(host, mH), oRP = pack(host, rbP),
                  oRR = pack(host, rbR);
+    // AMG: the V-cycle passes for the preconditioner applied to p and to r
+    struct AmgOff {
+        int kind;
+        size_t passes, map;
+        unsigned blocks;
+    };
+    std::vector<AmgOff> amgOffP, amgOffR;
+    if (B->amg) {
+        std::vector<std::vector<AmgLevel<PT>>> lp, lr;
+        std::vector<const KrylovState*> ks;
+        for (Slot* s : S) {
+            dxg_ctx* c = s->c;
+            lp.push_back(amgLevelsOf<PT>(c, Pre<PT>::A(c), Pre<PT>::Dinv(c), Pre<PT>::pIn(c), Pre<PT>::yOut(c)));
+            lr.push_back(amgLevelsOf<PT>(c, Pre<PT>::A(c), Pre<PT>::Dinv(c), Pre<PT>::rIn(c), Pre<PT>::yOut(c)));
+            ks.push_back(c->ks.get());
+        }
+        for (auto& pl : amgCycleSchedule<PT>(lp, ks, b))
+            amgOffP.push_back({pl.kind, pack(host, pl.passes), pack(host, pl.map), (unsigned)pl.map.size()});
+        for (auto& pl : amgCycleSchedule<PT>(lr, ks, b))
+            amgOffR.push_back({pl.kind, pack(host, pl.passes), pack(host, pl.map), (unsigned)pl.map.size()});
+    }
     std::vector<std::array<size_t, 3>> oc;
     for (const SweepClass& sc : G.classes) {
         std::vector<WaveArgs<PT>> cP, cR, cW;
@@ -835,6 +958,10 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.mapH = {reinterpret_cast<const uint2*>(d + oH), (unsigned)mH.size()};
     G.dRbP = d + oRP;
     G.dRbR = d + oRR;
+    for (const AmgOff& o : amgOffP)
+        G.amgP.push_back({o.kind, d + o.passes, BlockMap{reinterpret_cast<const uint2*>(d + o.map), o.blocks}});
+    for (const AmgOff& o : amgOffR)
+        G.amgR.push_back({o.kind, d + o.passes, BlockMap{reinterpret_cast<const uint2*>(d + o.map), o.blocks}});
     return G;
 }
 
@@ -847,6 +974,13 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
     const int nc = (int)G.classes.size();
     // forward + backward sweep of every class; classes after the first on forked streams
     auto precondition = [&](bool onP) {
+        if (B->amg) {
+            TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
+            for (const auto& a : onP ? G.amgP : G.amgR)
+                launchAmgPassBatch<PT>(a.kind, static_cast<const AmgPass<PT>*>(a.passes), a.map.map, a.map.blocks, dim,
+                                       b, st);
+            return;
+        }
         if (B->redBlack) {
             TimedB tb(B, DXG_KC_ILU_SWEEP, G.sweepBytes);
             launchRbApplyBatch<PT>(static_cast<const RbArgs<PT>*>(onP ? G.dRbP : G.dRbR), G.mapH, b, dim, st);
@@ -890,7 +1024,8 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
 template <class PT>
 void runChunk(dxg_batch* B, GroupState& G, int n, int dim, int b)
 {
-    const int launchesPerIt = 5 + (B->redBlack ? 4 : 4 * (int)G.classes.size());
+    const int launchesPerIt =
+        5 + (B->amg ? (int)(G.amgP.size() + G.amgR.size()) : (B->redBlack ? 4 : 4 * (int)G.classes.size()));
     cudaStream_t st = B->stream;
     if (B->graphs && !B->timing && !G.exec && !G.graphTried) {
         G.graphTried = true;
@@ -1003,7 +1138,7 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
         fl[k] = {c->ks.get(), c->scal.get(), c->singular.get()};
         // the factor must not skip: no Krylov state
         if (B->redBlack) rf[k] = rbArgsOf<PT>(c, nullptr);
-        else
+        else if (!B->amg)
             fa[k] = waveArgsOf<PT>(c, G.geo[idx[k]], Pre<PT>::A(c), Pre<PT>::L(c), Pre<PT>::Dinv(c), nullptr,
                                    nullptr, nullptr);
         BicgArgs<double> a = krylovArgs(c, mixed);
@@ -1024,6 +1159,47 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
     }
     clearFlagsKernel<<<(n + 127) / 128, 128, 0, st>>>(B->arena.put(fl, st), n);
     DXG_CUDA(cudaGetLastError());
+    if (B->amg) {
+        // AMG setup: pivots of level 0, each coarse operator from the one above, the last
+        // level's dense inverse
+        std::vector<std::vector<AmgLevel<PT>>> lv;
+        size_t dmax = 0;
+        int64_t maxLast = 1;
+        for (Slot* s : A) {
+            dxg_ctx* c = s->c;
+            lv.push_back(amgLevelsOf<PT>(c, Pre<PT>::A(c), Pre<PT>::Dinv(c), nullptr, nullptr));
+            dmax = std::max(dmax, lv.back().size());
+            maxLast = std::max(maxLast, lv.back().back().N);
+        }
+        auto run = [&](int kind, size_t l) {
+            std::vector<AmgPass<PT>> ps;
+            std::vector<uint2> mp;
+            for (size_t k = 0; k < lv.size(); ++k) {
+                if (l >= lv[k].size()) continue;
+                AmgPass<PT> p{};
+                p.L = kind == AMG_DIAGINV ? lv[k][0] : lv[k][l - 1];
+                if (kind == AMG_COARSEN) p.C = lv[k][l];
+                p.singular = A[k]->c->singular.get();
+                const unsigned nb = amgPassBlocks(kind == AMG_COARSEN ? p.C.N : p.L.N);
+                for (unsigned j = 0; j < nb; ++j) mp.push_back(make_uint2((unsigned)ps.size(), j));
+                ps.push_back(p);
+            }
+            if (ps.empty()) return;
+            launchAmgPassBatch<PT>(kind, B->arena.put(ps, st), B->arena.put(mp, st), (unsigned)mp.size(), dim, b, st);
+            B->launches += 1;
+        };
+        run(AMG_DIAGINV, 0);
+        for (size_t l = 1; l < dmax; ++l) run(AMG_COARSEN, l);
+        std::vector<AmgPass<PT>> inv;
+        for (size_t k = 0; k < lv.size(); ++k) {
+            AmgPass<PT> p{};
+            p.L = lv[k].back();
+            p.singular = A[k]->c->singular.get();
+            inv.push_back(p);
+        }
+        launchAmgInvertBatch<PT>(B->arena.put(inv, st), (int)inv.size(), (int)maxLast, dim, b, st);
+        B->launches += 1;
+    }
     if (B->redBlack) {
         std::vector<int64_t> lenH;
         for (Slot* s : A) lenH.push_back(rbSlots((int)s->c->pcHost.nx, (int)s->c->pcHost.ny, (int)s->c->pcHost.nz));
@@ -1261,6 +1437,13 @@ int dxg_batch_set_option(dxg_batch* b, int option, int value)
     else if (option == DXG_BATCH_OPT_AUTOTUNE) {
         b->autotune = value != 0;
         b->plans.clear();
+    } else if (option == DXG_BATCH_OPT_AMG) {
+        if (!b->slots.empty()) {
+            b->err = "the linear solver is chosen before problems are added";
+            return DXG_ERR_STATE;
+        }
+        b->amg = value != 0;
+        b->groups.clear();
     } else if (option == DXG_BATCH_OPT_ILU_REDBLACK) {
         if (!b->slots.empty()) {
             b->err = "the ILU(0) ordering is chosen before problems are added";
@@ -1433,6 +1616,7 @@ int dxg_batch_describe(const dxg_batch* b, char* buf, int64_t len)
         out += "group num_eq=" + std::to_string(std::get<0>(k)) + " dim=" + std::to_string(std::get<1>(k)) +
                " problems=" + std::to_string(G.ids.size()) + ":";
         if (b->redBlack) out += " [red-black ILU(0): two parallel passes per sweep]";
+        if (b->amg) out += " [AMG-BiCGSTAB: " + std::to_string(G.amgP.size()) + " batched passes per V-cycle]";
         for (const SweepClass& sc : G.classes)
             out += " [" + std::to_string(sc.members.size()) + " problems: cluster " + std::to_string(sc.plan.ctas) +
                    " x " + std::to_string(sc.plan.threads) + " threads, prefetch " + std::to_string(sc.plan.pf) +

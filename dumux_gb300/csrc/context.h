@@ -4,6 +4,7 @@
 #include <string>
 #include <vector>
 
+#include "amg.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 #include "linalg_kernels.cuh"
@@ -107,3 +108,11 @@ struct dxg_ctx {
     dxg::AssemblyArgs asmArgs() const;
     dxg::ReduceScratch scratch() const { return {partials.get(), counters.get()}; }
 };
+
+namespace dxg {
+// The aggregation AMG levels of a context in value type T (level 0: the Jacobian A with
+// the inverted pivots Dinv, the preconditioner input `in` and output `out`); the coarse
+// levels live in the context's AMG allocation, made on first use.
+template <class T>
+std::vector<AmgLevel<T>> amgLevelsOf(dxg_ctx* c, const T* A, T* Dinv, const T* in, T* out);
+}  // namespace dxg

@@ -32,9 +32,9 @@ class Server:
     """
 
     def __init__(self, device=0, precision="mixed", memory_budget=0, params=None, graphs=True, autotune=True,
-                 ilu="natural"):
+                 ilu="natural", solver="ilu"):
         self.batch = Batch(device=device, precision=precision, graphs=graphs, autotune=autotune,
-                           memory_budget=memory_budget, ilu=ilu)
+                           memory_budget=memory_budget, ilu=ilu, solver=solver)
         default_iter = 1000 if ilu == "redblack" else 500
         self.params = params if params is not None else newton_params(linear_max_iter=default_iter)
 

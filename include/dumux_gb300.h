@@ -338,7 +338,7 @@ typedef struct dxg_batch_problem_info {
     double seconds_finished;     /* engine clock when it finished or failed, else -1   */
 } dxg_batch_problem_info;
 
-enum { DXG_BATCH_OPT_GRAPHS = 0, DXG_BATCH_OPT_AUTOTUNE = 1, DXG_BATCH_OPT_ILU_REDBLACK = 2 };
+enum { DXG_BATCH_OPT_GRAPHS = 0, DXG_BATCH_OPT_AUTOTUNE = 1, DXG_BATCH_OPT_ILU_REDBLACK = 2, DXG_BATCH_OPT_AMG = 3 };
 
 int dxg_batch_create(dxg_batch** out, int device, int precision);
 int dxg_batch_destroy(dxg_batch* batch);
@@ -349,7 +349,9 @@ const char* dxg_batch_last_error(const dxg_batch* batch);
  * solve of each batch shape (default 1; 0 uses a fixed rule).  DXG_BATCH_OPT_ILU_REDBLACK:
  * red-black ordered ILU(0) (as DXG_ILU_REDBLACK for a context) for every problem of the
  * batch (default 0, natural order); set before the first dxg_batch_add, else
- * DXG_ERR_STATE. */
+ * DXG_ERR_STATE.  DXG_BATCH_OPT_AMG: AMG-BiCGSTAB (as DXG_LINEAR_SOLVER_AMG_BICGSTAB for a
+ * context) for every problem of the batch, each V-cycle pass batched over the problems
+ * that have that level (default 0); set before the first dxg_batch_add. */
 int dxg_batch_set_option(dxg_batch* batch, int option, int value);
 /* Device memory that admitting this problem takes (tables and all solver state). */
 int64_t dxg_problem_device_bytes(const dxg_problem_desc* desc, int precision);

@@ -171,3 +171,37 @@ def test_newton_with_amg_matches_oracle_fields(precision, tol):
     uo = u_orc.reshape(-1, 2)
     err = np.max(np.abs(u - uo), axis=0) / np.max(np.abs(uo), axis=0)
     assert np.all(err <= tol), err
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_amg_batch_equals_single_problems(precision):
+    """DXG_BATCH_OPT_AMG: uneven grids (different level counts) in one batch, each result
+    bit-identical to the same problem alone in a context with AMG-BiCGSTAB."""
+    from dumux_gb300 import Batch
+    params = newton_params(linear_max_iter=500)
+    cases = [((8, 6, 5), 11, 0.5), ((24, 20, 12), 12, 2.0), ((7, 9, 4), 13, 1.2), ((30, 22), 15, 1.0),
+             ((40, 33, 17), 16, 1.5)]
+    batch = Batch(precision=precision, solver="amg")
+    ids = []
+    for cells, seed, sigma in cases:
+        desc, u0 = problems.dnapl_2p(cells=cells, extent=(6.0, 4.0, 1.0)[:len(cells)], seed=seed, sigma=sigma,
+                                     corr_len=4.0)
+        ids.append((batch.add(desc, u0, dt=250.0, t_end=500.0, params=params), desc, u0))
+    batch.run()
+    assert "AMG" in batch.describe()
+    for pid, desc, u0 in ids:
+        info = batch.info(pid)
+        assert info["state"] == "finished"
+        ctx = Context(desc, precision=precision)
+        ctx.set_linear_solver("amg")
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        t, iters, dt = 0.0, 0, 250.0
+        while t < 500.0 - 1e-6:
+            rep = ctx.newton_solve(dt, params)
+            iters += rep["iterations"] + rep["wasted_iterations"]
+            t += rep["dt_used"]
+            ctx.advance_time_step()
+            dt = min(ctx.suggest_time_step(rep["dt_used"], params), 250.0, 500.0 - t)
+        assert info["newton_iterations"] == iters
+        assert np.array_equal(batch.solution(pid), ctx.solution()), desc.cells
