@@ -1365,6 +1365,27 @@ int64_t problemBytes(int64_t N, int64_t nb, int b, int dim, int method, int prec
     return by + 64 * 1024;                                                       // allocation granularity
 }
 
+// Device memory of a problem's AMG levels (the layout of amgLevelsOf): two fine-level
+// vectors, per coarse level its operator, pivots and four vectors, the last level's dense
+// inverse.
+int64_t amgBytes(const dxg_problem_desc* d, int precision)
+{
+    const int64_t val = precision == DXG_PRECISION_FP64 ? 8 : 4;
+    const int dim = d->dim, b = d->num_eq, S = 2 * dim + 1;
+    const int64_t bb = (int64_t)b * b;
+    int64_t N = 1;
+    for (int a = 0; a < dim; ++a) N *= d->cells[a];
+    auto align = [](int64_t v) { return (v + 255) & ~(int64_t)255; };
+    int64_t by = 2 * align(N * b * val);
+    const auto dims = amgLevelDims(dim, (int)d->cells[0], (int)d->cells[1], dim == 3 ? (int)d->cells[2] : 1);
+    for (const auto& l : dims) {
+        const int64_t n = (int64_t)l[0] * l[1] * l[2];
+        by += align(S * n * bb * val) + align(n * bb * val) + 4 * align(n * b * val);
+    }
+    const int64_t nLast = dims.empty() ? N : (int64_t)dims.back()[0] * dims.back()[1] * dims.back()[2];
+    return by + align(nLast * b * nLast * b * val);
+}
+
 }  // namespace
 
 // ================================================================ C ABI
@@ -1480,11 +1501,12 @@ int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, dou
                   double t_end, const dxg_newton_params* params, int64_t* id)
 {
     if (!b || !d || !u0 || !id) return DXG_ERR_ARG;
-    const int64_t need = dxg_problem_device_bytes(d, b->precision);
+    int64_t need = dxg_problem_device_bytes(d, b->precision);
     if (need < 0) {
         b->err = "invalid problem description";
         return DXG_ERR_ARG;
     }
+    if (b->amg) need += amgBytes(d, b->precision);
     if (b->budget > 0 && b->bytesInUse + need > b->budget) {
         b->err = "admission would exceed the device-memory budget";
         return DXG_ERR_BUDGET;
