@@ -205,3 +205,41 @@ def test_amg_batch_equals_single_problems(precision):
             dt = min(ctx.suggest_time_step(rep["dt_used"], params), 250.0, 500.0 - t)
         assert info["newton_iterations"] == iters
         assert np.array_equal(batch.solution(pid), ctx.solution()), desc.cells
+
+
+def test_amg_continuous_batching_mixed_kinds_equal_alone():
+    """AMG batches with requests of different kinds (1p 2D stationary, 2p 2D and 3D
+    transient) admitted while others are in flight: each result equals the one computed
+    alone with AMG-BiCGSTAB."""
+    from dumux_gb300 import Batch
+    params = newton_params(linear_max_iter=500)
+    first = [problems.dnapl_2p(cells=(9, 7, 5), seed=21, corr_len=4.0) + (250.0, 500.0),
+             problems.darcy_1p(cells=(30, 26), seed=22, corr_len=3.0) + (0.0, 0.0)]
+    later = [problems.dnapl_2p(cells=(20, 14), extent=(6.0, 4.0), seed=24, corr_len=4.0) + (100.0, 300.0),
+             problems.darcy_1p(cells=(9, 14), seed=25, corr_len=2.0) + (0.0, 0.0)]
+    batch = Batch(precision="mixed", solver="amg")
+    admitted = []
+    for desc, u0, dt, t_end in first:
+        admitted.append((batch.add(desc, u0, dt=dt, t_end=t_end, params=params), desc, u0, dt, t_end))
+    batch.iterate()
+    for desc, u0, dt, t_end in later:
+        admitted.append((batch.add(desc, u0, dt=dt, t_end=t_end, params=params), desc, u0, dt, t_end))
+    while batch.iterate() > 0:
+        pass
+    for pid, desc, u0, dt, t_end in admitted:
+        info = batch.info(pid)
+        assert info["state"] == "finished", (desc.cells, info)
+        ctx = Context(desc, precision="mixed")
+        ctx.set_linear_solver("amg")
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        if t_end <= 0.0:
+            ctx.newton_solve(0.0, params)
+        else:
+            t, cur = 0.0, min(dt, t_end)
+            while t_end - t > 1e-9 * t_end:
+                rep = ctx.newton_solve(cur, params)
+                t += rep["dt_used"]
+                ctx.advance_time_step()
+                cur = min(ctx.suggest_time_step(rep["dt_used"], params), dt, t_end - t)
+        assert np.array_equal(batch.solution(pid), ctx.solution()), (desc.cells, desc.num_eq)
