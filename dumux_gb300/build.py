@@ -71,7 +71,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

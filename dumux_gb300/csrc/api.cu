@@ -7,10 +7,13 @@
 // dumux/discretization/cellcentered/tpfa/computetransmissibility.hh:66-80) and so are
 // bit-identical to what the reference evaluates for every face.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
+#include <thread>
 #include <vector>
 
 #include "amg.cuh"
@@ -198,6 +201,34 @@ dxg::AssemblyArgs dxg_ctx::asmArgs() const
 
 namespace {
 
+// f(begin, end) over [0, n) in contiguous chunks on the host's cores (at most 16 threads);
+// every index belongs to exactly one chunk, so loops whose iterations write disjoint
+// entries give the same tables as the serial loop.  The first exception is rethrown.
+template <class F>
+void parallelFor(int64_t n, F&& f)
+{
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nt = (int)std::min<int64_t>({(int64_t)std::min(hw, 16), (n + 32767) / 32768, (int64_t)16});
+    if (nt <= 1) {
+        f((int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> err(nt);
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            try {
+                f(std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
+            } catch (...) {
+                err[t] = std::current_exception();
+            }
+        });
+    for (auto& x : th) x.join();
+    for (auto& e : err)
+        if (e) std::rethrow_exception(e);
+}
+
 // ---------------------------------------------------------------- tabulation
 void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
 {
@@ -293,7 +324,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     std::vector<uint8_t> nbmask(N, 0);
     auto K = [&](int64_t i) { return d->permeability[i]; };
     auto EX = [&](int64_t i) { return d->extrusion ? d->extrusion[i] : 1.0; };
-    for (int64_t i = 0; i < N; ++i) {
+    parallelFor(N, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
         int64_t id[3];
         g.ijk(i, id);
         vol[i] = g.volume(id);
@@ -318,9 +350,12 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
         }
         nbmask[i] = (uint8_t)m;
     }
+    });
     // interior faces: transmissibility of the + face of every axis, gravity terms of the
-    // vertical faces (both orientations)
-    for (int64_t i = 0; i < N; ++i) {
+    // vertical faces (both orientations; the entry of each (face side, cell) is written by
+    // exactly one iteration)
+    parallelFor(N, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
         int64_t id[3];
         g.ijk(i, id);
         double ci[3];
@@ -371,6 +406,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
             }
         }
     }
+    });
     // boundary faces
     std::vector<int8_t> btype(nb);
     std::vector<double> bTij(nb, 0.0), bG1((size_t)b * nb, 0.0), bP((size_t)b * nb, 0.0), bU((size_t)b * nb, 0.0),
