@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <tuple>
@@ -195,9 +196,7 @@ struct dxg_batch {
     DevBuf<int> tuneFlags;
     SlotReport* reportsHost = nullptr;
     size_t reportsCap = 0;
-    std::map<std::tuple<int, int, int, int, int>, WaveBatchPlan> plans;   // autotuned sweep shapes
     std::map<GroupKey, std::unique_ptr<GroupState>> groups;              // per kind: chunk arguments, graph
-    std::map<std::vector<int>, std::vector<WaveBatchPlan>> jointPlans;   // class shapes refined together
     std::chrono::steady_clock::time_point epoch = std::chrono::steady_clock::now();
 
     // optional event timing per kernel class (direct launches while it is on)
@@ -541,17 +540,36 @@ std::tuple<int, int, int, int, int> shapeKey(const Members& S, int dim, int b, i
                            (mx[2] + 15) / 16);
 }
 
+// Tuned sweep shapes, shared by every batch of the process on the same device (a shape
+// depends on the problems' extents and the GPU, not on the batch object): a new batch of
+// known shapes starts without re-timing candidates.
+struct TuneCache {
+    std::mutex m;
+    std::map<std::tuple<int, int, std::tuple<int, int, int, int, int>>, WaveBatchPlan> plans;
+    std::map<std::tuple<int, std::vector<int>>, std::vector<WaveBatchPlan>> joint;
+};
+TuneCache& tuneCache()
+{
+    static TuneCache c;
+    return c;
+}
+
 template <class PT>
 WaveBatchPlan planFor(dxg_batch* B, const Members& S, int dim, int b)
 {
-    const auto key = shapeKey(S, dim, b, (int)sizeof(PT));
-    auto it = B->plans.find(key);
-    if (it != B->plans.end()) {
-        WaveBatchPlan p = it->second;
-        if (completeWaveBatchPlan(p, geomsFor(S, p.ctas), dim, b, sizeof(PT) == 8) > 0) return p;
+    const auto key = std::make_tuple(B->device, (int)B->autotune, shapeKey(S, dim, b, (int)sizeof(PT)));
+    TuneCache& tc = tuneCache();
+    {
+        std::lock_guard<std::mutex> lock(tc.m);
+        auto it = tc.plans.find(key);
+        if (it != tc.plans.end()) {
+            WaveBatchPlan p = it->second;
+            if (completeWaveBatchPlan(p, geomsFor(S, p.ctas), dim, b, sizeof(PT) == 8) > 0) return p;
+        }
     }
     WaveBatchPlan p = tunePlan<PT>(B, S, dim, b);
-    B->plans[key] = p;
+    std::lock_guard<std::mutex> lock(tc.m);
+    tc.plans[key] = p;
     return p;
 }
 
@@ -635,10 +653,17 @@ void refineClassPlans(dxg_batch* B, std::vector<SweepClass>& classes, const Memb
         const auto k = shapeKey(subs[q], dim, b, (int)sizeof(PT));
         jkey.insert(jkey.end(), {std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k)});
     }
-    auto cached = B->jointPlans.find(jkey);
-    if (cached != B->jointPlans.end()) {
+    TuneCache& tc = tuneCache();
+    const auto ckey = std::make_tuple(B->device, jkey);
+    std::vector<WaveBatchPlan> known;
+    {
+        std::lock_guard<std::mutex> lock(tc.m);
+        auto cached = tc.joint.find(ckey);
+        if (cached != tc.joint.end()) known = cached->second;
+    }
+    if (!known.empty()) {
         bool ok = true;
-        std::vector<WaveBatchPlan> plans = cached->second;
+        std::vector<WaveBatchPlan> plans = known;
         for (int q = 0; q < nc && ok; ++q)
             ok = completeWaveBatchPlan(plans[q], geomsFor(subs[q], plans[q].ctas), dim, b, sizeof(PT) == 8) > 0;
         if (ok) {
@@ -712,7 +737,10 @@ void refineClassPlans(dxg_batch* B, std::vector<SweepClass>& classes, const Memb
     int flags[2] = {0, 0};
     DXG_CUDA(cudaMemcpy(flags, B->tuneFlags.get(), sizeof(flags), cudaMemcpyDeviceToHost));
     if (flags[1]) throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out while tuning");
-    B->jointPlans[jkey] = plans;
+    {
+        std::lock_guard<std::mutex> lock(tc.m);
+        tc.joint[ckey] = plans;
+    }
     for (int q = 0; q < nc; ++q) classes[q].plan = plans[q];
 }
 
@@ -1457,7 +1485,6 @@ int dxg_batch_set_option(dxg_batch* b, int option, int value)
     if (option == DXG_BATCH_OPT_GRAPHS) b->graphs = value != 0;
     else if (option == DXG_BATCH_OPT_AUTOTUNE) {
         b->autotune = value != 0;
-        b->plans.clear();
     } else if (option == DXG_BATCH_OPT_AMG) {
         if (!b->slots.empty()) {
             b->err = "the linear solver is chosen before problems are added";

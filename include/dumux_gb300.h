@@ -346,7 +346,8 @@ const char* dxg_batch_last_error(const dxg_batch* batch);
 /* DXG_BATCH_OPT_GRAPHS: replay the BiCGSTAB iterations of a solve from one captured
  * CUDA graph (default 1).  DXG_BATCH_OPT_AUTOTUNE: choose the cluster size, threads
  * and prefetch depth of the batched ILU(0) sweeps by timing candidates on the first
- * solve of each batch shape (default 1; 0 uses a fixed rule).  DXG_BATCH_OPT_ILU_REDBLACK:
+ * solve of each batch shape, kept for every batch of the process on that device
+ * (default 1; 0 uses a fixed rule).  DXG_BATCH_OPT_ILU_REDBLACK:
  * red-black ordered ILU(0) (as DXG_ILU_REDBLACK for a context) for every problem of the
  * batch (default 0, natural order); set before the first dxg_batch_add, else
  * DXG_ERR_STATE.  DXG_BATCH_OPT_AMG: AMG-BiCGSTAB (as DXG_LINEAR_SOLVER_AMG_BICGSTAB for a
