@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -509,6 +510,16 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     }
 
     cudaStream_t st = c->stream;
+    // the first upload carves its buffers from one allocation of the problem's size
+    std::unique_ptr<DevBlockScope> carve;
+    if (!c->uploadBlock.get()) {
+        const int64_t need = dxg_problem_device_bytes(d, c->precision);
+        if (need > 0) {
+            c->uploadBlock.alloc((size_t)need);
+            c->uploadCarve = DevBlock{c->uploadBlock.get(), (size_t)need, 0};
+            carve.reset(new DevBlockScope(&c->uploadCarve));
+        }
+    }
     c->pcDev.alloc(1);
     DXG_CUDA(cudaMemcpyAsync(c->pcDev.get(), &c->pcHost, sizeof(ProblemConsts), cudaMemcpyHostToDevice, st));
     upload(c->vol, vol, st);
@@ -1150,8 +1161,12 @@ int dxg_ctx_create(dxg_ctx** out, int device)
         c->device = device;
         DXG_CUDA(cudaSetDevice(device));
         DXG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-        DXG_CUDA(cudaMallocHost(&c->ksHost, sizeof(KrylovState)));
-        DXG_CUDA(cudaMallocHost(&c->scalHost, 4 * sizeof(double)));
+        // one pinned allocation for the Krylov state and the scalars read back
+        const size_t ksBytes = (sizeof(KrylovState) + 63) & ~(size_t)63;
+        void* pinned = nullptr;
+        DXG_CUDA(cudaMallocHost(&pinned, ksBytes + 4 * sizeof(double)));
+        c->ksHost = static_cast<KrylovState*>(pinned);
+        c->scalHost = reinterpret_cast<double*>(static_cast<unsigned char*>(pinned) + ksBytes);
         return DXG_OK;
     });
     if (st != DXG_OK) {
@@ -1174,8 +1189,7 @@ int dxg_ctx_destroy(dxg_ctx* c)
     }
     for (auto e : c->eventPool) cudaEventDestroy(e);
     c->dropGraphs();
-    if (c->ksHost) cudaFreeHost(c->ksHost);
-    if (c->scalHost) cudaFreeHost(c->scalHost);
+    if (c->ksHost) cudaFreeHost(c->ksHost);   // also holds scalHost
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return DXG_OK;

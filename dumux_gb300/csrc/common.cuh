@@ -25,26 +25,56 @@ struct Error : std::runtime_error {
                                std::string(#call) + ": " + cudaGetErrorString(e_));          \
     } while (0)
 
-// Owning device buffer.
+// One device allocation that the buffers of a problem upload are carved from: while a
+// thread has a block installed (DevBlockScope), DevBuf::alloc takes 256-byte aligned pieces
+// of it instead of calling cudaMalloc once per buffer.  The owner keeps the block alive
+// for as long as the buffers carved from it.
+struct DevBlock {
+    unsigned char* base = nullptr;
+    size_t cap = 0, used = 0;
+};
+inline DevBlock*& currentDevBlock()
+{
+    thread_local DevBlock* b = nullptr;
+    return b;
+}
+struct DevBlockScope {
+    DevBlock* prev;
+    explicit DevBlockScope(DevBlock* b) : prev(currentDevBlock()) { currentDevBlock() = b; }
+    ~DevBlockScope() { currentDevBlock() = prev; }
+};
+
+// Owning device buffer (or a piece of the installed DevBlock, which it does not free).
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
+    bool owned = true;
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p && owned) cudaFree(p);
         p = nullptr;
         n = 0;
+        owned = true;
     }
     void alloc(size_t count)
     {
         if (count == n && p) return;
         release();
         if (count == 0) return;
+        const size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+        DevBlock* blk = currentDevBlock();
+        if (blk && blk->used + bytes <= blk->cap) {
+            p = reinterpret_cast<T*>(blk->base + blk->used);
+            blk->used += bytes;
+            owned = false;
+            n = count;
+            return;
+        }
         DXG_CUDA(cudaMalloc(&p, count * sizeof(T)));
         n = count;
     }

@@ -11,6 +11,10 @@
 #include "wave.cuh"
 
 struct dxg_ctx {
+    // the device memory the first upload's buffers are carved from (declared first, so
+    // it is released after every buffer)
+    dxg::DevBuf<unsigned char> uploadBlock;
+    dxg::DevBlock uploadCarve;
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
