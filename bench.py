@@ -185,7 +185,7 @@ def measured_peaks():
 # dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
 # of the 64x64x32 FP64 system, from the ncu capture summarised in
 # profiles/ilu_sweep_64x64x32_fp64.md (cold-cache, serialised launches).
-ILU_TRAFFIC_PER_APPLY_64x64x32 = 14511616 + 18709760
+ILU_TRAFFIC_PER_APPLY_64x64x32 = 14537472 + 18714112
 # DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from the ncu capture
 # of the 32-problem ensemble (2,379,154 cells) in profiles/ilu_sweep_batched_ensemble32_mixed.md;
 # traffic scales with the cells swept (each block and vector entry is moved once)
