@@ -690,6 +690,16 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
                                 "sample": f"first {n_cpu} Newton iterations of one time step "
                                           f"({sec_cpu:.1f} s; threaded assembly, sequential ILU0-BiCGSTAB)"}
+        if args.cpu_sample_iters > 0:
+            # the same sample on one core (the reference's assembly without coloured threads)
+            threads = oracle.get_threads()
+            oracle.set_threads(1)
+            try:
+                rate1, sec1, n1 = cpu_sample(desc, u_start, args.dt, 1)
+            finally:
+                oracle.set_threads(threads)
+            line["cpu_baseline"]["single_core"] = {"value": rate1, "unit": UNIT,
+                                                   "sample": f"first {n1} Newton iteration ({sec1:.1f} s)"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
