@@ -104,6 +104,7 @@ def lib():
                                                   C.POINTER(C.c_double)]
         L.dxg_selftest_bounded_wait.argtypes = [C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
                                                 C.POINTER(C.c_double)]
+        L.dxg_device_pow.argtypes = [C.c_int, dp, dp, dp, C.c_int64]
         L.dxg_batch_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_batch_stream.argtypes = [vp]
@@ -381,6 +382,19 @@ def selftest_bounded_wait(kind="mbarrier", limit_ms=2.0, device=0):
     return STATUS_NAMES.get(st.value, st.value), ms.value
 
 
+def device_pow(x, y, device=0):
+    """pow(x, y) element-wise on the device with the material laws' correctly rounded pow
+    (dxg_device_pow); y broadcasts against x."""
+    import numpy as np
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.broadcast_to(y, x.shape), dtype=np.float64)
+    out = np.empty_like(x)
+    rc = lib().dxg_device_pow(int(device), _dp(x), _dp(y), _dp(out), x.size)
+    if rc != 0:
+        raise DxgError(rc, "dxg_device_pow failed")
+    return out
+
+
 def problem_device_bytes(desc, precision="mixed"):
     """Device memory a problem takes once admitted (dxg_problem_device_bytes)."""
     prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
@@ -501,4 +515,4 @@ class Batch:
 
 __all__ = ["Context", "FVAssembler", "ILUBiCGSTABIstlSolver", "NewtonSolver", "ProblemDesc", "newton_params",
            "DxgError", "NumericalProblem", "lib", "LIB_PATH", "Batch", "problem_device_bytes",
-           "selftest_bounded_wait"]
+           "selftest_bounded_wait", "device_pow"]

@@ -578,3 +578,35 @@ void launchRowBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, i
 }
 
 }  // namespace dxg
+
+// ---------------------------------------------------------------- device pow check
+namespace dxg {
+__global__ void powKernel(const double* x, const double* y, double* out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = crPow(x[i], y[i]);
+}
+
+int runDevicePow(const double* x, const double* y, double* out, int64_t n)
+{
+    if (n == 0) return DXG_OK;
+    double* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return DXG_ERR_OOM;
+    }
+    int rc = DXG_OK;
+    if (cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, y, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = DXG_ERR_CUDA;
+    if (rc == DXG_OK) {
+        const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+        powKernel<<<(unsigned)blocks, 256>>>(d, d + n, d + 2 * n, n);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = DXG_ERR_CUDA;
+    }
+    if (rc == DXG_OK && cudaMemcpy(out, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = DXG_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+}  // namespace dxg

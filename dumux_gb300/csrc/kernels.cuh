@@ -56,4 +56,8 @@ void launchPrevStorageBatch(const AssemblyArgs* batch, int count, int64_t maxN, 
 void launchRowBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, int dim, int method, bool jac, bool grav,
                     bool transient, bool fullup, cudaStream_t st);
 
+// Element-wise correctly rounded pow (crpow.cuh) of host arrays on the current device
+// (diagnostic: checks the device's pow against the host's).
+int runDevicePow(const double* x, const double* y, double* out, int64_t n);
+
 }  // namespace dxg

@@ -9,12 +9,15 @@
 //   kind 1: VanGenuchtenDefault (vangenuchten.hh:30-300 base law, 304-620 regularisation
 //           with two-point cubic splines, common/spline.hh and common/splinecommon_.hh)
 // The device compiles these without FMA contraction (assemble.cu, --fmad=false) and the
-// host with -ffp-contract=off, so both evaluate the reference's operation sequence.
+// host with -ffp-contract=off, so both evaluate the reference's operation sequence.  The
+// reference's std::pow is replaced by the correctly rounded crPow (crpow.cuh) on host and
+// device alike.
 #pragma once
 
 #include <cmath>
 
 #include "common.cuh"
+#include "crpow.cuh"
 
 namespace dxg {
 
@@ -44,38 +47,38 @@ __host__ __device__ inline double splineDerivative(const Spline2& s, double x)
 __host__ __device__ inline double vgPcBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
-    return pow(pow(swe, m.vgNegInvM) - 1, m.vgInvN) / m.vgAlpha;
+    return crPow(crPow(swe, m.vgNegInvM) - 1, m.vgInvN) / m.vgAlpha;
 }
 __host__ __device__ inline double vgDpcDsweBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
-    const double powSwe = pow(swe, -1 / m.vgM);
-    return -1.0 / m.vgAlpha * pow(powSwe - 1, 1.0 / m.vgN - 1) / m.vgN * powSwe / swe / m.vgM;
+    const double powSwe = crPow(swe, -1 / m.vgM);
+    return -1.0 / m.vgAlpha * crPow(powSwe - 1, 1.0 / m.vgN - 1) / m.vgN * powSwe / swe / m.vgM;
 }
 __host__ __device__ inline double vgKrwBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
-    const double r = 1.0 - pow(1.0 - pow(swe, m.vgInvM), m.vgM);
-    return pow(swe, m.vgL) * r * r;
+    const double r = 1.0 - crPow(1.0 - crPow(swe, m.vgInvM), m.vgM);
+    return crPow(swe, m.vgL) * r * r;
 }
 __host__ __device__ inline double vgDkrwDsweBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
-    const double x = 1.0 - pow(swe, 1.0 / m.vgM);
-    const double xToM = pow(x, m.vgM);
-    return (1.0 - xToM) * pow(swe, m.vgL - 1) * ((1.0 - xToM) * m.vgL + 2 * xToM * (1.0 - x) / x);
+    const double x = 1.0 - crPow(swe, 1.0 / m.vgM);
+    const double xToM = crPow(x, m.vgM);
+    return (1.0 - xToM) * crPow(swe, m.vgL - 1) * ((1.0 - xToM) * m.vgL + 2 * xToM * (1.0 - x) / x);
 }
 __host__ __device__ inline double vgKrnBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
-    return pow(1 - swe, m.vgL) * pow(1 - pow(swe, m.vgInvM), 2 * m.vgM);
+    return crPow(1 - swe, m.vgL) * crPow(1 - crPow(swe, m.vgInvM), 2 * m.vgM);
 }
 __host__ __device__ inline double vgDkrnDsweBase(const MaterialLaw& m, double swe)
 {
     swe = clamp01(swe);
     const double sne = 1.0 - swe;
-    const double x = 1.0 - pow(swe, 1.0 / m.vgM);
-    return -pow(sne, m.vgL - 1.0) * pow(x, 2 * m.vgM - 1.0) * (m.vgL * x + 2.0 * sne / swe * (1.0 - x));
+    const double x = 1.0 - crPow(swe, 1.0 / m.vgM);
+    return -crPow(sne, m.vgL - 1.0) * crPow(x, 2 * m.vgM - 1.0) * (m.vgL * x + 2.0 * sne / swe * (1.0 - x));
 }
 
 // ---------------------------------------------------------------- regularised laws
@@ -87,7 +90,7 @@ __host__ __device__ inline double lawPc(const MaterialLaw& m, double sw)
     if (m.kind == 0) {
         if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
         else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0) + m.entryPressure;
-        return m.pe * pow(clamp01(swe), m.expPc);
+        return m.pe * crPow(clamp01(swe), m.expPc);
     }
     if (swe <= m.pcLowSwe) return m.pcLowSwePcValue + m.pcDerivativeLowSw * (swe - m.pcLowSwe);
     else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * (swe - 1.0);
@@ -99,7 +102,7 @@ __host__ __device__ inline double lawKrw(const MaterialLaw& m, double sw)
     const double swe = lawSwe(m, sw);
     if (swe <= 0.0) return 0.0;
     else if (swe >= 1.0) return 1.0;
-    if (m.kind == 0) return pow(clamp01(swe), m.expKrw);
+    if (m.kind == 0) return crPow(clamp01(swe), m.expKrw);
     if (swe >= m.krwHighSwe) return splineEval(m.krwSpline, swe);
     return vgKrwBase(m, swe);
 }
@@ -111,7 +114,7 @@ __host__ __device__ inline double lawKrn(const MaterialLaw& m, double sw)
     if (m.kind == 0) {
         const double s = clamp01(swe);
         const double sne = 1.0 - s;
-        return sne * sne * (1.0 - pow(s, m.expKrn));
+        return sne * sne * (1.0 - crPow(s, m.expKrn));
     }
     if (swe <= m.krnLowSwe) return splineEval(m.krnSpline, swe);
     return vgKrnBase(m, swe);
@@ -121,7 +124,7 @@ __host__ __device__ inline double lawDpcDsw(const MaterialLaw& m, double sw)
     const double swe = lawSwe(m, sw);
     if (swe <= m.pcLowSwe) return m.pcDerivativeLowSw * m.dsweDsw;
     else if (swe >= 1.0) return m.pcDerivativeHighSwEnd * m.dsweDsw;
-    if (m.kind == 0) return m.dpcCoef * pow(clamp01(swe), m.dpcExp) * m.dsweDsw;
+    if (m.kind == 0) return m.dpcCoef * crPow(clamp01(swe), m.dpcExp) * m.dsweDsw;
     if (swe > m.pcHighSwe) return splineDerivative(m.pcSpline, swe) * m.dsweDsw;
     return vgDpcDsweBase(m, swe) * m.dsweDsw;
 }
@@ -129,7 +132,7 @@ __host__ __device__ inline double lawDkrwDsw(const MaterialLaw& m, double sw)
 {
     const double swe = lawSwe(m, sw);
     if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
-    if (m.kind == 0) return m.dkrwCoef * pow(clamp01(swe), m.dkrwExp) * m.dsweDsw;
+    if (m.kind == 0) return m.dkrwCoef * crPow(clamp01(swe), m.dkrwExp) * m.dsweDsw;
     if (swe >= m.krwHighSwe) return splineDerivative(m.krwSpline, swe) * m.dsweDsw;
     return vgDkrwDsweBase(m, swe) * m.dsweDsw;
 }
@@ -139,7 +142,7 @@ __host__ __device__ inline double lawDkrnDsw(const MaterialLaw& m, double sw)
     if (swe <= 0.0 || swe >= 1.0) return 0.0 * m.dsweDsw;
     if (m.kind == 0) {
         const double s = clamp01(swe);
-        const double swePow = pow(s, m.dkrnExp);
+        const double swePow = crPow(s, m.dkrnExp);
         return 2.0 * (s - 1.0) * (1.0 + (0.5 + m.lambdaInv) * swePow - (1.5 + m.lambdaInv) * swePow * s) *
                m.dsweDsw;
     }
@@ -187,7 +190,7 @@ inline MaterialLaw makeMaterialLaw(int kind, const double* prm)
         auto swToSwe = [&](double sw) { return (sw - m.swr) / (1.0 - m.swr - m.snr); };
         auto dpc_dswe = [&](double swe) {
             swe = clamp01(swe);
-            return -m.pe / m.lambda * std::pow(swe, -1.0 / m.lambda - 1.0);
+            return -m.pe / m.lambda * crPow(swe, -1.0 / m.lambda - 1.0);
         };
         const double dswe_dsw = 1.0 / (1.0 - m.swr - m.snr);
         const double dsw_dswe = 1.0 - m.swr - m.snr;
@@ -196,7 +199,7 @@ inline MaterialLaw makeMaterialLaw(int kind, const double* prm)
         m.entryPressure = m.pe;
         m.pcDerivativeLowSw = dpc_dswe(swToSwe(lowSw)) * dswe_dsw * dsw_dswe;
         m.pcDerivativeHighSwEnd = dpc_dswe(swToSwe(highSw)) * dswe_dsw * dsw_dswe;
-        m.pcLowSwePcValue = m.pe * std::pow(clamp01(swToSwe(lowSw)), -1.0 / m.lambda);
+        m.pcLowSwePcValue = m.pe * crPow(clamp01(swToSwe(lowSw)), -1.0 / m.lambda);
         m.dsweDsw = 1.0 / (1.0 - m.swr - m.snr);
         m.dpcCoef = -m.pe / m.lambda;
         m.dpcExp = -1.0 / m.lambda - 1.0;

@@ -300,6 +300,13 @@ int dxg_norm2_noalloc(const double* x, int64_t n, double* result, void* stream);
 int dxg_selftest_bounded_wait(int device, int32_t kind, int64_t limit_ns, int32_t* kernel_status,
                               double* waited_ms);
 
+/* Element-wise pow(x[i], y[i]) of n host values, evaluated on `device` with the library's
+ * device pow -- the pow of the material laws (Brooks-Corey, Van Genuchten), which is
+ * correctly rounded in binary64 on host and device alike -- and copied back to out.  For
+ * checking the device arithmetic against a host's.  No counterpart in the reference (its
+ * laws call the C library's std::pow). */
+int dxg_device_pow(int device, const double* x, const double* y, double* out, int64_t n);
+
 /* Kernel launches issued by this context since creation (all of them ours). */
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */

@@ -25,6 +25,10 @@ def lib():
         i32p = C.POINTER(C.c_int32)
         PD = C.POINTER(ProblemDescC)
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_pow_mode.argtypes = [C.c_int]
+        L.orc_set_linear_threads.argtypes = [C.c_int]
+        L.orc_get_pow_mode.restype = C.c_int
+        L.orc_pow_batch.argtypes = [C.c_int32, C.c_int64, dp, dp, dp]
         L.orc_get_threads.restype = C.c_int
         L.orc_num_blocks.argtypes = [PD, i64p]
         L.orc_pattern.argtypes = [PD, i64p, i32p]
@@ -53,6 +57,49 @@ def set_threads(n):
 
 def get_threads():
     return lib().orc_get_threads()
+
+
+def set_linear_threads(n):
+    """Threads of the oracle's linear solve: 1 (default) sequential as dune-istl, 0 all host
+    threads (level-scheduled ILU(0), row-parallel SpMV; results identical bit for bit)."""
+    lib().orc_set_linear_threads(int(n))
+
+
+POW_LIBM, POW_CORRECTLY_ROUNDED = 0, 1
+
+
+def set_pow_mode(mode):
+    """pow of the material laws: POW_LIBM (the C library's pow, as the reference calls it;
+    the default) or POW_CORRECTLY_ROUNDED (the device's correctly rounded pow)."""
+    lib().orc_set_pow_mode(int(mode))
+
+
+def get_pow_mode():
+    return lib().orc_get_pow_mode()
+
+
+class pow_mode:
+    """Context manager selecting the oracle's pow for a block of calls."""
+
+    def __init__(self, mode):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = get_pow_mode()
+        set_pow_mode(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        set_pow_mode(self.prev)
+
+
+def pow_batch(x, y, mode):
+    """Element-wise pow(x, y) in the given mode (broadcast y)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.broadcast_to(y, x.shape), dtype=np.float64)
+    out = np.empty_like(x)
+    lib().orc_pow_batch(int(mode), x.size, _dp(x), _dp(y), _dp(out))
+    return out
 
 
 def pattern(desc):

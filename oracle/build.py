@@ -13,7 +13,9 @@ LIB = os.path.join(HERE, "liborc.so")
 
 def build(force=False):
     src = os.path.join(HERE, "oracle.cc")
-    hdrs = [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "dumux_gb300.h")]
+    hdrs = [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "dumux_gb300.h"),
+            os.path.join(HERE, "..", "dumux_gb300", "csrc", "crpow.cuh"),
+            os.path.join(HERE, "..", "dumux_gb300", "csrc", "crpow_tables.inc")]
     if not force and os.path.exists(LIB):
         newest = max(os.path.getmtime(p) for p in [src] + hdrs)
         if os.path.getmtime(LIB) >= newest:

@@ -42,7 +42,17 @@
 #include <omp.h>
 #endif
 
+#include "../dumux_gb300/csrc/crpow.cuh"
+
 namespace orc {
+
+// pow of the material laws.  Mode 0 (default): the C library's pow, which the reference
+// calls (std::pow); for binary64 it is not correctly rounded in ~0.1% of arguments, and
+// its rounding may differ between C libraries.  Mode 1: the correctly rounded pow
+// (crpow.cuh, checked against 200-bit arithmetic in tests/test_crpow.py), which takes
+// the libm out of a comparison with the device, whose pow is correctly rounded.
+static int g_pow_mode = 0;
+static inline double lawPow(double x, double y) { return g_pow_mode == 1 ? dxg::crPow(x, y) : std::pow(x, y); }
 
 struct NumericalProblem : std::runtime_error { using std::runtime_error::runtime_error; };
 struct SolverAbort : std::runtime_error { using std::runtime_error::runtime_error; };
@@ -73,11 +83,11 @@ struct BrooksCoreyDefault {
     double sweToSw(double swe) const { return swe * (1.0 - swr - snr) + swr; }
     double dswe_dsw() const { return 1.0 / (1.0 - swr - snr); }
     static double clamp01(double x) { return std::clamp(x, 0.0, 1.0); }
-    double base_pc(double swe) const { swe = clamp01(swe); return pe * std::pow(swe, -1.0 / lambda); }
+    double base_pc(double swe) const { swe = clamp01(swe); return pe * lawPow(swe, -1.0 / lambda); }
     double base_dpc_dswe(double swe) const
     {
         swe = clamp01(swe);
-        return -pe / lambda * std::pow(swe, -1.0 / lambda - 1.0);
+        return -pe / lambda * lawPow(swe, -1.0 / lambda - 1.0);
     }
     double pc_noreg(double sw) const { return base_pc(swToSwe(sw)); }
     double dpc_dsw_noreg(double sw) const { return base_dpc_dswe(swToSwe(sw)) * dswe_dsw(); }
@@ -94,7 +104,7 @@ struct BrooksCoreyDefault {
         const double swe = swToSwe(sw);
         if (swe <= 0.0) return 0.0;
         else if (swe >= 1.0) return 1.0;
-        return std::pow(clamp01(swe), 2.0 / lambda + 3.0);
+        return lawPow(clamp01(swe), 2.0 / lambda + 3.0);
     }
     double krn(double sw) const
     {
@@ -104,7 +114,7 @@ struct BrooksCoreyDefault {
         const double s = clamp01(swe);
         const double exponent = 2.0 / lambda + 1.0;
         const double sne = 1.0 - s;
-        return sne * sne * (1.0 - std::pow(s, exponent));
+        return sne * sne * (1.0 - lawPow(s, exponent));
     }
     // TwoPMaterialLaw::dpc_dsw / dkrw_dsw / dkrn_dsw (materiallaw.hh:121-239): the
     // regularised slope (BrooksCoreyRegularization::dpc_dswe, dkrw_dswe, dkrn_dswe,
@@ -122,7 +132,7 @@ struct BrooksCoreyDefault {
         const double swe = swToSwe(sw);
         if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
         const double s = clamp01(swe);
-        return (2.0 / lambda + 3.0) * std::pow(s, 2.0 / lambda + 2.0) * dswe_dsw();
+        return (2.0 / lambda + 3.0) * lawPow(s, 2.0 / lambda + 2.0) * dswe_dsw();
     }
     double dkrn_dsw(double sw) const
     {
@@ -130,7 +140,7 @@ struct BrooksCoreyDefault {
         if (swe <= 0.0 || swe >= 1.0) return 0.0 * dswe_dsw();
         const double s = clamp01(swe);
         const double lambdaInv = 1.0 / lambda;
-        const double swePow = std::pow(s, 2 * lambdaInv);
+        const double swePow = lawPow(s, 2 * lambdaInv);
         return 2.0 * (s - 1.0) * (1.0 + (0.5 + lambdaInv) * swePow - (1.5 + lambdaInv) * swePow * s) * dswe_dsw();
     }
 };
@@ -206,37 +216,37 @@ struct VanGenuchtenDefault {
     double sweToSw(double swe) const { return swe * (1.0 - swr - snr) + swr; }
     double dswe_dsw() const { return 1.0 / (1.0 - swr - snr); }
     static double c01(double x) { return std::clamp(x, 0.0, 1.0); }
-    double base_pc(double swe) const { swe = c01(swe); return std::pow(std::pow(swe, -1.0 / m) - 1, 1.0 / n) / alpha; }
+    double base_pc(double swe) const { swe = c01(swe); return lawPow(lawPow(swe, -1.0 / m) - 1, 1.0 / n) / alpha; }
     double base_dpc_dswe(double swe) const
     {
         swe = c01(swe);
-        const double powSwe = std::pow(swe, -1 / m);
-        return -1.0 / alpha * std::pow(powSwe - 1, 1.0 / n - 1) / n * powSwe / swe / m;
+        const double powSwe = lawPow(swe, -1 / m);
+        return -1.0 / alpha * lawPow(powSwe - 1, 1.0 / n - 1) / n * powSwe / swe / m;
     }
     double base_krw(double swe) const
     {
         swe = c01(swe);
-        const double r = 1.0 - std::pow(1.0 - std::pow(swe, 1.0 / m), m);
-        return std::pow(swe, l) * r * r;
+        const double r = 1.0 - lawPow(1.0 - lawPow(swe, 1.0 / m), m);
+        return lawPow(swe, l) * r * r;
     }
     double base_dkrw_dswe(double swe) const
     {
         swe = c01(swe);
-        const double x = 1.0 - std::pow(swe, 1.0 / m);
-        const double xToM = std::pow(x, m);
-        return (1.0 - xToM) * std::pow(swe, l - 1) * ((1.0 - xToM) * l + 2 * xToM * (1.0 - x) / x);
+        const double x = 1.0 - lawPow(swe, 1.0 / m);
+        const double xToM = lawPow(x, m);
+        return (1.0 - xToM) * lawPow(swe, l - 1) * ((1.0 - xToM) * l + 2 * xToM * (1.0 - x) / x);
     }
     double base_krn(double swe) const
     {
         swe = c01(swe);
-        return std::pow(1 - swe, l) * std::pow(1 - std::pow(swe, 1.0 / m), 2 * m);
+        return lawPow(1 - swe, l) * lawPow(1 - lawPow(swe, 1.0 / m), 2 * m);
     }
     double base_dkrn_dswe(double swe) const
     {
         swe = c01(swe);
         const double sne = 1.0 - swe;
-        const double x = 1.0 - std::pow(swe, 1.0 / m);
-        return -std::pow(sne, l - 1.0) * std::pow(x, 2 * m - 1.0) * (l * x + 2.0 * sne / swe * (1.0 - x));
+        const double x = 1.0 - lawPow(swe, 1.0 / m);
+        return -lawPow(sne, l - 1.0) * lawPow(x, 2 * m - 1.0) * (l * x + 2.0 * sne / swe * (1.0 - x));
     }
     double pc(double sw) const
     {
@@ -864,7 +874,50 @@ struct BCRS {
     int64_t n; int b;
     const int64_t* rowPtr; const int32_t* col;
     std::vector<double> val;   // ILU copy
+    // level schedules of the lower (forward, factorisation) and upper (backward) triangle:
+    // rows of one level depend only on rows of earlier levels, so a level's rows may run in
+    // any order with identical results; empty when the linear solve runs sequentially
+    std::vector<int64_t> fwdRows, fwdStart, bwdRows, bwdStart;
 };
+
+// Threads of the linear solve: 1 (default) runs ILU(0) and BiCGSTAB sequentially as
+// dune-istl's SeqILU / BiCGSTABSolver; more threads run the SpMV rows, the vector updates and
+// the ILU(0) rows of each wavefront level in parallel.  Every row and every entry is computed
+// with the same operations in the same order, and the dot products stay sequential, so the
+// results are identical bit for bit.
+static int g_linear_threads = 1;
+
+static void buildLevels(BCRS& M)
+{
+    const int64_t n = M.n;
+    std::vector<int> lev(n, 0);
+    int maxLev = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        int l = 0;
+        for (int64_t k = M.rowPtr[i]; k < M.rowPtr[i + 1] && M.col[k] < i; ++k) l = std::max(l, lev[M.col[k]] + 1);
+        lev[i] = l;
+        maxLev = std::max(maxLev, l);
+    }
+    auto bucket = [&](std::vector<int64_t>& rows, std::vector<int64_t>& start, int nl) {
+        start.assign(nl + 2, 0);
+        for (int64_t i = 0; i < n; ++i) ++start[lev[i] + 1];
+        for (int l = 0; l <= nl; ++l) start[l + 1] += start[l];
+        rows.resize(n);
+        std::vector<int64_t> pos(start.begin(), start.end() - 1);
+        for (int64_t i = 0; i < n; ++i) rows[pos[lev[i]]++] = i;
+    };
+    bucket(M.fwdRows, M.fwdStart, maxLev);
+    std::fill(lev.begin(), lev.end(), 0);
+    maxLev = 0;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int64_t k = M.rowPtr[i]; k < M.rowPtr[i + 1]; ++k)
+            if (M.col[k] > i) l = std::max(l, lev[M.col[k]] + 1);
+        lev[i] = l;
+        maxLev = std::max(maxLev, l);
+    }
+    bucket(M.bwdRows, M.bwdStart, maxLev);
+}
 
 static void blkMul(int b, const double* A, const double* B, double* C)   // C = A*B
 {
@@ -890,11 +943,11 @@ static void blkInvert(int b, double* A)
 }
 
 // block ILU(0) in place; diagonal blocks hold the inverted pivots afterwards
-static void ilu0Decompose(BCRS& M)
+static void ilu0DecomposeRow(BCRS& M, int64_t i)
 {
     const int b = M.b, bb = b * b;
     double tmp[4], L[4];
-    for (int64_t i = 0; i < M.n; ++i) {
+    {
         int64_t ij = M.rowPtr[i];
         const int64_t endi = M.rowPtr[i + 1];
         for (; ij < endi && M.col[ij] < i; ++ij) {
@@ -919,10 +972,46 @@ static void ilu0Decompose(BCRS& M)
     }
 }
 
+// Runs body(i) over the rows in sequence, or level by level on the solve's threads.
+template <class F>
+static void forRows(const BCRS& M, bool forward, F&& body)
+{
+    if (g_linear_threads == 1 || M.fwdStart.empty()) {
+        if (forward)
+            for (int64_t i = 0; i < M.n; ++i) body(i);
+        else
+            for (int64_t i = M.n - 1; i >= 0; --i) body(i);
+        return;
+    }
+    const std::vector<int64_t>& rows = forward ? M.fwdRows : M.bwdRows;
+    const std::vector<int64_t>& start = forward ? M.fwdStart : M.bwdStart;
+    const int nl = (int)start.size() - 1;
+    bool failed = false;
+#pragma omp parallel num_threads(g_linear_threads > 0 ? g_linear_threads : orc_get_threads())
+    for (int l = 0; l < nl; ++l) {
+#pragma omp for schedule(static)
+        for (int64_t k = start[l]; k < start[l + 1]; ++k) {
+            try {
+                body(rows[k]);
+            } catch (...) {
+#pragma omp atomic write
+                failed = true;
+            }
+        }
+    }
+    if (failed) throw SolverAbort("singular pivot in ILU(0)");
+}
+
+static void ilu0Decompose(BCRS& M)
+{
+    if (g_linear_threads != 1) buildLevels(M);
+    forRows(M, true, [&](int64_t i) { ilu0DecomposeRow(M, i); });
+}
+
 static void ilu0Apply(const BCRS& M, const double* d, double* v)
 {
     const int b = M.b, bb = b * b;
-    for (int64_t i = 0; i < M.n; ++i) {
+    forRows(M, true, [&](int64_t i) {
         double rhs[2] = {d[i * b], b > 1 ? d[i * b + 1] : 0.0};
         for (int64_t ij = M.rowPtr[i]; ij < M.rowPtr[i + 1] && M.col[ij] < i; ++ij) {
             const double* L = &M.val[ij * bb];
@@ -934,8 +1023,8 @@ static void ilu0Apply(const BCRS& M, const double* d, double* v)
             }
         }
         for (int r = 0; r < b; ++r) v[i * b + r] = rhs[r];
-    }
-    for (int64_t i = M.n - 1; i >= 0; --i) {
+    });
+    forRows(M, false, [&](int64_t i) {
         double rhs[2] = {v[i * b], b > 1 ? v[i * b + 1] : 0.0};
         int64_t ii = -1;
         for (int64_t ij = M.rowPtr[i]; ij < M.rowPtr[i + 1]; ++ij) {
@@ -956,12 +1045,15 @@ static void ilu0Apply(const BCRS& M, const double* d, double* v)
             for (int c = 0; c < b; ++c) s += Dinv[r * b + c] * rhs[c];
             v[i * b + r] = s;
         }
-    }
+    });
 }
+
+static int linThreads() { return g_linear_threads > 0 ? g_linear_threads : orc_get_threads(); }
 
 static void spmv(int64_t n, int b, const int64_t* rowPtr, const int32_t* col, const double* A, const double* x, double* y)
 {
     const int bb = b * b;
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
     for (int64_t i = 0; i < n; ++i) {
         double acc[2] = {0.0, 0.0};
         for (int64_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
@@ -1015,8 +1107,11 @@ static dxg_linear_result bicgstab(int64_t n, int b, const int64_t* rowPtr, const
             p = r;
         else {
             beta = (rho_new / rho) * (alpha / omega);
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
             for (int64_t i = 0; i < m; ++i) p[i] += -omega * v[i];
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
             for (int64_t i = 0; i < m; ++i) p[i] *= beta;
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
             for (int64_t i = 0; i < m; ++i) p[i] += r[i];
         }
         ilu0Apply(M, p.data(), y.data());
@@ -1024,7 +1119,9 @@ static dxg_linear_result bicgstab(int64_t n, int b, const int64_t* rowPtr, const
         h = dot(m, rt.data(), v.data());
         if (std::abs(h) < EPSILON) throw SolverAbort("breakdown in BiCGSTAB - h");
         alpha = rho_new / h;
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
         for (int64_t i = 0; i < m; ++i) x[i] += alpha * y[i];
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
         for (int64_t i = 0; i < m; ++i) r[i] += -alpha * v[i];
         def = std::sqrt(dot(m, r.data(), r.data()));
         if (!std::isfinite(def)) throw SolverAbort("non-finite defect");
@@ -1033,7 +1130,9 @@ static dxg_linear_result bicgstab(int64_t n, int b, const int64_t* rowPtr, const
         ilu0Apply(M, r.data(), y.data());
         spmv(n, b, rowPtr, col, A, y.data(), t.data());
         omega = dot(m, t.data(), r.data()) / dot(m, t.data(), t.data());
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
         for (int64_t i = 0; i < m; ++i) x[i] += omega * y[i];
+#pragma omp parallel for schedule(static) num_threads(linThreads()) if (g_linear_threads != 1)
         for (int64_t i = 0; i < m; ++i) r[i] += -omega * t[i];
         rho = rho_new;
         def = std::sqrt(dot(m, r.data(), r.data()));
@@ -1246,6 +1345,13 @@ using namespace orc;
 extern "C" {
 
 void orc_set_threads(int n) { g_threads = n; }
+void orc_set_pow_mode(int mode) { g_pow_mode = mode; }
+int orc_get_pow_mode(void) { return g_pow_mode; }
+void orc_set_linear_threads(int n) { g_linear_threads = n; }
+void orc_pow_batch(int32_t mode, int64_t n, const double* x, const double* y, double* out)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = mode == 1 ? dxg::crPow(x[i], y[i]) : std::pow(x[i], y[i]);
+}
 int orc_get_threads(void)
 {
 #ifdef _OPENMP

@@ -29,6 +29,18 @@ extern "C" {
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
+/* pow of the material laws: 0 the C library's pow (as the reference, default), 1 the
+ * correctly rounded pow of dumux_gb300/csrc/crpow.cuh. */
+void orc_set_pow_mode(int mode);
+int orc_get_pow_mode(void);
+/* out[i] = pow(x[i], y[i]) in the given mode. */
+void orc_pow_batch(int32_t mode, int64_t n, const double* x, const double* y, double* out);
+
+/* Threads of the linear solve: 1 (default) sequential, as dune-istl's SeqILU and
+ * BiCGSTABSolver; 0 all, n > 1 that many -- SpMV rows, vector updates and the ILU(0) rows of
+ * each wavefront level in parallel, dot products sequential; identical results. */
+void orc_set_linear_threads(int n);
+
 /* Jacobian pattern: diagonal + (J, I) for each neighbour J of I, sorted columns. */
 int orc_num_blocks(const dxg_problem_desc* d, int64_t* nnzb);
 int orc_pattern(const dxg_problem_desc* d, int64_t* row_ptr, int32_t* col_idx);

@@ -65,21 +65,26 @@ def _run_time_loop_gpu(desc, u0, dt, steps, params, precision="fp64"):
     return ctx.solution(), reps
 
 
-def test_newton_2p_matches_oracle_fp64():
+@pytest.mark.parametrize("pow_mode", [oracle.POW_CORRECTLY_ROUNDED, oracle.POW_LIBM], ids=["crpow", "libm"])
+def test_newton_2p_matches_oracle_fp64(pow_mode):
     desc, u0 = problems.dnapl_2p(cells=(8, 6, 5), seed=4, inflow=0.04)
     p = newton_params(linear_reduction=1e-13, linear_max_iter=500, record_residual_norms=1)
     u_gpu, reps = _run_time_loop_gpu(desc, u0, 250.0, 3, p)
-    u_orc, oreps = oracle.time_loop(desc, u0, 250.0, 3, params=p, max_dt=250.0)
+    with oracle.pow_mode(pow_mode):
+        u_orc, oreps = oracle.time_loop(desc, u0, 250.0, 3, params=p, max_dt=250.0)
+    # with the same pow the assembly is bit-identical and the per-iteration residual norms
+    # differ only through the summation order of BiCGSTAB's dot products; with the C
+    # library's pow (not correctly rounded in ~0.1% of arguments) an ulp of a capillary
+    # pressure becomes a ~1e-8 relative Jacobian difference that moves the intermediate
+    # iterates (not the converged one)
+    tol = 1e-9 if pow_mode == oracle.POW_CORRECTLY_ROUNDED else 1e-6
     for rg, ro in zip(reps, oreps):
         assert rg["iterations"] == ro["iterations"]
         assert rg["dt_used"] == ro["dt_used"]
         assert rg["initial_residual"] == pytest.approx(ro["initial_residual"], rel=1e-12)
-        # Per-iteration residual norms: the residuals are evaluated with the same
-        # operation order, but CUDA's pow and the host libm's pow may differ in the last
-        # ulp; the numeric derivative amplifies that into ~1e-8 relative Jacobian
-        # differences, which move the intermediate iterates (not the converged one).
-        rn_g, rn_o = np.array(rg["residual_norm"]), np.array(ro["residual_norm"])
-        assert np.all(np.abs(rn_g - rn_o) <= 1e-6 * rg["initial_residual"])
+        n = rg["iterations"]
+        rn_g, rn_o = np.array(rg["residual_norm"][:n]), np.array(ro["residual_norm"][:n])
+        assert np.all(np.abs(rn_g - rn_o) <= tol * rg["initial_residual"])
     scale = np.max(np.abs(u_orc.reshape(-1, 2)), axis=0)
     err = np.max(np.abs((u_gpu - u_orc).reshape(-1, 2)), axis=0) / scale
     assert np.all(err <= 1e-9), err
