@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--problems", type=int, default=256, help="ensemble size")
     ap.add_argument("--requests", type=int, default=48, help="served-stream length")
     ap.add_argument("--ticks-per-step", type=int, default=25, help="ensemble: engine ticks per timed step")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="default workload: skip the forms, ensemble and served summaries")
     ap.add_argument("--plain-sample", type=int, default=8,
                     help="problems / requests of the workload also run alone on the plain FP64 path")
     return ap.parse_args()
@@ -183,12 +185,12 @@ def measured_peaks():
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
-# of the 64x64x32 FP64 system, from the ncu capture summarised in
-# profiles/ilu_sweep_64x64x32_fp64.md (cold-cache, serialised launches).
+# of the 64x64x32 FP64 system, from an ncu capture of the sweeps (cold-cache, serialised
+# launches).
 ILU_TRAFFIC_PER_APPLY_64x64x32 = 14537472 + 18714112
-# DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from the ncu capture
-# of the 32-problem ensemble (2,379,154 cells) in profiles/ilu_sweep_batched_ensemble32_mixed.md;
-# traffic scales with the cells swept (each block and vector entry is moved once)
+# DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from an ncu capture
+# of a 32-problem ensemble (2,379,154 cells); traffic scales with the cells swept (each block
+# and vector entry is moved once)
 ENSEMBLE_SWEEP_TRAFFIC_PER_CELL = (136113408 + 9772544 + 174257152 + 10788608) / 2379154
 
 
@@ -211,14 +213,33 @@ def cpu_sample(desc, u0, dt, iters):
     return desc.num_cells * n / sec, sec, n
 
 
+def bench_config(desc, steps, warmup, precision="fp64"):
+    """The workload description both arms print (the GPU arm and the reference arm run
+    exactly this work)."""
+    stationary = WORKLOAD == "1p"
+    return {"workload": workload_name(tuple(desc.cells[:desc.dim]), precision), "cells": int(desc.num_cells),
+            "unknowns": int(desc.num_dofs),
+            "time_steps": (f"{steps} timed stationary Newton steps from the same initial state after {warmup} "
+                           "warm-up steps" if stationary else
+                           f"time steps {warmup + 1}..{warmup + steps} of the seeded initial state "
+                           f"({warmup} warm-up steps advance the simulation), dt = 250 s each"),
+            "l2": "GPU arm: flushed between timed steps (256 MiB write)"}
+
+
 def run_reference(args, cells):
+    """The reference arm: the oracle's restatement of the reference's CPU path on the host
+    cores -- element assembly on all host threads (the reference's coloured threaded
+    assembly), ILU(0)-BiCGSTAB sequential as dune-istl's SeqILU / BiCGSTABSolver -- over the
+    same time steps as the GPU arm: the warm-up steps advance the simulation untimed, then
+    exactly `steps` time steps are timed."""
     global WORKLOAD
     WORKLOAD = args.workload
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     import oracle
-    metric, name = METRIC, workload_name(cells, "fp64")
+    metric = METRIC
+    name = None
     if WORKLOAD == "ensemble":
         from dumux_gb300 import problems
         desc, u0, _ = problems.ensemble_2p(count=1, seed=4)[0]
@@ -234,23 +255,39 @@ def run_reference(args, cells):
         desc, u0 = workload(cells)
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
+    oracle.set_linear_threads(1)
+    stationary = WORKLOAD == "1p"
+    params = step_params()
+    dt = 0.0 if stationary else args.dt
+    u = np.array(u0, dtype=np.float64)
+
+    def one_step(u):
+        st, u_new, rep = oracle.newton_solve(desc, u0 if stationary else u, u0 if stationary else u, dt, params)
+        if st != 0:
+            raise RuntimeError(f"oracle time step failed with status {st}")
+        return (u if stationary else u_new), rep["iterations"] + rep["wasted_iterations"]
+
     for _ in range(args.warmup):
-        cpu_sample(desc, u0, args.dt, args.cpu_sample_iters)
+        u, _ = one_step(u)
     t0 = time.perf_counter()
-    work = 0
+    work, iters = 0, []
     for _ in range(args.steps):
-        _, sec, n = cpu_sample(desc, u0, args.dt, args.cpu_sample_iters)
+        u, n = one_step(u)
+        iters.append(n)
         work += desc.num_cells * n
     total = time.perf_counter() - t0
     value = work / total
-    sample = (f"first {args.cpu_sample_iters} Newton iterations of the first time step per step "
-              f"(assembly on {threads} OpenMP threads, ILU0-BiCGSTAB sequential as dune-istl SeqILU)")
+    sample = (f"the same {args.steps} {'stationary Newton steps' if stationary else 'time steps'} as the GPU arm "
+              f"after {args.warmup} warm-up steps (assembly on {threads} OpenMP threads, ILU0-BiCGSTAB sequential "
+              "as dune-istl SeqILU)")
+    config = bench_config(desc, args.steps, args.warmup)
+    if name:
+        config = {"workload": name, "cells": int(desc.num_cells), "unknowns": int(desc.num_dofs)}
     line = {
         "impl": "reference", "metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": name, "cells": int(desc.num_cells), "unknowns": int(desc.num_dofs),
-                   "parallelism": "host threads"},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded ln K Gaussian field)", "config": config, "newton_iterations": iters,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "DuMux needs DUNE (not installed, no network): the reference arm runs the oracle's "
@@ -265,10 +302,48 @@ def stats_of(values):
             "mean": float(np.mean(values))} if values else None
 
 
+def plain_fp64_steady(items, params, device, warm_steps, steps):
+    """Each (desc, u0, dt) alone through one plain FP64 context (the single-problem drop-in
+    path): context creation, upload and `warm_steps` time steps (launch-shape tuning
+    included) untimed, then `steps` time steps timed with CUDA events on the context's
+    stream.  Returns cell*Newton-steps/s and time-step solves/s over the sample."""
+    import torch
+    import dumux_gb300
+    work, sec, solves = 0, 0.0, 0
+    for desc, u0, dt in items:
+        ctx = dumux_gb300.Context(desc, device=device, precision="fp64")
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        dtc = dt
+        for _ in range(warm_steps):
+            rep = ctx.newton_solve(dtc, params)
+            ctx.advance_time_step()
+            dtc = min(ctx.suggest_time_step(rep["dt_used"], params), dt)
+        stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=device)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its = 0
+        for _ in range(steps):
+            rep = ctx.newton_solve(dtc, params)
+            its += rep["iterations"] + rep["wasted_iterations"]
+            ctx.advance_time_step()
+            dtc = min(ctx.suggest_time_step(rep["dt_used"], params), dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec += e0.elapsed_time(e1) / 1e3
+        work += desc.num_cells * its
+        solves += steps
+        ctx.close()
+    return work / sec, solves / sec
+
+
 def plain_fp64_alone(items, params, device):
     """Each (desc, u0, dt, t_end) alone through one plain FP64 context (the
-    single-problem drop-in path, host time loop): cell*Newton-steps/s over the sample
-    and per-problem service seconds."""
+    single-problem drop-in path, host time loop), as a request served alone: its service
+    time runs from context creation to the result on the host.  Returns cell*Newton-steps/s
+    over the sample and per-problem service seconds."""
     import dumux_gb300
     work, total, service = 0, 0.0, []
     for desc, u0, dt, t_end in items:
@@ -293,6 +368,176 @@ def plain_fp64_alone(items, params, device):
         total += sec
         service.append(sec)
     return work / total, service
+
+
+# GB300 forms of the same problem measured beside the plain FP64 drop-in path: mixed
+# precision (FP32 preconditioner and operator products inside the FP64 Krylov, residual and
+# Newton), with the natural-order ILU(0), the red-black ordered ILU(0) or AMG-BiCGSTAB
+FORMS = (("mixed", "mixed", "natural", "ilu"), ("mixed+redblack", "mixed", "redblack", "ilu"),
+         ("mixed+amg", "mixed", "natural", "amg"))
+
+
+def run_forms(desc, u_start, u_ref, dt, steps, device, plain_ms_per_step, plain_value, flush):
+    """Each form of FORMS over the same time steps as the timed plain FP64 region: from
+    the same state u_start, `steps` implicit-Euler steps timed with CUDA events on the
+    context's stream (L2 flushed between steps); one untimed step from u_start first
+    (kernel loading, launch-shape tuning, AMG setup).  Reports the speed-up per time step
+    over plain FP64 and the error of p_w and S_n against the plain FP64 fields u_ref."""
+    import torch
+    import dumux_gb300
+    from dumux_gb300.abi import newton_params
+    b = desc.num_eq
+    ref = u_ref.reshape(-1, b)
+    out = {}
+    for name, precision, ilu, solver in FORMS:
+        ctx = dumux_gb300.Context(desc, device=device, precision=precision)
+        params = newton_params()
+        if ilu == "redblack":
+            ctx.set_ilu_kernel("redblack")
+            params = newton_params(linear_max_iter=1000)
+        if solver == "amg":
+            ctx.set_linear_solver("amg")
+        ctx.set_solution(u_start)
+        ctx.set_prev_solution(u_start)
+        ctx.newton_solve(dt, params)
+        ctx.set_solution(u_start)
+        ctx.set_prev_solution(u_start)
+        stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=device)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its, work = [], 0
+        for _ in range(steps):
+            rep = ctx.newton_solve(dt, params)
+            ctx.advance_time_step()
+            its.append(rep["iterations"] + rep["wasted_iterations"])
+            work += desc.num_cells * its[-1]
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        u = ctx.solution().reshape(-1, b)
+        ctx.close()
+        entry = {"value": work / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                 "speedup_per_time_step": plain_ms_per_step / (ms / steps),
+                 "speedup_metric": (work / (ms / 1e3)) / plain_value, "newton_iterations": its,
+                 "precision": precision, "ilu": ilu, "linear_solver": solver}
+        for k, fname in enumerate(("p_w", "S_n")[:b]):
+            d = u[:, k] - ref[:, k]
+            entry[f"max_rel_err_{fname}"] = float(np.max(np.abs(d)) / np.max(np.abs(ref[:, k])))
+            entry[f"l2_rel_err_{fname}"] = float(np.linalg.norm(d) / np.linalg.norm(ref[:, k]))
+        out[name] = entry
+    return out
+
+
+def ensemble_summary(device, count=64, T=25, warm=2, steps=2, plain_sample=4):
+    """A smaller instance of the batched ensemble (`count` problems of the ensemble workload,
+    mixed precision, natural ILU(0) and AMG-BiCGSTAB): time-step solves/s and
+    cell*Newton-steps/s over `steps` x T ticks after `warm` x T warm-up ticks, beside the
+    same problems alone on the plain FP64 path in steady state."""
+    import torch
+    import dumux_gb300
+    from dumux_gb300 import problems
+    from dumux_gb300.abi import newton_params
+    params = newton_params()
+    probs = problems.ensemble_2p(count=count, seed=4)
+    out = {"problems": count, "cells_total": int(sum(d.num_cells for d, _, _ in probs)), "ticks_per_step": T,
+           "steps": steps, "precision": "mixed"}
+    for solver in ("ilu", "amg"):
+        batch = dumux_gb300.Batch(device=device, precision="mixed", solver=solver)
+        ids = [batch.add(d, u0, dt=250.0, t_end=1e12, params=params) for d, u0, _ in probs]
+        for _ in range(warm * T):
+            batch.iterate()
+        before = {i: batch.info(i) for i in ids}
+        stream = torch.cuda.ExternalStream(batch.stream_handle(), device=device)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps * T):
+            batch.iterate()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        after = {i: batch.info(i) for i in ids}
+        work = sum(after[i]["cells"] * (after[i]["newton_iterations"] - before[i]["newton_iterations"]) for i in ids)
+        solves = sum(after[i]["time_steps"] - before[i]["time_steps"] for i in ids)
+        batch.close()
+        out[solver] = {"value": work / sec, "unit": UNIT, "solves_per_s": solves / sec}
+    sample = probs[::max(1, count // plain_sample)][:plain_sample]
+    plain, plain_solves = plain_fp64_steady([(d, u0, 250.0) for d, u0, _ in sample], params, device, 1, steps)
+    out["plain_fp64_same_problems"] = {"value": plain, "unit": UNIT, "solves_per_s": plain_solves,
+                                       "sample": f"{len(sample)} of the problems alone, 1 untimed and {steps} "
+                                                 "timed time steps each"}
+    for solver in ("ilu", "amg"):
+        out[solver]["speedup_vs_plain_fp64"] = out[solver]["value"] / plain
+    return out
+
+
+def serve_summary(device, requests=24, plain_sample=4):
+    """A shorter served stream (the first `requests` requests of the served workload,
+    mixed precision, AMG-BiCGSTAB): p50/p99 latency and solves/s, beside the same requests
+    served alone one after another on the plain FP64 path."""
+    import torch
+    from dumux_gb300 import problems
+    from dumux_gb300.abi import newton_params
+    from dumux_gb300.serve import Server
+    params = newton_params()
+    reqs = problems.served_requests(requests, rate=200.0, seed=5)
+    built = {r["index"]: problems.make_request_problem(r) for r in reqs}
+    free, _ = torch.cuda.mem_get_info(device)
+    server = Server(device=device, precision="mixed", memory_budget=int(0.8 * free), params=params, solver="amg")
+    warm = problems.served_requests(3, rate=1e6, seed=99, n_max=2e4)
+    server.serve(warm, problems.make_request_problem)
+    records, st = server.serve(reqs, lambda r: built[r["index"]])
+    server.batch.close()
+    sample = reqs[::max(1, len(reqs) // plain_sample)][:plain_sample]
+    items = [(built[r["index"]][0], built[r["index"]][1], r["dt"], r["t_end"]) for r in sample]
+    plain, service = plain_fp64_alone(items, params, device)
+    return {"requests": requests, "precision": "mixed", "linear_solver": "amg",
+            "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
+            "solves_per_s": st["solves_per_s"], "value": st["cell_newton_steps_per_s"], "unit": UNIT,
+            "makespan_s": st["makespan_s"],
+            "plain_fp64_alone": {"value": plain, "unit": UNIT, "service_s": stats_of(service),
+                                 "sample": f"{len(sample)} of the requests, each alone through one FP64 context "
+                                           "(creation to result)"},
+            "speedup_vs_plain_fp64": st["cell_newton_steps_per_s"] / plain}
+
+
+def fp64_peak(device):
+    """The device's dense FP64 FMA rate, measured here with CUDA events (None if unavailable)."""
+    import dumux_gb300
+    try:
+        rates = [dumux_gb300.fp64_fma_rate(device) for _ in range(3)]
+    except Exception:
+        return None
+    return {"tflops": max(rates), "unit": "TFLOP/s", "source": "measured in this run (dxg_fp64_fma_rate)"}
+
+
+def sweep_flops_per_apply(cells, b):
+    """FP64 flops of one ILU(0) apply (forward + backward sweep) on a structured grid: a
+    b x b block-vector product (2 b^2 flops) per off-diagonal block of L and of U (one each
+    per interior face) and one per inverted pivot."""
+    nx, ny, nz = (tuple(cells) + (1, 1))[:3]
+    faces = (nx - 1) * ny * nz + nx * (ny - 1) * nz + nx * ny * (nz - 1)
+    return 2.0 * b * b * (2 * faces + nx * ny * nz)
+
+
+def fp64_roof(roofline, peak_tflops, flops_per_apply, launches, ms):
+    """The FP64 side of the sweep's roofline: achieved FP64 rate, arithmetic intensity and
+    the fraction of min(HBM bandwidth x intensity, FP64 peak)."""
+    if not launches or not ms or not roofline.get("algorithmic_bytes"):
+        return None
+    sec = ms / launches / 1e3
+    intensity = flops_per_apply / roofline["algorithmic_bytes"]
+    bound = min(roofline["peak"] * 1e9 * intensity, peak_tflops * 1e12)
+    achieved = flops_per_apply / sec
+    return {"flops_per_launch": flops_per_apply, "intensity_flop_per_byte": intensity,
+            "achieved_tflops": achieved / 1e12, "peak_tflops": peak_tflops,
+            "bound_tflops": bound / 1e12, "bound_by": "fp64" if bound < roofline["peak"] * 1e9 * intensity else "hbm",
+            "frac": achieved / bound}
 
 
 def batch_roofline(batch):
@@ -364,8 +609,7 @@ def run_ensemble(args):
     batch.set_kernel_timing(False)
     if roofline["kernel"].startswith("waveKernel") and args.precision == "mixed":
         roofline["traffic"] = ENSEMBLE_SWEEP_TRAFFIC_PER_CELL * cells_total
-        roofline["traffic_note"] = ("ncu dram bytes of the 32-problem ensemble apply, scaled by cells "
-                                    "(profiles/ilu_sweep_batched_ensemble32_mixed.md)")
+        roofline["traffic_note"] = "ncu dram bytes of a 32-problem ensemble apply, scaled by cells"
 
     sweep_shapes = batch.describe().strip()
     before = {i: batch.info(i) for i in ids}
@@ -437,10 +681,12 @@ def run_ensemble(args):
     if rank == 0:
         if args.plain_sample > 0:
             sample = probs[::max(1, len(probs) // args.plain_sample)][:args.plain_sample]
-            plain, _ = plain_fp64_alone([(d, u0, dt, dt) for d, u0, _ in sample], params, local)
+            plain, plain_solves = plain_fp64_steady([(d, u0, dt) for d, u0, _ in sample], params, local,
+                                                    args.warmup, args.steps)
             line["plain_fp64_same_problems"] = {
-                "value": plain, "unit": UNIT, "sample": f"{len(sample)} of the problems, first time step each, "
-                                                         "alone through one FP64 context",
+                "value": plain, "unit": UNIT, "solves_per_s": plain_solves,
+                "sample": f"{len(sample)} of the problems alone through one FP64 context each: creation, upload "
+                          f"and {args.warmup} time steps untimed, then {args.steps} time steps timed on the device",
                 "speedup_of_batched": value / plain}
         if args.cpu_sample_iters > 0:
             desc0, u00, _ = probs[0]
@@ -601,7 +847,6 @@ def main():
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
     launches = ctx.kernel_launches() - launches0
     sec = ms / 1e3
@@ -625,6 +870,8 @@ def main():
         e2e_work += ctx.num_cells * (rep["iterations"] + rep["wasted_iterations"])
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
+    # the clock sampler ran through both timed regions, so both see its NVML polling
+    clocks = sampler.stop()
     e2e_sec, (e2e_work,) = reduce_over_ranks(e2e_sec, [e2e_work], f"cuda:{local}")
     e2e = {"value": e2e_work / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(ctx.num_dofs * 8),
            "d2h_bytes_per_step": int(ctx.num_dofs * 8)}
@@ -636,6 +883,7 @@ def main():
     ctx.set_kernel_timing(True)
     ctx.newton_solve(args.dt, params)
     sweep_n, sweep_ms, sweep_bytes = ctx.kernel_timing("ilu_sweep")
+    sweep_flops = sweep_flops_per_apply(cells, desc.num_eq)
     asm_n, asm_ms, asm_bytes = ctx.kernel_timing("assembly")
     spmv_n, spmv_ms, spmv_bytes = ctx.kernel_timing("spmv")
     ctx.set_kernel_timing(False)
@@ -676,14 +924,28 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded ln K Gaussian field)",
-        "config": {"workload": workload_name(cells, args.precision), "cells": int(np.prod(cells)),
-                   "unknowns": ctx.num_dofs, "newton_iterations": newton_iters, "global_batch": world,
-                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)",
-                   "step": "one stationary Newton step from the same initial state (includes its 80 KB h2d reset)"
-                           if stationary else "one implicit-Euler time step",
-                   "ilu_kernels": ctx.describe()},
+        "config": bench_config(desc, args.steps, args.warmup, args.precision),
+        "newton_iterations": newton_iters, "parallelism": f"replicas x{world}",
+        "step": "one stationary Newton step from the same initial state (includes its 80 KB h2d reset)"
+                if stationary else "one implicit-Euler time step",
+        "ilu_kernels": ctx.describe(),
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "kernels": kernels,
     }
+    headline = (args.workload == "2p" and cells == (64, 64, 32) and args.precision == "fp64"
+                and args.solver == "ilu" and args.ilu == "natural" and args.diff == "numeric")
+    if rank == 0 and world == 1 and headline and not args.no_forms:
+        # the GB300 forms of the same problem over the same time steps (from u_start), and
+        # shorter instances of the batched and served workloads
+        line["forms"] = run_forms(desc, u_start, u_after, args.dt, args.steps, local, ms / args.steps, value, flush)
+        line["forms"]["note"] = ("each form from the state the timed FP64 region started from, over the same "
+                                 f"{args.steps} time steps; errors against the FP64 fields at their end")
+        line["ensemble"] = ensemble_summary(local)
+        line["ensemble_solves_per_s"] = line["ensemble"]["amg"]["solves_per_s"]
+        line["serve"] = serve_summary(local)
+        line["fp64_peak"] = fp64_peak(local)
+        if line["fp64_peak"]:
+            line["roofline"]["fp64"] = fp64_roof(line["roofline"], line["fp64_peak"]["tflops"], sweep_flops, sweep_n,
+                                                 sweep_ms)
     if rank == 0:
         rate, sec_cpu, n_cpu = cpu_sample(desc, u_start, args.dt, args.cpu_sample_iters)
         import oracle

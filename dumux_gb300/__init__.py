@@ -105,6 +105,7 @@ def lib():
         L.dxg_selftest_bounded_wait.argtypes = [C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
                                                 C.POINTER(C.c_double)]
         L.dxg_device_pow.argtypes = [C.c_int, dp, dp, dp, C.c_int64]
+        L.dxg_fp64_fma_rate.argtypes = [C.c_int, dp]
         L.dxg_batch_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_describe.argtypes = [vp, C.c_char_p, C.c_int64]
         L.dxg_batch_stream.argtypes = [vp]
@@ -395,6 +396,15 @@ def device_pow(x, y, device=0):
     return out
 
 
+def fp64_fma_rate(device=0):
+    """Dense FP64 FMA rate of the device in TFLOP/s (dxg_fp64_fma_rate)."""
+    v = C.c_double(0.0)
+    rc = lib().dxg_fp64_fma_rate(int(device), C.byref(v))
+    if rc != 0:
+        raise DxgError(rc, "dxg_fp64_fma_rate failed")
+    return v.value
+
+
 def problem_device_bytes(desc, precision="mixed"):
     """Device memory a problem takes once admitted (dxg_problem_device_bytes)."""
     prec = {"fp64": DXG_PRECISION_FP64, "mixed": DXG_PRECISION_MIXED}[precision]
@@ -515,4 +525,4 @@ class Batch:
 
 __all__ = ["Context", "FVAssembler", "ILUBiCGSTABIstlSolver", "NewtonSolver", "ProblemDesc", "newton_params",
            "DxgError", "NumericalProblem", "lib", "LIB_PATH", "Batch", "problem_device_bytes",
-           "selftest_bounded_wait", "device_pow"]
+           "selftest_bounded_wait", "device_pow", "fp64_fma_rate"]

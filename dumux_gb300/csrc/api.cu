@@ -1563,6 +1563,18 @@ int dxg_selftest_bounded_wait(int device, int32_t kind, int64_t limit_ns, int32_
     return rc;
 }
 
+int dxg_fp64_fma_rate(int device, double* tflops)
+{
+    if (!tflops) return DXG_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return DXG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count || cudaSetDevice(device) != cudaSuccess) return DXG_ERR_ARG;
+    return dxg::runFp64Rate(tflops);
+}
+
 int dxg_device_pow(int device, const double* x, const double* y, double* out, int64_t n)
 {
     if (n < 0 || (n > 0 && (!x || !y || !out))) return DXG_ERR_ARG;

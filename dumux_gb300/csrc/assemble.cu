@@ -610,3 +610,48 @@ int runDevicePow(const double* x, const double* y, double* out, int64_t n)
     return rc;
 }
 }  // namespace dxg
+
+// ---------------------------------------------------------------- FP64 FMA rate
+namespace dxg {
+// Eight independent FMA chains per thread; the result is written so nothing is elided.
+__global__ void fmaRateKernel(double* out, int iters, double a, double c)
+{
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, c); x1 = fma(x1, a, c); x2 = fma(x2, a, c); x3 = fma(x3, a, c);
+        x4 = fma(x4, a, c); x5 = fma(x5, a, c); x6 = fma(x6, a, c); x7 = fma(x7, a, c);
+    }
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+int runFp64Rate(double* tflops)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return DXG_ERR_CUDA;
+    const int threads = 256, iters = 2048;
+    double* d = nullptr;
+    if (cudaMalloc(&d, (size_t)sms * threads * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return DXG_ERR_OOM;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = DXG_OK;
+    float ms = 0.f;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = DXG_ERR_CUDA;
+    if (rc == DXG_OK) {
+        fmaRateKernel<<<sms, threads>>>(d, iters, 1.0000001, 1e-9);   // warm-up
+        cudaEventRecord(e0);
+        fmaRateKernel<<<sms, threads>>>(d, iters, 1.0000001, 1e-9);
+        cudaEventRecord(e1);
+        if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f)
+            rc = DXG_ERR_CUDA;
+    }
+    if (rc == DXG_OK) *tflops = 2.0 * 8.0 * iters * (double)sms * threads / (ms * 1e-3) / 1e12;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return rc;
+}
+}  // namespace dxg

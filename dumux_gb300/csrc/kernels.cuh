@@ -59,5 +59,7 @@ void launchRowBatch(const AssemblyArgs* batch, int count, int64_t maxN, int b, i
 // Element-wise correctly rounded pow (crpow.cuh) of host arrays on the current device
 // (diagnostic: checks the device's pow against the host's).
 int runDevicePow(const double* x, const double* y, double* out, int64_t n);
+// Dense FP64 FMA rate of the current device (all SMs, independent chains), TFLOP/s.
+int runFp64Rate(double* tflops);
 
 }  // namespace dxg

@@ -307,6 +307,11 @@ int dxg_selftest_bounded_wait(int device, int32_t kind, int64_t limit_ns, int32_
  * laws call the C library's std::pow). */
 int dxg_device_pow(int device, const double* x, const double* y, double* out, int64_t n);
 
+/* Dense FP64 FMA rate of `device` in TFLOP/s (all SMs, independent FMA chains, timed with
+ * CUDA events): the FP64 roof of the FP64 kernels' roofline.  No counterpart in the
+ * reference. */
+int dxg_fp64_fma_rate(int device, double* tflops);
+
 /* Kernel launches issued by this context since creation (all of them ours). */
 int64_t dxg_kernel_launch_count(const dxg_ctx* ctx);
 /* Synchronises the context stream and reports any pending CUDA error. */

@@ -290,31 +290,97 @@ private:
     dxg_ctx* ctx_ = nullptr;
 };
 
-// Dumux::FVAssembler over the device: the same method names and meanings
-// (fvassembler.hh:101-390); jacobian() / residual() copy the device system to the host.
+class GpuFVAssembler;
+
+// The assembler's Jacobian, resident on the device: the JacobianMatrix the reference's
+// FVAssembler::jacobian() returns (a Dune::BCRSMatrix<FieldMatrix<double, b, b>>,
+// fvassembler.hh:339-341).  Host copies in the same BCRS layout on demand.
+class GpuJacobian {
+public:
+    explicit GpuJacobian(const GpuFVAssembler* a = nullptr) : a_(a) {}
+    const GpuFVAssembler& assembler() const { return *a_; }
+    int64_t N() const;             // block rows
+    int64_t M() const { return N(); }
+    int64_t nonzeroes() const;     // blocks
+    // row pointers, block columns (sorted per row), row-major block values
+    void copyToHost(std::vector<int64_t>& rowPtr, std::vector<int32_t>& col, std::vector<double>& values) const;
+
+private:
+    const GpuFVAssembler* a_;
+};
+
+// The assembler's residual, resident on the device: the ResidualType the reference's
+// FVAssembler::residual() returns (fvassembler.hh:343-345).  norm() and the linear
+// solver's right-hand side read it in place; host values on demand.
+class GpuResidual {
+public:
+    explicit GpuResidual(const GpuFVAssembler* a = nullptr) : a_(a) {}
+    const GpuFVAssembler& assembler() const { return *a_; }
+    int64_t size() const;
+    std::vector<double> toHost() const;
+
+private:
+    const GpuFVAssembler* a_;
+};
+
+// The state behind FVAssembler::gridVariables() (fvgridvariables.hh:54-129): the current
+// solution lives on the device and its volume variables are evaluated from it at each
+// assembly, so update / resetTimeStep / advanceTimeStep are solution transfers.
+class GpuGridVariables {
+public:
+    explicit GpuGridVariables(GpuFVAssembler* a = nullptr) : a_(a) {}
+    void update(const std::vector<double>& curSol);
+    void resetTimeStep(const std::vector<double>& curSol);
+    void advanceTimeStep();
+
+private:
+    GpuFVAssembler* a_;
+};
+
+// Dumux::FVAssembler over the device: the same method names, signatures and meanings
+// (fvassembler.hh:101-390).  jacobian() and residual() return device-resident handles.
 class GpuFVAssembler {
 public:
     using Scalar = double;
     using SolutionVector = std::vector<double>;
-    using ResidualType = std::vector<double>;
+    using ResidualType = GpuResidual;
+    using JacobianMatrix = GpuJacobian;
+    using GridVariables = GpuGridVariables;
 
     // Stationary (no previous solution) or transient (prevSol set, time step dt).
     GpuFVAssembler(Tabulation tab, int device = 0, int precision = DXG_PRECISION_FP64)
-        : tab_(std::move(tab)), ctx_(device, precision)
+        : tab_(std::move(tab)), ctx_(device, precision), jac_(this), res_(this), gv_(this)
     {
         ctx_.check(dxg_problem_upload(ctx_.get(), &tab_.descriptor()));
         int32_t b = 0;
         ctx_.check(dxg_sizes(ctx_.get(), &numCells_, &b, &numBlocks_));
         numEq_ = b;
     }
+    GpuFVAssembler(const GpuFVAssembler&) = delete;
+    GpuFVAssembler& operator=(const GpuFVAssembler&) = delete;
+
+    // FVAssembler::setLinearSystem (fvassembler.hh:294-302): the pattern and the device
+    // storage of the system exist from the upload on, so this only marks the system set up
+    void setLinearSystem() { linearSystemSet_ = true; }
     void setPreviousSolution(const SolutionVector& u)
     {
         ctx_.check(dxg_set_prev_solution(ctx_.get(), u.data()));
+        prevSol_ = u;
         stationary_ = false;
     }
-    void setTimeStepSize(double dt) { ctx_.check(dxg_set_time_step(ctx_.get(), dt)); }
+    const SolutionVector& prevSol() const { return prevSol_; }
+    void setTimeStepSize(double dt)
+    {
+        ctx_.check(dxg_set_time_step(ctx_.get(), dt));
+        dt_ = dt;
+    }
+    double timeStepSize() const { return dt_; }
     bool isStationaryProblem() const { return stationary_; }
-    void assembleJacobianAndResidual(const SolutionVector& u)
+    // FVAssembler::assembleJacobianAndResidual(curSol, partialReassembler): partial
+    // reassembly is a Newton option on the device (dxg_newton_params); a reassembler
+    // passed here is ignored
+    template <class PartialReassembler = void>
+    void assembleJacobianAndResidual(const SolutionVector& u, const PartialReassembler* = nullptr)
     {
         ctx_.check(dxg_set_solution(ctx_.get(), u.data()));
         ctx_.check(dxg_assemble_jacobian_and_residual(ctx_.get()));
@@ -324,14 +390,21 @@ public:
         ctx_.check(dxg_set_solution(ctx_.get(), u.data()));
         ctx_.check(dxg_assemble_residual(ctx_.get()));
     }
-    ResidualType residual() const
+    JacobianMatrix& jacobian() { return jac_; }
+    ResidualType& residual() { return res_; }
+    GridVariables& gridVariables() { return gv_; }
+    // FVAssembler::updateGridVariables / resetTimeStep (fvassembler.hh:379-390)
+    void updateGridVariables(const SolutionVector& u) { gv_.update(u); }
+    void resetTimeStep(const SolutionVector& u) { gv_.resetTimeStep(u); }
+
+    std::vector<double> residualHost() const
     {
-        ResidualType r(numDofs());
+        std::vector<double> r(numDofs());
         ctx_.check(dxg_get_residual(ctx_.get(), r.data()));
         return r;
     }
     // BCRS of FieldMatrix<double, numEq, numEq> blocks: row pointers, block columns, values
-    void jacobian(std::vector<int64_t>& rowPtr, std::vector<int32_t>& col, std::vector<double>& values) const
+    void jacobianHost(std::vector<int64_t>& rowPtr, std::vector<int32_t>& col, std::vector<double>& values) const
     {
         rowPtr.resize(numCells_ + 1);
         col.resize(numBlocks_);
@@ -346,21 +419,60 @@ public:
     }
     SolutionVector initialSolution() const { return tab_.initial; }
     int64_t numCells() const { return numCells_; }
+    int64_t numBlocks() const { return numBlocks_; }
     int numEq() const { return numEq_; }
     int64_t numDofs() const { return numCells_ * numEq_; }
     dxg_ctx* context() const { return ctx_.get(); }
     const Context& handle() const { return ctx_; }
 
 private:
+    friend class GpuGridVariables;
     Tabulation tab_;
     Context ctx_;
+    GpuJacobian jac_;
+    GpuResidual res_;
+    GpuGridVariables gv_;
+    SolutionVector prevSol_;
     int64_t numCells_ = 0, numBlocks_ = 0;
     int numEq_ = 1;
+    double dt_ = 0.0;
     bool stationary_ = true;
+    bool linearSystemSet_ = false;
+};
+
+inline int64_t GpuJacobian::N() const { return a_->numCells(); }
+inline int64_t GpuJacobian::nonzeroes() const { return a_->numBlocks(); }
+inline void GpuJacobian::copyToHost(std::vector<int64_t>& rowPtr, std::vector<int32_t>& col,
+                                    std::vector<double>& values) const
+{
+    a_->jacobianHost(rowPtr, col, values);
+}
+inline int64_t GpuResidual::size() const { return a_->numDofs(); }
+inline std::vector<double> GpuResidual::toHost() const { return a_->residualHost(); }
+inline void GpuGridVariables::update(const std::vector<double>& u)
+{
+    a_->ctx_.check(dxg_set_solution(a_->ctx_.get(), u.data()));
+}
+inline void GpuGridVariables::resetTimeStep(const std::vector<double>& u)
+{
+    a_->ctx_.check(dxg_set_solution(a_->ctx_.get(), u.data()));
+}
+inline void GpuGridVariables::advanceTimeStep()
+{
+    a_->ctx_.check(dxg_advance_time_step(a_->ctx_.get()));
+    a_->prevSol_.resize(a_->numDofs());
+    a_->ctx_.check(dxg_get_solution(a_->ctx_.get(), a_->prevSol_.data()));
+}
+
+// IstlSolverResult (istlsolvers.hh:153-163): converges-flag, bool-convertible.
+struct GpuSolverResult : dxg_linear_result {
+    explicit operator bool() const { return converged != 0; }
 };
 
 // Dumux::ILUBiCGSTABIstlSolver over the device (istlsolvers.hh:635-642): ILU(0)-
-// preconditioned BiCGSTAB on the system last assembled by the GpuFVAssembler.
+// preconditioned BiCGSTAB.  solve(A, x, b) and norm(x) take the assembler's device
+// handles as the reference's take its BCRS matrix and block vectors
+// (istlsolvers.hh:273, 306).
 class GpuILUBiCGSTABSolver {
 public:
     void setResidualReduction(double r) { reduction_ = r; }
@@ -369,19 +481,30 @@ public:
     // (red-black ordered ILU(0): not the reference's preconditioner, faster per time step);
     // takes effect at the assembler's next factorisation
     void setIluKernel(GpuFVAssembler& A, int kind) { A.handle().check(dxg_set_ilu_kernel(A.context(), kind)); }
-    // solve(A, x, b): A and b are the assembler's device system; x receives the update
-    bool solve(const GpuFVAssembler& A, std::vector<double>& x, const std::vector<double>& /*b*/)
+    // x = A^-1 b from x = 0: A and b are the assembler's device system (the b handle must
+    // be that assembler's residual); x receives the update on the host
+    GpuSolverResult solve(const GpuJacobian& A, std::vector<double>& x, const GpuResidual& b)
     {
-        A.handle().check(dxg_set_linear_solver(A.context(), kind_));
-        dxg_linear_result res{};
-        const int st = dxg_linear_solve(A.context(), reduction_, maxIter_, &res);
-        if (st != DXG_OK && !recoverable(st)) A.handle().check(st);
+        const GpuFVAssembler& asmb = A.assembler();
+        if (&b.assembler() != &asmb) throw Error(DXG_ERR_ARG, "solve: matrix and right-hand side of different assemblers");
+        asmb.handle().check(dxg_set_linear_solver(asmb.context(), kind_));
+        GpuSolverResult res{};
+        const int st = dxg_linear_solve(asmb.context(), reduction_, maxIter_, &res);
+        if (st != DXG_OK && !recoverable(st)) asmb.handle().check(st);
+        if (st != DXG_OK) res.converged = 0;
         last_ = res;
-        x.resize(A.numDofs());
-        A.handle().check(dxg_get_update(A.context(), x.data()));
-        return st == DXG_OK && res.converged;
+        x.resize(asmb.numDofs());
+        asmb.handle().check(dxg_get_update(asmb.context(), x.data()));
+        return res;
     }
-    double norm(const GpuFVAssembler& A) const { return A.residualNorm(); }
+    // Euclidean norm (IstlIterativeLinearSolver::norm, istlsolvers.hh:306-337)
+    double norm(const GpuResidual& r) const { return r.assembler().residualNorm(); }
+    double norm(const std::vector<double>& x) const
+    {
+        double s = 0.0;
+        for (double v : x) s += v * v;
+        return std::sqrt(s);
+    }
     const dxg_linear_result& result() const { return last_; }
 
 protected:
@@ -403,6 +526,7 @@ public:
 
 // Dumux::NewtonSolver over the device (newtonsolver.hh:179-852): the loop, the update,
 // the shift criterion, the dt retries and the time-step suggestion run in the library.
+// TimeLoop is anything with timeStepSize() and setTimeStepSize(dt), as Dumux::TimeLoop.
 class GpuNewtonSolver {
 public:
     explicit GpuNewtonSolver(GpuFVAssembler& assembler) : assembler_(assembler)
@@ -410,19 +534,36 @@ public:
         dxg_newton_default_params(&params_);
     }
     dxg_newton_params& params() { return params_; }
-    // solve(x, dt): one implicit Euler step from the assembler's previous solution (dt > 0),
-    // or the stationary solve (dt == 0); x is the initial guess and receives the solution.
-    // Throws NumericalProblem when all time-step divisions fail (NewtonSolver::solve).
-    void solve(std::vector<double>& x, double dt)
+    GpuFVAssembler& assembler() { return assembler_; }
+
+    // NewtonSolver::solve(vars, timeLoop) (newtonsolver.hh:309-355): one implicit Euler
+    // step of timeLoop.timeStepSize() from the assembler's previous solution, retried with
+    // dt * RetryTimeStepReductionFactor up to MaxTimeStepDivisions times; the time loop's
+    // step size is left at the one that succeeded.  Throws NumericalProblem when all fail.
+    template <class TimeLoop>
+    void solve(std::vector<double>& x, TimeLoop& timeLoop)
     {
-        dxg_ctx* c = assembler_.context();
-        assembler_.handle().check(dxg_set_solution(c, x.data()));
-        const int st = dxg_newton_solve(c, dt, &params_, &report_);
-        assembler_.handle().check(st);
-        assembler_.handle().check(dxg_get_solution(c, x.data()));
+        if (assembler_.isStationaryProblem())
+            throw Error(DXG_ERR_STATE, "time step control with a stationary problem");
+        run(x, timeLoop.timeStepSize(), params_);
+        timeLoop.setTimeStepSize(report_.dt_used);
+    }
+    // NewtonSolver::solve(vars) (newtonsolver.hh:362-368): the stationary solve, or one
+    // step of the assembler's time-step size when it is transient; no retries
+    void solve(std::vector<double>& x) { run(x, currentDt(), noRetry()); }
+    // NewtonSolver::apply(vars) (newtonsolver.hh:380-383): as solve(vars) but reports
+    // failure instead of throwing
+    bool apply(std::vector<double>& x)
+    {
+        try {
+            run(x, currentDt(), noRetry());
+            return true;
+        } catch (const NumericalProblem&) {
+            return false;
+        }
     }
     // TimeLoop::advanceTimeStep: the converged solution becomes the previous time level
-    void advanceTimeStep() { assembler_.handle().check(dxg_advance_time_step(assembler_.context())); }
+    void advanceTimeStep() { assembler_.gridVariables().advanceTimeStep(); }
     double suggestTimeStepSize(double oldDt) const
     {
         return dxg_suggest_time_step(assembler_.context(), oldDt, &params_);
@@ -430,6 +571,26 @@ public:
     const dxg_newton_report& report() const { return report_; }
 
 private:
+    double currentDt() const { return assembler_.isStationaryProblem() ? 0.0 : assembler_.timeStepSize(); }
+    dxg_newton_params noRetry() const
+    {
+        dxg_newton_params p = params_;
+        p.max_time_step_divisions = 0;
+        return p;
+    }
+    void run(std::vector<double>& x, double dt, const dxg_newton_params& p)
+    {
+        dxg_ctx* c = assembler_.context();
+        assembler_.handle().check(dxg_set_solution(c, x.data()));
+        const int st = dxg_newton_solve(c, dt, &p, &report_);
+        if (st != DXG_OK) {
+            // the library restored the previous solution; hand it back as the reference does
+            dxg_get_solution(c, x.data());
+            assembler_.handle().check(st);
+        }
+        assembler_.handle().check(dxg_get_solution(c, x.data()));
+    }
+
     GpuFVAssembler& assembler_;
     dxg_newton_params params_{};
     dxg_newton_report report_{};

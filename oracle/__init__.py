@@ -27,6 +27,7 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_pow_mode.argtypes = [C.c_int]
         L.orc_set_linear_threads.argtypes = [C.c_int]
+        L.orc_set_dot_order.argtypes = [C.c_int]
         L.orc_get_pow_mode.restype = C.c_int
         L.orc_pow_batch.argtypes = [C.c_int32, C.c_int64, dp, dp, dp]
         L.orc_get_threads.restype = C.c_int
@@ -63,6 +64,11 @@ def set_linear_threads(n):
     """Threads of the oracle's linear solve: 1 (default) sequential as dune-istl, 0 all host
     threads (level-scheduled ILU(0), row-parallel SpMV; results identical bit for bit)."""
     lib().orc_set_linear_threads(int(n))
+
+
+def set_dot_order(order):
+    """Summation order of the oracle's dot products: 0 sequential (dune-istl), 1 blocked."""
+    lib().orc_set_dot_order(int(order))
 
 
 POW_LIBM, POW_CORRECTLY_ROUNDED = 0, 1

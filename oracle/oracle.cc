@@ -1066,8 +1066,24 @@ static void spmv(int64_t n, int b, const int64_t* rowPtr, const int32_t* col, co
     }
 }
 
+// Summation order of the dot products: 0 (default) sequential, as dune-istl's
+// SeqScalarProduct; 1 blocked (sums of 256 consecutive products, then the block sums in
+// sequence) -- a second, equally valid order used to measure how far BiCGSTAB's results move
+// under a change of summation order alone.
+static int g_dot_order = 0;
+
 static double dot(int64_t m, const double* a, const double* c)
 {
+    if (g_dot_order == 1) {
+        double total = 0.0;
+        for (int64_t b0 = 0; b0 < m; b0 += 256) {
+            double s = 0.0;
+            const int64_t e = std::min<int64_t>(m, b0 + 256);
+            for (int64_t i = b0; i < e; ++i) s += a[i] * c[i];
+            total += s;
+        }
+        return total;
+    }
     double s = 0.0;
     for (int64_t i = 0; i < m; ++i) s += a[i] * c[i];
     return s;
@@ -1348,6 +1364,7 @@ void orc_set_threads(int n) { g_threads = n; }
 void orc_set_pow_mode(int mode) { g_pow_mode = mode; }
 int orc_get_pow_mode(void) { return g_pow_mode; }
 void orc_set_linear_threads(int n) { g_linear_threads = n; }
+void orc_set_dot_order(int order) { g_dot_order = order; }
 void orc_pow_batch(int32_t mode, int64_t n, const double* x, const double* y, double* out)
 {
     for (int64_t i = 0; i < n; ++i) out[i] = mode == 1 ? dxg::crPow(x[i], y[i]) : std::pow(x[i], y[i]);

@@ -40,6 +40,9 @@ void orc_pow_batch(int32_t mode, int64_t n, const double* x, const double* y, do
  * BiCGSTABSolver; 0 all, n > 1 that many -- SpMV rows, vector updates and the ILU(0) rows of
  * each wavefront level in parallel, dot products sequential; identical results. */
 void orc_set_linear_threads(int n);
+/* Summation order of the linear solver's dot products: 0 sequential (default, as dune-istl),
+ * 1 blocked by 256 -- for measuring the sensitivity of BiCGSTAB to the order alone. */
+void orc_set_dot_order(int order);
 
 /* Jacobian pattern: diagonal + (J, I) for each neighbour J of I, sorted columns. */
 int orc_num_blocks(const dxg_problem_desc* d, int64_t* nnzb);

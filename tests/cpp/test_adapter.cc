@@ -1,7 +1,10 @@
 // Drop-in check of the C++ adapter (include/dumux_gb300.hh): a DuMux-style 2p problem and
 // spatial-params class, written against the reference's *AtPos interface (the shape of
 // test/porousmediumflow/2p/incompressible/problem.hh and spatialparams.hh), driven through
-// GpuFVAssembler / GpuILUBiCGSTABSolver / GpuNewtonSolver.
+// GpuFVAssembler / GpuILUBiCGSTABSolver / GpuNewtonSolver with the reference's method
+// signatures, and by a Newton loop written only against the reference's Assembler /
+// LinearSolver concepts (the calls dumux/nonlinear/newtonsolver.hh makes; the concept's
+// mock is test/nonlinear/newton/test_newton.cc:30-78).
 //
 //   test_adapter NX NY NZ STEPS OUT.bin
 // writes the solution after STEPS implicit Euler steps of 250 s as raw doubles; exits 3
@@ -74,6 +77,50 @@ public:
     }
 };
 
+// Dumux::TimeLoop's step-size interface.
+struct FixedTimeLoop {
+    double dt;
+    double timeStepSize() const { return dt; }
+    void setTimeStepSize(double d) { dt = d; }
+};
+
+// The reference's Newton iteration over any Assembler / LinearSolver pair, using only the
+// calls NewtonSolver makes: setLinearSystem (newtonsolver.hh:228), setResidualReduction
+// (:232), assembleJacobianAndResidual (:469-475), norm(residual()) (:494-495),
+// solve(jacobian(), deltaU, residual()) (:1205), the update u = uLastIter - deltaU (:556-558),
+// updateGridVariables (:861-867), the maximum relative shift (:110-128, 1138-1144) and the
+// MinSteps / MaxSteps / shift-criterion decisions (:428-446, 657-701).
+template <class Assembler, class LinearSolver>
+int referenceShapedNewton(Assembler& assembler, LinearSolver& linearSolver, typename Assembler::SolutionVector& u,
+                          double maxRelativeShift = 1e-8, int minSteps = 2, int maxSteps = 18)
+{
+    assembler.setLinearSystem();
+    linearSolver.setResidualReduction(1e-6);
+    typename Assembler::SolutionVector uLastIter = u, deltaU(u.size(), 0.0);
+    double shift = 1e300;
+    int numSteps = 0;
+    double initialResidual = 0.0;
+    auto converged = [&] { return shift <= maxRelativeShift; };
+    while (numSteps < minSteps || (!converged() && numSteps < maxSteps)) {
+        uLastIter = u;
+        assembler.assembleJacobianAndResidual(u);
+        if (numSteps == 0) initialResidual = linearSolver.norm(assembler.residual());
+        std::fill(deltaU.begin(), deltaU.end(), 0.0);
+        if (!linearSolver.solve(assembler.jacobian(), deltaU, assembler.residual()))
+            throw NumericalProblem(DXG_ERR_LINEAR_NOT_CONVERGED, "linear solve did not converge");
+        for (size_t k = 0; k < u.size(); ++k) u[k] = uLastIter[k] - deltaU[k];
+        assembler.updateGridVariables(u);
+        shift = 0.0;
+        for (size_t k = 0; k < u.size(); ++k) {
+            const double rel = std::fabs(uLastIter[k] - u[k]) / std::max(1.0, std::fabs(uLastIter[k] + u[k]) / 2.0);
+            shift = std::max(shift, rel);
+        }
+        ++numSteps;
+    }
+    if (!(initialResidual > 0.0)) throw NumericalProblem(DXG_ERR_NAN, "no initial residual");
+    return converged() ? numSteps : -numSteps;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 6) {
@@ -94,24 +141,32 @@ int main(int argc, char** argv)
         assembler.setTimeStepSize(250.0);
 
         // assembler + linear solver as a LinearPDESolver would use them
+        assembler.setLinearSystem();
         assembler.assembleJacobianAndResidual(u);
         std::vector<int64_t> rowPtr;
         std::vector<int32_t> col;
         std::vector<double> vals;
-        assembler.jacobian(rowPtr, col, vals);
+        assembler.jacobian().copyToHost(rowPtr, col, vals);
+        if (rowPtr.back() != assembler.jacobian().nonzeroes() || assembler.jacobian().N() != assembler.numCells())
+            return 1;
         GpuILUBiCGSTABSolver linear;
         linear.setResidualReduction(1e-10);
         std::vector<double> du;
-        if (!linear.solve(assembler, du, assembler.residual())) {
+        if (!linear.solve(assembler.jacobian(), du, assembler.residual())) {
             std::fprintf(stderr, "linear solve did not converge\n");
             return 1;
         }
-        if ((int64_t)rowPtr.back() != (int64_t)col.size()) return 1;
+        // norm(residual()) reads the device residual; the host copy gives the same norm
+        const double rDev = linear.norm(assembler.residual()), rHost = linear.norm(assembler.residual().toHost());
+        if (std::fabs(rDev - rHost) > 1e-12 * rHost) {
+            std::fprintf(stderr, "norms differ: %g %g\n", rDev, rHost);
+            return 1;
+        }
         // the AMGBiCGSTAB solver type on the same system: the same update to the tolerance
         GpuAMGBiCGSTABSolver amg;
         amg.setResidualReduction(1e-10);
         std::vector<double> duAmg;
-        if (!amg.solve(assembler, duAmg, assembler.residual())) {
+        if (!amg.solve(assembler.jacobian(), duAmg, assembler.residual())) {
             std::fprintf(stderr, "AMG linear solve did not converge\n");
             return 1;
         }
@@ -127,19 +182,47 @@ int main(int argc, char** argv)
         // the Newton loop below uses the default ILU(0)-BiCGSTAB again
         if (dxg_set_linear_solver(assembler.context(), DXG_LINEAR_SOLVER_ILU_BICGSTAB) != DXG_OK) return 1;
 
-        // the Newton loop with the time loop of the reference's 2p test
+        // (1) the library's Newton loop through NewtonSolver::solve(vars, timeLoop)
         GpuNewtonSolver newton(assembler);
-        double dt = 250.0;
+        FixedTimeLoop timeLoop{250.0};
+        std::vector<int> itsLib;
         for (int s = 0; s < steps; ++s) {
-            newton.solve(u, dt);
+            newton.solve(u, timeLoop);
+            itsLib.push_back(newton.report().iterations);
             newton.advanceTimeStep();
+        }
+        // (2) the reference's Newton iteration over the same classes, on a second assembler
+        GpuFVAssembler asm2(tabulate<2>(grid, problem, params, fluids, AssemblyParams{}));
+        std::vector<double> u2 = asm2.initialSolution();
+        asm2.setPreviousSolution(u2);
+        asm2.setTimeStepSize(250.0);
+        GpuILUBiCGSTABSolver linear2;
+        linear2.setMaxIter(newton.params().linear_max_iter);
+        for (int s = 0; s < steps; ++s) {
+            const int its = referenceShapedNewton(asm2, linear2, u2);
+            if (its != itsLib[s]) {
+                std::fprintf(stderr, "step %d: reference-shaped loop %d iterations, library %d\n", s, its, itsLib[s]);
+                return 1;
+            }
+            asm2.gridVariables().advanceTimeStep();
+            if (asm2.prevSol() != u2) return 1;
+        }
+        double diff = 0, scale = 0;
+        for (size_t k = 0; k < u.size(); ++k) {
+            diff = std::max(diff, std::fabs(u[k] - u2[k]));
+            scale = std::max(scale, std::fabs(u[k]));
+        }
+        if (diff > 1e-12 * scale) {
+            std::fprintf(stderr, "reference-shaped loop differs from the library loop: %g of %g\n", diff, scale);
+            return 1;
         }
         std::FILE* f = std::fopen(argv[5], "wb");
         if (!f) return 1;
         std::fwrite(u.data(), sizeof(double), u.size(), f);
         std::fclose(f);
-        std::printf("ok cells=%lld newton_last=%d linear_first=%d\n", (long long)assembler.numCells(),
-                    newton.report().iterations, linear.result().iterations);
+        std::printf("ok cells=%lld newton_last=%d linear_first=%d loops_max_diff=%g\n",
+                    (long long)assembler.numCells(), newton.report().iterations, linear.result().iterations,
+                    diff / scale);
         return 0;
     } catch (const Error& e) {
         if (e.status == DXG_ERR_NO_DEVICE) {

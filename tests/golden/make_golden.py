@@ -1,7 +1,8 @@
 """Extracts the reference's golden vectors for the cc-TPFA hot path into small fixtures.
 
-Run in a container that has the DuMux source tree at REFERENCE (default
-/root/reference); the GPU host does not, so the extracted values are committed:
+Run with the DuMux source tree named by the environment variable DUMUX_REFERENCE
+(python make_golden.py with DUMUX_REFERENCE=<path to the DuMux tree>); the GPU host has
+no such tree, so the extracted values are committed:
   onep_lens_p.txt          cell field "p" of test/references/test_1p_cc-reference.vtu
                            (test_1p_incompressible_tpfa[_numdiff], 10x10 lens, 100 cells)
   pcsw_brookscorey.txt     test/references/test_pcsw_brookscorey-reference.dat
@@ -20,11 +21,13 @@ import os
 import re
 import sys
 
-REFERENCE = os.environ.get("DUMUX_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("DUMUX_REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
+    if not REFERENCE:
+        sys.exit("set DUMUX_REFERENCE to the DuMux source tree")
     vtu = open(os.path.join(REFERENCE, "test/references/test_1p_cc-reference.vtu")).read()
     m = re.search(r'Name="p"[^>]*>(.*?)</DataArray>', vtu, re.S)
     vals = m.group(1).split()

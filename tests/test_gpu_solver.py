@@ -65,6 +65,16 @@ def _run_time_loop_gpu(desc, u0, dt, steps, params, precision="fp64"):
     return ctx.solution(), reps
 
 
+def _norm_deviation(reps_a, reps_b):
+    """Largest per-iteration residual-norm difference, relative to each step's initial residual."""
+    dev = 0.0
+    for a, b in zip(reps_a, reps_b):
+        n = a["iterations"]
+        d = np.abs(np.array(a["residual_norm"][:n]) - np.array(b["residual_norm"][:n])) / b["initial_residual"]
+        dev = max(dev, float(d.max()))
+    return dev
+
+
 @pytest.mark.parametrize("pow_mode", [oracle.POW_CORRECTLY_ROUNDED, oracle.POW_LIBM], ids=["crpow", "libm"])
 def test_newton_2p_matches_oracle_fp64(pow_mode):
     desc, u0 = problems.dnapl_2p(cells=(8, 6, 5), seed=4, inflow=0.04)
@@ -72,19 +82,26 @@ def test_newton_2p_matches_oracle_fp64(pow_mode):
     u_gpu, reps = _run_time_loop_gpu(desc, u0, 250.0, 3, p)
     with oracle.pow_mode(pow_mode):
         u_orc, oreps = oracle.time_loop(desc, u0, 250.0, 3, params=p, max_dt=250.0)
-    # with the same pow the assembly is bit-identical and the per-iteration residual norms
-    # differ only through the summation order of BiCGSTAB's dot products; with the C
-    # library's pow (not correctly rounded in ~0.1% of arguments) an ulp of a capillary
-    # pressure becomes a ~1e-8 relative Jacobian difference that moves the intermediate
-    # iterates (not the converged one)
-    tol = 1e-9 if pow_mode == oracle.POW_CORRECTLY_ROUNDED else 1e-6
+        # the same oracle with its dot products summed in another order: BiCGSTAB's solution
+        # moves by its forward error (~condition number x rounding), and with it the
+        # intermediate Newton residuals, by ~1e-7 of r0 on this problem
+        oracle.set_dot_order(1)
+        try:
+            _, oreps2 = oracle.time_loop(desc, u0, 250.0, 3, params=p, max_dt=250.0)
+        finally:
+            oracle.set_dot_order(0)
+    floor = _norm_deviation(oreps2, oreps)
     for rg, ro in zip(reps, oreps):
         assert rg["iterations"] == ro["iterations"]
         assert rg["dt_used"] == ro["dt_used"]
         assert rg["initial_residual"] == pytest.approx(ro["initial_residual"], rel=1e-12)
-        n = rg["iterations"]
-        rn_g, rn_o = np.array(rg["residual_norm"][:n]), np.array(ro["residual_norm"][:n])
-        assert np.all(np.abs(rn_g - rn_o) <= tol * rg["initial_residual"])
+    # with the correctly rounded pow the assembly is bit-identical, and the device's
+    # per-iteration residual norms follow the oracle's to within the oracle's own
+    # sensitivity to the summation order; with the C library's pow (not correctly rounded in
+    # ~0.1% of arguments) an ulp of a capillary pressure adds a ~1e-8 relative Jacobian
+    # difference
+    dev = _norm_deviation(reps, oreps)
+    assert dev <= max(1e-9, (4.0 if pow_mode == oracle.POW_CORRECTLY_ROUNDED else 20.0) * floor), (dev, floor)
     scale = np.max(np.abs(u_orc.reshape(-1, 2)), axis=0)
     err = np.max(np.abs((u_gpu - u_orc).reshape(-1, 2)), axis=0) / scale
     assert np.all(err <= 1e-9), err
