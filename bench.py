@@ -222,7 +222,8 @@ def bench_config(desc, steps, warmup, precision="fp64"):
             "time_steps": (f"{steps} timed stationary Newton steps from the same initial state after {warmup} "
                            "warm-up steps" if stationary else
                            f"time steps {warmup + 1}..{warmup + steps} of the seeded initial state "
-                           f"({warmup} warm-up steps advance the simulation), dt = 250 s each"),
+                           f"({warmup} warm-up steps advance the simulation); TimeLoop.MaxTimeStepSize 250 s "
+                           "and the Newton solver's step-size suggestion below it"),
             "l2": "GPU arm: flushed between timed steps (256 MiB write)"}
 
 
@@ -261,18 +262,22 @@ def run_reference(args, cells):
     dt = 0.0 if stationary else args.dt
     u = np.array(u0, dtype=np.float64)
 
-    def one_step(u):
+    def one_step(u, dt):
         st, u_new, rep = oracle.newton_solve(desc, u0 if stationary else u, u0 if stationary else u, dt, params)
         if st != 0:
             raise RuntimeError(f"oracle time step failed with status {st}")
-        return (u if stationary else u_new), rep["iterations"] + rep["wasted_iterations"]
+        n = rep["iterations"] + rep["wasted_iterations"]
+        # TimeLoop with MaxTimeStepSize: NewtonSolver::suggestTimeStepSize, capped
+        dt_next = dt if stationary else min(oracle.suggest_time_step(rep["iterations"], rep["dt_used"], params),
+                                            args.dt)
+        return (u if stationary else u_new), n, dt_next
 
     for _ in range(args.warmup):
-        u, _ = one_step(u)
+        u, _, dt = one_step(u, dt)
     t0 = time.perf_counter()
     work, iters = 0, []
     for _ in range(args.steps):
-        u, n = one_step(u)
+        u, n, dt = one_step(u, dt)
         iters.append(n)
         work += desc.num_cells * n
     total = time.perf_counter() - t0
@@ -377,9 +382,9 @@ FORMS = (("mixed", "mixed", "natural", "ilu"), ("mixed+redblack", "mixed", "redb
          ("mixed+amg", "mixed", "natural", "amg"))
 
 
-def run_forms(desc, u_start, u_ref, dt, steps, device, plain_ms_per_step, plain_value, flush):
+def run_forms(desc, u_start, u_ref, dt_seq, device, plain_ms_per_step, plain_value, flush):
     """Each form of FORMS over the same time steps as the timed plain FP64 region: from
-    the same state u_start, `steps` implicit-Euler steps timed with CUDA events on the
+    the same state u_start, the implicit-Euler steps of sizes dt_seq timed with CUDA events on the
     context's stream (L2 flushed between steps); one untimed step from u_start first
     (kernel loading, launch-shape tuning, AMG setup).  Reports the speed-up per time step
     over plain FP64 and the error of p_w and S_n against the plain FP64 fields u_ref."""
@@ -397,9 +402,10 @@ def run_forms(desc, u_start, u_ref, dt, steps, device, plain_ms_per_step, plain_
             params = newton_params(linear_max_iter=1000)
         if solver == "amg":
             ctx.set_linear_solver("amg")
+        steps = len(dt_seq)
         ctx.set_solution(u_start)
         ctx.set_prev_solution(u_start)
-        ctx.newton_solve(dt, params)
+        ctx.newton_solve(dt_seq[0], params)
         ctx.set_solution(u_start)
         ctx.set_prev_solution(u_start)
         stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=device)
@@ -408,7 +414,7 @@ def run_forms(desc, u_start, u_ref, dt, steps, device, plain_ms_per_step, plain_
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         its, work = [], 0
-        for _ in range(steps):
+        for dt in dt_seq:
             rep = ctx.newton_solve(dt, params)
             ctx.advance_time_step()
             its.append(rep["iterations"] + rep["wasted_iterations"])
@@ -817,12 +823,20 @@ def main():
     # warm-up time steps (advance the simulation)
     ctx.set_solution(u0)
     ctx.set_prev_solution(u0)
+
+    def next_dt(dt, rep):
+        # TimeLoop with MaxTimeStepSize: NewtonSolver::suggestTimeStepSize, capped
+        return dt if stationary else min(ctx.suggest_time_step(rep["dt_used"], params), args.dt)
+
+    dt = args.dt
     for _ in range(args.warmup):
         if stationary:
             ctx.set_solution(u0)
-        ctx.newton_solve(args.dt, params)
+        rep = ctx.newton_solve(dt, params)
         ctx.advance_time_step()
+        dt = next_dt(dt, rep)
     u_start = u0 if stationary else ctx.solution()
+    dt_start = dt
 
     # ---- device-resident timed region
     launches0 = ctx.kernel_launches()
@@ -835,11 +849,14 @@ def main():
     ev0.record(stream)
     work = 0
     newton_iters = []
+    dt_seq = []
     for _ in range(args.steps):
         if stationary:
             ctx.set_solution(u0)            # each step solves the same stationary problem
-        rep = ctx.newton_solve(args.dt, params)
+        dt_seq.append(dt)
+        rep = ctx.newton_solve(dt, params)
         ctx.advance_time_step()
+        dt = next_dt(dt, rep)
         newton_iters.append(rep["iterations"] + rep["wasted_iterations"])
         work += ctx.num_cells * newton_iters[-1]
         with torch.cuda.stream(stream):
@@ -862,9 +879,9 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_work = 0
-    for _ in range(args.steps):
+    for k in range(args.steps):
         ctx.set_solution(u0 if stationary else host_u)   # h2d: initial guess of the step
-        rep = ctx.newton_solve(args.dt, params)
+        rep = ctx.newton_solve(dt_seq[k], params)
         host_u = ctx.solution()             # d2h: result of the step
         ctx.advance_time_step()
         e2e_work += ctx.num_cells * (rep["iterations"] + rep["wasted_iterations"])
@@ -881,7 +898,7 @@ def main():
     ctx.set_solution(u0 if stationary else u_after)
     ctx.set_prev_solution(u_after)
     ctx.set_kernel_timing(True)
-    ctx.newton_solve(args.dt, params)
+    ctx.newton_solve(dt, params)
     sweep_n, sweep_ms, sweep_bytes = ctx.kernel_timing("ilu_sweep")
     sweep_flops = sweep_flops_per_apply(cells, desc.num_eq)
     asm_n, asm_ms, asm_bytes = ctx.kernel_timing("assembly")
@@ -936,7 +953,7 @@ def main():
     if rank == 0 and world == 1 and headline and not args.no_forms:
         # the GB300 forms of the same problem over the same time steps (from u_start), and
         # shorter instances of the batched and served workloads
-        line["forms"] = run_forms(desc, u_start, u_after, args.dt, args.steps, local, ms / args.steps, value, flush)
+        line["forms"] = run_forms(desc, u_start, u_after, dt_seq, local, ms / args.steps, value, flush)
         line["forms"]["note"] = ("each form from the state the timed FP64 region started from, over the same "
                                  f"{args.steps} time steps; errors against the FP64 fields at their end")
         line["ensemble"] = ensemble_summary(local)
@@ -947,7 +964,7 @@ def main():
             line["roofline"]["fp64"] = fp64_roof(line["roofline"], line["fp64_peak"]["tflops"], sweep_flops, sweep_n,
                                                  sweep_ms)
     if rank == 0:
-        rate, sec_cpu, n_cpu = cpu_sample(desc, u_start, args.dt, args.cpu_sample_iters)
+        rate, sec_cpu, n_cpu = cpu_sample(desc, u_start, dt_start, args.cpu_sample_iters)
         import oracle
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
                                 "sample": f"first {n_cpu} Newton iterations of one time step "
@@ -957,7 +974,7 @@ def main():
             threads = oracle.get_threads()
             oracle.set_threads(1)
             try:
-                rate1, sec1, n1 = cpu_sample(desc, u_start, args.dt, 1)
+                rate1, sec1, n1 = cpu_sample(desc, u_start, dt_start, 1)
             finally:
                 oracle.set_threads(threads)
             line["cpu_baseline"]["single_core"] = {"value": rate1, "unit": UNIT,
