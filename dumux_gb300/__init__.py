@@ -71,6 +71,7 @@ def lib():
         L.dxg_suggest_time_step.restype = C.c_double
         L.dxg_advance_time_step.argtypes = [vp]
         L.dxg_set_ilu_kernel.argtypes = [vp, C.c_int]
+        L.dxg_set_wait_limit.argtypes = [vp, C.c_double]
         L.dxg_set_linear_solver.argtypes = [vp, C.c_int]
         L.dxg_stream_handle.argtypes = [vp]
         L.dxg_stream_handle.restype = C.c_void_p
@@ -252,11 +253,16 @@ class Context:
         return self._L.dxg_suggest_time_step(self._h, float(old_dt), C.byref(p))
 
     def set_ilu_kernel(self, kind):
-        """'auto' / 'wavefront' (one cluster launch per sweep) or 'levels' (one launch per
+        """'auto' / 'wavefront' (one cluster launch per sweep), 'lanes' (two lanes per grid line,
+        one plane per CTA over several clusters; 3D 2x2 blocks) or 'levels' (one launch per
         level): the natural-order ILU(0) of the reference; 'redblack': ILU(0) of the red-black
         reordered matrix (a different preconditioner, two parallel passes per sweep)."""
         self._check(self._L.dxg_set_ilu_kernel(self._h, {"auto": 0, "wavefront": 1, "levels": 2,
-                                                          "redblack": 3}[kind]))
+                                                          "redblack": 3, "lanes": 4}[kind]))
+
+    def set_wait_limit(self, seconds):
+        """Limit of every bounded wait inside the ILU(0) sweeps (dxg_set_wait_limit)."""
+        self._check(self._L.dxg_set_wait_limit(self._h, float(seconds)))
 
     def set_linear_solver(self, kind):
         """'ilu' (ILU(0)-BiCGSTAB, the default) or 'amg' (BiCGSTAB preconditioned by one

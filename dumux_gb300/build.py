@@ -23,6 +23,7 @@ UNITS = {
     "assemble.cu": ["--fmad=false"],
     "linalg.cu": [],
     "wave.cu": [],
+    "lanewave.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],

@@ -242,8 +242,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     if (d->diff_method != 0 && d->diff_method != 1) throw Error(DXG_ERR_ARG, "diff_method must be 0 or 1");
     // internal method code: 1 / 0 / -1 numeric differences, 3 analytic derivatives
     const int method = d->diff_method == 1 ? 3 : d->numeric_difference_method;
-    if (method != 1 && method != 0 && method != -1 && method != 3)
-        throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0 or -1 on the device");
+    if (method != 1 && method != 0 && method != -1 && method != 5 && method != 3)
+        throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0, -1 or 5");
     if (d->num_eq == 2 && d->material_law != 0 && d->material_law != 1)
         throw Error(DXG_ERR_ARG, "material_law must be 0 (Brooks-Corey) or 1 (Van Genuchten)");
     if (d->num_eq == 2 && (d->num_materials < 1 || d->num_materials > kMaxMaterials || !d->material_params))
@@ -504,7 +504,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
         c->bytesSpmv = nnzb * bb8 + N * 1.0 + 2.0 * N * v8;
         // assembly: u read, volume variables written and read back, coefficients,
         // Jacobian rows and residual written
-        const int NS = method == 3 ? 1 : 1 + (method == 0 ? 2 * b : b);
+        const int NS = method == 3 ? 1 : 1 + statesPerPv(method) * b;
         c->bytesAssembly = N * v8 + 3.0 * N * NS * v8 + N * b * 8.0 /*eps*/ + N * (8.0 * dim + 2.0 * 2 * b * 8.0) +
                            N * (3 * 8.0 + 1 + b * 8.0) + (double)c->slots * N * bb8 + N * v8;
     }
@@ -540,7 +540,7 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     upload(c->perm, perm, st);
     DXG_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
 
-    const int NS = method == 3 ? 1 : 1 + (method == 0 ? 2 * b : b);
+    const int NS = method == 3 ? 1 : 1 + statesPerPv(method) * b;
     const int64_t M = N * b;
     c->u.alloc(M);
     c->uprev.alloc(M);
@@ -573,7 +573,13 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->scal.alloc(4);
     c->singular.alloc(2);
     c->wavePlan = makeWavePlan(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b, c->precision == DXG_PRECISION_FP64);
+    c->lanePlan = c->precision == DXG_PRECISION_FP64 ? makeLanePlan<double>(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b)
+                                                      : makeLanePlan<float>(dim, (int)g.n[0], (int)g.n[1], (int)g.n[2], b);
     c->waveTuned = false;
+    c->laneWave = false;
+    c->laneTuneMs = 0.0;
+    c->laneHandoff.release();
+    c->laneHandoffBytes = 0;
     c->waveTuneCount = 0;
     c->dropGraphs();   // the captured chunks hold the old buffers' addresses
     DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
@@ -645,12 +651,58 @@ WaveArgs<T> waveArgs(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* rhs, T* v)
     w.err = c->singular.get() + 1;
     w.singular = c->singular.get();
     w.ks = c->ks.get();
+    w.waitNs = c->waitNs;
     return w;
 }
 
 bool useWave(const dxg_ctx* c)
 {
     return c->iluKernel != DXG_ILU_LEVELS && c->iluKernel != DXG_ILU_REDBLACK && c->wavePlan.ok;
+}
+
+// The lane sweeps apply the preconditioner (the factorisation stays with the cluster
+// wavefront or the level-scheduled kernels).
+bool useLane(const dxg_ctx* c)
+{
+    return c->lanePlan.ok && c->linearSolver == DXG_LINEAR_SOLVER_ILU_BICGSTAB &&
+           (c->iluKernel == DXG_ILU_LANES || (c->iluKernel == DXG_ILU_AUTO && c->laneWave));
+}
+
+// The hand-off buffer of the lane sweeps between clusters, all bits set (the kernels' "not
+// written yet" pattern); made on first use, refilled after a sweep gave up waiting.
+template <class T>
+T* laneHandoff(dxg_ctx* c)
+{
+    const size_t bytes = (size_t)c->lanePlan.ctas * c->pcHost.nx * 64 * 2 * sizeof(T);
+    if (c->laneHandoffBytes != bytes) {
+        c->laneHandoff.alloc(bytes);
+        c->laneHandoffBytes = bytes;
+        DXG_CUDA(cudaMemsetAsync(c->laneHandoff.get(), 0xff, bytes, c->stream));
+    }
+    return reinterpret_cast<T*>(c->laneHandoff.get());
+}
+
+template <class T>
+LaneWaveArgs<T> laneArgs(dxg_ctx* c, const T* A, const T* L, const T* Dinv, const T* rhs, T* v)
+{
+    LaneWaveArgs<T> w{};
+    w.nx = c->pcHost.nx;
+    w.ny = c->pcHost.ny;
+    w.nz = c->pcHost.nz;
+    w.N = c->N;
+    w.nyb = c->lanePlan.nyb;
+    w.ctas = c->lanePlan.ctas;
+    w.clusterSize = c->lanePlan.clusterSize;
+    w.Lf = L;
+    w.A = A;
+    w.Dinv = Dinv;
+    w.rhs = rhs;
+    w.v = v;
+    w.err = c->singular.get() + 1;
+    w.ks = c->ks.get();
+    w.handoff = laneHandoff<T>(c);
+    w.waitNs = c->waitNs ? c->waitNs : 500000000ull;
+    return w;
 }
 
 template <class T>
@@ -733,7 +785,7 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
     c->waveTuned = true;
     const std::vector<WavePlan> cand = wavePlanCandidates(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
                                                           (int)c->pcHost.nz, c->b, sizeof(T) == 8);
-    if (cand.size() < 2) return;
+    if (cand.size() < 2 && !(c->lanePlan.ok && c->iluKernel == DXG_ILU_AUTO)) return;
     cudaStream_t st = c->stream;
     cudaEvent_t e0, e1;
     DXG_CUDA(cudaEventCreate(&e0));
@@ -766,6 +818,24 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
             best = p;
         }
     }
+    // the lane sweeps (3D, 2x2 blocks), when their plan fits
+    if (c->lanePlan.ok && c->iluKernel == DXG_ILU_AUTO) {
+        LaneWaveArgs<T> lt = laneArgs<T>(c, A, L, Dinv, in, out);
+        lt.ks = nullptr;   // never skip while timing
+        launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);   // warm-up
+        DXG_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < kReps; ++r) launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);
+        DXG_CUDA(cudaEventRecord(e1, st));
+        DXG_CUDA(cudaEventSynchronize(e1));
+        c->launches += 2 * (1 + kReps);
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= kReps;
+        c->laneTuneMs = ms;
+        int flag = 0;
+        DXG_CUDA(cudaMemcpy(&flag, c->singular.get() + 1, sizeof(int), cudaMemcpyDeviceToHost));
+        c->laneWave = flag == 0 && ms < bestMs;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->wavePlan = best;
@@ -776,6 +846,11 @@ int64_t iluApply(dxg_ctx* c, const IluArgs<T, T>& ia, const T* A, T* L, T* Dinv,
 {
     TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(T) / 8.0);
     if (c->iluKernel == DXG_ILU_REDBLACK) return launchRbApply<T>(rbArgs<T>(c, A, Dinv), c->b, c->dim, d, v, c->stream);
+    if (useLane(c)) {
+        const LaneWaveArgs<T> la = laneArgs<T>(c, A, L, Dinv, d, v);
+        launchLaneWaveApply<T>(c->lanePlan, la, la, c->stream);
+        return 2;
+    }
     if (useWave(c)) {
         launchWaveApply<T>(c->wavePlan, waveArgs<T>(c, A, L, Dinv, d, v), waveArgs<T>(c, A, L, Dinv, d, v), c->b,
                            c->stream);
@@ -910,7 +985,7 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     const int chunk = graphs ? 8 : 4;
     dxg_ctx::ChunkGraph& G = c->chunkGraph[mixed ? 1 : 0];
     if (graphs) {
-        const int key[4] = {c->iluKernel + 16 * c->linearSolver, useWave(c) ? c->wavePlan.ctas : 0,
+        const int key[4] = {c->iluKernel + 16 * c->linearSolver, useLane(c) ? -1 : useWave(c) ? c->wavePlan.ctas : 0,
                             useWave(c) ? c->wavePlan.threads : 0, chunk};
         if (G.exec && !std::equal(key, key + 4, G.key)) {
             cudaGraphExecDestroy(G.exec);
@@ -952,7 +1027,14 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     DXG_CUDA(cudaMemcpyAsync(flags, c->singular.get(), 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     DXG_CUDA(cudaStreamSynchronize(st));
     const int sing = flags[0];
-    if (flags[1]) throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out");
+    if (flags[1]) {
+        // a sweep that gave up may leave hand-off entries written: start the next from scratch
+        if (c->laneHandoffBytes)
+            DXG_CUDA(cudaMemsetAsync(c->laneHandoff.get(), 0xff, c->laneHandoffBytes, st));
+        DXG_CUDA(cudaMemsetAsync(c->singular.get() + 1, 0, sizeof(int), st));
+        DXG_CUDA(cudaStreamSynchronize(st));
+        throw Error(DXG_ERR_TIMEOUT, "ILU(0) wavefront wait timed out");
+    }
     const KrylovState& ks = *c->ksHost;
     dxg_linear_result res{};
     res.converged = ks.status == KS_CONVERGED;
@@ -1468,13 +1550,25 @@ int dxg_advance_time_step(dxg_ctx* c)
 
 int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
 {
-    if (!c || kind < DXG_ILU_AUTO || kind > DXG_ILU_REDBLACK) return DXG_ERR_ARG;
+    if (!c || kind < DXG_ILU_AUTO || kind > DXG_ILU_LANES) return DXG_ERR_ARG;
     if (kind == DXG_ILU_WAVEFRONT && c->uploaded && !c->wavePlan.ok) {
         c->err = "no wavefront plan fits this grid";
         return DXG_ERR_ARG;
     }
+    if (kind == DXG_ILU_LANES && c->uploaded && !c->lanePlan.ok) {
+        c->err = "the lane sweeps need a 3D grid of 2x2 blocks that fits them";
+        return DXG_ERR_ARG;
+    }
     c->iluKernel = kind;
     c->haveFactor = false;
+    return DXG_OK;
+}
+
+int dxg_set_wait_limit(dxg_ctx* c, double seconds)
+{
+    if (!c || !(seconds > 0.0) || seconds > 60.0) return DXG_ERR_ARG;
+    c->waitNs = (unsigned long long)(seconds * 1e9);
+    c->dropGraphs();   // the captured chunks hold the old limit in their arguments
     return DXG_OK;
 }
 
@@ -1496,7 +1590,22 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
                                                                (int)c->pcHost.nz).size() + 1) +
               " levels of 2x2(x2) aggregation, damped block-Jacobi smoothing";
     else if (c->iluKernel == DXG_ILU_REDBLACK) out = "ILU(0): red-black ordering, two parallel passes per sweep";
-    else if (!useWave(c)) out = "ILU(0): level-scheduled kernels";
+    else if (useLane(c)) {
+        const LanePlan& p = c->lanePlan;
+        char tmp[200];
+        std::snprintf(tmp, sizeof tmp, "ILU(0): lane wavefront, %d CTAs of 128 threads in clusters of %d", p.ctas,
+                      p.clusterSize);
+        out = tmp;
+        if (c->laneTuneMs > 0) {
+            std::snprintf(tmp, sizeof tmp, ", tuned (ms per apply: lanes %.3f", c->laneTuneMs);
+            out += tmp;
+            for (int k = 0; k < c->waveTuneCount; ++k) {
+                std::snprintf(tmp, sizeof tmp, ", cluster wavefront %d CTAs %.3f", c->waveTuneCtas[k], c->waveTuneMs[k]);
+                out += tmp;
+            }
+            out += ")";
+        }
+    } else if (!useWave(c)) out = "ILU(0): level-scheduled kernels";
     else {
         const WavePlan& p = c->wavePlan;
         out = "ILU(0): wavefront, cluster " + std::to_string(p.ctas) + " x " + std::to_string(p.threads) +
@@ -1506,6 +1615,10 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
             char tmp[64];
             for (int k = 0; k < c->waveTuneCount; ++k) {
                 std::snprintf(tmp, sizeof tmp, " %d CTAs %.3f", c->waveTuneCtas[k], c->waveTuneMs[k]);
+                out += tmp;
+            }
+            if (c->laneTuneMs > 0) {
+                std::snprintf(tmp, sizeof tmp, "; lane wavefront %.3f", c->laneTuneMs);
                 out += tmp;
             }
             out += ")";

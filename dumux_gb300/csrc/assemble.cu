@@ -72,11 +72,14 @@ __device__ __forceinline__ double numericEps(const ProblemConsts& pc, double x, 
 }
 
 // States per cell: 0 = own solution; forward/backward: 1+pv = x[pv] +/- eps;
-// central: 1+2pv = x+eps, 2+2pv = x-eps.  METHOD 2 selects state 0 only (residual).
+// central: 1+2pv = x+eps, 2+2pv = x-eps; five-point stencil (NumericDifferentiation,
+// dumux/common/numericdifferentiation.hh:79-88, in its order of evaluation): 1+4pv = x+eps,
+// 2+4pv = x-eps, 3+4pv = x-2eps, 4+4pv = x+2eps.  METHOD 2 selects state 0 only (residual).
 template <int B, int METHOD>
 __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ batch)
 {
-    constexpr int NS = 1 + (METHOD == 0 ? 2 * B : ((METHOD == 2 || METHOD == 3) ? 0 : B));
+    constexpr int SP = statesPerPv(METHOD);
+    constexpr int NS = 1 + SP * B;
     const AssemblyArgs a = batch ? batch[blockIdx.y] : a0;
     const ProblemConsts& pc = *a.pc;
     const int64_t N = a.N;
@@ -95,11 +98,18 @@ __global__ void volvarsKernel(AssemblyArgs a0, const AssemblyArgs* __restrict__ 
 #pragma unroll
             for (int e = 0; e < B; ++e) q[e] = x[e];
             if (s > 0) {
-                const int pv = (METHOD == 0) ? (s - 1) / 2 : s - 1;
+                const int pv = (s - 1) / SP, t = (s - 1) % SP;
                 const double ep = numericEps(pc, x[pv], pv);
-                const bool minus = (METHOD == -1) || (METHOD == 0 && ((s - 1) & 1));
-                q[pv] = minus ? x[pv] - ep : x[pv] + ep;
-                if (METHOD != 0 || !((s - 1) & 1)) a.eps[pv * N + i] = ep;
+                if (METHOD == 5) {
+                    if (t == 0) q[pv] = x[pv] + ep;
+                    else if (t == 1) q[pv] = x[pv] - ep;
+                    else if (t == 2) q[pv] = x[pv] - 2.0 * ep;
+                    else q[pv] = x[pv] + 2.0 * ep;
+                } else {
+                    const bool minus = (METHOD == -1) || (METHOD == 0 && t == 1);
+                    q[pv] = minus ? x[pv] - ep : x[pv] + ep;
+                }
+                if (t == 0) a.eps[pv * N + i] = ep;
             }
             double p[B], up[B], st[B];
             volVars<B>(pc, q, ph, ex, m, p, up, st);
@@ -155,11 +165,25 @@ __device__ __forceinline__ double phaseFlux(double tij, double pin, double pout,
     return flux * mult;
 }
 
+// Five-point stencil of NumericDifferentiation::partialDerivative (method 5,
+// dumux/common/numericdifferentiation.hh:79-88), in its operation order: f(x+e) - f(x-e),
+// times 8, + f(x-2e), - f(x+2e), divided by 12 e.
+__device__ __forceinline__ double fivePoint(double fp, double fm, double fm2, double fp2, double eps)
+{
+    double d = fp;
+    d -= fm;
+    d *= 8.0;
+    d += fm2;
+    d -= fp2;
+    return d / (12.0 * eps);
+}
+
 template <int B, int DIM, int METHOD, bool GRAV, bool TRANSIENT, bool FULLUP, bool WANT_JAC>
 __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
 {
     constexpr bool ANALYTIC = METHOD == 3;
-    constexpr int NS = ANALYTIC ? 1 : 1 + (METHOD == 0 ? 2 * B : B);
+    constexpr int SP = statesPerPv(METHOD);
+    constexpr int NS = ANALYTIC ? 1 : 1 + SP * B;
     constexpr int BB = B * B;
     constexpr int NF = 2 * DIM;
     constexpr int VA = DIM - 1;                 // vertical axis (gravity)
@@ -301,10 +325,10 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
 #pragma unroll
                 for (int pv = 0; pv < B; ++pv) {
                     const double epsJ = a.eps[pv * N + J];
-                    double Fa[B], Fb[B];
+                    double Fs[SP > 0 ? SP : 1][B];
 #pragma unroll
-                    for (int t = 0; t < (METHOD == 0 ? 2 : 1); ++t) {
-                        const int sJ = (METHOD == 0) ? 1 + 2 * pv + t : 1 + pv;
+                    for (int t = 0; t < SP; ++t) {
+                        const int sJ = 1 + SP * pv + t;
                         double pJs[B], uJs[B];
 #pragma unroll
                         for (int k = 0; k < B; ++k) {
@@ -316,16 +340,16 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
                             const double F = (GRAV && ax == VA)
                                 ? phaseFlux<true, FULLUP>(tij, pI[0][k], pJs[k], uI[0][k], uJs[k], g1[k], g2[k], w)
                                 : phaseFlux<false, FULLUP>(tij, pI[0][k], pJs[k], uI[0][k], uJs[k], 0.0, 0.0, w);
-                            if (t == 0) Fa[k] = F;
-                            else Fb[k] = F;
+                            Fs[t][k] = F;
                         }
                     }
 #pragma unroll
                     for (int e = 0; e < B; ++e) {
                         double d;
-                        if (METHOD == 1) d = (Fa[e] - F0[e]) / epsJ;
-                        else if (METHOD == -1) d = (F0[e] - Fa[e]) / epsJ;
-                        else d = (Fa[e] - Fb[e]) / (epsJ + epsJ);
+                        if (METHOD == 1) d = (Fs[0][e] - F0[e]) / epsJ;
+                        else if (METHOD == -1) d = (F0[e] - Fs[0][e]) / epsJ;
+                        else if (METHOD == 0) d = (Fs[0][e] - Fs[1][e]) / (epsJ + epsJ);
+                        else d = fivePoint(Fs[0][e], Fs[1][e], Fs[2][e], Fs[3][e], epsJ);
                         blk[e * B + pv] = d;
                     }
                 }
@@ -430,7 +454,8 @@ __device__ __forceinline__ void rowCell(const AssemblyArgs& a, const int64_t I)
                 double d;
                 if (METHOD == 1) d = (r[1 + pv][e] - r[0][e]) / epsI;
                 else if (METHOD == -1) d = (r[0][e] - r[1 + pv][e]) / epsI;
-                else d = (r[1 + 2 * pv][e] - r[2 + 2 * pv][e]) / (epsI + epsI);
+                else if (METHOD == 0) d = (r[1 + 2 * pv][e] - r[2 + 2 * pv][e]) / (epsI + epsI);
+                else d = fivePoint(r[1 + 4 * pv][e], r[2 + 4 * pv][e], r[3 + 4 * pv][e], r[4 + 4 * pv][e], epsI);
                 blk[e * B + pv] = d;
             }
         }
@@ -477,12 +502,14 @@ static void volvarsDispatch(const AssemblyArgs& a, const Geo& g, int b, int meth
         else if (method == 3) volvarsT<1, 3>(a, g, st);
         else if (method == 1) volvarsT<1, 1>(a, g, st);
         else if (method == -1) volvarsT<1, -1>(a, g, st);
+        else if (method == 5) volvarsT<1, 5>(a, g, st);
         else volvarsT<1, 0>(a, g, st);
     } else {
         if (method == 2) volvarsT<2, 2>(a, g, st);
         else if (method == 3) volvarsT<2, 3>(a, g, st);
         else if (method == 1) volvarsT<2, 1>(a, g, st);
         else if (method == -1) volvarsT<2, -1>(a, g, st);
+        else if (method == 5) volvarsT<2, 5>(a, g, st);
         else volvarsT<2, 0>(a, g, st);
     }
     DXG_CUDA(cudaGetLastError());
@@ -551,6 +578,7 @@ static void launchRow1(const AssemblyArgs& a, const Geo& g, int method, bool jac
     if (method == 1) launchRow2<B, DIM, 1>(a, g, jac, grav, transient, fullup, st);
     else if (method == 3) launchRow2<B, DIM, 3>(a, g, jac, grav, transient, fullup, st);
     else if (method == -1) launchRow2<B, DIM, -1>(a, g, jac, grav, transient, fullup, st);
+    else if (method == 5) launchRow2<B, DIM, 5>(a, g, jac, grav, transient, fullup, st);
     else launchRow2<B, DIM, 0>(a, g, jac, grav, transient, fullup, st);
 }
 static void rowDispatch(const AssemblyArgs& a, const Geo& g, int b, int dim, int method, bool jac, bool grav,

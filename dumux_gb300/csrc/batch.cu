@@ -1380,7 +1380,7 @@ GroupKey keyOf(const Slot* s)
 int64_t problemBytes(int64_t N, int64_t nb, int b, int dim, int method, int precision)
 {
     const int64_t bb = (int64_t)b * b, slots = 2 * dim + 1, M = N * b;
-    const int NS = 1 + (method == 0 ? 2 * b : b);
+    const int NS = 1 + statesPerPv(method) * b;
     int64_t by = 0;
     by += (3 + dim) * N * 8 + b * N * 8 + 2 * (2 * b * N * 8) + N * 4 * 2 + N;   // cell tables, mask, level order
     by += nb * (1 + 8 + 4 * 8 * b);                                             // boundary tables

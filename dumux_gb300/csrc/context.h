@@ -94,6 +94,15 @@ struct dxg_ctx {
     double waveTuneMs[5] = {0, 0, 0, 0, 0};   // ms per apply of each candidate tried
     int waveTuneCtas[5] = {0, 0, 0, 0, 0};
     int waveTuneCount = 0;
+    // lane sweeps (lanewave.cu): chosen by the timing at the first factorisation when faster
+    // (DXG_ILU_AUTO) or forced (DXG_ILU_LANES); their inter-cluster hand-off buffer
+    dxg::LanePlan lanePlan;
+    bool laneWave = false;
+    double laneTuneMs = 0.0;
+    dxg::DevBuf<unsigned char> laneHandoff;
+    size_t laneHandoffBytes = 0;
+    // limit of every bounded wait of the sweeps (0: the kernels' default, 0.5 s)
+    unsigned long long waitNs = 0;
 
     // optional event timing per kernel class (pairs resolved lazily)
     struct TimedLaunch {

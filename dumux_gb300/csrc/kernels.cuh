@@ -5,6 +5,14 @@
 
 namespace dxg {
 
+// Perturbed states per primary variable of a numeric difference method: 1 forward /
+// backward, 2 central, 4 five-point stencil (1, -1, 0, 5); none for the residual-only pass
+// (2) and the analytic Jacobian (3).
+__host__ __device__ constexpr int statesPerPv(int method)
+{
+    return method == 0 ? 2 : method == 5 ? 4 : (method == 2 || method == 3) ? 0 : 1;
+}
+
 // Everything the assembly kernels read or write (device pointers).
 struct AssemblyArgs {
     const ProblemConsts* pc;

@@ -39,7 +39,7 @@ namespace cg = cooperative_groups;
 namespace dxg {
 
 constexpr int kRing = 8;
-constexpr unsigned long long kWaitNs = 500000000ull;   // 0.5 s per wait
+constexpr unsigned long long kWaitNs = 500000000ull;   // default limit of a wait: 0.5 s
 constexpr size_t kWaveSmemLimit = 200 * 1024;
 
 __device__ __forceinline__ unsigned long long globalTimer()
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
             if (!haveHalo && ((st.nbY != kNone && st.nbY < 0) || (st.nbZ != kNone && st.nbZ < 0))) {
                 const uint32_t parity = (uint32_t)(((gIn - gInFirst) / kRing) & 1);
                 if (!mbarTryWait(barIn, parity)) {
-                    const unsigned long long deadline = globalTimer() + kWaitNs;
+                    const unsigned long long deadline = globalTimer() + (a.waitNs ? a.waitNs : kWaitNs);
                     bool ok = false;
                     while (!(ok = mbarTryWait(barIn, parity))) {
                         if (*(volatile int*)&abortFlag) break;
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(1024) waveKernel(WaveArgs<T> a0, const WaveArg
                     // already covers the target needs no new load
                     const int target = gstep - kRing + 1;
                     if (roomSeen < target && (roomSeen = ldAcquireCluster(&consumerDone)) < target) {
-                        const unsigned long long deadline = globalTimer() + kWaitNs;
+                        const unsigned long long deadline = globalTimer() + (a.waitNs ? a.waitNs : kWaitNs);
                         bool ok = true;
                         while ((roomSeen = ldAcquireCluster(&consumerDone)) < target) {
                             if (*(volatile int*)&abortFlag) { ok = false; break; }

@@ -21,7 +21,38 @@ struct WaveArgs {
     int* err;                 // DXG_ERR_TIMEOUT on an expired wait
     int* singular;            // set on a singular pivot
     const KrylovState* ks;    // sweeps are skipped once the solve has stopped
+    unsigned long long waitNs;   // limit of every wait (0: the default 0.5 s)
 };
+
+// Sweeps of lanewave.cu (3D, 2x2 blocks): two lanes per x-line, one plane of up to 64 lines
+// per CTA, clusters along z.
+template <class T>
+struct LaneWaveArgs {
+    int nx, ny, nz;
+    int64_t N;
+    int nyb;                  // CTAs per plane (64 lines each)
+    int ctas;                 // working CTAs (nz * nyb); the grid is padded to whole clusters
+    int clusterSize;
+    const T* Lf;              // lower factor (forward sweep)
+    const T* A;               // matrix, upper slots (backward sweep)
+    const T* Dinv;            // inverted pivots
+    const T* rhs;             // forward input
+    T* v;                     // forward output, backward in/out
+    int* err;                 // DXG_ERR_TIMEOUT on an expired wait
+    const KrylovState* ks;    // sweeps are skipped once the solve has stopped
+    T* handoff;               // [ctas][nx][64][2] hand-offs between clusters, all bits set between launches
+    unsigned long long waitNs;
+};
+struct LanePlan {
+    bool ok = false;
+    int nyb = 0, ctas = 0, clusterSize = 0, grid = 0, pfFwd = 0, pfBwd = 0;
+};
+// Plan of the lane sweeps for a dim-D grid of b x b blocks (ok only for 3D, b == 2, grids whose
+// sweeps fit: every cluster resident at once, the plane history in shared memory).
+template <class T>
+LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b);
+template <class T>
+void launchLaneWaveApply(const LanePlan& p, const LaneWaveArgs<T>& fwd, const LaneWaveArgs<T>& bwd, cudaStream_t st);
 
 struct WavePlan {
     int ctas = 0, linesPerCta = 0, haloLines = 0, threads = 0, lpt = 0;

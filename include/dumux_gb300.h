@@ -76,7 +76,8 @@ typedef struct dxg_problem_desc {
     /* numeric differentiation (dumux/assembly/numericepsilon.hh)                   */
     double base_epsilon;         /* Assembly.NumericDifference.BaseEpsilon (1e-10)  */
     double privar_magnitude[2];  /* Assembly.NumericDifference.PriVarMagnitude (<=0: |x|+1) */
-    int32_t numeric_difference_method; /* Assembly.NumericDifferenceMethod: 1 forward, 0 central, -1 backward */
+    int32_t numeric_difference_method; /* Assembly.NumericDifferenceMethod: 1 forward, 0 central, -1 backward,
+                                          5 five-point stencil (common/numericdifferentiation.hh:79-88) */
     double upwind_weight;        /* Flux.UpwindWeight (1.0)                         */
     /* Jacobian differentiation (the assembler's DiffMethod): 0 numeric (default), 1
      * analytic -- CCLocalAssembler<DiffMethod::analytic>, dumux/assembly/cclocalassembler.hh:
@@ -246,8 +247,18 @@ int dxg_advance_time_step(dxg_ctx* ctx);
  * parallel passes instead of nx+ny+nz-2 dependent levels; the Newton solution is the
  * same to the linear and Newton tolerances.  No counterpart in the reference (dune-istl's
  * SeqILU is sequential, natural order). */
-enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2, DXG_ILU_REDBLACK = 3 };
+enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2, DXG_ILU_REDBLACK = 3, DXG_ILU_LANES = 4 };
+/* DXG_ILU_LANES: the natural-order sweeps of 3D 2x2-block systems with two lanes per grid line
+ * and one z-plane per CTA over several thread-block clusters (more SMs on the level chain);
+ * the same factors and arithmetic per cell as DXG_ILU_WAVEFRONT, so the same results.
+ * DXG_ILU_AUTO takes it when the timing at the first factorisation finds it faster. */
 int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
+/* Limit of every bounded wait inside the ILU(0) sweeps, in seconds (default 0.5; at most
+ * 60).  A wait that runs out ends the sweep with DXG_ERR_TIMEOUT, which the Newton driver
+ * treats like a failed linear solve (a time-step retry).  Raise it where the GPU is
+ * time-sliced with other processes, whose turns can stall a sweep for longer.  No
+ * counterpart in the reference (its sweeps run on one CPU thread). */
+int dxg_set_wait_limit(dxg_ctx* ctx, double seconds);
 /* The linear solver of dxg_linear_solve / dxg_newton_solve, as the reference's solver
  * types: DXG_LINEAR_SOLVER_ILU_BICGSTAB (ILUBiCGSTABIstlSolver, istlsolvers.hh:635-642;
  * default) or DXG_LINEAR_SOLVER_AMG_BICGSTAB (AMGBiCGSTABIstlSolver, istlsolvers.hh:729-736):
@@ -286,6 +297,8 @@ int dxg_get_kernel_timing(dxg_ctx* ctx, int kernel_class, int64_t* launches, dou
  * the process exits; vectors longer than 8,388,608 entries are refused with
  * DXG_ERR_SIZE.  The first call on a device looks up that array's device address (once
  * per device, with the device current); make that first call before any stream capture.
+ * The address is kept for the life of the process: after a cudaDeviceReset of a device the
+ * entry point must not be called on that device again.
  * All calls on a device share the array, so calls whose kernels may overlap on the GPU
  * (unordered streams) race and must be ordered by the caller.  No counterpart in the
  * reference (dune-istl's norms run on the host). */

@@ -76,8 +76,10 @@ def test_residual_and_jacobian_match_oracle(name, desc, u, up, dt, pow_mode):
     assert np.max(np.abs(J_gpu - J_orc)) <= 1e-7 * np.max(np.abs(J_orc))
 
 
-@pytest.mark.parametrize("method", [1, -1, 0])
+@pytest.mark.parametrize("method", [1, -1, 0, 5])
 def test_numeric_difference_methods(method):
+    # forward, backward, central differences and the five-point stencil
+    # (NumericDifferentiation::partialDerivative, dumux/common/numericdifferentiation.hh:67-123)
     d, u0 = problems.dnapl_2p(cells=(5, 4, 3), seed=9)
     d.numeric_difference_method = method
     u = _random_2p_state(d, u0, 3)
