@@ -106,6 +106,7 @@ def test_config2_dnapl_64x64x32_ten_steps():
     print(f"config 2 parity: residual-norm deviation of r0 {worst:.2e} (first steps {worst_first:.2e}, oracle "
           f"against itself with another summation order {floor:.2e}); fields p_w {err_p:.2e}, S_n {err_s:.2e}")
     assert worst_first <= max(1e-9, 4.0 * floor)
-    assert worst <= 1e-6
+    # later steps start from states that already differ by the earlier steps' rounding
+    assert worst <= max(1e-9, 10.0 * floor)
     assert err_p <= 1e-9 and err_s <= 1e-9
     assert np.max(uo[:, 1]) > 1e-2            # DNAPL has entered
