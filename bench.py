@@ -45,9 +45,15 @@ def parse():
     ap.add_argument("--cells", default="64,64,32")
     ap.add_argument("--dt", type=float, default=250.0)
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
-    ap.add_argument("--workload", default="2p", choices=["2p", "1p", "ensemble", "serve"],
+    ap.add_argument("--workload", default="2p", choices=["2p", "1p", "ensemble", "serve", "accuracy"],
                     help="2p: transient water-DNAPL (default); 1p: stationary Darcy, 100x100, one Newton step; "
-                         "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching")
+                         "ensemble: 256 uneven 2p problems batched; serve: Poisson request stream, continuous batching; "
+                         "accuracy: the 128x128x64 2p case over --steps time steps in plain FP64 and the GB300 forms, "
+                         "field errors against FP64 (and against the oracle's first time step with --oracle-step)")
+    ap.add_argument("--save-first-step", default="",
+                    help="accuracy workload: write the FP64 solution after the first time step (.npy)")
+    ap.add_argument("--oracle-step", action="store_true",
+                    help="accuracy workload: also compare the first FP64 time step with the CPU oracle's")
     ap.add_argument("--diff", default="numeric", choices=["numeric", "analytic"],
                     help="Jacobian by numeric differentiation (default, the reference's default) or analytic")
     ap.add_argument("--ilu", default="natural", choices=["natural", "redblack"],
@@ -382,6 +388,16 @@ FORMS = (("mixed", "mixed", "natural", "ilu"), ("mixed+redblack", "mixed", "redb
          ("mixed+amg", "mixed", "natural", "amg"))
 
 
+def form_params(precision, ilu, solver):
+    """Newton parameters of a form: the reference's defaults, with LinearSolver.MaxIterations
+    1000 where an FP32 or red-black ILU(0) preconditioner needs more BiCGSTAB iterations than
+    the default 250 allows (on the 128x128x64 case the FP32 ILU(0) needs up to ~270)."""
+    from dumux_gb300.abi import newton_params
+    if solver == "ilu" and (precision == "mixed" or ilu == "redblack"):
+        return newton_params(linear_max_iter=1000)
+    return newton_params()
+
+
 def run_forms(desc, u_start, u_ref, dt_seq, device, plain_ms_per_step, plain_value, flush):
     """Each form of FORMS over the same time steps as the timed plain FP64 region: from
     the same state u_start, the implicit-Euler steps of sizes dt_seq timed with CUDA events on the
@@ -396,10 +412,9 @@ def run_forms(desc, u_start, u_ref, dt_seq, device, plain_ms_per_step, plain_val
     out = {}
     for name, precision, ilu, solver in FORMS:
         ctx = dumux_gb300.Context(desc, device=device, precision=precision)
-        params = newton_params()
+        params = form_params(precision, ilu, solver)
         if ilu == "redblack":
             ctx.set_ilu_kernel("redblack")
-            params = newton_params(linear_max_iter=1000)
         if solver == "amg":
             ctx.set_linear_solver("amg")
         steps = len(dt_seq)
@@ -776,6 +791,88 @@ def run_serve(args):
     return 0
 
 
+def field_errors(u, ref, b=2):
+    """Max and L2 relative errors of p_w and S_n of u against ref."""
+    u, ref = u.reshape(-1, b), ref.reshape(-1, b)
+    out = {}
+    for k, name in enumerate(("p_w", "S_n")[:b]):
+        d = u[:, k] - ref[:, k]
+        out[f"max_rel_err_{name}"] = float(np.max(np.abs(d)) / np.max(np.abs(ref[:, k])))
+        out[f"l2_rel_err_{name}"] = float(np.linalg.norm(d) / np.linalg.norm(ref[:, k]))
+    return out
+
+
+def run_accuracy(args, cells):
+    """The 2p case at `cells` (default 128x128x64, 1,048,576 cells) over --steps implicit-Euler
+    steps (TimeLoop.MaxTimeStepSize --dt with the Newton solver's suggestion below it) in
+    plain FP64 and in the GB300 forms: per-step Newton iterations, time-step divisions and
+    sizes, wall time, and the forms' field errors against FP64 at the end; with
+    --oracle-step also the FP64 first time step against the CPU oracle's."""
+    import torch
+    import dumux_gb300
+    from dumux_gb300.abi import newton_params
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    desc, u0 = workload(cells)
+    params = newton_params()
+    runs = {}
+    first_step = None
+    for name, precision, ilu, solver in (("fp64", "fp64", "natural", "ilu"),) + FORMS:
+        ctx = dumux_gb300.Context(desc, device=local, precision=precision)
+        p = form_params(precision, ilu, solver)
+        if ilu == "redblack":
+            ctx.set_ilu_kernel("redblack")
+        if solver == "amg":
+            ctx.set_linear_solver("amg")
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        dt, t = args.dt, 0.0
+        steps = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            rep = ctx.newton_solve(dt, p)
+            ctx.advance_time_step()
+            if k == 0 and name == "fp64":
+                first_step = ctx.solution()
+                if args.save_first_step:
+                    np.save(args.save_first_step, first_step)
+            t += rep["dt_used"]
+            steps.append({"dt": dt, "dt_used": rep["dt_used"], "iterations": rep["iterations"],
+                          "divisions": rep["time_step_divisions"], "wasted_iterations": rep["wasted_iterations"],
+                          "linear_iterations": rep["linear_iterations"]})
+            dt = min(ctx.suggest_time_step(rep["dt_used"], p), args.dt)
+        torch.cuda.synchronize()
+        runs[name] = {"seconds": time.perf_counter() - t0, "time": t, "steps": steps, "u": ctx.solution(),
+                      "ilu_kernels": ctx.describe()}
+        ctx.close()
+    ref = runs["fp64"]["u"]
+    out = {}
+    for name, r in runs.items():
+        e = {"seconds": r["seconds"], "simulated_time_s": r["time"], "steps": r["steps"], "ilu_kernels": r["ilu_kernels"],
+             "newton_iterations": sum(s["iterations"] + s["wasted_iterations"] for s in r["steps"])}
+        if name != "fp64":
+            e.update(field_errors(r["u"], ref))
+            e["same_time"] = r["time"] == runs["fp64"]["time"]
+        out[name] = e
+    line = {"workload": "accuracy", "config": {"workload": workload_name(cells, "fp64"), "cells": int(desc.num_cells),
+                                               "time_steps": args.steps, "max_dt": args.dt},
+            "runs": out}
+    if args.oracle_step:
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+        oracle.set_linear_threads(0)
+        t0 = time.perf_counter()
+        st, uo, orep = oracle.newton_solve(desc, u0, u0, args.dt, params)
+        line["oracle_first_step"] = {
+            "status": st, "seconds": time.perf_counter() - t0, "iterations": orep["iterations"],
+            "divisions": orep["time_step_divisions"], "dt_used": orep["dt_used"],
+            "gpu_iterations": runs["fp64"]["steps"][0]["iterations"],
+            "gpu_divisions": runs["fp64"]["steps"][0]["divisions"], **field_errors(first_step, uo)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     global WORKLOAD, DIFF, ILU, SOLVER
     args = parse()
@@ -795,6 +892,13 @@ def main():
         args.dt = 0.0
     if args.impl == "reference":
         return run_reference(args, cells)
+    if args.workload == "accuracy":
+        WORKLOAD = "2p"
+        if args.cells == "64,64,32" and "--cells" not in sys.argv:
+            cells = (128, 128, 64)
+        if "--steps" not in sys.argv:
+            args.steps = 10
+        return run_accuracy(args, cells)
 
     rank, world, local = dist_info()
     import torch

@@ -933,10 +933,12 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     DXG_CUDA(cudaMemcpyAsync(c->ks.get(), &init, sizeof(KrylovState), cudaMemcpyHostToDevice, st));
     launchBicgInit<double>(ba, rhs, st);
     c->launches += 1;
-    // SpMV: the FP64 Jacobian times the FP64 preconditioner output, or (mixed) the FP32
-    // Jacobian copy times the FP32 preconditioner output, FP64 result and dots
-    SpmvArgs<PT, double, PT> sv{};
-    sv.A = PA;
+    // SpMV: the FP64 Jacobian times the preconditioner output (FP64, or the FP32 output of the
+    // mixed form's FP32 preconditioner, widened on load), FP64 row sums, result and dots: the
+    // operator is exact in both precisions, so BiCGSTAB converges on the FP64 system and the
+    // FP32 factors only shape the preconditioner
+    SpmvArgs<double, double, PT> sv{};
+    sv.A = c->A.get();
     sv.nbmask = c->nbmask.get();
     sv.N = c->N;
     for (int s = 0; s < 7; ++s) sv.off[s] = c->off[s];
@@ -964,15 +966,15 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
         n += 1 + precondition(pIn);
         sv.x = yOut; sv.y = v; sv.w = rt;
         {
-            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
-            launchSpmv<PT, double, PT>(sv, c->b, c->dim, 1, st);
+            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv - (mixed ? 0.5 * c->N * c->b * 8.0 : 0.0));
+            launchSpmv<double, double, PT>(sv, c->b, c->dim, 1, st);
         }
         launchBicgAxpyNorm<double>(ba, 0, st);
         n += 2 + precondition(rIn);
         sv.x = yOut; sv.y = t; sv.w = r;
         {
-            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv * (mixed ? 0.5 : 1.0));
-            launchSpmv<PT, double, PT>(sv, c->b, c->dim, 2, st);
+            TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv - (mixed ? 0.5 * c->N * c->b * 8.0 : 0.0));
+            launchSpmv<double, double, PT>(sv, c->b, c->dim, 2, st);
         }
         launchBicgAxpyNorm<double>(ba, 1, st);
         return n + 2;

@@ -605,7 +605,7 @@ struct GroupState {
     std::vector<WaveGeom> geo;      // per member, from its class's launch shape
     DevBuf<unsigned char> args;
     const BicgArgs<double>* dBicg = nullptr;
-    const void* dSv1 = nullptr;      // SpmvArgs<PT, double, PT>
+    const void* dSv1 = nullptr;      // SpmvArgs<double, double, PT>
     const void* dSv2 = nullptr;
     const ToDoubleArgs* dTd = nullptr;
     const void* dRbP = nullptr;      // red-black order: RbArgs<PT> applied to p / to r
@@ -884,17 +884,21 @@ GroupState& groupState(dxg_batch* B, const GroupKey& key, const Members& S)
     G.maxN = maxCells(S);
     G.maxM = maxDofs(S);
     G.sweepBytes = bytesOf(S, &dxg_ctx::bytesSweep, sizeof(PT) / 8.0);
-    G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, sizeof(PT) / 8.0);
+    // the operator is the FP64 Jacobian in both precisions (mixed: times the FP32 preconditioner
+    // output, whose entries are read at half the bytes)
+    G.spmvBytes = bytesOf(S, &dxg_ctx::bytesSpmv, 1.0);
+    if (mixed)
+        for (Slot* q : S) G.spmvBytes -= 0.5 * (double)q->c->N * q->c->b * 8.0;
     std::vector<BicgArgs<double>> ba(n);
-    std::vector<SpmvArgs<PT, double, PT>> sv1(n), sv2(n);
+    std::vector<SpmvArgs<double, double, PT>> sv1(n), sv2(n);
     std::vector<WaveArgs<PT>> fwP(n), fwR(n), bw(n);   // member order; repacked per class below
     std::vector<RbArgs<PT>> rbP(n), rbR(n);
     std::vector<ToDoubleArgs> td(n);
     for (int k = 0; k < n; ++k) {
         dxg_ctx* c = S[k]->c;
         ba[k] = krylovArgs(c, mixed);
-        SpmvArgs<PT, double, PT> sv{};
-        sv.A = Pre<PT>::A(c);
+        SpmvArgs<double, double, PT> sv{};
+        sv.A = c->A.get();
         sv.nbmask = c->nbmask.get();
         sv.N = c->N;
         for (int q = 0; q < 7; ++q) sv.off[q] = c->off[q];
@@ -1035,14 +1039,14 @@ void enqueueChunk(dxg_batch* B, const GroupState& G, int n, int dim, int b)
         precondition(true);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<PT, double, PT>(static_cast<const SpmvArgs<PT, double, PT>*>(G.dSv1), G.mapN, b, dim, 1,
+            launchSpmvBatch<double, double, PT>(static_cast<const SpmvArgs<double, double, PT>*>(G.dSv1), G.mapN, b, dim, 1,
                                             st);
         }
         launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 0, st);
         precondition(false);
         {
             TimedB tb(B, DXG_KC_SPMV, G.spmvBytes);
-            launchSpmvBatch<PT, double, PT>(static_cast<const SpmvArgs<PT, double, PT>*>(G.dSv2), G.mapN, b, dim, 2,
+            launchSpmvBatch<double, double, PT>(static_cast<const SpmvArgs<double, double, PT>*>(G.dSv2), G.mapN, b, dim, 2,
                                             st);
         }
         launchBicgAxpyNormBatch<double>(G.dBicg, G.mapM, 1, st);

@@ -1089,10 +1089,13 @@ void launchDefectBatch(const DefectArgs* batch, int count, int64_t maxN, int b, 
 template void launchSpmv<double, double, double>(const SpmvArgs<double, double, double>&, int, int, int,
                                                 cudaStream_t);
 template void launchSpmv<float, double, float>(const SpmvArgs<float, double, float>&, int, int, int, cudaStream_t);
+template void launchSpmv<double, double, float>(const SpmvArgs<double, double, float>&, int, int, int, cudaStream_t);
 template void launchSpmvBatch<double, double, double>(const SpmvArgs<double, double, double>*, const BlockMap&, int,
                                                       int, int, cudaStream_t);
 template void launchSpmvBatch<float, double, float>(const SpmvArgs<float, double, float>*, const BlockMap&, int, int,
                                                     int, cudaStream_t);
+template void launchSpmvBatch<double, double, float>(const SpmvArgs<double, double, float>*, const BlockMap&, int, int,
+                                                     int, cudaStream_t);
 template void launchBicgInitBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);
 template void launchBicgInitBatch<float>(const BicgArgs<float>*, const BlockMap&, cudaStream_t);
 template void launchBicgUpdatePBatch<double>(const BicgArgs<double>*, const BlockMap&, cudaStream_t);

@@ -109,11 +109,12 @@ int dxg_ctx_destroy(dxg_ctx* ctx);
 const char* dxg_last_error(const dxg_ctx* ctx);
 
 /* Precision of the linear solve: FP64 everywhere (the plain drop-in), or the mixed
- * form: an FP32 copy of the Jacobian, FP32 ILU(0) factors and triangular sweeps, and
- * the BiCGSTAB operator products on the FP32 Jacobian (FP32 block products and row sums
- * of the FP32 preconditioner output), while the Krylov vectors, their updates and all dot
- * products stay FP64 -- an inexact Newton step inside the FP64 residual, numeric
- * differentiation, Newton update and norms.  Must be set before upload. */
+ * form: the preconditioner in FP32 (an FP32 copy of the Jacobian, FP32 ILU(0) factors and
+ * triangular sweeps, or the FP32 AMG hierarchy) inside an FP64 BiCGSTAB whose operator
+ * products take the FP64 Jacobian times the FP32 preconditioner output, with FP64 Krylov
+ * vectors, updates and dot products -- iterative refinement of the FP64 system by an FP32
+ * preconditioner, inside the FP64 residual, numeric differentiation, Newton update and
+ * norms.  Must be set before upload. */
 enum { DXG_PRECISION_FP64 = 0, DXG_PRECISION_MIXED = 1 };
 int dxg_set_precision(dxg_ctx* ctx, int precision);
 
