@@ -56,9 +56,11 @@ def parse():
                     help="accuracy workload: also compare the first FP64 time step with the CPU oracle's")
     ap.add_argument("--diff", default="numeric", choices=["numeric", "analytic"],
                     help="Jacobian by numeric differentiation (default, the reference's default) or analytic")
-    ap.add_argument("--ilu", default="natural", choices=["natural", "redblack"],
-                    help="ILU(0) ordering of the single-problem workloads: natural (the reference's "
-                         "SeqILU, default) or red-black (two parallel passes per sweep, more iterations)")
+    ap.add_argument("--ilu", default="natural", choices=["natural", "lanes", "wavefront", "redblack"],
+                    help="ILU(0) of the single-problem workloads: natural order (the reference's SeqILU, "
+                         "default; the context times the lane sweeps and the cluster wavefront and keeps "
+                         "the faster), natural order forced onto the lane sweeps or onto the cluster "
+                         "wavefront, or red-black (two parallel passes per sweep, more iterations)")
     ap.add_argument("--solver", default="ilu", choices=["ilu", "amg"],
                     help="ILU(0)-BiCGSTAB (default, the reference's ILUBiCGSTABIstlSolver) or "
                          "AMG-BiCGSTAB (AMGBiCGSTABIstlSolver)")
@@ -191,9 +193,10 @@ def measured_peaks():
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
-# of the 64x64x32 FP64 system, from an ncu capture of the sweeps (cold-cache, serialised
-# launches).
+# of the 64x64x32 FP64 system, from ncu captures of the sweeps (cold-cache, serialised
+# launches): the cluster wavefront kernels and the lane sweeps.
 ILU_TRAFFIC_PER_APPLY_64x64x32 = 14537472 + 18714112
+LANE_TRAFFIC_PER_APPLY_64x64x32 = 14533376 + 18735616
 # DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from an ncu capture
 # of a 32-problem ensemble (2,379,154 cells); traffic scales with the cells swept (each block
 # and vector entry is moved once)
@@ -880,6 +883,8 @@ def main():
     DIFF = args.diff
     ILU = args.ilu
     SOLVER = args.solver
+    if args.workload in ("ensemble", "serve") and args.ilu in ("lanes", "wavefront"):
+        sys.exit("--ilu lanes/wavefront applies to the single-problem workloads")
     if args.workload in ("ensemble", "serve") and args.impl == "gb300":
         if args.precision == "fp64" and "--precision" not in sys.argv:
             args.precision = "mixed"
@@ -911,8 +916,8 @@ def main():
     desc, u0 = workload(cells, seed=2 + rank)
     desc.analytic = args.diff == "analytic"
     ctx = dumux_gb300.Context(desc, device=local, precision=args.precision)
-    if args.ilu == "redblack":
-        ctx.set_ilu_kernel("redblack")
+    if args.ilu != "natural":
+        ctx.set_ilu_kernel(args.ilu)
     if args.solver == "amg":
         ctx.set_linear_solver("amg")
     params = step_params()
@@ -1012,7 +1017,8 @@ def main():
 
     peak, peak_kind = measured_peaks()
     achieved = (sweep_bytes / sweep_n) / (sweep_ms / sweep_n / 1e3) / 1e9 if sweep_n else None
-    traffic = (ILU_TRAFFIC_PER_APPLY_64x64x32
+    lanes = "lane wavefront" in ctx.describe().split(";")[0]
+    traffic = ((LANE_TRAFFIC_PER_APPLY_64x64x32 if lanes else ILU_TRAFFIC_PER_APPLY_64x64x32)
                if (args.workload == "2p" and cells == (64, 64, 32) and args.precision == "fp64") else None)
     if args.solver == "amg":
         rkernel = "AMG V-cycle (amg.cu passes, one preconditioner application)"
@@ -1021,6 +1027,10 @@ def main():
     elif args.ilu == "redblack":
         rkernel = "rbApplyBlack + rbApplyRed (red-black ILU(0) apply, two parallel passes)"
         rnote = "bandwidth-bound passes, latency bound at small grids"
+    elif lanes:
+        rkernel = "laneWaveKernel (ILU(0) forward+backward lane sweeps, one apply)"
+        rnote = ("latency/FP64-bound wavefront (one dependent level per grid line step and plane), "
+                 "far below the HBM roof")
     else:
         rkernel = "waveKernel (ILU(0) forward+backward sweep, one apply)"
         rnote = "latency/FP64-bound wavefront (nx+ny+nz-2 dependent levels), far below the HBM roof"

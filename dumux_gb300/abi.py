@@ -51,6 +51,8 @@ class ProblemDescC(C.Structure):
         ("upwind_weight", C.c_double),
         ("diff_method", C.c_int32),
         ("material_law", C.c_int32),
+        ("discretization", C.c_int32),
+        ("permeability_tensor", _dp),
     ]
 
 
@@ -197,7 +199,8 @@ class ProblemDesc:
                  enable_gravity=True, gravity=None, density=(1000.0, 1000.0),
                  viscosity=(1e-3, 1e-3), extrusion=None, material=None, source=None,
                  material_params=None, base_epsilon=1e-10, privar_magnitude=(-1.0, -1.0),
-                 numeric_difference_method=1, upwind_weight=1.0, analytic=False, material_law="brooks-corey"):
+                 numeric_difference_method=1, upwind_weight=1.0, analytic=False, material_law="brooks-corey",
+                 discretization="tpfa", permeability_tensor=None):
         self.coords = [np.ascontiguousarray(c, dtype=np.float64) for c in coords]
         self.dim = len(self.coords)
         self.cells = [len(c) - 1 for c in self.coords] + [1] * (3 - self.dim)
@@ -229,6 +232,10 @@ class ProblemDesc:
         self.numeric_difference_method = numeric_difference_method
         self.upwind_weight = upwind_weight
         self.analytic = bool(analytic)
+        self.discretization = {"tpfa": 0, "mpfa": 1}[discretization]
+        self.permeability_tensor = (None if permeability_tensor is None else
+                                    np.ascontiguousarray(permeability_tensor, dtype=np.float64)
+                                    .reshape(n * self.dim * self.dim))
         self._c = None
 
     @property
@@ -260,6 +267,8 @@ class ProblemDesc:
         d.upwind_weight = self.upwind_weight
         d.diff_method = 1 if self.analytic else 0
         d.material_law = self.material_law
+        d.discretization = self.discretization
+        d.permeability_tensor = _ptr(self.permeability_tensor)
         self._c = d          # keep alive while the caller uses it
         return d
 

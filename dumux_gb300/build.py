@@ -1,8 +1,8 @@
 """In-tree build of libdumux_gb300.so (sm_103a) with nvcc.
 
 Translation units are compiled in parallel and linked into
-dumux_gb300/_lib/libdumux_gb300.so.  assemble.cu is compiled without FMA contraction
-so the residual and the numeric-difference Jacobian follow the reference's
+dumux_gb300/_lib/libdumux_gb300.so.  assemble.cu and mpfa.cu are compiled without FMA
+contraction so the residual and the numeric-difference Jacobian follow the reference's
 operation order exactly; host code everywhere is compiled with -ffp-contract=off so
 the tabulated coefficients are identical on x86 and Arm hosts.
 """
@@ -28,6 +28,7 @@ UNITS = {
     "noalloc.cu": [],
     "batch.cu": [],
     "amg.cu": [],
+    "mpfa.cu": ["--fmad=false"],
 }
 
 

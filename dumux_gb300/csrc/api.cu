@@ -231,9 +231,19 @@ void parallelFor(int64_t n, F&& f)
 }
 
 // ---------------------------------------------------------------- tabulation
+void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d);
+
 void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
 {
     if (!d) throw Error(DXG_ERR_ARG, "null problem description");
+    if (d->discretization != DXG_DISC_TPFA && d->discretization != DXG_DISC_MPFA_O)
+        throw Error(DXG_ERR_ARG, "discretization must be DXG_DISC_TPFA or DXG_DISC_MPFA_O");
+    if (d->discretization == DXG_DISC_MPFA_O) {
+        tabulateMpfa(c, d);
+        return;
+    }
+    if (d->permeability_tensor) throw Error(DXG_ERR_ARG, "a permeability tensor needs the MPFA-O discretization");
+    c->mpfa = false;
     if (d->dim != 2 && d->dim != 3) throw Error(DXG_ERR_ARG, "dim must be 2 or 3");
     if (d->num_eq != 1 && d->num_eq != 2) throw Error(DXG_ERR_ARG, "num_eq must be 1 or 2");
     for (int a = 0; a < d->dim; ++a)
@@ -593,6 +603,220 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->haveJac = c->haveRes = c->haveFactor = false;
 }
 
+// MPFA-O (1p, FP64 single contexts): the interaction volumes solved on the host
+// (mpfaTabulate), the per-cell flux rows, the 3^dim stencil and the Krylov buffers.
+void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
+{
+    if (d->dim != 2 && d->dim != 3) throw Error(DXG_ERR_ARG, "dim must be 2 or 3");
+    if (d->num_eq != 1) throw Error(DXG_ERR_ARG, "MPFA-O is available for the 1p model (num_eq 1)");
+    if (c->precision != DXG_PRECISION_FP64) throw Error(DXG_ERR_ARG, "MPFA-O runs in FP64");
+    for (int a = 0; a < d->dim; ++a)
+        if (d->cells[a] < 1 || !d->coords[a]) throw Error(DXG_ERR_ARG, "invalid cells/coords");
+    if (!d->permeability || !d->porosity || !d->bc_type || !d->bc_values) throw Error(DXG_ERR_ARG, "missing tables");
+    if (d->diff_method != 0) throw Error(DXG_ERR_ARG, "MPFA-O assembles by numeric differentiation");
+    const int method = d->numeric_difference_method;
+    if (method != 1 && method != 0 && method != -1 && method != 5)
+        throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0, -1 or 5");
+    const int dim = d->dim;
+    HostGrid g{};
+    g.dim = dim;
+    for (int a = 0; a < 3; ++a) g.n[a] = a < dim ? d->cells[a] : 1;
+    for (int a = 0; a < dim; ++a) g.x[a] = d->coords[a];
+    const int64_t N = g.n[0] * g.n[1] * g.n[2];
+    if (N > (int64_t)INT32_MAX) throw Error(DXG_ERR_ARG, "too many cells");
+    if (g.n[1] * g.n[2] > (int64_t)INT32_MAX) throw Error(DXG_ERR_ARG, "too many grid lines");
+    const MpfaLayout L = mpfaLayout(dim);
+    c->mpfa = true;
+    c->mpLayout = L;
+    c->dim = dim;
+    c->b = 1;
+    c->N = N;
+    c->M = N;
+    c->slots = L.S;
+    c->bb = 1;
+    c->method = method;
+    c->gravity = d->enable_gravity != 0;
+    c->fullUpwind = false;
+    ProblemConsts& pc = c->pcHost;
+    pc = ProblemConsts{};
+    pc.dim = dim;
+    pc.b = 1;
+    pc.nx = (int)g.n[0];
+    pc.ny = (int)g.n[1];
+    pc.nz = (int)g.n[2];
+    pc.N = N;
+    pc.sideOffset[0] = 0;
+    for (int f = 0; f < 2 * dim; ++f) {
+        const int a = f / 2;
+        int64_t cnt = 1;
+        for (int k = 0; k < dim; ++k)
+            if (k != a) cnt *= g.n[k];
+        pc.sideOffset[f + 1] = pc.sideOffset[f] + cnt;
+    }
+    c->nb = pc.sideOffset[2 * dim];
+    for (int64_t k = 0; k < c->nb; ++k)
+        if (d->bc_type[k] != 1 && d->bc_type[k] != 2)
+            throw Error(DXG_ERR_ARG, "boundary type must be 1 (Dirichlet) or 2 (Neumann)");
+    pc.density[0] = d->density[0];
+    pc.viscosity[0] = d->viscosity[0];
+    pc.magnitude[0] = d->privar_magnitude[0];
+    pc.baseEps = d->base_epsilon > 0 ? d->base_epsilon : 1e-10;
+    pc.method = method;
+    c->mpMob = d->density[0] * (1.0 / d->viscosity[0]);
+    const int64_t strides[3] = {1, g.n[0], g.n[0] * g.n[1]};
+    for (int s = 0; s < L.S; ++s) {
+        int o[3] = {0, 0, 0}, q = s;
+        for (int a = 0; a < dim; ++a) {
+            o[a] = q % 3 - 1;
+            q /= 3;
+        }
+        c->mpOff[s] = o[0] * strides[0] + o[1] * strides[1] + o[2] * strides[2];
+    }
+    mpfaTriples(dim, c->mpNTri, c->mpTri);
+
+    // per cell: source * volume * extrusion (the TPFA order), the stencil mask
+    std::vector<double> srcterm(N, 0.0);
+    std::vector<uint32_t> mask(N, 0);
+    parallelFor(N, [&](int64_t i0, int64_t i1) {
+        for (int64_t i = i0; i < i1; ++i) {
+            int64_t id[3];
+            g.ijk(i, id);
+            const double sV = g.volume(id) * (d->extrusion ? d->extrusion[i] : 1.0);
+            double src = 0.0;
+            if (d->source) src += d->source[i];
+            src *= sV;
+            srcterm[i] = src;
+            uint32_t m = 0;
+            for (int s = 0; s < L.S; ++s) {
+                int q = s;
+                bool ok = true;
+                for (int a = 0; a < dim; ++a) {
+                    const int64_t x = id[a] + (q % 3 - 1);
+                    q /= 3;
+                    if (x < 0 || x >= g.n[a]) ok = false;
+                }
+                if (ok) m |= 1u << s;
+            }
+            mask[i] = m;
+        }
+    });
+    std::vector<double> coef, cst;
+    std::vector<int8_t> kind;
+    mpfaTabulate(d, L, pc.sideOffset, coef, cst, kind);
+    int64_t nnz = 0;
+    for (int64_t i = 0; i < N; ++i) nnz += __builtin_popcount(mask[i]);
+    c->nnzb = nnz;
+    c->mpMaskHost = mask;
+    c->bytesAssembly = (double)N * (8.0 * L.F * (L.K + 1) + L.F + 4.0 + 8.0 * (L.S + 3) + 8.0 * L.S + 8.0);
+    c->bytesSpmv = (double)nnz * 8.0 + N * 4.0 + 2.0 * N * 8.0;
+    c->bytesSweep = (double)nnz * 8.0 + N * (8.0 + 4.0 * 8.0);
+
+    cudaStream_t st = c->stream;
+    c->uploadBlock.release();
+    c->pcDev.alloc(1);
+    DXG_CUDA(cudaMemcpyAsync(c->pcDev.get(), &c->pcHost, sizeof(ProblemConsts), cudaMemcpyHostToDevice, st));
+    upload(c->srcterm, srcterm, st);
+    upload(c->mpMask, mask, st);
+    upload(c->mpCoef, coef, st);
+    upload(c->mpCst, cst, st);
+    upload(c->mpKind, kind, st);
+    DXG_CUDA(cudaStreamSynchronize(st));
+    c->u.alloc(N);
+    c->uprev.alloc(N);
+    c->uLast.alloc(N);
+    c->A.alloc((size_t)L.S * N);
+    c->r.alloc(N);
+    c->delta.alloc(N);
+    DXG_CUDA(cudaMemsetAsync(c->u.get(), 0, N * sizeof(double), st));
+    DXG_CUDA(cudaMemsetAsync(c->uprev.get(), 0, N * sizeof(double), st));
+    DXG_CUDA(cudaMemsetAsync(c->delta.get(), 0, N * sizeof(double), st));
+    DXG_CUDA(cudaMemsetAsync(c->A.get(), 0, (size_t)L.S * N * sizeof(double), st));
+    for (auto* v : {&c->kx, &c->kr, &c->krt, &c->kp, &c->kv, &c->kt, &c->ky}) v->alloc(N);
+    c->L.alloc((size_t)L.S * N);
+    c->Dinv.alloc(N);
+    c->ks.alloc(1);
+    c->partials.alloc(3 * kMaxReduceBlocks);
+    c->counters.alloc(8);
+    c->scal.alloc(4);
+    c->singular.alloc(2);
+    c->wavePlan = WavePlan{};
+    c->lanePlan = LanePlan{};
+    c->waveTuned = true;
+    c->laneWave = false;
+    c->laneTuneMs = 0.0;
+    c->laneHandoff.release();
+    c->laneHandoffBytes = 0;
+    c->waveTuneCount = 0;
+    c->dropGraphs();
+    DXG_CUDA(cudaMemsetAsync(c->counters.get(), 0, 8 * sizeof(unsigned), st));
+    DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
+    DXG_CUDA(cudaMemsetAsync(c->ks.get(), 0, sizeof(KrylovState), st));
+    DXG_CUDA(cudaMemsetAsync(c->scal.get(), 0, 4 * sizeof(double), st));
+    DXG_CUDA(cudaStreamSynchronize(st));
+    c->uploaded = true;
+    c->havePrev = false;
+    c->stPrevValid = false;
+    c->haveJac = c->haveRes = c->haveFactor = false;
+}
+
+MpfaArgs mpfaArgs(const dxg_ctx* c)
+{
+    const MpfaLayout& L = c->mpLayout;
+    MpfaArgs a{};
+    a.N = c->N;
+    a.S = L.S;
+    a.F = L.F;
+    a.K = L.K;
+    for (int s = 0; s < L.S; ++s) a.off[s] = c->mpOff[s];
+    std::memcpy(a.slotOf, L.slotOf, sizeof(a.slotOf));
+    std::memcpy(a.scvfSlots, L.scvfSlots, sizeof(a.scvfSlots));
+    a.coef = c->mpCoef.get();
+    a.cst = c->mpCst.get();
+    a.kind = c->mpKind.get();
+    a.mask = c->mpMask.get();
+    a.srcterm = c->srcterm.get();
+    a.u = c->u.get();
+    a.mob = c->mpMob;
+    a.baseEps = c->pcHost.baseEps;
+    a.magnitude = c->pcHost.magnitude[0];
+    a.transient = c->dt > 0.0;
+    a.A = c->A.get();
+    a.r = c->r.get();
+    return a;
+}
+
+StencilArgs stencilArgs(dxg_ctx* c)
+{
+    StencilArgs a{};
+    a.nx = c->pcHost.nx;
+    a.ny = c->pcHost.ny;
+    a.nz = c->pcHost.nz;
+    a.N = c->N;
+    a.S = c->mpLayout.S;
+    a.center = c->mpLayout.center;
+    for (int s = 0; s < a.S; ++s) a.off[s] = c->mpOff[s];
+    a.mask = c->mpMask.get();
+    a.A = c->A.get();
+    a.LU = c->L.get();
+    a.Dinv = c->Dinv.get();
+    a.singular = c->singular.get();
+    a.ks = c->ks.get();
+    a.scratch = c->scratch();
+    a.nTri = c->mpNTri;
+    std::memcpy(a.tri, c->mpTri, sizeof(a.tri));
+    return a;
+}
+
+// slot s of row i: inside the pattern, and its column offset
+bool slotInPattern(const dxg_ctx* c, int64_t i, int s)
+{
+    if (c->mpfa) return (c->mpMaskHost[i] >> s) & 1u;
+    if (s == c->dim) return true;
+    const int f = s < c->dim ? 2 * (c->dim - 1 - s) : 2 * (s - c->dim - 1) + 1;
+    return (c->nbmaskHost[i] >> f) & 1u;
+}
+int64_t slotOffset(const dxg_ctx* c, int s) { return c->mpfa ? c->mpOff[s] : c->off[s]; }
+
 // ---------------------------------------------------------------- assembly
 void ensurePrevStorage(dxg_ctx* c)
 {
@@ -607,6 +831,17 @@ void assemble(dxg_ctx* c, bool jac)
 {
     requireUploaded(c);
     if (c->dt > 0.0 && !c->havePrev) throw Error(DXG_ERR_STATE, "transient assembly needs the previous solution");
+    if (c->mpfa) {
+        TimedScope ts(c, DXG_KC_ASSEMBLY, jac ? c->bytesAssembly : 0.0);
+        launchMpfaAssemble(mpfaArgs(c), c->method, jac, c->stream);
+        c->launches += 1;
+        c->haveRes = true;
+        if (jac) {
+            c->haveJac = true;
+            c->haveFactor = false;
+        }
+        return;
+    }
     ensurePrevStorage(c);
     const AssemblyArgs a = c->asmArgs();
     TimedScope ts(c, DXG_KC_ASSEMBLY, jac ? c->bytesAssembly : 0.0);
@@ -895,7 +1130,12 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
             c->launches += 1;
         }
         DXG_CUDA(cudaMemsetAsync(c->singular.get(), 0, 2 * sizeof(int), st));
-        if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB) {
+        if (c->mpfa) {
+            if constexpr (!mixed) {
+                launchStencilFactor(stencilArgs(c), st);
+                c->launches += 1;
+            }
+        } else if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB) {
             // AMG setup: fine pivots, then each coarse operator (with its pivots) from the one above
             std::vector<AmgLevel<PT>> L = amgLevels<PT>(c, PA, PD, nullptr, nullptr);
             launchAmgDiagInv<PT>(L[0], c->dim, c->b, c->singular.get(), st);
@@ -951,7 +1191,15 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
         amgP = amgLevels<PT>(c, PA, PD, pIn, yOut);
         amgR = amgLevels<PT>(c, PA, PD, rIn, yOut);
     }
+    const StencilArgs sa = c->mpfa ? stencilArgs(c) : StencilArgs{};
     auto precondition = [&](const PT* in) -> int64_t {
+        if constexpr (!mixed) {
+            if (c->mpfa) {
+                TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep);
+                launchStencilApply(sa, in, yOut, st);
+                return 1;
+            }
+        }
         if (amg) {
             TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(PT) / 8.0);
             return launchAmgVcycle<PT>(in == pIn ? amgP : amgR, c->dim, c->b, c->ks.get(), st);
@@ -967,14 +1215,24 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
         sv.x = yOut; sv.y = v; sv.w = rt;
         {
             TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv - (mixed ? 0.5 * c->N * c->b * 8.0 : 0.0));
-            launchSpmv<double, double, PT>(sv, c->b, c->dim, 1, st);
+            if constexpr (!mixed) {
+                if (c->mpfa) launchStencilSpmv(sa, yOut, v, rt, 1, st);
+                else launchSpmv<double, double, PT>(sv, c->b, c->dim, 1, st);
+            } else {
+                launchSpmv<double, double, PT>(sv, c->b, c->dim, 1, st);
+            }
         }
         launchBicgAxpyNorm<double>(ba, 0, st);
         n += 2 + precondition(rIn);
         sv.x = yOut; sv.y = t; sv.w = r;
         {
             TimedScope ts(c, DXG_KC_SPMV, c->bytesSpmv - (mixed ? 0.5 * c->N * c->b * 8.0 : 0.0));
-            launchSpmv<double, double, PT>(sv, c->b, c->dim, 2, st);
+            if constexpr (!mixed) {
+                if (c->mpfa) launchStencilSpmv(sa, yOut, t, r, 2, st);
+                else launchSpmv<double, double, PT>(sv, c->b, c->dim, 2, st);
+            } else {
+                launchSpmv<double, double, PT>(sv, c->b, c->dim, 2, st);
+            }
         }
         launchBicgAxpyNorm<double>(ba, 1, st);
         return n + 2;
@@ -1123,6 +1381,8 @@ struct NewtonRun {
         numSteps = 0;
         bool conv = false;
         // newtonBegin: all colors red (resetColors); numeric differentiation only
+        if (p.enable_partial_reassembly && c->mpfa)
+            throw Error(DXG_ERR_ARG, "partial reassembly is not available for MPFA-O");
         c->partialActive = p.enable_partial_reassembly != 0 && c->method != 3;
         if (c->partialActive) {
             c->partialDist.alloc(c->N);
@@ -1391,13 +1651,9 @@ int dxg_get_jacobian(dxg_ctx* c, int64_t* row_ptr, int32_t* col_idx, double* val
         int64_t k = 0;
         for (int64_t i = 0; i < c->N; ++i) {
             if (row_ptr) row_ptr[i] = k;
-            const unsigned m = c->nbmaskHost[i];
             for (int s = 0; s < c->slots; ++s) {
-                if (s != c->dim) {
-                    const int f = s < c->dim ? 2 * (c->dim - 1 - s) : 2 * (s - c->dim - 1) + 1;
-                    if (!((m >> f) & 1u)) continue;
-                }
-                if (col_idx) col_idx[k] = (int32_t)(i + c->off[s]);
+                if (!slotInPattern(c, i, s)) continue;
+                if (col_idx) col_idx[k] = (int32_t)(i + slotOffset(c, s));
                 if (values)
                     std::memcpy(values + k * c->bb, h.data() + ((size_t)s * c->N + i) * c->bb, sizeof(double) * c->bb);
                 ++k;
@@ -1421,7 +1677,7 @@ int dxg_set_linear_system(dxg_ctx* c, const int64_t* row_ptr, const int32_t* col
                 const int64_t dc = (int64_t)col_idx[k] - i;
                 int slot = -1;
                 for (int s = 0; s < c->slots; ++s)
-                    if (c->off[s] == dc) slot = s;
+                    if (slotOffset(c, s) == dc && slotInPattern(c, i, s)) slot = s;
                 if (slot < 0) throw Error(DXG_ERR_ARG, "entry outside the stencil pattern");
                 std::memcpy(h.data() + ((size_t)slot * c->N + i) * c->bb, values + k * c->bb, sizeof(double) * c->bb);
             }
@@ -1557,6 +1813,10 @@ int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
         c->err = "no wavefront plan fits this grid";
         return DXG_ERR_ARG;
     }
+    if (c->mpfa && kind != DXG_ILU_AUTO && kind != DXG_ILU_LEVELS) {
+        c->err = "MPFA-O contexts use the natural-order ILU(0) of their stencil";
+        return DXG_ERR_ARG;
+    }
     if (kind == DXG_ILU_LANES && c->uploaded && !c->lanePlan.ok) {
         c->err = "the lane sweeps need a 3D grid of 2x2 blocks that fits them";
         return DXG_ERR_ARG;
@@ -1577,6 +1837,10 @@ int dxg_set_wait_limit(dxg_ctx* c, double seconds)
 int dxg_set_linear_solver(dxg_ctx* c, int kind)
 {
     if (!c || (kind != DXG_LINEAR_SOLVER_ILU_BICGSTAB && kind != DXG_LINEAR_SOLVER_AMG_BICGSTAB)) return DXG_ERR_ARG;
+    if (c->mpfa && kind != DXG_LINEAR_SOLVER_ILU_BICGSTAB) {
+        c->err = "MPFA-O contexts solve with ILU(0)-BiCGSTAB";
+        return DXG_ERR_ARG;
+    }
     c->linearSolver = kind;
     c->haveFactor = false;
     return DXG_OK;
@@ -1587,6 +1851,9 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
     if (!c || !buf || len <= 0) return DXG_ERR_ARG;
     std::string out;
     if (!c->uploaded) out = "no problem uploaded";
+    else if (c->mpfa)
+        out = std::string("MPFA-O, ") + std::to_string(c->mpLayout.S) +
+              "-point stencil; ILU(0): natural order, hyperplanes x+2y+4z in one CTA";
     else if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB)
         out = "AMG-BiCGSTAB: " + std::to_string(amgLevelDims(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
                                                                (int)c->pcHost.nz).size() + 1) +

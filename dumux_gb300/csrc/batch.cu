@@ -157,6 +157,7 @@ struct Slot {
     // Newton state of the current attempt
     int numSteps = 0, divisions = 0;
     double shift = 0.0, lastShift = 0.0;
+    double reduction = 0.0, lastReduction = 1.0, initialResidual = 0.0;
     // linear solve of the current iteration
     bool solving = false, linConv = false;
     int chunks = 0, linIters = 0;
@@ -1121,6 +1122,69 @@ void finish(dxg_batch* B, Slot* s, int state, int status)
     s->tFinish = B->clock();
 }
 
+// ---------------------------------------------------------------- residual reduction
+// Members that need the residual norm after an update: Newton.UseLineSearch and
+// Newton.EnableResidualCriterion.
+bool needsResidual(const Slot* s) { return s->p.use_line_search || s->p.enable_residual_criterion; }
+
+// FVAssembler::assembleResidual for members of one group: own-state volume variables and
+// residual rows, the launches of the single context's residual assembly.
+void assembleResiduals(dxg_batch* B, const Members& S)
+{
+    cudaStream_t st = B->stream;
+    const dxg_ctx* c0 = S[0]->c;
+    std::vector<AssemblyArgs> aa;
+    for (Slot* s : S) {
+        AssemblyArgs a = s->c->asmArgs();
+        a.u = s->c->u.get();
+        aa.push_back(a);
+    }
+    const AssemblyArgs* daa = B->arena.put(aa, st);
+    const int64_t maxN = maxCells(S);
+    launchVolvarsBatch(daa, (int)S.size(), maxN, c0->b, 2, st);
+    launchRowBatch(daa, (int)S.size(), maxN, c0->b, c0->dim, c0->method, false, c0->gravity && c0->pcHost.gravAxisMask,
+                   S[0]->transient, c0->fullUpwind, st);
+    B->launches += 2;
+}
+
+// Euclidean norms of the members' residuals (IstlIterativeLinearSolver::norm) through the
+// single context's reduction kernel, so a member's norm is the same alone and batched.
+std::vector<double> residualNorms(dxg_batch* B, const Members& S)
+{
+    for (Slot* s : S) {
+        launchNorm2(s->c->r.get(), s->c->M, s->c->scratch(), s->c->scal.get() + 1, B->stream);
+        B->launches += 1;
+    }
+    gather(B, S);
+    std::vector<double> n(S.size());
+    for (size_t k = 0; k < S.size(); ++k) n[k] = B->reportsHost[k].norm;
+    return n;
+}
+
+// u = uLast - lambda * delta and the relative shift for each member (in place, u == uLast,
+// when `fromLast` is false); the shifts come back through a gather.
+std::vector<double> newtonUpdates(dxg_batch* B, const Members& S, const std::vector<double>& lambda,
+                                  const std::vector<bool>& fromLast)
+{
+    std::vector<NewtonUpdArgs> ua;
+    std::vector<int64_t> lenM;
+    for (size_t k = 0; k < S.size(); ++k) {
+        dxg_ctx* c = S[k]->c;
+        ua.push_back({fromLast[k] ? c->uLast.get() : c->u.get(), c->kx.get(), c->u.get(), lambda[k], c->M,
+                      c->scratch(), c->scal.get()});
+        lenM.push_back(c->M);
+    }
+    std::vector<uint2> mM;
+    buildBlockMap(lenM, false, mM);
+    launchNewtonUpdateBatch(B->arena.put(ua, B->stream), BlockMap{B->arena.put(mM, B->stream), (unsigned)mM.size()},
+                            B->stream);
+    B->launches += 1;
+    gather(B, S);
+    std::vector<double> shift(S.size());
+    for (size_t k = 0; k < S.size(); ++k) shift[k] = B->reportsHost[k].shift;
+    return shift;
+}
+
 // Assembly, ILU(0) factorisation and BiCGSTAB start for members that begin a Newton
 // iteration (FVAssembler::assembleJacobianAndResidual + the solver's setup).
 template <class PT>
@@ -1184,6 +1248,17 @@ void beginIterations(dxg_batch* B, const GroupState& G, const Members& S, const 
         TimedB tb(B, DXG_KC_ASSEMBLY, bytesOf(A, &dxg_ctx::bytesAssembly, 1.0));
         launchVolvarsBatch(daa, n, maxN, b, method, st);
         launchRowBatch(daa, n, maxN, b, dim, method, true, grav, transient, c0->fullUpwind, st);
+    }
+    // the initial residual of an attempt, for the residual reduction (solveImpl_)
+    Members R;
+    for (Slot* s : A) {
+        if (!needsResidual(s)) continue;
+        s->lastReduction = s->numSteps == 0 ? 1.0 : s->reduction;
+        if (s->numSteps == 0) R.push_back(s);
+    }
+    if (!R.empty()) {
+        const std::vector<double> r0 = residualNorms(B, R);
+        for (size_t k = 0; k < R.size(); ++k) R[k]->initialResidual = r0[k];
     }
     if (mixed) {
         launchToFloatBatch(B->arena.put(tf, st), n, maxA, st);
@@ -1294,22 +1369,51 @@ void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
         if (s->linConv) U.push_back(s);
     }
     if (ended.empty()) return;
-    // u -= delta and the relative shift for members whose solve converged
-    if (!U.empty()) {
-        std::vector<NewtonUpdArgs> ua;
-        for (Slot* s : U)
-            ua.push_back({s->c->u.get(), s->c->kx.get(), s->c->u.get(), 1.0, s->c->M, s->c->scratch(),
-                          s->c->scal.get()});
-        std::vector<int64_t> lenM;
-        for (Slot* s : U) lenM.push_back(s->c->M);
-        std::vector<uint2> mM;
-        buildBlockMap(lenM, false, mM);
-        launchNewtonUpdateBatch(B->arena.put(ua, st), BlockMap{B->arena.put(mM, st), (unsigned)mM.size()}, st);
-        B->launches += 1;
-        gather(B, U);
-    }
+    // u -= delta and the relative shift for members whose solve converged; members with a
+    // line search keep the last iterate (uLastIter) for their backtracking
     std::map<Slot*, double> shifts;
-    for (size_t k = 0; k < U.size(); ++k) shifts[U[k]] = B->reportsHost[k].shift;
+    if (!U.empty()) {
+        std::vector<CopyArgs> keep;
+        std::vector<bool> fromLast;
+        for (Slot* s : U) {
+            fromLast.push_back(s->p.use_line_search != 0);
+            if (s->p.use_line_search) keep.push_back({s->c->uLast.get(), s->c->u.get(), s->c->M});
+        }
+        batchCopy(B, keep);
+        const std::vector<double> sh = newtonUpdates(B, U, std::vector<double>(U.size(), 1.0), fromLast);
+        for (size_t k = 0; k < U.size(); ++k) shifts[U[k]] = sh[k];
+    }
+    // residual reduction (Newton.EnableResidualCriterion) and the backtracking line search
+    // (Newton.UseLineSearch, lineSearchUpdate_, newtonsolver.hh:1154-1178): lambda halves
+    // from 1 until the reduction falls below the last iteration's or lambda reaches
+    // Newton.LineSearchMinRelaxationFactor; the shift is the accepted iterate's
+    Members R;
+    std::map<Slot*, double> lambda;
+    for (Slot* s : U)
+        if (needsResidual(s)) {
+            R.push_back(s);
+            lambda[s] = 1.0;
+        }
+    while (!R.empty()) {
+        assembleResiduals(B, R);
+        const std::vector<double> norms = residualNorms(B, R);
+        Members again;
+        std::vector<double> lam;
+        for (size_t k = 0; k < R.size(); ++k) {
+            Slot* s = R[k];
+            s->reduction = norms[k] / s->initialResidual;
+            if (!s->p.use_line_search || s->reduction < s->lastReduction ||
+                lambda[s] <= s->p.line_search_min_relaxation)
+                continue;
+            lambda[s] *= 0.5;
+            again.push_back(s);
+            lam.push_back(lambda[s]);
+        }
+        if (again.empty()) break;
+        const std::vector<double> sh = newtonUpdates(B, again, lam, std::vector<bool>(again.size(), true));
+        for (size_t k = 0; k < again.size(); ++k) shifts[again[k]] = sh[k];
+        R = again;
+    }
 
     std::vector<CopyArgs> restore, advance;
     for (int k : ended) {
@@ -1328,7 +1432,10 @@ void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
             s->lastShift = s->shift;
             s->shift = shifts[s];
             s->numSteps += 1;
-            const bool conv = s->shift <= s->p.max_relative_shift;
+            // newtonConverged (newtonsolver.hh:657-701): the shift, or with the residual
+            // criterion either of the shift and the residual reduction
+            const bool conv = s->shift <= s->p.max_relative_shift ||
+                              (s->p.enable_residual_criterion && s->reduction <= s->p.residual_reduction);
             if (!std::isfinite(s->shift)) failed = true;
             else if (!proceed(*s, conv)) {
                 if (!conv) failed = true;
@@ -1350,6 +1457,7 @@ void tickGroup(dxg_batch* B, const GroupKey& key, const Members& S)
                     s->dt = std::min(std::min(suggest(*s, s->dt), s->dtMax), remaining);
                     s->numSteps = 0;
                     s->shift = s->lastShift = 0.0;
+                    s->reduction = 0.0;
                     s->divisions = 0;
                 }
             }
@@ -1516,6 +1624,12 @@ int64_t dxg_problem_device_bytes(const dxg_problem_desc* d, int precision)
         N *= d->cells[a];
     }
     const int64_t nb = dxg_num_boundary_faces(d);
+    if (d->discretization == DXG_DISC_MPFA_O) {
+        // flux rows (F scvfs x (2^dim coefficients + constant) + kind), stencil mask and
+        // source, the Jacobian and its factor over 3^dim slots, eleven vectors
+        const int64_t S = d->dim == 2 ? 9 : 27, K = 1 << d->dim, F = 2 * d->dim * (K / 2);
+        return N * (F * (K + 1) * 8 + F + 4 + 8) + N * S * 8 * 2 + N * 8 * 12;
+    }
     return problemBytes(N, nb, d->num_eq, d->dim, d->numeric_difference_method, precision);
 }
 
@@ -1532,6 +1646,10 @@ int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, dou
                   double t_end, const dxg_newton_params* params, int64_t* id)
 {
     if (!b || !d || !u0 || !id) return DXG_ERR_ARG;
+    if (d->discretization != DXG_DISC_TPFA) {
+        b->err = "batched problems use the TPFA discretization";
+        return DXG_ERR_ARG;
+    }
     int64_t need = dxg_problem_device_bytes(d, b->precision);
     if (need < 0) {
         b->err = "invalid problem description";
@@ -1559,8 +1677,8 @@ int dxg_batch_add(dxg_batch* b, const dxg_problem_desc* d, const double* u0, dou
     if ((st = step(dxg_set_prev_solution(s->c, u0))) != DXG_OK) return st;
     if (params) s->p = *params;
     else dxg_newton_default_params(&s->p);
-    if (s->p.use_line_search || s->p.enable_residual_criterion || s->p.enable_partial_reassembly) {
-        b->err = "batched problems use the shift criterion, full reassembly and no line search";
+    if (s->p.enable_partial_reassembly) {
+        b->err = "batched problems reassemble the full Jacobian (no partial reassembly)";
         return DXG_ERR_ARG;
     }
     s->transient = t_end > 0.0 && dt > 0.0;

@@ -8,6 +8,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "linalg_kernels.cuh"
+#include "mpfa.cuh"
 #include "wave.cuh"
 
 struct dxg_ctx {
@@ -37,6 +38,19 @@ struct dxg_ctx {
     dxg::DevBuf<int8_t> btype;
     dxg::DevBuf<double> bTij, bG1, bP, bU, bNeu;
     dxg::DevBuf<uint8_t> nbmask;
+
+    // MPFA-O (1p): per-(cell, scvf) flux rows, the 3^dim stencil of the Jacobian and its
+    // ILU(0) (L holds the LU factor [S][N], Dinv the inverted pivots)
+    bool mpfa = false;
+    dxg::MpfaLayout mpLayout{};
+    int64_t mpOff[27] = {};
+    dxg::DevBuf<double> mpCoef, mpCst;
+    dxg::DevBuf<int8_t> mpKind;
+    dxg::DevBuf<uint32_t> mpMask;
+    std::vector<uint32_t> mpMaskHost;
+    double mpMob = 0.0;
+    int mpNTri = 0;
+    int8_t mpTri[104][3] = {};
 
     // state
     dxg::DevBuf<double> u, uprev, uLast, stPrev;

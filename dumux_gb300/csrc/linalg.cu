@@ -1125,4 +1125,164 @@ template void launchBicgAxpyNorm<float>(const BicgArgs<float>&, int, cudaStream_
 template void launchCopyToDouble<double>(const double*, double*, int64_t, cudaStream_t);
 template void launchCopyToDouble<float>(const float*, double*, int64_t, cudaStream_t);
 
+// ---------------------------------------------------------------- scalar stencil operators
+// Rows of one unknown over the 3^dim neighbourhood of a cell (the MPFA-O Jacobian): values
+// A[slot][row], slot s = (ox+1) + 3(oy+1) + 9(oz+1) in ascending column order, valid for row
+// i when bit s of mask[i] is set.
+
+// y = A x; MODE 1: also dot(w, y) -> h, alpha; MODE 2: dots (y,w),(y,y) -> omega (the
+// Krylov-state updates of spmvKernel)
+template <int S, int MODE>
+__global__ void __launch_bounds__(kReduceThreads) stencilSpmvKernel(StencilArgs a, const double* __restrict__ x,
+                                                                     double* __restrict__ y, const double* __restrict__ w)
+{
+    const unsigned nblk = cellBlocksFor(a.N);
+    const unsigned lb = blockIdx.x;
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    double part[2] = {0.0, 0.0};
+    for (int64_t i = lb * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
+        const uint32_t m = __ldg(a.mask + i);
+        double sum = 0.0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const bool valid = (m >> s) & 1u;
+            const double aij = __ldg(a.A + (int64_t)s * a.N + i);
+            const double xj = __ldg(x + i + (valid ? a.off[s] : 0));
+            sum += valid ? aij * xj : 0.0;
+        }
+        y[i] = sum;
+        if (MODE == 1) {
+            part[0] += w[i] * sum;
+        } else if (MODE == 2) {
+            part[0] += sum * w[i];
+            part[1] += sum * sum;
+        }
+    }
+    if (MODE == 0) return;
+    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE, nblk, lb)) {
+        KrylovState& ks = *a.ks;
+        if (MODE == 1) {
+            ks.h = part[0];
+            if (fabs(ks.h) < 1e-80) ks.status = KS_BREAKDOWN;
+            else ks.alpha = ks.rho_new / ks.h;
+        } else {
+            ks.tr = part[0];
+            ks.tt = part[1];
+            ks.omega = ks.tr / ks.tt;
+        }
+    }
+}
+
+// Rows of hyperplane level L of the natural ordering: x + 2y + 4z = L.  Every lower
+// neighbour of a row (dz = -1; dz = 0, dy = -1; dz = dy = 0, dx = -1) sits on a lower
+// level, so the rows of one level are independent.
+template <class F>
+__device__ __forceinline__ void forLevelRows(const StencilArgs& a, int L, F&& body)
+{
+    const int lines = a.ny * a.nz;
+    for (int q = threadIdx.x; q < lines; q += blockDim.x) {
+        const int yy = q % a.ny, zz = q / a.ny;
+        const int xx = L - 2 * yy - 4 * zz;
+        if (xx >= 0 && xx < a.nx) body(((int64_t)zz * a.ny + yy) * a.nx + xx);
+    }
+}
+
+// ILU(0) of the stencil matrix in one CTA, level by level (Saad's row-wise IKJ variant as
+// the block ILU(0) of the linear solver: for each lower entry j of row i in column order,
+// l_ij = a_ij / u_jj, then a_ik -= l_ij u_jk for every later entry k of row i that row j
+// holds; pivots stored inverted).  LU keeps the multipliers in the lower slots and U in the
+// upper slots.
+__global__ void __launch_bounds__(1024) stencilFactorKernel(StencilArgs a)
+{
+    const int levels = (a.nx - 1) + 2 * (a.ny - 1) + 4 * (a.nz - 1) + 1;
+    for (int L = 0; L < levels; ++L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            for (int s = 0; s < a.S; ++s) a.LU[(int64_t)s * a.N + i] = a.A[(int64_t)s * a.N + i];
+            int t0 = 0;
+            for (int s = 0; s < a.center; ++s) {
+                if (!((m >> s) & 1u)) continue;
+                const int64_t j = i + a.off[s];
+                const double l = a.LU[(int64_t)s * a.N + i] * a.Dinv[j];
+                a.LU[(int64_t)s * a.N + i] = l;
+                const uint32_t mj = a.mask[j];
+                // the update triples (s, t, u) of this s, t ascending
+                while (t0 < a.nTri && a.tri[t0][0] < s) ++t0;
+                for (int k = t0; k < a.nTri && a.tri[k][0] == s; ++k) {
+                    const int t = a.tri[k][1], u = a.tri[k][2];
+                    if (!((m >> t) & 1u) || !((mj >> u) & 1u)) continue;
+                    a.LU[(int64_t)t * a.N + i] -= l * a.LU[(int64_t)u * a.N + j];
+                }
+            }
+            const double piv = a.LU[(int64_t)a.center * a.N + i];
+            if (piv == 0.0) atomicExch(a.singular, 1);
+            a.Dinv[i] = 1.0 / piv;
+        });
+        __syncthreads();
+    }
+}
+
+// v = (LU)^-1 d: forward sweep with the multipliers, backward sweep with U and the inverted
+// pivots, both level by level in one CTA.
+__global__ void __launch_bounds__(1024) stencilApplyKernel(StencilArgs a, const double* __restrict__ d,
+                                                            double* __restrict__ v)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    const int levels = (a.nx - 1) + 2 * (a.ny - 1) + 4 * (a.nz - 1) + 1;
+    for (int L = 0; L < levels; ++L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            double rhs = d[i];
+            for (int s = 0; s < a.center; ++s)
+                if ((m >> s) & 1u) rhs -= a.LU[(int64_t)s * a.N + i] * v[i + a.off[s]];
+            v[i] = rhs;
+        });
+        __syncthreads();
+    }
+    for (int L = levels - 1; L >= 0; --L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            double rhs = v[i];
+            for (int s = a.center + 1; s < a.S; ++s)
+                if ((m >> s) & 1u) rhs -= a.LU[(int64_t)s * a.N + i] * v[i + a.off[s]];
+            v[i] = a.Dinv[i] * rhs;
+        });
+        __syncthreads();
+    }
+}
+
+void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st)
+{
+    const dim3 g((unsigned)cellBlocksFor(a.N));
+    if (a.S == 9) {
+        if (mode == 0) stencilSpmvKernel<9, 0><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        else if (mode == 1) stencilSpmvKernel<9, 1><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        else stencilSpmvKernel<9, 2><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+    } else {
+        if (mode == 0) stencilSpmvKernel<27, 0><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        else if (mode == 1) stencilSpmvKernel<27, 1><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        else stencilSpmvKernel<27, 2><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+    }
+    DXG_CUDA(cudaGetLastError());
+}
+
+static unsigned stencilThreads(const StencilArgs& a)
+{
+    const int lines = a.ny * a.nz;
+    const int t = ((lines + 31) / 32) * 32;
+    return (unsigned)std::min(1024, std::max(32, t));
+}
+
+void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
+{
+    stencilFactorKernel<<<1, stencilThreads(a), 0, st>>>(a);
+    DXG_CUDA(cudaGetLastError());
+}
+
+void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
+{
+    stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
+    DXG_CUDA(cudaGetLastError());
+}
+
 }  // namespace dxg

@@ -119,6 +119,30 @@ struct DefectArgs {
 
 int reduceBlocks(int64_t M);
 
+// Scalar rows over the 3^dim neighbourhood of a cell (MPFA-O): A[slot][row] with slot
+// s = (ox+1) + 3(oy+1) + 9(oz+1), valid for row i when bit s of mask[i] is set; LU / Dinv the
+// ILU(0) factors (multipliers in the lower slots, U in the upper ones, inverted pivots).
+// The ILU(0) update of row i by its lower entry s touches entry t of row i with entry u of
+// row i + off[s]: tri[k] = {s, t, u}, s then t ascending.
+struct StencilArgs {
+    int nx = 1, ny = 1, nz = 1;
+    int64_t N = 0;
+    int S = 0, center = 0;
+    int64_t off[27] = {};
+    const uint32_t* mask = nullptr;
+    const double* A = nullptr;
+    double* LU = nullptr;
+    double* Dinv = nullptr;
+    int* singular = nullptr;
+    KrylovState* ks = nullptr;
+    ReduceScratch scratch{};
+    int nTri = 0;
+    int8_t tri[104][3] = {};
+};
+void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st);
+void launchStencilFactor(const StencilArgs& a, cudaStream_t st);
+void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+
 template <class MT, class VT, class XT = VT>
 void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);
 template <class MT>

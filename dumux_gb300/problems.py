@@ -20,10 +20,12 @@ def equidistant(lower, upper, cells):
     return lower + np.arange(cells + 1, dtype=np.float64) * h
 
 
-def onep_lens_problem(cells=(10, 10), numeric_epsilon=True):
+def onep_lens_problem(cells=(10, 10), numeric_epsilon=True, discretization="tpfa"):
     """test/porousmediumflow/1p/incompressible (problem.hh, spatialparams.hh, params.input):
     unit square, lens [0.2,0.8]^2 with K=1e-12 in K=1e-10, Dirichlet top/bottom with
-    p = 1e5 - 1e5*(y - ymax), no-flow left/right, gravity on, stationary."""
+    p = 1e5 - 1e5*(y - ymax), no-flow left/right, gravity on, stationary.  With
+    discretization="mpfa" it is the reference's test_1p_incompressible_mpfa, which compares
+    against the same reference solution as the TPFA test (CMakeLists.txt:41-51)."""
     coords = [equidistant(0.0, 1.0, n) for n in cells]
     cc = cell_centers(coords)
     eps = 1.5e-7
@@ -41,8 +43,76 @@ def onep_lens_problem(cells=(10, 10), numeric_epsilon=True):
                        bc_type=bc_type, bc_values=bc_values, enable_gravity=True,
                        density=(WATER_DENSITY, WATER_DENSITY), viscosity=(WATER_VISCOSITY, WATER_VISCOSITY),
                        base_epsilon=0.1 if numeric_epsilon else 1e-10,
-                       privar_magnitude=(1e5, -1.0) if numeric_epsilon else (-1.0, -1.0))
+                       privar_magnitude=(1e5, -1.0) if numeric_epsilon else (-1.0, -1.0),
+                       discretization=discretization)
     return desc, np.zeros(desc.num_dofs)
+
+
+# test/porousmediumflow/1p/convergence/analyticsolution: omega = pi (spatialparams.hh:70)
+_CONV_OMEGA = np.pi
+
+
+def mpfa_convergence_exact(x, y):
+    """Pressure of the analytic solution (problem.hh:125-139): (e^(y+1) + 2 - e^2) sin(w x) + 10."""
+    return (np.exp(y + 1.0) + 2.0 - np.exp(2.0)) * np.sin(_CONV_OMEGA * x) + 10.0
+
+
+def mpfa_convergence_problem(cells=10, c=0.9, discretization="mpfa"):
+    """test/porousmediumflow/1p/convergence/analyticsolution (problem.hh, spatialparams.hh,
+    params.input, properties.hh): unit square with `cells` x `cells` cells, the full
+    permeability tensor K = [[1, -c/(2w) sin(w x)], [., e^-2 (1 + c cos(w x))]] at the cell
+    centres, the source term of the analytic solution at the cell centres, Dirichlet values
+    of the analytic solution at every boundary face centre, no gravity, a constant liquid of
+    density 1 and kinematic viscosity 1 (dynamic viscosity 1).  Returns the description, the
+    zero initial solution and the exact pressures at the cell centres."""
+    coords = [equidistant(0.0, 1.0, cells) for _ in range(2)]
+    cc = cell_centers(coords)
+    x, y = cc[:, 0], cc[:, 1]
+    w = _CONV_OMEGA
+    K = np.zeros((len(cc), 2, 2))
+    K[:, 0, 0] = 1.0
+    K[:, 0, 1] = -c / (2 * w) * np.sin(w * x)
+    K[:, 1, 0] = K[:, 0, 1]
+    K[:, 1, 1] = np.exp(-2.0) * (1.0 + c * np.cos(w * x))
+    cosx = np.cos(w * x)
+    src = (-(c * cosx + 1.0) * np.exp(y - 1.0) + 1.5 * c * np.exp(y + 1.0) * cosx
+           + w * w * (np.exp(y + 1.0) - np.exp(2.0) + 2.0)) * np.sin(w * x)
+    fc = boundary_face_centers(2, coords)
+    bc_values = mpfa_convergence_exact(fc[:, 0], fc[:, 1])
+    desc = ProblemDesc(coords=coords, num_eq=1, permeability=np.ones(len(cc)), porosity=np.full(len(cc), 0.4),
+                       bc_type=np.ones(len(fc), dtype=np.int8), bc_values=bc_values, enable_gravity=False,
+                       density=(1.0, 1.0), viscosity=(1.0, 1.0), source=src,
+                       permeability_tensor=K if discretization == "mpfa" else None,
+                       discretization=discretization)
+    return desc, np.zeros(desc.num_dofs), mpfa_convergence_exact(x, y)
+
+
+def mpfa_linear_field_problem(cells=(6, 5), K=((2.0, 0.5), (0.5, 1.0)), grad=(1.0, -2.0, 0.5), p0=3.0,
+                              spacing_seed=None, gravity=False):
+    """A constant full permeability tensor and Dirichlet values of the linear pressure
+    p = p0 + grad . x on every boundary face, no source: MPFA-O reproduces the linear
+    field exactly at the cell centres (the O-method is exact for linear pressures on
+    parallelepiped cells), TPFA does not once K has off-diagonal entries.  With
+    `spacing_seed` the vertex coordinates are perturbed per axis (still a tensor grid)."""
+    dim = len(cells)
+    rng = np.random.default_rng(spacing_seed) if spacing_seed is not None else None
+    coords = []
+    for a, n in enumerate(cells):
+        x = equidistant(0.0, 1.0, n)
+        if rng is not None:
+            x[1:-1] += rng.uniform(-0.3, 0.3, n - 1) / n
+        coords.append(x)
+    cc = cell_centers(coords)
+    N = len(cc)
+    Kt = np.tile(np.asarray(K, dtype=np.float64).reshape(1, dim, dim), (N, 1, 1))
+    fc = boundary_face_centers(dim, coords)
+    g = np.asarray(grad[:dim])
+    bc_values = p0 + fc[:, :dim] @ g
+    desc = ProblemDesc(coords=coords, num_eq=1, permeability=np.ones(N), porosity=np.full(N, 0.3),
+                       bc_type=np.ones(len(fc), dtype=np.int8), bc_values=bc_values, enable_gravity=gravity,
+                       density=(WATER_DENSITY, WATER_DENSITY), viscosity=(WATER_VISCOSITY, WATER_VISCOSITY),
+                       permeability_tensor=Kt, discretization="mpfa")
+    return desc, np.zeros(N), p0 + cc[:, :dim] @ g
 
 
 def gaussian_lnk_field(cells, mean, sigma, corr_len, seed):

@@ -90,7 +90,20 @@ typedef struct dxg_problem_desc {
      * Swr, Snr, pcLowSwe, pcHighSwe, krnLowSwe, krwHighSwe -- the reference's defaults
      * for the last four are 0.01, 0.99, 0.1, 0.9)                                        */
     int32_t material_law;
+    /* Discretisation of the fluxes: DXG_DISC_TPFA (0, default) two-point flux approximation
+     * (discretization/cellcentered/tpfa), or DXG_DISC_MPFA_O (1) the multi-point flux
+     * approximation O-method (discretization/cellcentered/mpfa/omethod, flux/ccmpfa/darcyslaw.hh)
+     * with continuity points at the face centres (MPFA.Q = 0), for the 1p model (num_eq == 1)
+     * in FP64 single contexts: one interaction volume per grid vertex, its local flux-continuity
+     * system solved once at upload (the transmissibilities of the incompressible model do not
+     * depend on the solution), a 3^dim-point Jacobian stencil and ILU(0) over it.          */
+    int32_t discretization;
+    /* Full intrinsic permeability tensor per cell, N*dim*dim values (row-major, symmetric
+     * positive definite), or NULL: the isotropic `permeability` above.  MPFA-O only.      */
+    const double* permeability_tensor;
 } dxg_problem_desc;
+
+enum { DXG_DISC_TPFA = 0, DXG_DISC_MPFA_O = 1 };
 
 /* Number of boundary faces implied by the grid of desc. */
 int64_t dxg_num_boundary_faces(const dxg_problem_desc* desc);
@@ -389,7 +402,8 @@ int64_t dxg_batch_device_bytes(const dxg_batch* batch);
 /* Admit a problem: initial solution u0 (N*num_eq values, also the first previous
  * time level), initial time step dt, maximum time step max_dt (TimeLoop.MaxTimeStepSize;
  * <= 0: unlimited) and end time t_end (t_end <= 0: one stationary Newton solve), Newton
- * and linear-solver parameters (NULL: defaults).  *id receives its handle. */
+ * and linear-solver parameters (NULL: defaults; line search and the residual criterion
+ * as in a context, partial reassembly refused with DXG_ERR_ARG).  *id receives its handle. */
 int dxg_batch_add(dxg_batch* batch, const dxg_problem_desc* desc, const double* u0, double dt, double max_dt,
                   double t_end, const dxg_newton_params* params, int64_t* id);
 /* One tick (see above); *active receives the number of problems still active. */

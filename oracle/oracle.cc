@@ -635,8 +635,10 @@ struct Pattern {
     std::vector<int64_t> rowBlock;           // per cell I, per face f: block index of (I,J), -1 if none
 };
 
+static Pattern mpfaPattern(const Problem& P);
 static Pattern buildPattern(const Problem& P)
 {
+    if (P.d.discretization == 1) return mpfaPattern(P);
     Pattern pt;
     const int nf = 2 * P.dim;
     std::vector<std::vector<int32_t>> rows(P.N);
@@ -675,6 +677,354 @@ static Pattern buildPattern(const Problem& P)
         }
     }
     return pt;
+}
+
+// ---------------------------------------------------------------- MPFA-O (1p)
+// Cell-centred MPFA-O of dumux/discretization/cellcentered/mpfa/omethod for the 1p model on
+// the tensor-product grid, continuity points at the face centres (MPFA.Q = 0):
+//   * sub control volume faces: every element face split at its corners, the scvf of corner
+//     c joining the facet centre and the corner vertex (helper.hh:122-167, 344-462;
+//     fvgridgeometry.hh:300-350); scvfs in element order: faces by index in the element,
+//     corners in reference-element order;
+//   * interaction volume of a vertex: the scvs and scvfs around it; in each scv the basis
+//     vectors from the cell centre to the integration points of its scvfs at the vertex, their
+//     inner normals and determinant (localsubcontrolentities.hh:43-83, helper.hh:58-109,
+//     255-299), w = n^T K nu area extrusion / detX (computetransmissibility.hh:32-50);
+//   * local matrices A, B, C, D with the Dirichlet faces as knowns and interior/Neumann
+//     faces as unknowns (omethod/localassembler.hh:150-330), T = D + (C A^-1) B
+//     (localassemblerhelper.hh:70-80); gravity g = alpha rho area + C A^-1 deltaG
+//     (localassemblerbase.hh:125-222);
+//   * the advective flux of an scvf: (T u + g) * density * mobility (flux/ccmpfa/
+//     darcyslaw.hh:150-205), negated for the element on the outside of the IV face;
+//     Neumann scvfs: the given flux times area and extrusion (cclocalresidual.hh:89-97);
+//   * numeric Jacobian as CCLocalAssembler<numeric> (cclocalassembler.hh:164-348): column I
+//     from the perturbation of element I's unknown, the diagonal from I's whole residual, the
+//     entry of neighbour J from J's scvf fluxes whose interaction volume contains I.
+// The IV transmissibilities of the incompressible model are solution independent and are
+// computed once per assembly call.
+
+struct MpIvTerm { int64_t cell; double t; };
+struct MpScvfRow {
+    bool neumann = false;
+    double c0 = 0.0;                 // Dirichlet part + gravity (IV faces), flux (Neumann)
+    std::vector<MpIvTerm> terms;     // IV cells in position order (existing cells only)
+};
+
+// Gauss-Jordan elimination with partial pivoting: the inverse of A (n x n), in place
+static void gjInverse(std::vector<double>& A, int n)
+{
+    std::vector<double> I((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) I[(size_t)i * n + i] = 1.0;
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(A[(size_t)r * n + c]) > std::fabs(A[(size_t)p * n + c])) p = r;
+        if (A[(size_t)p * n + c] == 0.0) throw std::invalid_argument("singular interaction-volume system");
+        if (p != c)
+            for (int k = 0; k < n; ++k) { std::swap(A[(size_t)p * n + k], A[(size_t)c * n + k]); std::swap(I[(size_t)p * n + k], I[(size_t)c * n + k]); }
+        const double inv = 1.0 / A[(size_t)c * n + c];
+        for (int k = 0; k < n; ++k) { A[(size_t)c * n + k] *= inv; I[(size_t)c * n + k] *= inv; }
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = A[(size_t)r * n + c];
+            if (f == 0.0) continue;
+            for (int k = 0; k < n; ++k) { A[(size_t)r * n + k] -= f * A[(size_t)c * n + k]; I[(size_t)r * n + k] -= f * I[(size_t)c * n + k]; }
+        }
+    }
+    A.swap(I);
+}
+
+static double mpVtmv(const Problem& P, int64_t cell, const double* n, const double* v)
+{
+    const int dim = P.dim;
+    if (!P.d.permeability_tensor) {
+        double s = 0.0;
+        for (int i = 0; i < dim; ++i) s += n[i] * v[i];
+        return P.d.permeability[cell] * s;
+    }
+    const double* K = P.d.permeability_tensor + (size_t)cell * dim * dim;
+    double Kv[3] = {0, 0, 0};
+    for (int i = 0; i < dim; ++i) { double s = 0.0; for (int j = 0; j < dim; ++j) s += K[i * dim + j] * v[j]; Kv[i] = s; }
+    double s = 0.0;
+    for (int i = 0; i < dim; ++i) s += n[i] * Kv[i];
+    return s;
+}
+
+// The flux rows of every scvf of every element.
+static std::vector<std::vector<MpScvfRow>> mpfaRows(const Problem& P)
+{
+    const int dim = P.dim, corners = 1 << (dim - 1), nPos = 1 << dim;
+    const int nScvf = 2 * dim * corners;
+    std::vector<std::vector<MpScvfRow>> rows(P.N, std::vector<MpScvfRow>(nScvf));
+    const double rho = P.d.density[0];
+    const bool grav = P.d.enable_gravity != 0;
+    const int64_t nv[3] = {P.n[0] + 1, P.n[1] + 1, dim == 3 ? P.n[2] + 1 : 1};
+    // the cell at IV position `pos` of vertex v, or -1
+    auto cellAt = [&](const int64_t* v, int pos, int64_t* id) -> int64_t {
+        for (int a = 0; a < 3; ++a) id[a] = a < dim ? v[a] - 1 + ((pos >> a) & 1) : 0;
+        for (int a = 0; a < dim; ++a) if (id[a] < 0 || id[a] >= P.n[a]) return -1;
+        return id[0] + P.n[0] * (id[1] + P.n[1] * id[2]);
+    };
+#pragma omp parallel for schedule(dynamic, 64) num_threads(orc_get_threads())
+    for (int64_t vi = 0; vi < nv[0] * nv[1] * nv[2]; ++vi) {
+        const int64_t v[3] = {vi % nv[0], (vi / nv[0]) % nv[1], vi / (nv[0] * nv[1])};
+        double xv[3] = {0, 0, 0};
+        for (int a = 0; a < dim; ++a) xv[a] = P.d.coords[a][v[a]];
+        int64_t cell[8], cid[8][3];
+        for (int q = 0; q < nPos; ++q) cell[q] = cellAt(v, q, cid[q]);
+        // faces of the IV: for each axis the corners-many pairs (lower, upper) of positions
+        struct F { int a, lo, hi, P, Q; bool bnd, dir; double uD, n[3], area; int64_t bidx; int dof, kn; };
+        std::vector<F> faces;
+        for (int a = 0; a < dim; ++a)
+            for (int q = 0; q < nPos; ++q) {
+                if ((q >> a) & 1) continue;
+                F f{};
+                f.a = a; f.lo = q; f.hi = q | (1 << a);
+                if (cell[f.lo] < 0 && cell[f.hi] < 0) continue;
+                f.P = cell[f.lo] >= 0 ? f.lo : f.hi;
+                f.Q = (cell[f.lo] >= 0 && cell[f.hi] >= 0) ? f.hi : -1;
+                f.bnd = f.Q < 0;
+                f.n[a] = f.P == f.lo ? 1.0 : -1.0;
+                const int64_t* pid = cid[f.P];
+                f.area = 1.0;
+                for (int k = 0; k < dim; ++k) if (k != a) f.area *= 0.5 * (P.hi(k, pid[k]) - P.lo(k, pid[k]));
+                f.bidx = -1; f.dir = false; f.uD = 0.0;
+                if (f.bnd) {
+                    const Face fc = P.face(cell[f.P], 2 * a + (f.P == f.lo ? 1 : 0));
+                    f.bidx = fc.bidx;
+                    f.dir = P.d.bc_type[f.bidx] == 1;
+                    f.uD = P.d.bc_values[f.bidx];
+                }
+                faces.push_back(f);
+            }
+        const int nF = (int)faces.size();
+        // knowns: existing cells by position, then Dirichlet faces; unknowns: the other faces
+        int cellKnown[8], nCells = 0, nU = 0, nD = 0;
+        for (int q = 0; q < nPos; ++q) cellKnown[q] = cell[q] >= 0 ? nCells++ : -1;
+        for (F& f : faces) { if (f.dir) f.kn = nCells + nD++; else f.dof = nU++; }
+        const int nK = nCells + nD;
+        auto faceOf = [&](int pos, int a) -> int {
+            const int lo = pos & ~(1 << a);
+            for (int k = 0; k < nF; ++k) if (faces[k].a == a && faces[k].lo == lo) return k;
+            return -1;
+        };
+        // scv bases and inner normals
+        double nu[8][3][3] = {}, detX[8] = {};
+        for (int q = 0; q < nPos; ++q) {
+            if (cell[q] < 0) continue;
+            double xc[3]; P.center(cell[q], xc);
+            double e[3][3] = {};
+            for (int a = 0; a < dim; ++a) {
+                double ip[3];
+                for (int k = 0; k < 3; ++k) ip[k] = xc[k];
+                ip[a] = xv[a];                               // facet centre of the face toward v
+                for (int k = 0; k < 3; ++k) e[a][k] = ip[k] - xc[k];
+            }
+            if (dim == 2) {
+                const double cr = e[0][0] * e[1][1] - e[0][1] * e[1][0];
+                double n0[2] = {e[1][1], -e[1][0]}, n1[2] = {e[0][1], -e[0][0]};
+                if (std::signbit(cr)) { n0[0] = -n0[0]; n0[1] = -n0[1]; }
+                else { n1[0] = -n1[0]; n1[1] = -n1[1]; }
+                nu[q][0][0] = n0[0]; nu[q][0][1] = n0[1];
+                nu[q][1][0] = n1[0]; nu[q][1][1] = n1[1];
+                detX[q] = std::abs(cr);
+            } else {
+                auto crossP = [](const double* x, const double* y, double* o) {
+                    o[0] = x[1] * y[2] - x[2] * y[1]; o[1] = x[2] * y[0] - x[0] * y[2]; o[2] = x[0] * y[1] - x[1] * y[0];
+                };
+                double c12[3]; crossP(e[1], e[2], c12);
+                const double tp = e[0][0] * c12[0] + e[0][1] * c12[1] + e[0][2] * c12[2];
+                crossP(e[1], e[2], nu[q][0]); crossP(e[2], e[0], nu[q][1]); crossP(e[0], e[1], nu[q][2]);
+                if (std::signbit(tp)) for (auto& r : nu[q]) for (double& z : r) z = -z;
+                detX[q] = std::abs(tp);
+            }
+        }
+        auto omega = [&](int q, const F& f, double* w) {
+            const int64_t c = cell[q];
+            for (int a = 0; a < dim; ++a) {
+                double t = mpVtmv(P, c, f.n, nu[q][a]);
+                t *= f.area * P.extr(c);
+                t /= detX[q];
+                w[a] = t;
+            }
+        };
+        std::vector<double> A((size_t)nU * nU, 0.0), B((size_t)nU * nK, 0.0), C((size_t)nF * nU, 0.0),
+            D((size_t)nF * nK, 0.0);
+        for (int fi = 0; fi < nF; ++fi) {
+            const F& f = faces[fi];
+            double w[3];
+            omega(f.P, f, w);
+            for (int a = 0; a < dim; ++a) {
+                const F& o = faces[faceOf(f.P, a)];
+                if (!o.dir) { C[(size_t)fi * nU + o.dof] -= w[a]; if (!f.dir) A[(size_t)f.dof * nU + o.dof] -= w[a]; }
+                else { D[(size_t)fi * nK + o.kn] -= w[a]; if (!f.dir) B[(size_t)f.dof * nK + o.kn] += w[a]; }
+                D[(size_t)fi * nK + cellKnown[f.P]] += w[a];
+                if (!f.dir) B[(size_t)f.dof * nK + cellKnown[f.P]] -= w[a];
+            }
+            if (!f.bnd) {
+                double wq[3];
+                omega(f.Q, f, wq);
+                for (int a = 0; a < dim; ++a) {
+                    const F& o = faces[faceOf(f.Q, a)];
+                    if (!o.dir) A[(size_t)f.dof * nU + o.dof] += wq[a];
+                    else B[(size_t)f.dof * nK + o.kn] -= wq[a];
+                    B[(size_t)f.dof * nK + cellKnown[f.Q]] += wq[a];
+                }
+            }
+        }
+        std::vector<double> T = D, CA((size_t)nF * nU, 0.0);
+        if (nU > 0) {
+            gjInverse(A, nU);
+            for (int fi = 0; fi < nF; ++fi)
+                for (int j = 0; j < nU; ++j) { double s2 = 0.0; for (int k = 0; k < nU; ++k) s2 += C[(size_t)fi * nU + k] * A[(size_t)k * nU + j]; CA[(size_t)fi * nU + j] = s2; }
+            for (int fi = 0; fi < nF; ++fi)
+                for (int j = 0; j < nK; ++j) { double s2 = 0.0; for (int k = 0; k < nU; ++k) s2 += CA[(size_t)fi * nU + k] * B[(size_t)k * nK + j]; T[(size_t)fi * nK + j] += s2; }
+        }
+        std::vector<double> g(nF, 0.0);
+        if (grav) {
+            std::vector<double> dG(nU, 0.0);
+            for (int fi = 0; fi < nF; ++fi) {
+                const F& f = faces[fi];
+                const double aIn = P.extr(cell[f.P]) * mpVtmv(P, cell[f.P], f.n, P.g);
+                double r = rho;
+                if (!f.dir) {
+                    double d = 0.0; int nOut = 0;
+                    if (!f.bnd) { r += rho; d += P.extr(cell[f.Q]) * mpVtmv(P, cell[f.Q], f.n, P.g); nOut = 1; }
+                    r /= nOut + 1;
+                    d -= aIn;
+                    d *= r * f.area;
+                    dG[f.dof] = d;
+                }
+                g[fi] = aIn * r * f.area;
+            }
+            for (int fi = 0; fi < nF; ++fi) { double s2 = g[fi]; for (int k = 0; k < nU; ++k) s2 += CA[(size_t)fi * nU + k] * dG[k]; g[fi] = s2; }
+        }
+        // rows of the scvfs of P (as computed) and of Q (negated)
+        for (int fi = 0; fi < nF; ++fi) {
+            const F& f = faces[fi];
+            double c0 = 0.0;
+            for (const F& fd : faces) if (fd.dir) c0 += T[(size_t)fi * nK + fd.kn] * fd.uD;
+            c0 += g[fi];
+            for (int side = 0; side < 2; ++side) {
+                const int q = side == 0 ? f.P : f.Q;
+                if (q < 0) continue;
+                const int64_t I = cell[q];
+                const int fSide = ((q >> f.a) & 1) ? 0 : 1;          // the element face toward v
+                int corner = 0, bit = 0;
+                for (int k = 0; k < dim; ++k) if (k != f.a) corner |= (((q >> k) & 1) ? 0 : 1) << bit++;
+                MpScvfRow& row = rows[I][(2 * f.a + fSide) * corners + corner];
+                const Face fc = P.face(I, 2 * f.a + fSide);
+                if (fc.boundary && P.d.bc_type[fc.bidx] == 2) {
+                    double area = 1.0;
+                    int64_t id[3]; P.ijk(I, id);
+                    for (int k = 0; k < dim; ++k) if (k != f.a) area *= 0.5 * (P.hi(k, id[k]) - P.lo(k, id[k]));
+                    const double sA = area * P.extr(I);
+                    row.neumann = true;
+                    double qn = 0.0;
+                    qn += P.d.bc_values[fc.bidx] * sA;
+                    row.c0 = qn;
+                    continue;
+                }
+                row.terms.clear();
+                for (int qq = 0; qq < nPos; ++qq)
+                    if (cell[qq] >= 0) {
+                        const double t = T[(size_t)fi * nK + cellKnown[qq]];
+                        row.terms.push_back({cell[qq], side == 0 ? t : -t});
+                    }
+                row.c0 = side == 0 ? c0 : -c0;
+            }
+        }
+    }
+    return rows;
+}
+
+static Pattern mpfaPattern(const Problem& P)
+{
+    Pattern pt;
+    pt.rowPtr.assign(P.N + 1, 0);
+    pt.diag.assign(P.N, -1);
+    for (int64_t I = 0; I < P.N; ++I) {
+        int64_t id[3]; P.ijk(I, id);
+        for (int oz = (P.dim == 3 ? -1 : 0); oz <= (P.dim == 3 ? 1 : 0); ++oz)
+            for (int oy = -1; oy <= 1; ++oy)
+                for (int ox = -1; ox <= 1; ++ox) {
+                    const int64_t x = id[0] + ox, y = id[1] + oy, z = id[2] + oz;
+                    if (x < 0 || x >= P.n[0] || y < 0 || y >= P.n[1] || z < 0 || z >= P.n[2]) continue;
+                    const int64_t J = x + P.n[0] * (y + P.n[1] * z);
+                    if (J == I) pt.diag[I] = (int64_t)pt.col.size();
+                    pt.col.push_back((int32_t)J);
+                }
+        pt.rowPtr[I + 1] = (int64_t)pt.col.size();
+    }
+    return pt;
+}
+
+static double mpScvfFlux(const MpScvfRow& row, const double* u, int64_t pert, double q, double mob)
+{
+    if (row.neumann) return row.c0;
+    double t = 0.0;
+    for (const MpIvTerm& k : row.terms) t += k.t * (k.cell == pert ? q : u[k.cell]);
+    t += row.c0;
+    return t * mob;
+}
+
+// Residual and numeric-difference Jacobian of the MPFA-O 1p model (column-wise as the
+// reference's local assembler: element I perturbs its unknown and differentiates its own
+// residual and the fluxes of its neighbours' scvfs that depend on it)
+static void mpfaAssemble(const Problem& P, const Pattern& pt, const double* u, double dt, double* values, double* r)
+{
+    const auto rows = mpfaRows(P);
+    const double mob = P.d.density[0] * (1.0 / P.d.viscosity[0]);
+    const int method = P.d.numeric_difference_method;
+    auto residual = [&](int64_t I, int64_t pert, double q) {
+        double res = 0.0;
+        {
+            double src = 0.0;
+            if (P.d.source) src += P.d.source[I];
+            src *= P.volume(I) * P.extr(I);
+            res -= src;
+        }
+        for (const MpScvfRow& row : rows[I]) res += mpScvfFlux(row, u, pert, q, mob);
+        if (dt > 0.0) res += 0.0;      // incompressible 1p: the storage does not change
+        return res;
+    };
+    auto dependsOn = [&](const MpScvfRow& row, int64_t I) {
+        if (row.neumann) return false;
+        for (const MpIvTerm& k : row.terms) if (k.cell == I) return true;
+        return false;
+    };
+    auto neighbourFlux = [&](int64_t J, int64_t I, double q) {
+        double s = 0.0;
+        for (const MpScvfRow& row : rows[J]) if (dependsOn(row, I)) s += mpScvfFlux(row, u, I, q, mob);
+        return s;
+    };
+    auto find = [&](int64_t row, int64_t c) -> int64_t {
+        for (int64_t k = pt.rowPtr[row]; k < pt.rowPtr[row + 1]; ++k) if (pt.col[k] == c) return k;
+        return -1;
+    };
+    if (values) std::fill(values, values + pt.rowPtr[P.N], 0.0);
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t I = 0; I < P.N; ++I) {
+        r[I] = residual(I, -1, 0.0);
+        if (!values) continue;
+        const double x = u[I];
+        const double eps = numericEpsilon(P, x, 0);
+        // column I: rows J of the neighbourhood (J == I: whole residual)
+        for (int64_t k = pt.rowPtr[I]; k < pt.rowPtr[I + 1]; ++k) {
+            const int64_t J = pt.col[k];
+            auto f = [&](double q) { return J == I ? residual(I, I, q) : neighbourFlux(J, I, q); };
+            const double f0 = J == I ? r[I] : neighbourFlux(J, I, x);
+            double d;
+            if (method == 1) d = (f(x + eps) - f0) / eps;
+            else if (method == -1) d = (f0 - f(x - eps)) / eps;
+            else if (method == 0) d = (f(x + eps) - f(x - eps)) / (eps + eps);
+            else {
+                const double fp = f(x + eps), fm = f(x - eps), fm2 = f(x - 2.0 * eps), fp2 = f(x + 2.0 * eps);
+                d = fp; d -= fm; d *= 8.0; d += fm2; d -= fp2; d /= 12.0 * eps;
+            }
+            values[find(J, I)] = d;
+        }
+    }
 }
 
 // CCLocalAssembler<numeric, implicit>::assembleJacobianAndResidualImpl for element I
@@ -842,6 +1192,10 @@ static void assembleElementAnalytic(const Problem& P, const Pattern& pt, int64_t
 static void assemble(const Problem& P, const Pattern& pt, const double* u, const double* uprev, double dt,
                      double* values, double* r, const uint8_t* colors = nullptr)
 {
+    if (P.d.discretization == 1) {
+        mpfaAssemble(P, pt, u, dt, values, r);
+        return;
+    }
     const int b = P.b, bb = b * b, nf = 2 * P.dim;
     if (values && colors && P.d.diff_method != 1) {
         // reset the columns of the non-green elements only
@@ -1383,8 +1737,10 @@ int orc_num_blocks(const dxg_problem_desc* d, int64_t* nnzb)
     try {
         Problem P(*d);
         int64_t cnt = P.N;
-        for (int64_t I = 0; I < P.N; ++I)
-            for (int f = 0; f < 2 * P.dim; ++f) if (!P.face(I, f).boundary) ++cnt;
+        if (P.d.discretization == 1) cnt = buildPattern(P).rowPtr[P.N];
+        else
+            for (int64_t I = 0; I < P.N; ++I)
+                for (int f = 0; f < 2 * P.dim; ++f) if (!P.face(I, f).boundary) ++cnt;
         *nnzb = cnt;
         return 0;
     } catch (...) { return DXG_ERR_ARG; }

@@ -148,3 +148,31 @@ def test_time_step_retries_follow_the_single_problem_path():
     if state == "finished":
         assert info["newton_iterations"] == iters
         _check_same(batch.solution(pid), ua, "retried step")
+
+
+def test_line_search_and_residual_criterion_in_a_batch_equal_alone():
+    """Newton.UseLineSearch and Newton.EnableResidualCriterion members batched beside a
+    plain member of the same kind: each follows its single-problem path bit for bit."""
+    plain = newton_params(linear_max_iter=500)
+    search = newton_params(linear_max_iter=500, use_line_search=1)
+    resid = newton_params(linear_max_iter=500, enable_residual_criterion=1, residual_reduction=1e-6)
+    cases = [((8, 6, 5), 21, plain), ((10, 7, 6), 22, search), ((9, 8, 5), 23, resid), ((7, 9, 6), 24, search)]
+    batch = Batch(precision="fp64")
+    ids = []
+    for cells, seed, params in cases:
+        desc, u0 = _two_phase(cells, seed, sigma=1.5, inflow=0.08)
+        ids.append((batch.add(desc, u0, dt=500.0, t_end=1500.0, params=params), desc, u0, params))
+    batch.run()
+    for pid, desc, u0, params in ids:
+        info = batch.info(pid)
+        ua, iters, state = run_alone(desc, u0, 500.0, 1500.0, params, "fp64")
+        assert info["state"] == state == "finished"
+        assert info["newton_iterations"] == iters
+        _check_same(batch.solution(pid), ua, f"problem {desc.cells}")
+
+
+def test_partial_reassembly_is_refused_by_a_batch():
+    desc, u0 = _two_phase((6, 5, 4), 25)
+    batch = Batch(precision="fp64")
+    with pytest.raises(Exception):
+        batch.add(desc, u0, dt=250.0, t_end=250.0, params=newton_params(enable_partial_reassembly=1))

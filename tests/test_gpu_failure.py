@@ -43,3 +43,29 @@ def test_failing_problem_is_isolated_in_a_batch():
         ctx.newton_solve(250.0, good)
         ctx.advance_time_step()
     assert np.array_equal(batch.solution(p_ok), ctx.solution())
+
+
+def test_lane_sweep_wait_limit_expires_and_the_context_recovers():
+    """A wait limit far below the hand-off latency of the lane sweeps (plane 31 of a 32-plane
+    grid receives its first value after 31 plane steps): the sweeps give up and the solve
+    reports DXG_ERR_TIMEOUT; with the limit restored, the same context solves to the same
+    bits as before (the hand-off buffer is reset after a timeout)."""
+    desc, u0 = problems.dnapl_2p(cells=(16, 16, 32), seed=8)
+    u = u0.reshape(-1, 2).copy()
+    u[:, 1] = np.random.default_rng(5).uniform(0.0, 0.4, len(u))
+    ctx = Context(desc)
+    ctx.set_ilu_kernel("lanes")
+    ctx.set_solution(u.reshape(-1))
+    ctx.set_prev_solution(u0)
+    ctx.set_time_step(250.0)
+    ctx.assemble_jacobian_and_residual()
+    first = ctx.linear_solve(1e-10, 500)          # factorises with the default limit
+    assert first["converged"]
+    x0 = ctx.update()
+    ctx.set_wait_limit(1e-6)
+    with pytest.raises(Exception, match="timed out"):
+        ctx.linear_solve(1e-10, 500)
+    ctx.set_wait_limit(0.5)
+    again = ctx.linear_solve(1e-10, 500)
+    assert again["converged"] and again["iterations"] == first["iterations"]
+    assert np.array_equal(ctx.update(), x0)

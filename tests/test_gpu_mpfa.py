@@ -1,0 +1,94 @@
+"""MPFA-O on the device against the oracle and the reference's MPFA tests.
+
+The host tabulation (interaction-volume systems) and the oracle follow the same operation
+order, and the device evaluates the scvf fluxes and the numeric-difference Jacobian in the
+oracle's order without FMA contraction: residual and Jacobian are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from dumux_gb300 import Context, newton_params, problems
+from test_oracle_mpfa import _load
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    rng = np.random.default_rng(7)
+    out = []
+    d, u = problems.onep_lens_problem(numeric_epsilon=True, discretization="mpfa")
+    out.append(("lens-2d-gravity", d, 1e5 + rng.uniform(-1e3, 1e3, d.num_cells)))
+    d, u, _ = problems.mpfa_convergence_problem(12)
+    out.append(("tensor-2d-source", d, 10.0 + rng.uniform(-1, 1, d.num_cells)))
+    d, u, _ = problems.mpfa_linear_field_problem(cells=(5, 4, 3), K=((2.0, 0.3, 0.1), (0.3, 1.0, 0.2),
+                                                                     (0.1, 0.2, 1.5)), gravity=True, spacing_seed=5)
+    d.bc_type[:12] = 2
+    d.bc_values[:12] = rng.uniform(-1e-3, 1e-3, 12)
+    d.source = rng.uniform(-1e-2, 1e-2, d.num_cells)
+    d.extrusion = rng.uniform(0.5, 2.0, d.num_cells)
+    out.append(("tensor-3d-gravity-neumann", d, 1e5 + rng.uniform(-1e3, 1e3, d.num_cells)))
+    return out
+
+
+@pytest.mark.parametrize("name,desc,u", _cases(), ids=lambda v: v if isinstance(v, str) else "")
+@pytest.mark.parametrize("method", [1, 0, -1, 5])
+def test_mpfa_residual_and_jacobian_equal_the_oracle(name, desc, u, method):
+    desc.numeric_difference_method = method
+    ctx = Context(desc)
+    ctx.set_solution(u)
+    ctx.assemble_jacobian_and_residual()
+    row_ptr, col, vals = ctx.jacobian()
+    orow, ocol, ovals, r_orc = oracle.assemble(desc, u)
+    assert np.array_equal(row_ptr, orow) and np.array_equal(col, ocol)
+    assert np.array_equal(ctx.residual(), r_orc)
+    assert np.array_equal(vals, ovals)
+
+
+def test_mpfa_lens_on_the_device_matches_reference_vtu():
+    ref = _load("onep_lens_p.txt")
+    desc, u0 = problems.onep_lens_problem(numeric_epsilon=True, discretization="mpfa")
+    ctx = Context(desc)
+    ctx.set_solution(u0)
+    ctx.assemble_jacobian_and_residual()
+    res = ctx.linear_solve(1e-13, 500)
+    assert res["converged"]
+    p = u0 - ctx.update()
+    assert np.max(np.abs(p - ref)) <= 0.5 + 1e-9
+    orow, ocol, ovals, r = oracle.assemble(desc, u0)
+    st, dx, ores = oracle.linear_solve(orow, ocol, ovals, r, 1, reduction=1e-13, max_iter=500)
+    assert np.max(np.abs(p - (u0 - dx))) <= 1e-9 * np.max(np.abs(p))
+
+
+def test_mpfa_convergence_rate_on_the_device():
+    p = newton_params(min_steps=1, max_steps=1, max_relative_shift=1e300, linear_reduction=1e-12,
+                      max_time_step_divisions=0, linear_max_iter=2000)
+    errs = []
+    for cells in (10, 20, 40, 80):
+        desc, u0, exact = problems.mpfa_convergence_problem(cells)
+        ctx = Context(desc)
+        ctx.set_solution(u0)
+        ctx.set_prev_solution(u0)
+        rep = ctx.newton_solve(0.0, p)
+        u = ctx.solution()
+        st, uo, _ = oracle.newton_solve(desc, u0, u0, 0.0, p)
+        assert st == 0 and np.max(np.abs(u - uo)) <= 1e-9 * np.max(np.abs(uo))
+        h = 1.0 / cells
+        errs.append(np.sqrt(np.sum(h * h * (u - exact) ** 2)))
+    rates = [np.log2(errs[i] / errs[i + 1]) for i in range(3)]
+    assert np.mean(rates) >= 1.8, rates
+
+
+def test_mpfa_newton_3d_linear_field_and_oracle_iterations():
+    desc, u0, exact = problems.mpfa_linear_field_problem(cells=(9, 7, 6), K=((2.0, 0.3, 0.1), (0.3, 1.0, 0.2),
+                                                                             (0.1, 0.2, 1.5)), spacing_seed=2)
+    p = newton_params(max_relative_shift=1e-12, linear_reduction=1e-13, linear_max_iter=2000, max_steps=30)
+    ctx = Context(desc)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    rep = ctx.newton_solve(0.0, p)
+    assert rep["converged"]
+    assert np.max(np.abs(ctx.solution() - exact)) <= 1e-9 * np.max(np.abs(exact))
+    st, uo, orep = oracle.newton_solve(desc, u0, u0, 0.0, p)
+    assert st == 0 and orep["iterations"] == rep["iterations"]
+    assert "MPFA-O" in ctx.describe()
