@@ -1196,8 +1196,12 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
         if constexpr (!mixed) {
             if (c->mpfa) {
                 TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep);
+                if (c->iluKernel == DXG_ILU_LEVELS) {
+                    launchStencilApplyLevels(sa, in, yOut, st);
+                    return 1;
+                }
                 launchStencilApply(sa, in, yOut, st);
-                return 1;
+                return stencilWave2dFits(sa) ? 2 : 1;
             }
         }
         if (amg) {
@@ -1851,9 +1855,15 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
     if (!c || !buf || len <= 0) return DXG_ERR_ARG;
     std::string out;
     if (!c->uploaded) out = "no problem uploaded";
-    else if (c->mpfa)
-        out = std::string("MPFA-O, ") + std::to_string(c->mpLayout.S) +
-              "-point stencil; ILU(0): natural order, hyperplanes x+2y+4z in one CTA";
+    else if (c->mpfa) {
+        StencilArgs sa{};
+        sa.S = c->mpLayout.S;
+        sa.ny = c->pcHost.ny;
+        const bool lines = c->iluKernel != DXG_ILU_LEVELS && stencilWave2dFits(sa);
+        out = std::string("MPFA-O, ") + std::to_string(c->mpLayout.S) + "-point stencil; ILU(0): natural order, " +
+              (lines ? "line sweeps (one thread per grid line, levels x+2y) in one CTA"
+                     : "hyperplanes x+2y+4z level by level in one CTA");
+    }
     else if (c->linearSolver == DXG_LINEAR_SOLVER_AMG_BICGSTAB)
         out = "AMG-BiCGSTAB: " + std::to_string(amgLevelDims(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
                                                                (int)c->pcHost.nz).size() + 1) +

@@ -1211,7 +1211,7 @@ __global__ void __launch_bounds__(1024) stencilFactorKernel(StencilArgs a)
                 for (int k = t0; k < a.nTri && a.tri[k][0] == s; ++k) {
                     const int t = a.tri[k][1], u = a.tri[k][2];
                     if (!((m >> t) & 1u) || !((mj >> u) & 1u)) continue;
-                    a.LU[(int64_t)t * a.N + i] -= l * a.LU[(int64_t)u * a.N + j];
+                    a.LU[(int64_t)t * a.N + i] = fma(-l, a.LU[(int64_t)u * a.N + j], a.LU[(int64_t)t * a.N + i]);
                 }
             }
             const double piv = a.LU[(int64_t)a.center * a.N + i];
@@ -1234,7 +1234,7 @@ __global__ void __launch_bounds__(1024) stencilApplyKernel(StencilArgs a, const 
             const uint32_t m = a.mask[i];
             double rhs = d[i];
             for (int s = 0; s < a.center; ++s)
-                if ((m >> s) & 1u) rhs -= a.LU[(int64_t)s * a.N + i] * v[i + a.off[s]];
+                if ((m >> s) & 1u) rhs = fma(-a.LU[(int64_t)s * a.N + i], v[i + a.off[s]], rhs);
             v[i] = rhs;
         });
         __syncthreads();
@@ -1244,12 +1244,126 @@ __global__ void __launch_bounds__(1024) stencilApplyKernel(StencilArgs a, const 
             const uint32_t m = a.mask[i];
             double rhs = v[i];
             for (int s = a.center + 1; s < a.S; ++s)
-                if ((m >> s) & 1u) rhs -= a.LU[(int64_t)s * a.N + i] * v[i + a.off[s]];
+                if ((m >> s) & 1u) rhs = fma(-a.LU[(int64_t)s * a.N + i], v[i + a.off[s]], rhs);
             v[i] = a.Dinv[i] * rhs;
         });
         __syncthreads();
     }
 }
+
+// The sweeps of a 2D 9-point stencil with one thread per grid line y (levels L = x + 2y):
+// line y needs, besides its own previous cell, line y-1's cells x+1, x, x-1, which that line
+// computed at levels L-1, L-2, L-3 (backward: line y+1's cells x-1, x, x+1 at L+1, L+2,
+// L+3).  Every thread keeps its last three results; a warp passes them on by shuffle, the
+// boundary lane of each warp through a double-buffered shared-memory slot, and one CTA
+// barrier ends each level.  The cells' factor entries, right-hand side (and pivot) are
+// copied PF levels ahead into a shared-memory ring with cp.async.  The arithmetic is that
+// of stencilApplyKernel (same operand order, explicit FMAs), so both give the same bits.
+__device__ __forceinline__ void stCpAsync8(uint32_t dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void stCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void stCpWait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <int DIR, int PF>
+__global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const double* __restrict__ d,
+                                                             double* __restrict__ v)
+{
+    // record per cell: forward L0..L3 (slots 0..3), d; backward U5..U8 (slots 5..8), Dinv, v
+    constexpr int REC = DIR > 0 ? 5 : 6;
+    extern __shared__ __align__(16) double stRing[];   // [PF][blockDim][REC]
+    __shared__ double hist[32][2][3];                  // per warp, level parity: boundary lane's r1..r3
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    const int nx = a.nx, ny = a.ny;
+    const int y = threadIdx.x;
+    const bool lineOk = y < ny;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int Lmax = (nx - 1) + 2 * (ny - 1);
+    const int64_t N = a.N;
+    const int64_t rowBase = (int64_t)y * nx;
+    const uint32_t ringBase = (uint32_t)__cvta_generic_to_shared(stRing + (size_t)threadIdx.x * REC);
+    const uint32_t slotBytes = blockDim.x * REC * 8u;
+    // sweep step s: level L = s (forward) or Lmax - s (backward)
+    auto cellX = [&](int s) -> int {
+        const int L = DIR > 0 ? s : Lmax - s;
+        const int x = L - 2 * y;
+        return (lineOk && s <= Lmax && x >= 0 && x < nx) ? x : -1;
+    };
+    auto issue = [&](int s) {
+        const int x = cellX(s);
+        if (x >= 0) {
+            const int64_t i = rowBase + x;
+            const uint32_t rec = ringBase + (uint32_t)(s % PF) * slotBytes;
+            if (DIR > 0) {
+                for (int k = 0; k < 4; ++k) stCpAsync8(rec + 8u * k, a.LU + (int64_t)k * N + i);
+                stCpAsync8(rec + 32u, d + i);
+            } else {
+                for (int k = 0; k < 4; ++k) stCpAsync8(rec + 8u * k, a.LU + (int64_t)(5 + k) * N + i);
+                stCpAsync8(rec + 32u, a.Dinv + i);
+                stCpAsync8(rec + 40u, v + i);
+            }
+        }
+        stCommit();
+    };
+#pragma unroll
+    for (int s = 0; s < PF; ++s) issue(s);
+    double r1 = 0.0, r2 = 0.0, r3 = 0.0;
+    for (int s = 0; s <= Lmax; ++s) {
+        // the neighbour line's last three results (after its previous level)
+        double n1 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r1, 1) : __shfl_down_sync(0xffffffffu, r1, 1);
+        double n2 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r2, 1) : __shfl_down_sync(0xffffffffu, r2, 1);
+        double n3 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r3, 1) : __shfl_down_sync(0xffffffffu, r3, 1);
+        const int par = (s - 1) & 1;
+        if (DIR > 0 && lane == 0 && warp > 0 && s > 0) {
+            n1 = hist[warp - 1][par][0];
+            n2 = hist[warp - 1][par][1];
+            n3 = hist[warp - 1][par][2];
+        } else if (DIR < 0 && lane == 31 && s > 0 && (warp + 1) * 32 < (int)blockDim.x) {
+            n1 = hist[warp + 1][par][0];
+            n2 = hist[warp + 1][par][1];
+            n3 = hist[warp + 1][par][2];
+        }
+        stCpWait<PF - 1>();
+        const int x = cellX(s);
+        double res = 0.0;
+        if (x >= 0) {
+            const double* rec = stRing + ((size_t)(s % PF) * blockDim.x + threadIdx.x) * REC;
+            const int64_t i = rowBase + x;
+            if (DIR > 0) {
+                double rhs = rec[4];
+                if (x > 0 && y > 0) rhs = fma(-rec[0], n3, rhs);        // (x-1, y-1)
+                if (y > 0) rhs = fma(-rec[1], n2, rhs);                 // (x,   y-1)
+                if (x < nx - 1 && y > 0) rhs = fma(-rec[2], n1, rhs);   // (x+1, y-1)
+                if (x > 0) rhs = fma(-rec[3], r1, rhs);                 // (x-1, y)
+                res = rhs;
+            } else {
+                double rhs = rec[5];
+                if (x < nx - 1) rhs = fma(-rec[0], r1, rhs);             // (x+1, y)
+                if (x > 0 && y < ny - 1) rhs = fma(-rec[1], n1, rhs);   // (x-1, y+1)
+                if (y < ny - 1) rhs = fma(-rec[2], n2, rhs);            // (x,   y+1)
+                if (x < nx - 1 && y < ny - 1) rhs = fma(-rec[3], n3, rhs);   // (x+1, y+1)
+                res = rec[4] * rhs;
+            }
+            v[i] = res;
+        }
+        r3 = r2;
+        r2 = r1;
+        r1 = res;
+        if ((DIR > 0 && lane == 31) || (DIR < 0 && lane == 0)) {
+            hist[warp][s & 1][0] = r1;
+            hist[warp][s & 1][1] = r2;
+            hist[warp][s & 1][2] = r3;
+        }
+        issue(s + PF);
+        __syncthreads();
+    }
+    stCpWait<0>();
+}
+
+// dynamic shared memory of the 2D sweeps at prefetch depth pf
+static size_t wave2dSmem(unsigned threads, int pf) { return (size_t)pf * threads * 6 * sizeof(double); }
 
 void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st)
 {
@@ -1279,7 +1393,42 @@ void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
     DXG_CUDA(cudaGetLastError());
 }
 
+bool stencilWave2dFits(const StencilArgs& a) { return a.S == 9 && a.ny >= 1 && a.ny <= 1024; }
+
 void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
+{
+    if (!stencilWave2dFits(a)) {
+        stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
+        DXG_CUDA(cudaGetLastError());
+        return;
+    }
+    const unsigned threads = (unsigned)((a.ny + 31) / 32 * 32);
+    const int pf = threads <= 512 ? 8 : 4;
+    const size_t smem = wave2dSmem(threads, pf);
+    // the opt-in shared-memory size, once per device
+    static bool attrSet[64] = {};
+    int dev = 0;
+    DXG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error(DXG_ERR_ARG, "device index out of range");
+    if (!attrSet[dev]) {
+        const int maxSmem = (int)wave2dSmem(512, 8);
+        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<-1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<-1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
+        attrSet[dev] = true;
+    }
+    if (pf == 8) {
+        stencilWave2dKernel<1, 8><<<1, threads, smem, st>>>(a, d, v);
+        stencilWave2dKernel<-1, 8><<<1, threads, smem, st>>>(a, d, v);
+    } else {
+        stencilWave2dKernel<1, 4><<<1, threads, smem, st>>>(a, d, v);
+        stencilWave2dKernel<-1, 4><<<1, threads, smem, st>>>(a, d, v);
+    }
+    DXG_CUDA(cudaGetLastError());
+}
+
+void launchStencilApplyLevels(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
 {
     stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
     DXG_CUDA(cudaGetLastError());

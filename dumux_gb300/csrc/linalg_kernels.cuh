@@ -141,7 +141,11 @@ struct StencilArgs {
 };
 void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st);
 void launchStencilFactor(const StencilArgs& a, cudaStream_t st);
+// the preconditioner apply: 2D 9-point stencils with ny <= 1024 on the line sweeps
+// (stencilWave2dKernel), otherwise the level-by-level kernel; the level kernel alone too
 void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+void launchStencilApplyLevels(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+bool stencilWave2dFits(const StencilArgs& a);
 
 template <class MT, class VT, class XT = VT>
 void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);

@@ -140,26 +140,17 @@ __device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity)
 }
 
 template <int B, class T>
-__device__ __forceinline__ void mvSub(const T* blk, const T* x, T* acc)
-{
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-        T s = 0;
-#pragma unroll
-        for (int c = 0; c < B; ++c) s += blk[r * B + c] * x[c];
-        acc[r] -= s;
-    }
-}
-template <int B, class T>
 __device__ __forceinline__ void mmul(const T* X, const T* Y, T* Z)
 {
+    // explicit fused multiply-adds: every instantiation of the kernels (launch shapes,
+    // single and batched) rounds the same way, whatever contraction the compiler chooses
 #pragma unroll
     for (int r = 0; r < B; ++r)
 #pragma unroll
         for (int c = 0; c < B; ++c) {
             T s = 0;
 #pragma unroll
-            for (int k = 0; k < B; ++k) s += X[r * B + k] * Y[k * B + c];
+            for (int k = 0; k < B; ++k) s = fma(X[r * B + k], Y[k * B + c], s);
             Z[r * B + c] = s;
         }
 }
@@ -170,7 +161,8 @@ __device__ __forceinline__ bool minv(const T* A, T* inv)
         inv[0] = (T)1 / A[0];
         return A[0] != (T)0;
     } else {
-        const T det = A[0] * A[3] - A[1] * A[2];
+        const T p12 = A[1] * A[2];
+        const T det = fma(A[0], A[3], -p12);
         if (det == (T)0) return false;
         const T detInv = (T)1 / det;
         inv[0] = A[3] * detInv;

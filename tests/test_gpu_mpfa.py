@@ -92,3 +92,24 @@ def test_mpfa_newton_3d_linear_field_and_oracle_iterations():
     st, uo, orep = oracle.newton_solve(desc, u0, u0, 0.0, p)
     assert st == 0 and orep["iterations"] == rep["iterations"]
     assert "MPFA-O" in ctx.describe()
+
+
+@pytest.mark.parametrize("cells", [(40, 40), (37, 70), (20, 9), (200, 300)])
+def test_mpfa_line_sweeps_equal_level_kernel(cells):
+    """The 2D line sweeps (one thread per grid line, warp shuffles, several warps) and the
+    level-by-level kernel compute the same preconditioner bit for bit."""
+    desc, u0, _ = problems.mpfa_convergence_problem(cells[0])
+    if cells[0] != cells[1]:
+        desc, u0, _ = problems.mpfa_linear_field_problem(cells=cells, spacing_seed=1)
+    out = {}
+    for kind in ("auto", "levels"):
+        ctx = Context(desc)
+        ctx.set_ilu_kernel(kind)
+        ctx.set_solution(u0)
+        ctx.assemble_jacobian_and_residual()
+        res = ctx.linear_solve(1e-12, 2000)
+        assert res["converged"]
+        out[kind] = (res["iterations"], ctx.update(), ctx.describe())
+    assert "line sweeps" in out["auto"][2] and "level by level" in out["levels"][2]
+    assert out["auto"][0] == out["levels"][0]
+    assert np.array_equal(out["auto"][1], out["levels"][1])
