@@ -29,6 +29,7 @@ UNITS = {
     "batch.cu": [],
     "amg.cu": [],
     "mpfa.cu": ["--fmad=false"],
+    "stencilwave.cu": [],
 }
 
 

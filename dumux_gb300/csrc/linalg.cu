@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT
         for (int e = 0; e < B; ++e) sum[e] = 0;
         // straight-line code: every slot's block (always allocated) and x entry (the
         // cell's own for a missing neighbour) is loaded without a branch, so all loads of
-        // the row are in flight together; a missing neighbour's block enters as zero
+        // the row are in flight together; a missing neighbour's block is stored as zeros
+        // (the assembly and dxg_set_linear_system write them), so it adds 0 * x_i
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             const bool valid = slotValid(m, DIM, s);
@@ -232,9 +233,7 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT
             ldgVec<B>(a.x + (i + (valid ? a.off[s] : 0)) * B, xs);
             AT xj[B];
 #pragma unroll
-            for (int e = 0; e < B; ++e) xj[e] = valid ? (AT)xs[e] : (AT)0;
-#pragma unroll
-            for (int e = 0; e < BB; ++e) blk[e] = valid ? blk[e] : (MT)0;
+            for (int e = 0; e < B; ++e) xj[e] = (AT)xs[e];
             blkMv<B>(blk, xj, sum);
         }
         VT acc[B];
@@ -1242,8 +1241,9 @@ __global__ void __launch_bounds__(1024) stencilApplyKernel(StencilArgs a, const 
     for (int L = levels - 1; L >= 0; --L) {
         forLevelRows(a, L, [&](int64_t i) {
             const uint32_t m = a.mask[i];
+            // descending column order: the entries of the latest levels come last
             double rhs = v[i];
-            for (int s = a.center + 1; s < a.S; ++s)
+            for (int s = a.S - 1; s > a.center; --s)
                 if ((m >> s) & 1u) rhs = fma(-a.LU[(int64_t)s * a.N + i], v[i + a.off[s]], rhs);
             v[i] = a.Dinv[i] * rhs;
         });
@@ -1311,10 +1311,11 @@ __global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const
     for (int s = 0; s < PF; ++s) issue(s);
     double r1 = 0.0, r2 = 0.0, r3 = 0.0;
     for (int s = 0; s <= Lmax; ++s) {
-        // the neighbour line's last three results (after its previous level)
-        double n1 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r1, 1) : __shfl_down_sync(0xffffffffu, r1, 1);
-        double n2 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r2, 1) : __shfl_down_sync(0xffffffffu, r2, 1);
+        // the neighbour line's results of two and three levels back first, then the last
+        // level's (see stencilLane2dKernel): the same operand order as stencilApplyKernel
         double n3 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r3, 1) : __shfl_down_sync(0xffffffffu, r3, 1);
+        double n2 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r2, 1) : __shfl_down_sync(0xffffffffu, r2, 1);
+        double n1 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r1, 1) : __shfl_down_sync(0xffffffffu, r1, 1);
         const int par = (s - 1) & 1;
         if (DIR > 0 && lane == 0 && warp > 0 && s > 0) {
             n1 = hist[warp - 1][par][0];
@@ -1332,19 +1333,19 @@ __global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const
             const double* rec = stRing + ((size_t)(s % PF) * blockDim.x + threadIdx.x) * REC;
             const int64_t i = rowBase + x;
             if (DIR > 0) {
-                double rhs = rec[4];
-                if (x > 0 && y > 0) rhs = fma(-rec[0], n3, rhs);        // (x-1, y-1)
-                if (y > 0) rhs = fma(-rec[1], n2, rhs);                 // (x,   y-1)
-                if (x < nx - 1 && y > 0) rhs = fma(-rec[2], n1, rhs);   // (x+1, y-1)
-                if (x > 0) rhs = fma(-rec[3], r1, rhs);                 // (x-1, y)
-                res = rhs;
+                double acc = rec[4];
+                if (x > 0 && y > 0) acc = fma(-rec[0], n3, acc);        // (x-1, y-1)
+                if (y > 0) acc = fma(-rec[1], n2, acc);                 // (x,   y-1)
+                if (x < nx - 1 && y > 0) acc = fma(-rec[2], n1, acc);   // (x+1, y-1)
+                if (x > 0) acc = fma(-rec[3], r1, acc);                 // (x-1, y)
+                res = acc;
             } else {
-                double rhs = rec[5];
-                if (x < nx - 1) rhs = fma(-rec[0], r1, rhs);             // (x+1, y)
-                if (x > 0 && y < ny - 1) rhs = fma(-rec[1], n1, rhs);   // (x-1, y+1)
-                if (y < ny - 1) rhs = fma(-rec[2], n2, rhs);            // (x,   y+1)
-                if (x < nx - 1 && y < ny - 1) rhs = fma(-rec[3], n3, rhs);   // (x+1, y+1)
-                res = rec[4] * rhs;
+                double acc = rec[5];
+                if (x < nx - 1 && y < ny - 1) acc = fma(-rec[3], n3, acc);   // (x+1, y+1)
+                if (y < ny - 1) acc = fma(-rec[2], n2, acc);                 // (x,   y+1)
+                if (x > 0 && y < ny - 1) acc = fma(-rec[1], n1, acc);        // (x-1, y+1)
+                if (x < nx - 1) acc = fma(-rec[0], r1, acc);                  // (x+1, y)
+                res = rec[4] * acc;
             }
             v[i] = res;
         }
@@ -1395,13 +1396,8 @@ void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
 
 bool stencilWave2dFits(const StencilArgs& a) { return a.S == 9 && a.ny >= 1 && a.ny <= 1024; }
 
-void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
+void launchStencilWave2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
 {
-    if (!stencilWave2dFits(a)) {
-        stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
-        DXG_CUDA(cudaGetLastError());
-        return;
-    }
     const unsigned threads = (unsigned)((a.ny + 31) / 32 * 32);
     const int pf = threads <= 512 ? 8 : 4;
     const size_t smem = wave2dSmem(threads, pf);

@@ -138,14 +138,20 @@ struct StencilArgs {
     ReduceScratch scratch{};
     int nTri = 0;
     int8_t tri[104][3] = {};
+    int* err = nullptr;                    // DXG_ERR_TIMEOUT of a sweep that gave up waiting
+    unsigned long long waitNs = 0;         // wait limit of the cluster sweeps (0: 0.5 s)
 };
 void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st);
 void launchStencilFactor(const StencilArgs& a, cudaStream_t st);
-// the preconditioner apply: 2D 9-point stencils with ny <= 1024 on the line sweeps
-// (stencilWave2dKernel), otherwise the level-by-level kernel; the level kernel alone too
-void launchStencilApply(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+// the preconditioner apply: the level-by-level kernel (any stencil), the one-CTA line sweeps
+// of 2D stencils with ny <= 1024 (stencilWave2dKernel)
 void launchStencilApplyLevels(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+void launchStencilWave2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
 bool stencilWave2dFits(const StencilArgs& a);
+// 2D 9-point sweeps over a cluster (stencilwave.cu): lines spread over up to 16 CTAs of four
+// warps, point-to-point hand-offs through shared-memory histories
+bool stencilLane2dFits(const StencilArgs& a);
+void launchStencilLane2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
 
 template <class MT, class VT, class XT = VT>
 void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);

@@ -94,22 +94,46 @@ def test_mpfa_newton_3d_linear_field_and_oracle_iterations():
     assert "MPFA-O" in ctx.describe()
 
 
-@pytest.mark.parametrize("cells", [(40, 40), (37, 70), (20, 9), (200, 300)])
+@pytest.mark.parametrize("cells", [(40, 40), (37, 70), (20, 9), (200, 300), (30, 600), (12, 1100)])
 def test_mpfa_line_sweeps_equal_level_kernel(cells):
-    """The 2D line sweeps (one thread per grid line, warp shuffles, several warps) and the
+    """The 2D line sweeps, in one CTA (warp shuffles and a barrier per level) and over a
+    cluster (four warps per CTA, up to nine CTAs here, point-to-point hand-offs), and the
     level-by-level kernel compute the same preconditioner bit for bit."""
     desc, u0, _ = problems.mpfa_convergence_problem(cells[0])
     if cells[0] != cells[1]:
         desc, u0, _ = problems.mpfa_linear_field_problem(cells=cells, spacing_seed=1)
     out = {}
-    for kind in ("auto", "levels"):
+    for kind in ("lanes", "wavefront", "levels"):
         ctx = Context(desc)
         ctx.set_ilu_kernel(kind)
         ctx.set_solution(u0)
         ctx.assemble_jacobian_and_residual()
-        res = ctx.linear_solve(1e-12, 2000)
+        res = ctx.linear_solve(1e-12, 3000)
         assert res["converged"]
         out[kind] = (res["iterations"], ctx.update(), ctx.describe())
-    assert "line sweeps" in out["auto"][2] and "level by level" in out["levels"][2]
-    assert out["auto"][0] == out["levels"][0]
-    assert np.array_equal(out["auto"][1], out["levels"][1])
+    assert "over a cluster" in out["lanes"][2] and "level by level" in out["levels"][2]
+    if cells[1] <= 1024:
+        assert "in one CTA" in out["wavefront"][2]
+    for kind in ("lanes", "wavefront"):
+        assert out[kind][0] == out["levels"][0]
+        assert np.array_equal(out[kind][1], out["levels"][1])
+
+
+def test_mpfa_cluster_sweep_wait_limit_expires_and_recovers():
+    """A 1 us wait limit: the cluster line sweeps give up (later warps wait for their
+    neighbours' first results far longer), the solve reports DXG_ERR_TIMEOUT, and with the
+    limit restored the same context solves to the same bits."""
+    desc, u0, _ = problems.mpfa_convergence_problem(300)
+    ctx = Context(desc)
+    ctx.set_ilu_kernel("lanes")
+    ctx.set_solution(u0)
+    ctx.assemble_jacobian_and_residual()
+    first = ctx.linear_solve(1e-12, 3000)
+    assert first["converged"] and "over a cluster" in ctx.describe()
+    x0 = ctx.update()
+    ctx.set_wait_limit(1e-6)
+    with pytest.raises(Exception, match="timed out"):
+        ctx.linear_solve(1e-12, 3000)
+    ctx.set_wait_limit(0.5)
+    again = ctx.linear_solve(1e-12, 3000)
+    assert again["iterations"] == first["iterations"] and np.array_equal(ctx.update(), x0)
