@@ -916,8 +916,10 @@ def main():
         if args.cells == "64,64,32":
             args.cells = "256,256"
         args.cpu_sample_iters = 1
-        if args.ilu != "natural" or args.solver != "ilu" or args.precision != "fp64" or args.diff != "numeric":
-            sys.exit("--workload mpfa: FP64, numeric Jacobian, natural-order ILU(0)-BiCGSTAB")
+        if args.ilu == "redblack" or args.solver != "ilu" or args.precision != "fp64" or args.diff != "numeric":
+            sys.exit("--workload mpfa: FP64, numeric Jacobian, natural-order ILU(0)-BiCGSTAB "
+                     "(--ilu natural: the context's choice, wavefront: one-CTA line sweeps, "
+                     "lanes: cluster line sweeps)")
     cells = tuple(int(c) for c in args.cells.split(","))
     if args.workload in STATIONARY:
         args.dt = 0.0
@@ -1066,9 +1068,12 @@ def main():
         rkernel = "rbApplyBlack + rbApplyRed (red-black ILU(0) apply, two parallel passes)"
         rnote = "bandwidth-bound passes, latency bound at small grids"
     elif args.workload == "mpfa":
-        rkernel = "stencilApplyKernel (ILU(0) forward+backward sweep of the 9-point MPFA-O stencil, one apply)"
-        rnote = ("latency-bound hyperplane sweeps (nx + 2 ny - 2 levels each) in one CTA, far below the HBM "
-                 "roof; algorithmic bytes: every factor entry, pivot and vector entry once")
+        dsc = ctx.describe()
+        kname = ("stencilLane2dKernel" if "over a cluster" in dsc else
+                 "stencilWave2dKernel" if "line sweeps" in dsc else "stencilApplyKernel")
+        rkernel = f"{kname} (ILU(0) forward+backward sweep of the 9-point MPFA-O stencil, one apply)"
+        rnote = ("latency-bound natural-order sweeps (nx + 2 ny - 1 levels each), far below the HBM roof; "
+                 "algorithmic bytes: every factor entry, pivot and vector entry once")
         traffic = None
     elif lanes:
         rkernel = "laneWaveKernel (ILU(0) forward+backward lane sweeps, one apply)"

@@ -222,8 +222,7 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT
         for (int e = 0; e < B; ++e) sum[e] = 0;
         // straight-line code: every slot's block (always allocated) and x entry (the
         // cell's own for a missing neighbour) is loaded without a branch, so all loads of
-        // the row are in flight together; a missing neighbour's block is stored as zeros
-        // (the assembly and dxg_set_linear_system write them), so it adds 0 * x_i
+        // the row are in flight together; a missing neighbour's block enters as zero
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             const bool valid = slotValid(m, DIM, s);
@@ -233,7 +232,9 @@ __global__ void __launch_bounds__(kReduceThreads) spmvKernel(SpmvArgs<MT, VT, XT
             ldgVec<B>(a.x + (i + (valid ? a.off[s] : 0)) * B, xs);
             AT xj[B];
 #pragma unroll
-            for (int e = 0; e < B; ++e) xj[e] = (AT)xs[e];
+            for (int e = 0; e < B; ++e) xj[e] = valid ? (AT)xs[e] : (AT)0;
+#pragma unroll
+            for (int e = 0; e < BB; ++e) blk[e] = valid ? blk[e] : (MT)0;
             blkMv<B>(blk, xj, sum);
         }
         VT acc[B];

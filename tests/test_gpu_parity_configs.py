@@ -53,9 +53,16 @@ def test_config1_darcy_100x100_one_step():
     p_orc = u0 - dx
     assert np.max(np.abs(p_gpu - p_orc)) <= 1e-9 * np.max(np.abs(p_orc))
     # BiCGSTAB's iterates depend on the summation order of its dot products (sequential on
-    # the host, tree-shaped on the device); on this field (sigma = 1) that moves the
-    # iteration count at 1e-12 by a few percent, not the solution
-    assert abs(res["iterations"] - ores.iterations) <= max(2, 0.03 * ores.iterations)
+    # the host, tree-shaped on the device) and on the rounding of the factor; on this field
+    # (sigma = 1) that moves the iteration count at 1e-12 by several percent, not the
+    # solution.  The bound is the oracle's own spread under another summation order.
+    oracle.set_dot_order(1)
+    try:
+        _, _, ores2 = oracle.linear_solve(orow, ocol, ovals, r_orc, 1, reduction=1e-12, max_iter=250)
+    finally:
+        oracle.set_dot_order(0)
+    floor = abs(ores2.iterations - ores.iterations)
+    assert abs(res["iterations"] - ores.iterations) <= max(2, 0.03 * ores.iterations, 1.5 * floor)
 
 
 def test_config2_dnapl_64x64x32_ten_steps():
