@@ -613,9 +613,10 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     for (int a = 0; a < d->dim; ++a)
         if (d->cells[a] < 1 || !d->coords[a]) throw Error(DXG_ERR_ARG, "invalid cells/coords");
     if (!d->permeability || !d->porosity || !d->bc_type || !d->bc_values) throw Error(DXG_ERR_ARG, "missing tables");
-    if (d->diff_method != 0) throw Error(DXG_ERR_ARG, "MPFA-O assembles by numeric differentiation");
-    const int method = d->numeric_difference_method;
-    if (method != 1 && method != 0 && method != -1 && method != 5)
+    if (d->diff_method != 0 && d->diff_method != 1) throw Error(DXG_ERR_ARG, "diff_method must be 0 or 1");
+    // internal method code as for TPFA: 1 / 0 / -1 / 5 numeric differences, 3 analytic
+    const int method = d->diff_method == 1 ? 3 : d->numeric_difference_method;
+    if (method != 1 && method != 0 && method != -1 && method != 5 && method != 3)
         throw Error(DXG_ERR_ARG, "numeric difference method must be 1, 0, -1 or 5");
     const int dim = d->dim;
     HostGrid g{};
@@ -663,6 +664,7 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     pc.baseEps = d->base_epsilon > 0 ? d->base_epsilon : 1e-10;
     pc.method = method;
     c->mpMob = d->density[0] * (1.0 / d->viscosity[0]);
+    c->mpUp = d->density[0] / d->viscosity[0];
     const int64_t strides[3] = {1, g.n[0], g.n[0] * g.n[1]};
     for (int s = 0; s < L.S; ++s) {
         int o[3] = {0, 0, 0}, q = s;
@@ -777,6 +779,7 @@ MpfaArgs mpfaArgs(const dxg_ctx* c)
     a.srcterm = c->srcterm.get();
     a.u = c->u.get();
     a.mob = c->mpMob;
+    a.up = c->mpUp;
     a.baseEps = c->pcHost.baseEps;
     a.magnitude = c->pcHost.magnitude[0];
     a.transient = c->dt > 0.0;

@@ -48,7 +48,7 @@ struct dxg_ctx {
     dxg::DevBuf<int8_t> mpKind;
     dxg::DevBuf<uint32_t> mpMask;
     std::vector<uint32_t> mpMaskHost;
-    double mpMob = 0.0;
+    double mpMob = 0.0, mpUp = 0.0;
     int mpNTri = 0;
     int8_t mpTri[104][3] = {};
 

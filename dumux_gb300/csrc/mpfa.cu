@@ -581,6 +581,24 @@ __global__ void __launch_bounds__(128) mpfaAssembleKernel(MpfaArgs a, bool jac)
         const double r0 = residual(-1, 0.0);
         a.r[i] = r0;
         if (!jac) continue;
+        if (METHOD == 3) {
+            // CCLocalAssembler<analytic> with the incompressible 1p flux derivatives for MPFA
+            // (porousmediumflow/1p/incompressiblelocalresidual.hh:126-160, 221-233): every
+            // non-Neumann scvf adds (+/-) t_k * rho / mu to the column of its IV cell k, scvfs
+            // in element order
+            for (int s = 0; s < S; ++s) {
+                double dv = 0.0;
+                if ((m >> s) & 1u) {
+                    for (int f = 0; f < a.F; ++f) {
+                        if (!((a.scvfSlots[f] >> s) & 1u) || a.kind[(int64_t)f * N + i] == 1) continue;
+                        for (int k = 0; k < a.K; ++k)
+                            if (a.slotOf[f][k] == s) dv += a.coef[((int64_t)f * a.K + k) * N + i] * a.up;
+                    }
+                }
+                a.A[(int64_t)s * N + i] = dv;
+            }
+            continue;
+        }
         for (int s = 0; s < S; ++s) {
             double dv = 0.0;
             if ((m >> s) & 1u) {
@@ -611,6 +629,7 @@ void assembleS(const MpfaArgs& a, int method, bool jac, cudaStream_t st)
     if (method == 1) mpfaAssembleKernel<S, 1><<<g, threads, 0, st>>>(a, jac);
     else if (method == -1) mpfaAssembleKernel<S, -1><<<g, threads, 0, st>>>(a, jac);
     else if (method == 0) mpfaAssembleKernel<S, 0><<<g, threads, 0, st>>>(a, jac);
+    else if (method == 3) mpfaAssembleKernel<S, 3><<<g, threads, 0, st>>>(a, jac);
     else mpfaAssembleKernel<S, 5><<<g, threads, 0, st>>>(a, jac);
     DXG_CUDA(cudaGetLastError());
 }

@@ -41,13 +41,15 @@ struct MpfaArgs {
     const uint32_t* mask = nullptr;
     const double* srcterm = nullptr;   // source * volume * extrusion
     const double* u = nullptr;
-    double mob = 0.0;                  // density * (1 / viscosity)
+    double mob = 0.0;                  // density * (1 / viscosity): the flux's upwind term
+    double up = 0.0;                   // density / viscosity: the analytic derivatives' factor
     double baseEps = 1e-10, magnitude = -1.0;
     bool transient = false;
     double* A = nullptr;               // [S][N]
     double* r = nullptr;
 };
-// Residual (and with jac the numeric-difference Jacobian rows, method 1 / -1 / 0 / 5).
+// Residual (and with jac the Jacobian rows: numeric differences, method 1 / -1 / 0 / 5, or
+// the analytic derivatives, method 3).
 void launchMpfaAssemble(const MpfaArgs& a, int method, bool jac, cudaStream_t st);
 
 }  // namespace dxg

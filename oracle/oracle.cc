@@ -1003,10 +1003,21 @@ static void mpfaAssemble(const Problem& P, const Pattern& pt, const double* u, d
         return -1;
     };
     if (values) std::fill(values, values + pt.rowPtr[P.N], 0.0);
+    // analytic (CCLocalAssembler<analytic>, incompressiblelocalresidual.hh:126-160, 221-233):
+    // row I collects, scvf by scvf in element order, (+/-) t_J * rho / mu for every IV cell J of
+    // its non-Neumann scvfs
+    const double up = P.d.density[0] / P.d.viscosity[0];
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
     for (int64_t I = 0; I < P.N; ++I) {
         r[I] = residual(I, -1, 0.0);
         if (!values) continue;
+        if (P.d.diff_method == 1) {
+            for (const MpScvfRow& row : rows[I]) {
+                if (row.neumann) continue;
+                for (const MpIvTerm& k : row.terms) values[find(I, k.cell)] += k.t * up;
+            }
+            continue;
+        }
         const double x = u[I];
         const double eps = numericEpsilon(P, x, 0);
         // column I: rows J of the neighbourhood (J == I: whole residual)

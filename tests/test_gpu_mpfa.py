@@ -32,9 +32,10 @@ def _cases():
 
 
 @pytest.mark.parametrize("name,desc,u", _cases(), ids=lambda v: v if isinstance(v, str) else "")
-@pytest.mark.parametrize("method", [1, 0, -1, 5])
+@pytest.mark.parametrize("method", [1, 0, -1, 5, "analytic"])
 def test_mpfa_residual_and_jacobian_equal_the_oracle(name, desc, u, method):
-    desc.numeric_difference_method = method
+    desc.analytic = method == "analytic"
+    desc.numeric_difference_method = 1 if method == "analytic" else method
     ctx = Context(desc)
     ctx.set_solution(u)
     ctx.assemble_jacobian_and_residual()
@@ -45,9 +46,12 @@ def test_mpfa_residual_and_jacobian_equal_the_oracle(name, desc, u, method):
     assert np.array_equal(vals, ovals)
 
 
-def test_mpfa_lens_on_the_device_matches_reference_vtu():
+@pytest.mark.parametrize("analytic", [False, True])
+def test_mpfa_lens_on_the_device_matches_reference_vtu(analytic):
+    # the reference's test_1p_incompressible_mpfa assembles the analytic Jacobian
     ref = _load("onep_lens_p.txt")
     desc, u0 = problems.onep_lens_problem(numeric_epsilon=True, discretization="mpfa")
+    desc.analytic = analytic
     ctx = Context(desc)
     ctx.set_solution(u0)
     ctx.assemble_jacobian_and_residual()
@@ -137,3 +141,24 @@ def test_mpfa_cluster_sweep_wait_limit_expires_and_recovers():
     ctx.set_wait_limit(0.5)
     again = ctx.linear_solve(1e-12, 3000)
     assert again["iterations"] == first["iterations"] and np.array_equal(ctx.update(), x0)
+
+
+@pytest.mark.parametrize("cells", [(1, 7), (7, 1), (1, 1), (2, 2), (1, 1, 3), (3, 1, 1), (2, 1, 2)])
+def test_mpfa_degenerate_grids(cells):
+    """Grids of one or two cells per axis: interaction volumes with one, two or four cells,
+    every face a boundary face on some axis."""
+    K = ((2.0, 0.5), (0.5, 1.0)) if len(cells) == 2 else ((2.0, 0.3, 0.1), (0.3, 1.0, 0.2), (0.1, 0.2, 1.5))
+    desc, u0, exact = problems.mpfa_linear_field_problem(cells=cells, K=K)
+    u = exact + 0.25
+    ctx = Context(desc)
+    ctx.set_solution(u)
+    ctx.assemble_jacobian_and_residual()
+    row_ptr, col, vals = ctx.jacobian()
+    orow, ocol, ovals, r_orc = oracle.assemble(desc, u)
+    assert np.array_equal(row_ptr, orow) and np.array_equal(col, ocol)
+    assert np.array_equal(vals, ovals) and np.array_equal(ctx.residual(), r_orc)
+    p = newton_params(max_relative_shift=1e-12, linear_reduction=1e-14, linear_max_iter=500, max_steps=30)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    assert ctx.newton_solve(0.0, p)["converged"]
+    assert np.max(np.abs(ctx.solution() - exact)) <= 1e-12 * np.max(np.abs(exact))

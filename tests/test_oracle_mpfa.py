@@ -108,3 +108,26 @@ def test_mpfa_gravity_neumann_and_source_are_consistent():
     assert st == 0
     rn = oracle.assemble(desc, un, jacobian=False)
     assert np.max(np.abs(rn)) <= 1e-10 * np.max(np.abs(r))
+
+
+def test_mpfa_analytic_jacobian_equals_numeric_differences():
+    """The analytic Jacobian of the incompressible 1p MPFA-O residual (transmissibility times
+    density / viscosity) against central differences of the residual; the lens with it (the
+    reference test's own configuration) against the reference file."""
+    desc, u0, _ = problems.mpfa_linear_field_problem(cells=(5, 4, 3), K=((2.0, 0.3, 0.1), (0.3, 1.0, 0.2),
+                                                                         (0.1, 0.2, 1.5)), gravity=True,
+                                                      spacing_seed=5)
+    desc.bc_type[:12] = 2
+    u = 1e5 + np.random.default_rng(9).uniform(-1e3, 1e3, desc.num_cells)
+    desc.analytic = True
+    row_ptr, col, va, r = oracle.assemble(desc, u)
+    desc.analytic = False
+    desc.numeric_difference_method = 0
+    _, _, vn, rn = oracle.assemble(desc, u)
+    assert np.array_equal(r, rn)
+    np.testing.assert_allclose(va, vn, rtol=1e-5, atol=1e-6 * np.max(np.abs(va)))
+    ref = _load("onep_lens_p.txt")
+    dl, ul = problems.onep_lens_problem(numeric_epsilon=True, discretization="mpfa")
+    dl.analytic = True
+    p, _ = _linear_step(dl, ul)
+    assert np.max(np.abs(p - ref)) <= 0.5 + 1e-9
