@@ -605,11 +605,17 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
 
 // MPFA-O (1p, FP64 single contexts): the interaction volumes solved on the host
 // (mpfaTabulate), the per-cell flux rows, the 3^dim stencil and the Krylov buffers.
+void tabulateMpfa2p(dxg_ctx* c, const dxg_problem_desc* d);
+
 void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
 {
     if (d->dim != 2 && d->dim != 3) throw Error(DXG_ERR_ARG, "dim must be 2 or 3");
-    if (d->num_eq != 1) throw Error(DXG_ERR_ARG, "MPFA-O is available for the 1p model (num_eq 1)");
+    if (d->num_eq != 1 && d->num_eq != 2) throw Error(DXG_ERR_ARG, "num_eq must be 1 or 2");
     if (c->precision != DXG_PRECISION_FP64) throw Error(DXG_ERR_ARG, "MPFA-O runs in FP64");
+    if (d->num_eq == 2) {
+        tabulateMpfa2p(c, d);
+        return;
+    }
     for (int a = 0; a < d->dim; ++a)
         if (d->cells[a] < 1 || !d->coords[a]) throw Error(DXG_ERR_ARG, "invalid cells/coords");
     if (!d->permeability || !d->porosity || !d->bc_type || !d->bc_values) throw Error(DXG_ERR_ARG, "missing tables");
@@ -704,7 +710,7 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     });
     std::vector<double> coef, cst;
     std::vector<int8_t> kind;
-    mpfaTabulate(d, L, pc.sideOffset, coef, cst, kind);
+    mpfaTabulate(d, L, pc.sideOffset, nullptr, coef, cst, kind);
     int64_t nnz = 0;
     for (int64_t i = 0; i < N; ++i) nnz += __builtin_popcount(mask[i]);
     c->nnzb = nnz;
@@ -761,6 +767,106 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     c->haveJac = c->haveRes = c->haveFactor = false;
 }
 
+// MPFA-O for the 2p model: the TPFA tabulation supplies the volume variables, storage,
+// sources and the Dirichlet ghosts of the 2p model; the interaction volumes add the flux rows
+// (per phase constants from the ghosts' phase pressures and gravity), and the Jacobian, its
+// factor and the pivots take the 3^dim stencil of 2x2 blocks.
+void tabulateMpfa2p(dxg_ctx* c, const dxg_problem_desc* d)
+{
+    if (d->diff_method != 0) throw Error(DXG_ERR_ARG, "MPFA-O with the 2p model assembles by numeric differentiation");
+    dxg_problem_desc dt = *d;
+    dt.discretization = DXG_DISC_TPFA;
+    dt.permeability_tensor = nullptr;
+    tabulate(c, &dt);
+    const int dim = d->dim;
+    const MpfaLayout L = mpfaLayout(dim);
+    const ProblemConsts& pc = c->pcHost;
+    const int64_t n[3] = {pc.nx, pc.ny, pc.nz};
+    const int64_t N = c->N, nb = c->nb;
+    // the Dirichlet ghosts' phase pressures (p_n = p_w + pc(1 - S_n) with the inside cell's law)
+    std::vector<double> dirP((size_t)2 * nb, 0.0);
+    for (int f = 0; f < 2 * dim; ++f) {
+        const int a = f / 2, side = f & 1;
+        int o1 = -1, o2 = -1;
+        for (int k = 0; k < dim; ++k)
+            if (k != a) { if (o1 < 0) o1 = k; else o2 = k; }
+        const int64_t n1 = n[o1], n2 = o2 >= 0 ? n[o2] : 1;
+        for (int64_t q2 = 0; q2 < n2; ++q2)
+            for (int64_t q1 = 0; q1 < n1; ++q1) {
+                const int64_t bidx = pc.sideOffset[f] + q1 + n1 * q2;
+                if (d->bc_type[bidx] != 1) continue;
+                int64_t id[3] = {0, 0, 0};
+                id[a] = side ? n[a] - 1 : 0;
+                id[o1] = q1;
+                if (o2 >= 0) id[o2] = q2;
+                const int64_t i = id[0] + n[0] * (id[1] + n[1] * id[2]);
+                const MaterialLaw& m = pc.law[d->material ? d->material[i] : 0];
+                const double* bv = d->bc_values + bidx * 2;
+                const double Sw = 1 - bv[1];
+                const double pcap = lawPc(m, Sw);
+                dirP[bidx] = bv[0];
+                dirP[nb + bidx] = bv[0] + pcap;
+            }
+    }
+    c->mpfa = true;
+    c->mpLayout = L;
+    c->slots = L.S;
+    const int64_t strides[3] = {1, n[0], n[0] * n[1]};
+    for (int s = 0; s < L.S; ++s) {
+        int o[3] = {0, 0, 0}, q = s;
+        for (int a = 0; a < dim; ++a) {
+            o[a] = q % 3 - 1;
+            q /= 3;
+        }
+        c->mpOff[s] = o[0] * strides[0] + o[1] * strides[1] + o[2] * strides[2];
+    }
+    mpfaTriples(dim, c->mpNTri, c->mpTri);
+    std::vector<uint32_t> mask(N, 0);
+    for (int64_t i = 0; i < N; ++i) {
+        const int64_t id[3] = {i % n[0], (i / n[0]) % n[1], i / (n[0] * n[1])};
+        uint32_t mm = 0;
+        for (int s = 0; s < L.S; ++s) {
+            int q = s;
+            bool ok = true;
+            for (int a = 0; a < dim; ++a) {
+                const int64_t x = id[a] + (q % 3 - 1);
+                q /= 3;
+                if (x < 0 || x >= n[a]) ok = false;
+            }
+            if (ok) mm |= 1u << s;
+        }
+        mask[i] = mm;
+    }
+    std::vector<double> coef, cst;
+    std::vector<int8_t> kind;
+    mpfaTabulate(d, L, pc.sideOffset, dirP.data(), coef, cst, kind);
+    int64_t nnz = 0;
+    for (int64_t i = 0; i < N; ++i) nnz += __builtin_popcount(mask[i]);
+    c->nnzb = nnz;
+    c->mpMaskHost = mask;
+    c->mpMob = 0.0;
+    c->mpUp = 0.0;
+    c->bytesAssembly += (double)N * (8.0 * L.F * (L.K + 2) + L.F + 4.0);
+    c->bytesSpmv = (double)nnz * 32.0 + N * 4.0 + 2.0 * N * 16.0;
+    c->bytesSweep = (double)nnz * 32.0 + N * (32.0 + 4.0 * 16.0);
+    cudaStream_t st = c->stream;
+    upload(c->mpMask, mask, st);
+    upload(c->mpCoef, coef, st);
+    upload(c->mpCst, cst, st);
+    upload(c->mpKind, kind, st);
+    c->A.alloc((size_t)L.S * N * 4);
+    c->L.alloc((size_t)L.S * N * 4);
+    c->Dinv.alloc((size_t)N * 4);
+    DXG_CUDA(cudaMemsetAsync(c->A.get(), 0, (size_t)L.S * N * 4 * sizeof(double), st));
+    DXG_CUDA(cudaStreamSynchronize(st));
+    c->wavePlan = WavePlan{};
+    c->lanePlan = LanePlan{};
+    c->waveTuned = true;
+    c->laneWave = false;
+    c->dropGraphs();
+    c->haveJac = c->haveRes = c->haveFactor = false;
+}
+
 MpfaArgs mpfaArgs(const dxg_ctx* c)
 {
     const MpfaLayout& L = c->mpLayout;
@@ -785,6 +891,23 @@ MpfaArgs mpfaArgs(const dxg_ctx* c)
     a.transient = c->dt > 0.0;
     a.A = c->A.get();
     a.r = c->r.get();
+    a.b = c->b;
+    if (c->b == 2) {
+        a.nx = c->pcHost.nx;
+        a.ny = c->pcHost.ny;
+        a.nz = c->pcHost.nz;
+        a.nb = c->nb;
+        for (int f = 0; f < 7; ++f) a.sideOffset[f] = c->pcHost.sideOffset[f];
+        a.vvP = c->vvP.get();
+        a.vvU = c->vvU.get();
+        a.vvS = c->vvS.get();
+        a.eps = c->eps.get();
+        a.stPrev = c->stPrev.get();
+        a.vol = c->vol.get();
+        a.bU = c->bU.get();
+        a.w = c->pcHost.upwindWeight;
+        a.dt = c->dt;
+    }
     return a;
 }
 
@@ -807,6 +930,7 @@ int mpfaSweep(const dxg_ctx* c, const StencilArgs& sa)
 StencilArgs stencilArgs(dxg_ctx* c)
 {
     StencilArgs a{};
+    a.b = c->b;
     a.nx = c->pcHost.nx;
     a.ny = c->pcHost.ny;
     a.nz = c->pcHost.nz;
@@ -854,6 +978,12 @@ void assemble(dxg_ctx* c, bool jac)
     if (c->dt > 0.0 && !c->havePrev) throw Error(DXG_ERR_STATE, "transient assembly needs the previous solution");
     if (c->mpfa) {
         TimedScope ts(c, DXG_KC_ASSEMBLY, jac ? c->bytesAssembly : 0.0);
+        if (c->b == 2) {
+            // the volume variables of every cell at its own and perturbed states
+            ensurePrevStorage(c);
+            launchVolvars(c->asmArgs(), 2, jac ? c->method : 2, c->u.get(), c->stream);
+            c->launches += 1;
+        }
         launchMpfaAssemble(mpfaArgs(c), c->method, jac, c->stream);
         c->launches += 1;
         c->haveRes = true;
@@ -1883,6 +2013,7 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
     if (!c->uploaded) out = "no problem uploaded";
     else if (c->mpfa) {
         StencilArgs sa{};
+        sa.b = c->b;
         sa.S = c->mpLayout.S;
         sa.nx = c->pcHost.nx;
         sa.ny = c->pcHost.ny;

@@ -1367,9 +1367,176 @@ __global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const
 // dynamic shared memory of the 2D sweeps at prefetch depth pf
 static size_t wave2dSmem(unsigned threads, int pf) { return (size_t)pf * threads * 6 * sizeof(double); }
 
+// 2x2 blocks over the same stencil (the 2p MPFA-O Jacobian, A[slot][row][4] row-major
+// blocks): SpMV with the same fused dots, and the block ILU(0) factor and sweeps level by
+// level (block products with explicit FMAs, pivot blocks inverted as in the wavefront factor)
+template <int S, int MODE>
+__global__ void __launch_bounds__(kReduceThreads) stencilSpmv2Kernel(StencilArgs a, const double* __restrict__ x,
+                                                                      double* __restrict__ y, const double* __restrict__ w)
+{
+    const unsigned nblk = cellBlocksFor(a.N);
+    const unsigned lb = blockIdx.x;
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    double part[2] = {0.0, 0.0};
+    for (int64_t i = lb * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)nblk * blockDim.x) {
+        const uint32_t m = __ldg(a.mask + i);
+        double sum[2] = {0.0, 0.0};
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const bool valid = (m >> s) & 1u;
+            double blk[4], xs[2];
+            ldgBlock<2>(a.A + ((int64_t)s * a.N + i) * 4, blk);
+            ldgVec<2>(x + (i + (valid ? a.off[s] : 0)) * 2, xs);
+#pragma unroll
+            for (int e = 0; e < 2; ++e) xs[e] = valid ? xs[e] : 0.0;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) blk[e] = valid ? blk[e] : 0.0;
+            blkMv<2>(blk, xs, sum);
+        }
+        y[i * 2] = sum[0];
+        y[i * 2 + 1] = sum[1];
+        if (MODE == 1) {
+            for (int e = 0; e < 2; ++e) part[0] += w[i * 2 + e] * sum[e];
+        } else if (MODE == 2) {
+            for (int e = 0; e < 2; ++e) {
+                part[0] += sum[e] * w[i * 2 + e];
+                part[1] += sum[e] * sum[e];
+            }
+        }
+    }
+    if (MODE == 0) return;
+    if (gridSum<2>(part, a.scratch.partials, a.scratch.counter + MODE, nblk, lb)) {
+        KrylovState& ks = *a.ks;
+        if (MODE == 1) {
+            ks.h = part[0];
+            if (fabs(ks.h) < 1e-80) ks.status = KS_BREAKDOWN;
+            else ks.alpha = ks.rho_new / ks.h;
+        } else {
+            ks.tr = part[0];
+            ks.tt = part[1];
+            ks.omega = ks.tr / ks.tt;
+        }
+    }
+}
+
+__device__ __forceinline__ void st2Mul(const double* X, const double* Y, double* Z)
+{
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            double t = 0.0;
+            t = fma(X[r * 2 + 0], Y[0 * 2 + c], t);
+            t = fma(X[r * 2 + 1], Y[1 * 2 + c], t);
+            Z[r * 2 + c] = t;
+        }
+}
+
+__global__ void __launch_bounds__(1024) stencilFactor2Kernel(StencilArgs a)
+{
+    const int levels = (a.nx - 1) + 2 * (a.ny - 1) + 4 * (a.nz - 1) + 1;
+    for (int L = 0; L < levels; ++L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            for (int s = 0; s < a.S; ++s)
+                for (int e = 0; e < 4; ++e) a.LU[((int64_t)s * a.N + i) * 4 + e] = a.A[((int64_t)s * a.N + i) * 4 + e];
+            int t0 = 0;
+            for (int s = 0; s < a.center; ++s) {
+                if (!((m >> s) & 1u)) continue;
+                const int64_t j = i + a.off[s];
+                double* Lis = a.LU + ((int64_t)s * a.N + i) * 4;
+                double l[4];
+                st2Mul(Lis, a.Dinv + j * 4, l);
+                for (int e = 0; e < 4; ++e) Lis[e] = l[e];
+                const uint32_t mj = a.mask[j];
+                while (t0 < a.nTri && a.tri[t0][0] < s) ++t0;
+                for (int k = t0; k < a.nTri && a.tri[k][0] == s; ++k) {
+                    const int t = a.tri[k][1], u = a.tri[k][2];
+                    if (!((m >> t) & 1u) || !((mj >> u) & 1u)) continue;
+                    double pr[4];
+                    st2Mul(l, a.LU + ((int64_t)u * a.N + j) * 4, pr);
+                    double* Lit = a.LU + ((int64_t)t * a.N + i) * 4;
+                    for (int e = 0; e < 4; ++e) Lit[e] -= pr[e];
+                }
+            }
+            const double* D = a.LU + ((int64_t)a.center * a.N + i) * 4;
+            const double p12 = D[1] * D[2];
+            const double det = fma(D[0], D[3], -p12);
+            if (det == 0.0) atomicExch(a.singular, 1);
+            const double di = 1.0 / det;
+            a.Dinv[i * 4 + 0] = D[3] * di;
+            a.Dinv[i * 4 + 1] = -D[1] * di;
+            a.Dinv[i * 4 + 2] = -D[2] * di;
+            a.Dinv[i * 4 + 3] = D[0] * di;
+        });
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) stencilApply2Kernel(StencilArgs a, const double* __restrict__ d,
+                                                             double* __restrict__ v)
+{
+    if (a.ks && a.ks->status != KS_RUNNING) return;
+    const int levels = (a.nx - 1) + 2 * (a.ny - 1) + 4 * (a.nz - 1) + 1;
+    for (int L = 0; L < levels; ++L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            double r0 = d[i * 2], r1 = d[i * 2 + 1];
+            for (int s = 0; s < a.center; ++s)
+                if ((m >> s) & 1u) {
+                    const double* B = a.LU + ((int64_t)s * a.N + i) * 4;
+                    const double* vj = v + (i + a.off[s]) * 2;
+                    r0 = fma(-B[0], vj[0], r0);
+                    r0 = fma(-B[1], vj[1], r0);
+                    r1 = fma(-B[2], vj[0], r1);
+                    r1 = fma(-B[3], vj[1], r1);
+                }
+            v[i * 2] = r0;
+            v[i * 2 + 1] = r1;
+        });
+        __syncthreads();
+    }
+    for (int L = levels - 1; L >= 0; --L) {
+        forLevelRows(a, L, [&](int64_t i) {
+            const uint32_t m = a.mask[i];
+            double r0 = v[i * 2], r1 = v[i * 2 + 1];
+            for (int s = a.S - 1; s > a.center; --s)
+                if ((m >> s) & 1u) {
+                    const double* B = a.LU + ((int64_t)s * a.N + i) * 4;
+                    const double* vj = v + (i + a.off[s]) * 2;
+                    r0 = fma(-B[0], vj[0], r0);
+                    r0 = fma(-B[1], vj[1], r0);
+                    r1 = fma(-B[2], vj[0], r1);
+                    r1 = fma(-B[3], vj[1], r1);
+                }
+            const double* D = a.Dinv + i * 4;
+            double t0 = D[0] * r0;
+            t0 = fma(D[1], r1, t0);
+            double t1 = D[2] * r0;
+            t1 = fma(D[3], r1, t1);
+            v[i * 2] = t0;
+            v[i * 2 + 1] = t1;
+        });
+        __syncthreads();
+    }
+}
+
 void launchStencilSpmv(const StencilArgs& a, const double* x, double* y, const double* w, int mode, cudaStream_t st)
 {
     const dim3 g((unsigned)cellBlocksFor(a.N));
+    if (a.b == 2) {
+        if (a.S == 9) {
+            if (mode == 0) stencilSpmv2Kernel<9, 0><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+            else if (mode == 1) stencilSpmv2Kernel<9, 1><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+            else stencilSpmv2Kernel<9, 2><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        } else {
+            if (mode == 0) stencilSpmv2Kernel<27, 0><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+            else if (mode == 1) stencilSpmv2Kernel<27, 1><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+            else stencilSpmv2Kernel<27, 2><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
+        }
+        DXG_CUDA(cudaGetLastError());
+        return;
+    }
     if (a.S == 9) {
         if (mode == 0) stencilSpmvKernel<9, 0><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
         else if (mode == 1) stencilSpmvKernel<9, 1><<<g, kReduceThreads, 0, st>>>(a, x, y, w);
@@ -1391,11 +1558,12 @@ static unsigned stencilThreads(const StencilArgs& a)
 
 void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
 {
-    stencilFactorKernel<<<1, stencilThreads(a), 0, st>>>(a);
+    if (a.b == 2) stencilFactor2Kernel<<<1, stencilThreads(a), 0, st>>>(a);
+    else stencilFactorKernel<<<1, stencilThreads(a), 0, st>>>(a);
     DXG_CUDA(cudaGetLastError());
 }
 
-bool stencilWave2dFits(const StencilArgs& a) { return a.S == 9 && a.ny >= 1 && a.ny <= 1024; }
+bool stencilWave2dFits(const StencilArgs& a) { return a.b == 1 && a.S == 9 && a.ny >= 1 && a.ny <= 1024; }
 
 void launchStencilWave2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
 {
@@ -1427,7 +1595,8 @@ void launchStencilWave2d(const StencilArgs& a, const double* d, double* v, cudaS
 
 void launchStencilApplyLevels(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
 {
-    stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
+    if (a.b == 2) stencilApply2Kernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
+    else stencilApplyKernel<<<1, stencilThreads(a), 0, st>>>(a, d, v);
     DXG_CUDA(cudaGetLastError());
 }
 

@@ -125,6 +125,7 @@ int reduceBlocks(int64_t M);
 // The ILU(0) update of row i by its lower entry s touches entry t of row i with entry u of
 // row i + off[s]: tri[k] = {s, t, u}, s then t ascending.
 struct StencilArgs {
+    int b = 1;                             // block size: 1 (1p) or 2 (2p, blocks [slot][row][4])
     int nx = 1, ny = 1, nz = 1;
     int64_t N = 0;
     int S = 0, center = 0;

@@ -230,9 +230,11 @@ void mpfaTriples(int dim, int& n, int8_t (*tri)[3])
         }
 }
 
-void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t* sideOffset,
+void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t* sideOffset, const double* dirP,
                   std::vector<double>& coef, std::vector<double>& cst, std::vector<int8_t>& kind)
 {
+    const int b = d->num_eq;
+    const int64_t nb = sideOffset[2 * d->dim];
     const int dim = d->dim;
     MpGrid g;
     g.dim = dim;
@@ -245,7 +247,7 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
     const int64_t N = g.n[0] * g.n[1] * g.n[2];
     const int K = L.K, F = L.F, corners = 1 << (dim - 1);
     coef.assign((size_t)F * K * N, 0.0);
-    cst.assign((size_t)F * N, 0.0);
+    cst.assign((size_t)F * b * N, 0.0);
     kind.assign((size_t)F * N, 0);
     const bool grav = d->enable_gravity != 0;
     double gvec[3] = {0, 0, 0};
@@ -255,8 +257,6 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
         return d->permeability_tensor ? d->permeability_tensor + (size_t)i * dim * dim : nullptr;
     };
     auto EX = [&](int64_t i) { return d->extrusion ? d->extrusion[i] : 1.0; };
-    const double rho = d->density[0];
-
     // Neumann scvfs: the given flux times the scvf area and the extrusion (cclocalresidual.hh:89-97)
     mpParallel(N, [&](int64_t i0, int64_t i1) {
         for (int64_t i = i0; i < i1; ++i) {
@@ -280,9 +280,11 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
                 for (int c = 0; c < corners; ++c) {
                     const int f = face * corners + c;
                     kind[(size_t)f * N + i] = 1;
-                    double q = 0.0;
-                    q += d->bc_values[bidx] * s;
-                    cst[(size_t)f * N + i] = q;
+                    for (int e = 0; e < b; ++e) {
+                        double q = 0.0;
+                        q += d->bc_values[bidx * b + e] * s;
+                        cst[((size_t)f * b + e) * N + i] = q;
+                    }
                 }
             }
         }
@@ -342,7 +344,7 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
                             }
                         fc.bidx = sideOffset[face] + pos;
                         fc.dirichlet = d->bc_type[fc.bidx] == 1;
-                        fc.uD = d->bc_values[fc.bidx];
+                        fc.uD = d->bc_values[fc.bidx * b];
                     }
                 }
             int nD = 0;
@@ -449,9 +451,10 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
                         T[(size_t)f * nK + j] += s;
                     }
             }
-            // gravity per face, then the continuity defect of the neighbours' alphas
-            double gF[12] = {0};
-            if (grav) {
+            // gravity per phase and face, then the continuity defect of the neighbours' alphas
+            double gF[2][12] = {};
+            for (int ph = 0; ph < b && grav; ++ph) {
+                const double rho = d->density[ph];
                 std::vector<double> deltaG((size_t)nU, 0.0);
                 for (int f = 0; f < nF; ++f) {
                     const IvFace& fc = faces[f];
@@ -474,27 +477,33 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
                         dg *= r * fc.area;
                         deltaG[fc.dof] = dg;
                     }
-                    gF[f] = alphaIn * r * fc.area;
+                    gF[ph][f] = alphaIn * r * fc.area;
                 }
                 for (int f = 0; f < nF; ++f) {
                     if (faces[f].P < 0) continue;
-                    double s = gF[f];
+                    double s = gF[ph][f];
                     for (int k = 0; k < nU; ++k) s += CA[(size_t)f * nU + k] * deltaG[k];
-                    gF[f] = s;
+                    gF[ph][f] = s;
                 }
             }
             // scatter: each face's flux row to the scvf of P (as computed) and of Q (negated)
             for (int f = 0; f < nF; ++f) {
                 const IvFace& fc = faces[f];
                 if (fc.P < 0) continue;
-                double c0 = 0.0;
-                for (int j = nKnown; j < nK; ++j) {
-                    const IvFace* fd = nullptr;
-                    for (int q = 0; q < nF; ++q)
-                        if (faces[q].P >= 0 && faces[q].dIdx == j) fd = &faces[q];
-                    c0 += T[(size_t)f * nK + j] * fd->uD;
+                // per phase: the Dirichlet ghosts' phase pressures times their transmissibilities,
+                // then gravity (1p: the Dirichlet values themselves)
+                double c0[2] = {0.0, 0.0};
+                for (int ph = 0; ph < b; ++ph) {
+                    double cp = 0.0;
+                    for (int j = nKnown; j < nK; ++j) {
+                        const IvFace* fd = nullptr;
+                        for (int q = 0; q < nF; ++q)
+                            if (faces[q].P >= 0 && faces[q].dIdx == j) fd = &faces[q];
+                        cp += T[(size_t)f * nK + j] * (b == 1 ? fd->uD : dirP[(size_t)ph * nb + fd->bidx]);
+                    }
+                    cp += gF[ph][f];
+                    c0[ph] = cp;
                 }
-                c0 += gF[f];
                 for (int side = 0; side < 2; ++side) {
                     const int k = side == 0 ? fc.P : fc.Q;
                     if (k < 0) continue;
@@ -512,7 +521,7 @@ void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t*
                         const double t = known[kk] >= 0 ? T[(size_t)f * nK + known[kk]] : 0.0;
                         coef[((size_t)sf * K + kk) * N + i] = side == 0 ? t : -t;
                     }
-                    cst[(size_t)sf * N + i] = side == 0 ? c0 : -c0;
+                    for (int ph = 0; ph < b; ++ph) cst[((size_t)sf * b + ph) * N + i] = side == 0 ? c0[ph] : -c0[ph];
                 }
             }
         }
@@ -620,6 +629,161 @@ __global__ void __launch_bounds__(128) mpfaAssembleKernel(MpfaArgs a, bool jac)
     }
 }
 
+// The 2p immiscible model (p0s1): per scvf and phase the Darcy flux T p_alpha + c_alpha over
+// the IV's cells' phase pressures, times the upwinded density * mobility of the scvf's inside
+// cell and the cell across the face (or the Dirichlet ghost); source and storage as the TPFA
+// rows; numeric Jacobian from the volume-variable kernel's perturbed states, the entry of
+// neighbour j from the cell's scvf fluxes whose IV holds j (both phases), the diagonal from the
+// whole residual.  Same operation order as the oracle.
+template <int S, int DIM, int METHOD>
+__global__ void __launch_bounds__(128) mpfa2pKernel(MpfaArgs a, bool jac)
+{
+    constexpr int center = (S - 1) / 2;
+    constexpr int SP = statesPerPv(METHOD);
+    const int64_t N = a.N;
+    const int corners = 1 << (DIM - 1);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = a.mask[i];
+        int64_t id[3] = {i % a.nx, (i / a.nx) % a.ny, i / ((int64_t)a.nx * a.ny)};
+        double P0[S][2], U0[S][2];
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int ph = 0; ph < 2; ++ph) {
+                const bool ok = (m >> s) & 1u;
+                const int64_t j = i + (ok ? a.off[s] : 0);
+                P0[s][ph] = ok ? a.vvP[(int64_t)ph * N + j] : 0.0;
+                U0[s][ph] = ok ? a.vvU[(int64_t)ph * N + j] : 0.0;
+            }
+        // phase pressure / upwind term of the cell at slot s, at state stp when s == sp
+        auto pAt = [&](int s, int ph, int sp, int stp) {
+            return s == sp ? a.vvP[((int64_t)stp * 2 + ph) * N + i + a.off[s]] : P0[s][ph];
+        };
+        auto uAt = [&](int s, int ph, int sp, int stp) {
+            return s == sp ? a.vvU[((int64_t)stp * 2 + ph) * N + i + a.off[s]] : U0[s][ph];
+        };
+        auto flux = [&](int f, int ph, int sp, int stp) {
+            double t = 0.0;
+            for (int k = 0; k < a.K; ++k)
+                t += a.coef[((int64_t)f * a.K + k) * N + i] * pAt(a.slotOf[f][k], ph, sp, stp);
+            t += a.cst[((int64_t)f * 2 + ph) * N + i];
+            const int face = f / corners, ax = face >> 1, side = face & 1;
+            int pw = 1;
+            for (int q = 0; q < ax; ++q) pw *= 3;
+            const int so = center + (side ? pw : -pw);
+            const double upIn = uAt(center, ph, sp, stp);
+            double upOut;
+            if ((m >> so) & 1u) upOut = uAt(so, ph, sp, stp);
+            else {
+                int64_t pos = 0, mul = 1;
+                for (int q = 0; q < DIM; ++q)
+                    if (q != ax) {
+                        pos += id[q] * mul;
+                        mul *= q == 0 ? a.nx : q == 1 ? a.ny : a.nz;
+                    }
+                upOut = a.bU[(int64_t)ph * a.nb + a.sideOffset[face] + pos];
+            }
+            double mult;
+            if (signbit(t)) mult = a.w * upOut + (1.0 - a.w) * upIn;
+            else mult = a.w * upIn + (1.0 - a.w) * upOut;
+            return t * mult;
+        };
+        auto residual = [&](int sp, int stp, double* out) {
+            double r0 = 0.0, r1 = 0.0;
+            r0 -= a.srcterm[i];
+            r1 -= a.srcterm[N + i];
+            for (int f = 0; f < a.F; ++f) {
+                if (a.kind[(int64_t)f * N + i] == 1) {
+                    r0 += a.cst[((int64_t)f * 2 + 0) * N + i];
+                    r1 += a.cst[((int64_t)f * 2 + 1) * N + i];
+                    continue;
+                }
+                r0 += flux(f, 0, sp, stp);
+                r1 += flux(f, 1, sp, stp);
+            }
+            if (a.transient) {
+                const int sti = sp == center ? stp : 0;
+                const double V = a.vol[i];
+                double st0 = a.vvS[((int64_t)sti * 2 + 0) * N + i];
+                st0 -= a.stPrev[i];
+                st0 *= V;
+                st0 /= a.dt;
+                double st1 = a.vvS[((int64_t)sti * 2 + 1) * N + i];
+                st1 -= a.stPrev[N + i];
+                st1 *= V;
+                st1 /= a.dt;
+                r0 += st0;
+                r1 += st1;
+            }
+            out[0] = r0;
+            out[1] = r1;
+        };
+        auto partial = [&](int s, int sp, int stp, double* out) {
+            double p0 = 0.0, p1 = 0.0;
+            for (int f = 0; f < a.F; ++f)
+                if (((a.scvfSlots[f] >> s) & 1u) && a.kind[(int64_t)f * N + i] != 1) {
+                    p0 += flux(f, 0, sp, stp);
+                    p1 += flux(f, 1, sp, stp);
+                }
+            out[0] = p0;
+            out[1] = p1;
+        };
+        double r0[2];
+        residual(-1, 0, r0);
+        a.r[i * 2] = r0[0];
+        a.r[i * 2 + 1] = r0[1];
+        if (!jac) continue;
+        for (int s = 0; s < S; ++s) {
+            double blk[4] = {0.0, 0.0, 0.0, 0.0};
+            if ((m >> s) & 1u) {
+                const int64_t j = i + a.off[s];
+                auto eval = [&](int stp, double* out) {
+                    if (s == center) residual(s, stp, out);
+                    else partial(s, s, stp, out);
+                };
+                double f0[2];
+                if (s == center) { f0[0] = r0[0]; f0[1] = r0[1]; }
+                else partial(s, -1, 0, f0);
+                for (int pv = 0; pv < 2; ++pv) {
+                    const double ep = a.eps[(int64_t)pv * N + j];
+                    double d[2];
+                    if (METHOD == 1) {
+                        double fp[2]; eval(1 + pv, fp);
+                        for (int e = 0; e < 2; ++e) d[e] = (fp[e] - f0[e]) / ep;
+                    } else if (METHOD == -1) {
+                        double fm[2]; eval(1 + pv, fm);
+                        for (int e = 0; e < 2; ++e) d[e] = (f0[e] - fm[e]) / ep;
+                    } else if (METHOD == 0) {
+                        double fp[2], fm[2]; eval(1 + SP * pv, fp); eval(2 + SP * pv, fm);
+                        for (int e = 0; e < 2; ++e) d[e] = (fp[e] - fm[e]) / (ep + ep);
+                    } else {
+                        double fp[2], fm[2], fm2[2], fp2[2];
+                        eval(1 + SP * pv, fp); eval(2 + SP * pv, fm); eval(3 + SP * pv, fm2); eval(4 + SP * pv, fp2);
+                        for (int e = 0; e < 2; ++e) d[e] = fivePointMp(fp[e], fm[e], fm2[e], fp2[e], ep);
+                    }
+                    blk[0 * 2 + pv] = d[0];
+                    blk[1 * 2 + pv] = d[1];
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) a.A[((int64_t)s * N + i) * 4 + e] = blk[e];
+        }
+    }
+}
+
+template <int S, int DIM>
+void assemble2p(const MpfaArgs& a, int method, bool jac, cudaStream_t st)
+{
+    const int threads = 128;
+    const int64_t blocks = std::min<int64_t>((a.N + threads - 1) / threads, 152 * 16);
+    const dim3 g((unsigned)std::max<int64_t>(blocks, 1));
+    if (method == 1) mpfa2pKernel<S, DIM, 1><<<g, threads, 0, st>>>(a, jac);
+    else if (method == -1) mpfa2pKernel<S, DIM, -1><<<g, threads, 0, st>>>(a, jac);
+    else if (method == 0) mpfa2pKernel<S, DIM, 0><<<g, threads, 0, st>>>(a, jac);
+    else mpfa2pKernel<S, DIM, 5><<<g, threads, 0, st>>>(a, jac);
+    DXG_CUDA(cudaGetLastError());
+}
+
 template <int S>
 void assembleS(const MpfaArgs& a, int method, bool jac, cudaStream_t st)
 {
@@ -638,6 +802,11 @@ void assembleS(const MpfaArgs& a, int method, bool jac, cudaStream_t st)
 
 void launchMpfaAssemble(const MpfaArgs& a, int method, bool jac, cudaStream_t st)
 {
+    if (a.b == 2) {
+        if (a.S == 9) assemble2p<9, 2>(a, method, jac, st);
+        else assemble2p<27, 3>(a, method, jac, st);
+        return;
+    }
     if (a.S == 9) assembleS<9>(a, method, jac, st);
     else assembleS<27>(a, method, jac, st);
 }

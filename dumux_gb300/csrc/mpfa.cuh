@@ -24,9 +24,11 @@ MpfaLayout mpfaLayout(int dim);
 void mpfaTriples(int dim, int& n, int8_t (*tri)[3]);
 
 // Flux rows of every (cell, scvf): coef[(f*K + k)*N + i] the transmissibility of IV cell k
-// signed for cell i, cst[f*N + i] the IV's Dirichlet and gravity part (or, kind 1, the
-// Neumann flux times area and extrusion), kind[f*N + i] 0 (IV flux) / 1 (Neumann).
-void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t* sideOffset,
+// signed for cell i, cst[(f*b + e)*N + i] the IV's Dirichlet and gravity part of phase e (or,
+// kind 1, the Neumann flux of equation e times area and extrusion), kind[f*N + i] 0 (IV flux)
+// / 1 (Neumann).
+// dirP: 2p, the Dirichlet ghosts' phase pressures [phase][boundary face] (unused for 1p).
+void mpfaTabulate(const dxg_problem_desc* d, const MpfaLayout& L, const int64_t* sideOffset, const double* dirP,
                   std::vector<double>& coef, std::vector<double>& cst, std::vector<int8_t>& kind);
 
 struct MpfaArgs {
@@ -45,8 +47,23 @@ struct MpfaArgs {
     double up = 0.0;                   // density / viscosity: the analytic derivatives' factor
     double baseEps = 1e-10, magnitude = -1.0;
     bool transient = false;
-    double* A = nullptr;               // [S][N]
-    double* r = nullptr;
+    double* A = nullptr;               // [S][N][b*b]
+    double* r = nullptr;               // [N][b]
+    // 2p: the volume variables of every cell at its own and perturbed states (the TPFA
+    // volume-variable kernel's [state][phase][N] arrays), numeric epsilons, previous storage,
+    // cell volumes, the Dirichlet ghosts' upwind terms [phase][boundary face], upwind weight
+    int b = 1;
+    int nx = 1, ny = 1, nz = 1;
+    int64_t nb = 0;
+    int64_t sideOffset[7] = {};
+    const double* vvP = nullptr;
+    const double* vvU = nullptr;
+    const double* vvS = nullptr;
+    const double* eps = nullptr;
+    const double* stPrev = nullptr;
+    const double* vol = nullptr;
+    const double* bU = nullptr;
+    double w = 1.0, dt = 0.0;
 };
 // Residual (and with jac the Jacobian rows: numeric differences, method 1 / -1 / 0 / 5, or
 // the analytic derivatives, method 3).

@@ -255,7 +255,7 @@ constexpr size_t kSwSmemLimit = 200 * 1024;
 // CTAs and whose histories and ring fit the shared memory.
 bool stencilLane2dFits(const StencilArgs& a)
 {
-    if (a.S != 9 || a.nz != 1 || a.ny < 1 || a.nx < 1) return false;
+    if (a.b != 1 || a.S != 9 || a.nz != 1 || a.ny < 1 || a.nx < 1) return false;
     const int ctas = (a.ny + kSwLines - 1) / kSwLines;
     if (ctas > 16) return false;
     const int levels = (a.nx - 1) + 2 * (a.ny - 1) + 1;

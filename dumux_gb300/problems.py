@@ -208,6 +208,25 @@ def dnapl_2p(cells=(64, 64, 32), extent=(6.0, 4.0, 1.0), seed=2, sigma=1.0, corr
     return desc, u0.reshape(-1)
 
 
+def dnapl_2p_mpfa(cells=(12, 8), seed=2, anisotropy=4.0, angle=0.4, **kw):
+    """The 2p water-DNAPL problem of dnapl_2p with a full permeability tensor per cell for the
+    MPFA-O discretization: K_i = k_i R diag(1, 1/anisotropy, 1) R^T with R the rotation by
+    `angle` in the x-z plane (x-y in 2D), k_i the seeded ln K field."""
+    desc, u0 = dnapl_2p(cells=cells, seed=seed, **kw)
+    dim = len(cells)
+    c, s_ = np.cos(angle), np.sin(angle)
+    R = np.eye(dim)
+    v = dim - 1
+    R[0, 0], R[0, v], R[v, 0], R[v, v] = c, -s_, s_, c
+    D = np.ones(dim)
+    D[v] = 1.0 / anisotropy
+    base = R @ np.diag(D) @ R.T
+    Kt = desc.permeability[:, None, None] * base[None, :, :]
+    desc.permeability_tensor = np.ascontiguousarray(Kt.reshape(-1))
+    desc.discretization = 1
+    return desc, u0
+
+
 def ensemble_2p(count=256, seed=4, n_min=16, n_max=64, extent=(6.0, 4.0, 1.0)):
     """Batched ensemble workload: `count` independent 2p DNAPL problems (dnapl_2p) with
     uneven grids, each axis drawn uniformly from the integers n_min..n_max, and per

@@ -93,10 +93,10 @@ typedef struct dxg_problem_desc {
     /* Discretisation of the fluxes: DXG_DISC_TPFA (0, default) two-point flux approximation
      * (discretization/cellcentered/tpfa), or DXG_DISC_MPFA_O (1) the multi-point flux
      * approximation O-method (discretization/cellcentered/mpfa/omethod, flux/ccmpfa/darcyslaw.hh)
-     * with continuity points at the face centres (MPFA.Q = 0), for the 1p model (num_eq == 1)
-     * in FP64 single contexts: one interaction volume per grid vertex, its local flux-continuity
-     * system solved once at upload (the transmissibilities of the incompressible model do not
-     * depend on the solution), a 3^dim-point Jacobian stencil and ILU(0) over it.          */
+     * with continuity points at the face centres (MPFA.Q = 0), for the 1p and 2p models in
+     * FP64 single contexts: one interaction volume per grid vertex, its local flux-continuity
+     * system solved once at upload (the transmissibilities depend on geometry and permeability
+     * only), a 3^dim-point Jacobian stencil and ILU(0) over it.                            */
     int32_t discretization;
     /* Full intrinsic permeability tensor per cell, N*dim*dim values (row-major, symmetric
      * positive definite), or NULL: the isotropic `permeability` above.  MPFA-O only.      */

@@ -706,8 +706,12 @@ static Pattern buildPattern(const Problem& P)
 struct MpIvTerm { int64_t cell; double t; };
 struct MpScvfRow {
     bool neumann = false;
-    double c0 = 0.0;                 // Dirichlet part + gravity (IV faces), flux (Neumann)
+    double c0 = 0.0;                 // 1p: Dirichlet part + gravity (IV faces), flux (Neumann)
+    double c0p[2] = {0.0, 0.0};      // 2p: per phase Dirichlet part + gravity (IV faces)
+    double neu[2] = {0.0, 0.0};      // 2p: per equation Neumann flux * area * extrusion
     std::vector<MpIvTerm> terms;     // IV cells in position order (existing cells only)
+    int64_t outside = -1;            // the cell across the face, or -1 (boundary: bidx)
+    int64_t bidx = -1;
 };
 
 // Gauss-Jordan elimination with partial pivoting: the inverse of A (n x n), in place
@@ -793,7 +797,7 @@ static std::vector<std::vector<MpScvfRow>> mpfaRows(const Problem& P)
                     const Face fc = P.face(cell[f.P], 2 * a + (f.P == f.lo ? 1 : 0));
                     f.bidx = fc.bidx;
                     f.dir = P.d.bc_type[f.bidx] == 1;
-                    f.uD = P.d.bc_values[f.bidx];
+                    f.uD = P.d.bc_values[f.bidx * P.b];
                 }
                 faces.push_back(f);
             }
@@ -880,31 +884,52 @@ static std::vector<std::vector<MpScvfRow>> mpfaRows(const Problem& P)
             for (int fi = 0; fi < nF; ++fi)
                 for (int j = 0; j < nK; ++j) { double s2 = 0.0; for (int k = 0; k < nU; ++k) s2 += CA[(size_t)fi * nU + k] * B[(size_t)k * nK + j]; T[(size_t)fi * nK + j] += s2; }
         }
-        std::vector<double> g(nF, 0.0);
+        // gravity per phase (rho the phase's density, averaged over the face's cells)
+        std::vector<double> gph[2] = {std::vector<double>(nF, 0.0), std::vector<double>(nF, 0.0)};
         if (grav) {
-            std::vector<double> dG(nU, 0.0);
-            for (int fi = 0; fi < nF; ++fi) {
-                const F& f = faces[fi];
-                const double aIn = P.extr(cell[f.P]) * mpVtmv(P, cell[f.P], f.n, P.g);
-                double r = rho;
-                if (!f.dir) {
-                    double d = 0.0; int nOut = 0;
-                    if (!f.bnd) { r += rho; d += P.extr(cell[f.Q]) * mpVtmv(P, cell[f.Q], f.n, P.g); nOut = 1; }
-                    r /= nOut + 1;
-                    d -= aIn;
-                    d *= r * f.area;
-                    dG[f.dof] = d;
+            for (int ph = 0; ph < P.b; ++ph) {
+                const double rhoPh = P.d.density[ph];
+                std::vector<double>& g = gph[ph];
+                std::vector<double> dG(nU, 0.0);
+                for (int fi = 0; fi < nF; ++fi) {
+                    const F& f = faces[fi];
+                    const double aIn = P.extr(cell[f.P]) * mpVtmv(P, cell[f.P], f.n, P.g);
+                    double r = rhoPh;
+                    if (!f.dir) {
+                        double d = 0.0; int nOut = 0;
+                        if (!f.bnd) { r += rhoPh; d += P.extr(cell[f.Q]) * mpVtmv(P, cell[f.Q], f.n, P.g); nOut = 1; }
+                        r /= nOut + 1;
+                        d -= aIn;
+                        d *= r * f.area;
+                        dG[f.dof] = d;
+                    }
+                    g[fi] = aIn * r * f.area;
                 }
-                g[fi] = aIn * r * f.area;
+                for (int fi = 0; fi < nF; ++fi) { double s2 = g[fi]; for (int k = 0; k < nU; ++k) s2 += CA[(size_t)fi * nU + k] * dG[k]; g[fi] = s2; }
             }
-            for (int fi = 0; fi < nF; ++fi) { double s2 = g[fi]; for (int k = 0; k < nU; ++k) s2 += CA[(size_t)fi * nU + k] * dG[k]; g[fi] = s2; }
         }
+        const std::vector<double>& g = gph[0];
+        (void)rho;
         // rows of the scvfs of P (as computed) and of Q (negated)
         for (int fi = 0; fi < nF; ++fi) {
             const F& f = faces[fi];
             double c0 = 0.0;
             for (const F& fd : faces) if (fd.dir) c0 += T[(size_t)fi * nK + fd.kn] * fd.uD;
             c0 += g[fi];
+            // 2p: the Dirichlet ghosts' phase pressures (built with the inside cell's spatial
+            // parameters, elementvolumevariables.hh) and each phase's gravity
+            double c0p[2] = {0.0, 0.0};
+            if (P.b == 2)
+                for (int ph = 0; ph < 2; ++ph) {
+                    double cp = 0.0;
+                    for (const F& fd : faces)
+                        if (fd.dir) {
+                            const VolVars gv = volVars(P, P.d.bc_values + fd.bidx * 2, cell[fd.P]);
+                            cp += T[(size_t)fi * nK + fd.kn] * gv.p[ph];
+                        }
+                    cp += gph[ph][fi];
+                    c0p[ph] = cp;
+                }
             for (int side = 0; side < 2; ++side) {
                 const int q = side == 0 ? f.P : f.Q;
                 if (q < 0) continue;
@@ -921,8 +946,13 @@ static std::vector<std::vector<MpScvfRow>> mpfaRows(const Problem& P)
                     const double sA = area * P.extr(I);
                     row.neumann = true;
                     double qn = 0.0;
-                    qn += P.d.bc_values[fc.bidx] * sA;
+                    qn += P.d.bc_values[fc.bidx * P.b] * sA;
                     row.c0 = qn;
+                    for (int e = 0; e < P.b; ++e) {
+                        double q2 = 0.0;
+                        q2 += P.d.bc_values[fc.bidx * P.b + e] * sA;
+                        row.neu[e] = q2;
+                    }
                     continue;
                 }
                 row.terms.clear();
@@ -932,6 +962,9 @@ static std::vector<std::vector<MpScvfRow>> mpfaRows(const Problem& P)
                         row.terms.push_back({cell[qq], side == 0 ? t : -t});
                     }
                 row.c0 = side == 0 ? c0 : -c0;
+                for (int ph = 0; ph < 2; ++ph) row.c0p[ph] = side == 0 ? c0p[ph] : -c0p[ph];
+                row.outside = fc.boundary ? -1 : fc.outside;
+                row.bidx = fc.boundary ? fc.bidx : -1;
             }
         }
     }
@@ -1034,6 +1067,137 @@ static void mpfaAssemble(const Problem& P, const Pattern& pt, const double* u, d
                 d = fp; d -= fm; d *= 8.0; d += fm2; d -= fp2; d /= 12.0 * eps;
             }
             values[find(J, I)] = d;
+        }
+    }
+}
+
+// The 2p immiscible model (p0s1) with MPFA-O fluxes: per phase the Darcy flux T p_alpha + g_alpha
+// over the IV's cells (the phase pressures of their volume variables) times the upwinded
+// density * mobility (flux/upwindscheme.hh), the source, and the storage of the time
+// derivative; numeric Jacobian column-wise as the reference's local assembler, the element's
+// unknowns perturbed one at a time (cclocalassembler.hh:164-348).
+static void mpfaAssemble2p(const Problem& P, const Pattern& pt, const double* u, const double* uprev, double dt,
+                           double* values, double* r)
+{
+    const auto rows = mpfaRows(P);
+    const int method = P.d.numeric_difference_method;
+    const double w = P.d.upwind_weight;
+    std::vector<VolVars> vv(P.N);
+    for (int64_t c = 0; c < P.N; ++c) vv[c] = volVars(P, u + c * 2, c);
+    auto flux = [&](const MpScvfRow& row, int64_t I, int ph, int64_t pert, const VolVars* vp) {
+        double t = 0.0;
+        for (const MpIvTerm& k : row.terms) t += k.t * (k.cell == pert ? vp->p[ph] : vv[k.cell].p[ph]);
+        t += row.c0p[ph];
+        const VolVars& vin = I == pert ? *vp : vv[I];
+        VolVars gh;
+        const VolVars* vo;
+        if (row.outside >= 0) vo = row.outside == pert ? vp : &vv[row.outside];
+        else {
+            gh = volVars(P, P.d.bc_values + row.bidx * 2, I);
+            vo = &gh;
+        }
+        const double upIn = vin.rho[ph] * vin.mob[ph];
+        const double upOut = vo->rho[ph] * vo->mob[ph];
+        double mult;
+        if (std::signbit(t)) mult = w * upOut + (1.0 - w) * upIn;
+        else mult = w * upIn + (1.0 - w) * upOut;
+        return t * mult;
+    };
+    auto residual = [&](int64_t I, int64_t pert, const VolVars* vp, double* res) {
+        const double V = P.volume(I);
+        double rr[2] = {0.0, 0.0};
+        {
+            double src[2] = {0.0, 0.0};
+            if (P.d.source) for (int e = 0; e < 2; ++e) src[e] += P.d.source[I * 2 + e];
+            const double sV = V * P.extr(I);
+            for (int e = 0; e < 2; ++e) { src[e] *= sV; rr[e] -= src[e]; }
+        }
+        for (const MpScvfRow& row : rows[I]) {
+            if (row.neumann) {
+                for (int e = 0; e < 2; ++e) rr[e] += row.neu[e];
+                continue;
+            }
+            for (int ph = 0; ph < 2; ++ph) rr[ph] += flux(row, I, ph, pert, vp);
+        }
+        if (dt > 0.0) {
+            const VolVars vpr = volVars(P, uprev + I * 2, I);
+            const VolVars& vi = I == pert ? *vp : vv[I];
+            double st[2] = {0.0, 0.0};
+            for (int ph = 0; ph < 2; ++ph) {
+                double prevS = vpr.phi * vpr.rho[ph] * vpr.S[ph];
+                double curS = vi.phi * vi.rho[ph] * vi.S[ph];
+                prevS *= vpr.extr;
+                curS *= vi.extr;
+                curS -= prevS;
+                curS *= V;
+                curS /= dt;
+                st[ph] += curS;
+            }
+            for (int e = 0; e < 2; ++e) rr[e] += st[e];
+        }
+        res[0] = rr[0];
+        res[1] = rr[1];
+    };
+    auto dependsOn = [&](const MpScvfRow& row, int64_t I) {
+        if (row.neumann) return false;
+        for (const MpIvTerm& k : row.terms) if (k.cell == I) return true;
+        return false;
+    };
+    auto neighbourFlux = [&](int64_t J, int64_t I, const VolVars* vp, double* out) {
+        double s2[2] = {0.0, 0.0};
+        for (const MpScvfRow& row : rows[J])
+            if (dependsOn(row, I))
+                for (int ph = 0; ph < 2; ++ph) s2[ph] += flux(row, J, ph, vp ? I : -1, vp);
+        out[0] = s2[0];
+        out[1] = s2[1];
+    };
+    auto find = [&](int64_t row, int64_t c) -> int64_t {
+        for (int64_t k = pt.rowPtr[row]; k < pt.rowPtr[row + 1]; ++k) if (pt.col[k] == c) return k;
+        return -1;
+    };
+    if (values) std::fill(values, values + pt.rowPtr[P.N] * 4, 0.0);
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t I = 0; I < P.N; ++I) {
+        residual(I, -1, nullptr, r + I * 2);
+        if (!values) continue;
+        for (int pv = 0; pv < 2; ++pv) {
+            const double x = u[I * 2 + pv];
+            const double eps = numericEpsilon(P, x, pv);
+            auto state = [&](double q) {
+                double pvq[2] = {u[I * 2], u[I * 2 + 1]};
+                pvq[pv] = q;
+                return volVars(P, pvq, I);
+            };
+            for (int64_t k = pt.rowPtr[I]; k < pt.rowPtr[I + 1]; ++k) {
+                const int64_t J = pt.col[k];
+                auto f = [&](double q, double* o) {
+                    const VolVars vp = state(q);
+                    if (J == I) residual(I, I, &vp, o);
+                    else neighbourFlux(J, I, &vp, o);
+                };
+                double f0[2];
+                if (J == I) { f0[0] = r[I * 2]; f0[1] = r[I * 2 + 1]; }
+                else neighbourFlux(J, I, nullptr, f0);
+                double d[2];
+                if (method == 1) {
+                    double fp[2]; f(x + eps, fp);
+                    for (int e = 0; e < 2; ++e) d[e] = (fp[e] - f0[e]) / eps;
+                } else if (method == -1) {
+                    double fm[2]; f(x - eps, fm);
+                    for (int e = 0; e < 2; ++e) d[e] = (f0[e] - fm[e]) / eps;
+                } else if (method == 0) {
+                    double fp[2], fm[2]; f(x + eps, fp); f(x - eps, fm);
+                    for (int e = 0; e < 2; ++e) d[e] = (fp[e] - fm[e]) / (eps + eps);
+                } else {
+                    double fp[2], fm[2], fm2[2], fp2[2];
+                    f(x + eps, fp); f(x - eps, fm); f(x - 2.0 * eps, fm2); f(x + 2.0 * eps, fp2);
+                    for (int e = 0; e < 2; ++e) {
+                        double t = fp[e]; t -= fm[e]; t *= 8.0; t += fm2[e]; t -= fp2[e]; d[e] = t / (12.0 * eps);
+                    }
+                }
+                const int64_t blk = find(J, I);
+                for (int e = 0; e < 2; ++e) values[blk * 4 + e * 2 + pv] = d[e];
+            }
         }
     }
 }
@@ -1204,7 +1368,8 @@ static void assemble(const Problem& P, const Pattern& pt, const double* u, const
                      double* values, double* r, const uint8_t* colors = nullptr)
 {
     if (P.d.discretization == 1) {
-        mpfaAssemble(P, pt, u, dt, values, r);
+        if (P.b == 2) mpfaAssemble2p(P, pt, u, uprev, dt, values, r);
+        else mpfaAssemble(P, pt, u, dt, values, r);
         return;
     }
     const int b = P.b, bb = b * b, nf = 2 * P.dim;

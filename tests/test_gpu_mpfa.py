@@ -162,3 +162,76 @@ def test_mpfa_degenerate_grids(cells):
     ctx.set_prev_solution(u0)
     assert ctx.newton_solve(0.0, p)["converged"]
     assert np.max(np.abs(ctx.solution() - exact)) <= 1e-12 * np.max(np.abs(exact))
+
+
+@pytest.fixture
+def _cr_pow():
+    prev = oracle.get_pow_mode()
+    oracle.set_pow_mode(oracle.POW_CORRECTLY_ROUNDED)
+    yield
+    oracle.set_pow_mode(prev)
+
+
+@pytest.mark.parametrize("cells", [(7, 5), (5, 4, 3)])
+@pytest.mark.parametrize("method", [1, 0, -1, 5])
+def test_mpfa_2p_residual_and_jacobian_equal_the_oracle(cells, method, _cr_pow):
+    """2p MPFA-O with a rotated anisotropic tensor, gravity, Dirichlet and Neumann faces and
+    the storage term: the device residual and Jacobian blocks bit for bit."""
+    desc, u0 = problems.dnapl_2p_mpfa(cells=cells, seed=5)
+    desc.numeric_difference_method = method
+    u = u0.reshape(-1, 2).copy()
+    u[:, 1] = np.random.default_rng(6).uniform(0.0, 0.5, len(u))
+    u[:, 0] += np.random.default_rng(7).uniform(-100.0, 100.0, len(u))
+    u = u.reshape(-1)
+    ctx = Context(desc)
+    ctx.set_solution(u)
+    ctx.set_prev_solution(u0)
+    ctx.set_time_step(250.0)
+    ctx.assemble_jacobian_and_residual()
+    row_ptr, col, vals = ctx.jacobian()
+    orow, ocol, ovals, r_orc = oracle.assemble(desc, u, u0, 250.0)
+    assert np.array_equal(row_ptr, orow) and np.array_equal(col, ocol)
+    assert np.array_equal(ctx.residual(), r_orc)
+    assert np.array_equal(vals, ovals)
+
+
+def test_mpfa_2p_newton_matches_oracle(_cr_pow):
+    desc, u0 = problems.dnapl_2p_mpfa(cells=(9, 6, 4), seed=8)
+    p = newton_params(linear_reduction=1e-13, linear_max_iter=1000)
+    ctx = Context(desc)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    reps = []
+    dt = 250.0
+    for _ in range(3):
+        reps.append(ctx.newton_solve(dt, p))
+        ctx.advance_time_step()
+        dt = min(ctx.suggest_time_step(reps[-1]["dt_used"], p), 250.0)
+    u_orc, oreps = oracle.time_loop(desc, u0, 250.0, 3, params=p, max_dt=250.0)
+    assert [r["iterations"] for r in reps] == [r["iterations"] for r in oreps]
+    uo, ug = u_orc.reshape(-1, 2), ctx.solution().reshape(-1, 2)
+    assert np.max(np.abs(ug[:, 0] - uo[:, 0])) <= 1e-9 * np.max(np.abs(uo[:, 0]))
+    assert np.max(np.abs(ug[:, 1] - uo[:, 1])) <= 1e-9 * max(1e-3, np.max(np.abs(uo[:, 1])))
+    assert np.max(uo[:, 1]) > 1e-3
+
+
+def test_mpfa_2p_lens_on_the_device_matches_reference_vtu():
+    """test_2p_incompressible_mpfa on the device: the lens to t = 3000 s against the
+    reference file."""
+    from test_oracle_vangenuchten import _compare_with_golden
+    desc, u0 = problems.twop_lens_problem(analytic=False)
+    desc.discretization = 1
+    p = newton_params()
+    ctx = Context(desc)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    t, dt, times = 0.0, 250.0, []
+    while t < 3000.0 - 1e-9:
+        rep = ctx.newton_solve(dt, p)
+        t += rep["dt_used"]
+        times.append(t)
+        ctx.advance_time_step()
+        dt = min(ctx.suggest_time_step(rep["dt_used"], p), 3000.0 - t)
+    assert len(times) == 7 and abs(times[4] - 2054.01) < 5e-3
+    err_p, err_s, small = _compare_with_golden(ctx.solution())
+    assert err_p <= 2e-5 and err_s <= 1e-4 and small <= 1e-6, (err_p, err_s, small)

@@ -131,3 +131,60 @@ def test_mpfa_analytic_jacobian_equals_numeric_differences():
     dl.analytic = True
     p, _ = _linear_step(dl, ul)
     assert np.max(np.abs(p - ref)) <= 0.5 + 1e-9
+
+
+def test_mpfa_2p_lens_matches_reference_vtu():
+    """test/porousmediumflow/2p/incompressible, test_2p_incompressible_mpfa (CMakeLists.txt:
+    93-102): the 2p lens with MPFA-O against the same reference file as the TPFA test, to its
+    print precision; with isotropic cell permeabilities the O-method's fluxes are the
+    two-point ones, so Newton takes the TPFA run's iterations."""
+    from test_oracle_vangenuchten import _compare_with_golden
+    desc, u0 = problems.twop_lens_problem(analytic=False)
+    desc.discretization = 1
+    u, reps = oracle.time_loop(desc, u0, 250.0, 100, newton_params(), t_end=3000.0)
+    times = [r["time"] for r in reps]
+    assert len(times) == 7 and abs(times[-1] - 3000.0) < 1e-6 and abs(times[4] - 2054.01) < 5e-3
+    err_p, err_s, small = _compare_with_golden(u)
+    assert err_p <= 2e-5 and err_s <= 1e-4 and small <= 1e-6, (err_p, err_s, small)
+    dt, ut = problems.twop_lens_problem(analytic=False)
+    ut_end, reps_t = oracle.time_loop(dt, ut, 250.0, 100, newton_params(), t_end=3000.0)
+    assert [r["iterations"] for r in reps] == [r["iterations"] for r in reps_t]
+    assert np.max(np.abs(u - ut_end)) <= 1e-9 * np.max(np.abs(ut_end))
+
+
+@pytest.mark.parametrize("cells", [(6, 5), (4, 3, 3)])
+def test_mpfa_2p_jacobian_equals_central_differences(cells):
+    """2p with a rotated anisotropic tensor, gravity, Dirichlet and Neumann faces, a
+    transient storage term: the Jacobian columns against forward differences of larger steps
+    wherever the residual is smooth (two step sizes agree: upwind switches at near-zero
+    fluxes make it kinked), and Newton from the previous state converging superlinearly."""
+    desc, u0 = problems.dnapl_2p_mpfa(cells=cells, seed=3)
+    u = u0.reshape(-1, 2).copy()
+    u[:, 1] = np.random.default_rng(4).uniform(0.05, 0.5, len(u))
+    u = u.reshape(-1)
+    row_ptr, col, vals, r = oracle.assemble(desc, u, u0, 250.0)
+    n = desc.num_dofs
+    J = np.zeros((n, n))
+    for i in range(desc.num_cells):
+        for k in range(row_ptr[i], row_ptr[i + 1]):
+            J[2 * i:2 * i + 2, 2 * col[k]:2 * col[k] + 2] = vals[4 * k:4 * k + 4].reshape(2, 2)
+    checked = 0
+    for j in range(n):
+        cols = []
+        # forward differences (the side of the assembler's own perturbation: a flux that is
+        # zero at u makes the residual kinked there) with two step sizes
+        for h in ((1e-4, 1e-5) if j % 2 == 0 else (1e-8, 1e-9)):
+            e = np.zeros(n)
+            e[j] = h
+            rp = oracle.assemble(desc, u + e, u0, 250.0, jacobian=False)
+            cols.append((rp - r) / h)
+        scale = np.max(np.abs(J[:, j])) + 1e-300
+        smooth = np.abs(cols[0] - cols[1]) <= 1e-4 * scale
+        np.testing.assert_allclose(J[smooth, j], cols[1][smooth], rtol=1e-3, atol=1e-5 * scale)
+        checked += int(np.count_nonzero(smooth & (J[:, j] != 0)))
+    assert checked > 0.5 * np.count_nonzero(J)
+    p = newton_params(max_relative_shift=1e-10)
+    st, un, rep = oracle.newton_solve(desc, u0, u0, 250.0, p)
+    assert st == 0 and rep["iterations"] <= 8
+    sh = rep["shift"][:rep["iterations"]]
+    assert sh[-1] <= 1e-10 and sh[-1] < 1e-3 * sh[-3]
