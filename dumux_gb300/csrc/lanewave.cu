@@ -2,12 +2,20 @@
 // x-line, one warp per 16 lines, one z-plane (of up to 64 lines) per CTA.
 //
 // On GB300 an FP64 warp instruction holds its SM sub-partition for ~64 cycles whatever the
-// number of active lanes, and a dependent FP64 FMA takes as long: a wavefront level costs
-// about (FP64 instructions one sub-partition issues for it) x 64 cycles.  The cluster
-// wavefront of wave.cu runs one thread per line and 128 lines per CTA: 12 FP64 FMAs per
-// sub-partition per forward level.  Here the two rows of a 2x2 block go to two lanes and a
-// CTA holds one plane of at most 64 lines in 4 warps, one per sub-partition: 6 FMAs per
-// sub-partition and level (8 in the backward sweep with the pivot product), on twice the SMs.
+// number of active lanes, and a dependent FP64 FMA takes as long: a wavefront level costs at
+// least (dependent FP64 instructions of one step) x 64 cycles.  The two rows of a 2x2 block go
+// to two lanes, so a step is one chain of 6 dependent FMAs per lane (forward; 8 backward with
+// the pivot product), and a CTA holds one plane in 4 warps, one per sub-partition.  Everything
+// else a step does is kept short and off that chain:
+//   * the cells' factor rows and right-hand side are loaded PF steps ahead into registers (a
+//     ring unrolled by PF), the entries of missing neighbours as zeros, so the chain has no
+//     branches: a zero multiplier times a zero neighbour value leaves the accumulator's bits
+//     unchanged, so the results are those of the sweeps that skip the term;
+//   * a neighbour value from another warp or CTA is one vector load of both block rows, polled
+//     after the terms that do not need it were issued;
+//   * no vote and no barrier per step: a wait that expires records DXG_ERR_TIMEOUT and sets the
+//     CTA's stop flag, after which every wait of the CTA returns at once (the sweep runs out on
+//     stale values, which the error discards).
 //
 // Dependencies of cell (x, y, z) at level x+y+z: (x-1, y, z), (x, y-1, z), (x, y, z-1) at the
 // level before (forward; mirrored for the backward sweep).
@@ -24,10 +32,8 @@
 // relaxed store, seen whole, so neither side needs a fence, a flag or a barrier per level.  The
 // consumer of a global hand-off puts the pattern back after reading, so every launch starts
 // from it; the shared-memory histories are filled at the start of each launch.
-// No CTA-wide barrier inside the level loop: warps advance on their own and wait only for the
-// data they consume.  Producers always have lower CTA indices than their consumers.  Every
-// wait has a time limit; on expiry the kernel records DXG_ERR_TIMEOUT, stops all its warps and
-// drains its copies before it leaves.
+// Warps advance on their own and wait only for the data they consume.  Producers always have
+// lower CTA indices than their consumers.
 //
 // The arithmetic per row and cell is the one of wave.cu and of the level-scheduled kernels of
 // linalg.cu (same operands, same order, explicit FMAs), so all give the same sweep results.
@@ -53,17 +59,22 @@ constexpr int kLwTile = kLwWarps * kLwLinesPerWarp;   // lines of one CTA
 constexpr int kLwThreads = kLwWarps * 32;
 constexpr size_t kLwSmemLimit = 220 * 1024;
 
-// Elements of a prefetched record: forward L_x, L_y, L_z rows and d; backward U_x, U_y,
-// U_z rows, the pivot-inverse row and v.
-template <int DIR>
-struct LwRec {
-    static constexpr int n = DIR > 0 ? 8 : 10;
+// both rows of a block-vector entry, or one row of a 2x2 block
+template <class T>
+struct LwPair;
+template <>
+struct LwPair<double> {
+    using type = double2;
+};
+template <>
+struct LwPair<float> {
+    using type = float2;
 };
 
 struct LwSmem {
-    size_t zin, ybuf, yin, ring, total;
+    size_t zin, ybuf, yin, total;
 };
-__host__ __device__ inline LwSmem lwSmem(int nx, int levels, int tsize, int recElems, int pf)
+__host__ __device__ inline LwSmem lwSmem(int nx, int levels, int tsize)
 {
     LwSmem s{};
     size_t o = 0;
@@ -73,10 +84,7 @@ __host__ __device__ inline LwSmem lwSmem(int nx, int levels, int tsize, int recE
     o += (size_t)kLwWarps * levels * 2 * tsize;
     s.yin = o;
     o += (size_t)levels * 2 * tsize;
-    o = (o + 15) & ~(size_t)15;
-    s.ring = o;
-    o += (size_t)pf * kLwThreads * recElems * tsize;
-    s.total = o;
+    s.total = (o + 15) & ~(size_t)15;
     return s;
 }
 
@@ -93,24 +101,17 @@ __device__ __forceinline__ uint32_t lwMapa(uint32_t addr, int rank)
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
     return r;
 }
-// relaxed store into the shared memory of a CTA of the cluster, and its reading
+// The hand-off stores and polls carry no "memory" clobber: they need no order against the
+// step's other memory operations (a poll issued early sees the empty pattern and repeats;
+// volatile keeps every poll), so the compiler may schedule the record loads across them.
+// relaxed store into the shared memory of a CTA of the cluster
 template <class T>
 __device__ __forceinline__ void lwStRemote(uint32_t dst, T v)
 {
     if constexpr (sizeof(T) == 8)
-        asm volatile("st.relaxed.cluster.shared::cluster.f64 [%0], %1;" ::"r"(dst), "d"(v) : "memory");
+        asm volatile("st.relaxed.cluster.shared::cluster.f64 [%0], %1;" ::"r"(dst), "d"(v));
     else
-        asm volatile("st.relaxed.cluster.shared::cluster.f32 [%0], %1;" ::"r"(dst), "f"(v) : "memory");
-}
-template <class T>
-__device__ __forceinline__ T lwLdRelaxedShared(const T* p)
-{
-    T v;
-    if constexpr (sizeof(T) == 8)
-        asm volatile("ld.relaxed.cluster.shared::cta.f64 %0, [%1];" : "=d"(v) : "r"(lwSmemAddr(p)) : "memory");
-    else
-        asm volatile("ld.relaxed.cluster.shared::cta.f32 %0, [%1];" : "=f"(v) : "r"(lwSmemAddr(p)) : "memory");
-    return v;
+        asm volatile("st.relaxed.cluster.shared::cluster.f32 [%0], %1;" ::"r"(dst), "f"(v));
 }
 // The "not written yet" pattern of the hand-off histories: all bits set (a NaN that no
 // arithmetic yields; cudaMemset with 0xff produces it).
@@ -127,49 +128,102 @@ __device__ __forceinline__ bool lwIsEmpty(T v)
     else return __float_as_int(v) == -1;
 }
 template <class T>
-__device__ __forceinline__ T lwLdRelaxedGpu(const T* p)
+__device__ __forceinline__ bool lwPairEmpty(typename LwPair<T>::type v)
 {
-    T v;
-    if constexpr (sizeof(T) == 8) asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
-    else asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return lwIsEmpty<T>(v.x) || lwIsEmpty<T>(v.y);
+}
+// one relaxed vector load of a pair from this CTA's shared memory / from global memory (each
+// half is one single-copy-atomic element)
+template <class T>
+__device__ __forceinline__ typename LwPair<T>::type lwLdPairShared(const T* p)
+{
+    typename LwPair<T>::type v;
+    if constexpr (sizeof(T) == 8)
+        asm volatile("ld.relaxed.cluster.shared::cta.v2.f64 {%0, %1}, [%2];"
+                     : "=d"(v.x), "=d"(v.y)
+                     : "r"(lwSmemAddr(p)));
+    else
+        asm volatile("ld.relaxed.cluster.shared::cta.v2.f32 {%0, %1}, [%2];"
+                     : "=f"(v.x), "=f"(v.y)
+                     : "r"(lwSmemAddr(p)));
+    return v;
+}
+template <class T>
+__device__ __forceinline__ typename LwPair<T>::type lwLdPairGpu(const T* p)
+{
+    typename LwPair<T>::type v;
+    if constexpr (sizeof(T) == 8)
+        asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+    else
+        asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
     return v;
 }
 template <class T>
 __device__ __forceinline__ void lwStRelaxedGpu(T* p, T v)
 {
-    if constexpr (sizeof(T) == 8) asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
-    else asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+    if constexpr (sizeof(T) == 8) asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v));
+    else asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v));
 }
-template <int BYTES>
-__device__ __forceinline__ void lwCpAsync(uint32_t dst, const void* src)
+// putting the empty pattern back must stay behind the warp barrier that follows the reads
+template <class T>
+__device__ __forceinline__ void lwStPairGpu(T* p, T x, T y)
 {
-    if constexpr (BYTES == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+    if constexpr (sizeof(T) == 8)
+        asm volatile("st.relaxed.gpu.global.v2.f64 [%0], {%1, %2};" ::"l"(p), "d"(x), "d"(y) : "memory");
+    else
+        asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(x), "f"(y) : "memory");
 }
-__device__ __forceinline__ void lwCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void lwCpWait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+// read-only loads of the records (the factor, pivots and the sweep's input vector)
+template <class T>
+__device__ __forceinline__ typename LwPair<T>::type lwLdg2(const T* p)
+{
+    return __ldg(reinterpret_cast<const typename LwPair<T>::type*>(p));
+}
+
+// The slow path of a poll: waits, bounded, until neither half of the pair at p holds the empty
+// pattern, and returns it.  Returns zeros once the CTA's sweep has stopped or when the wait
+// expires (which records DXG_ERR_TIMEOUT and stops the CTA's sweep).
+template <class T>
+__device__ __noinline__ typename LwPair<T>::type lwWaitPair(const T* p, bool global, int* stop, int* err,
+                                                          unsigned long long waitNs)
+{
+    using P = typename LwPair<T>::type;
+    const unsigned long long deadline = lwTimer() + waitNs;
+    for (;;) {
+        const P v = global ? lwLdPairGpu(p) : lwLdPairShared(p);
+        if (!lwPairEmpty<T>(v)) return v;
+        if (*(volatile int*)stop) break;
+        if (lwTimer() > deadline) {
+            atomicExch(err, DXG_ERR_TIMEOUT);
+            *(volatile int*)stop = 1;
+            break;
+        }
+    }
+    P zero;
+    zero.x = 0;
+    zero.y = 0;
+    return zero;
+}
 
 }  // namespace
 
 // One sweep: DIR +1 forward (z_i = d_i - L_ix z_x - L_iy z_y - L_iz z_z), DIR -1 backward
-// (y_i = D_i^-1 (v_i - U_ix y_x - U_iy y_y - U_iz y_z), in place in v).
+// (y_i = D_i^-1 (v_i - U_ix y_x - U_iy y_y - U_iz y_z), in place in v).  PF: depth of the
+// register ring of prefetched records.
 template <class T, int DIR, int PF>
 __global__ void __launch_bounds__(kLwThreads) laneWaveKernel(LaneWaveArgs<T> a)
 {
-    constexpr int REC = LwRec<DIR>::n;
-    constexpr int RB = 2 * (int)sizeof(T);   // bytes of one block row
+    using P = typename LwPair<T>::type;
     extern __shared__ __align__(16) unsigned char lwRaw[];
-    __shared__ int abortFlag;
+    __shared__ int stopFlag;
 
     cg::cluster_group cluster = cg::this_cluster();
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int levels = nx + ny + nz - 2;
-    const LwSmem lay = lwSmem(nx, levels, (int)sizeof(T), REC, PF);
+    const LwSmem lay = lwSmem(nx, levels, (int)sizeof(T));
     T* zin = reinterpret_cast<T*>(lwRaw + lay.zin);     // [nx][kLwTile][2]
     T* ybuf = reinterpret_cast<T*>(lwRaw + lay.ybuf);   // [kLwWarps][levels][2]
     T* yin = reinterpret_cast<T*>(lwRaw + lay.yin);     // [levels][2]
-    T* ring = reinterpret_cast<T*>(lwRaw + lay.ring);   // [PF][kLwThreads][REC]
 
     const int cta = (int)blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -205,20 +259,10 @@ __global__ void __launch_bounds__(kLwThreads) laneWaveKernel(LaneWaveArgs<T> a)
     for (int k = threadIdx.x; k < kLwWarps * levels * 2; k += kLwThreads) ybuf[k] = lwEmpty<T>();
     if (hasYUp)
         for (int k = threadIdx.x; k < levels * 2; k += kLwThreads) yin[k] = lwEmpty<T>();
-    if (threadIdx.x == 0) abortFlag = 0;
+    if (threadIdx.x == 0) stopFlag = 0;
     cluster.sync();
     const bool skip = a.ks && a.ks->status != KS_RUNNING;
 
-    const uint32_t zinDown = zDownLocal ? lwMapa(lwSmemAddr(zin), zDown % cs) : 0u;
-    const uint32_t yinDown = hasYDown ? lwMapa(lwSmemAddr(yin), (cta + 1) % cs) : 0u;
-
-    // cell of step s on this lane's line (sweep x), or -1
-    const int sx0 = Lfirst - sy - sz;
-    auto cellX = [&](int s) -> int {
-        const int sx = sx0 + s;
-        return (lineOk && s < nSteps && sx >= 0 && sx < nx) ? sx : -1;
-    };
-    auto cellIndex = [&](int sx) -> int64_t { return lineBase + (DIR > 0 ? sx : nx - 1 - sx); };
     // record sources of this lane's line at x = 0 (slots: forward -x 2, -y 1, -z 0; backward
     // +x 4, +y 5, +z 6); a cell adds 4 (blocks) or 2 (vectors) elements per x
     const T* mat = DIR > 0 ? a.Lf : a.A;
@@ -227,155 +271,138 @@ __global__ void __launch_bounds__(kLwThreads) laneWaveKernel(LaneWaveArgs<T> a)
     const T* srcZ = mat + ((int64_t)(DIR > 0 ? 0 : 6) * N + lineBase) * 4 + 2 * r;
     const T* srcD = a.Dinv + lineBase * 4 + 2 * r;
     const T* srcV = (DIR > 0 ? a.rhs : a.v) + lineBase * 2 + r;
-    const uint32_t ringBase = lwSmemAddr(ring + (size_t)threadIdx.x * REC);
-    // copies of the records of step s into ring slot s % PF
-    auto issue = [&](int s) {
-        const int sx = cellX(s);
-        if (sx >= 0) {
-            const int x = DIR > 0 ? sx : nx - 1 - sx;
-            const uint32_t rec = ringBase + (uint32_t)((s % PF) * kLwThreads * REC * (int)sizeof(T));
-            if (sx > 0) lwCpAsync<RB>(rec + 0 * RB, srcX + 4 * x);
-            if (sy > 0) lwCpAsync<RB>(rec + 1 * RB, srcY + 4 * x);
-            if (sz > 0) lwCpAsync<RB>(rec + 2 * RB, srcZ + 4 * x);
-            if (DIR > 0) {
-                lwCpAsync<(int)sizeof(T)>(rec + 3 * RB, srcV + 2 * x);
-            } else {
-                lwCpAsync<RB>(rec + 3 * RB, srcD + 4 * x);
-                lwCpAsync<(int)sizeof(T)>(rec + 4 * RB, srcV + 2 * x);
-            }
-        }
-        lwCommit();
-    };
-    // inter-cluster hand-off entries of this lane's line
-    const T* zGlobal = a.handoff + ((size_t)cta * nx * kLwTile + jl) * 2;
-    // bounded wait; false when it gave up or another warp stopped the sweep
-    auto waitFor = [&](auto&& ready) -> bool {
-        if (ready()) return true;
-        const unsigned long long deadline = lwTimer() + a.waitNs;
-        while (!ready()) {
-            if (*(volatile int*)&abortFlag) return false;
-            if (lwTimer() > deadline) {
-                atomicExch(a.err, DXG_ERR_TIMEOUT);
-                abortFlag = 1;
-                return false;
-            }
-        }
-        return true;
+    const bool hasY = sy > 0, hasZ = sz > 0;
+
+    // where the neighbour values from other warps and CTAs arrive (pairs of both rows) ...
+    const bool zGlobalIn = hasZUp && !zUpLocal;
+    const bool zLocalIn = hasZUp && zUpLocal;
+    const bool yPoll = lineOk && j == 0 && hasY;   // warp > 0: ybuf; warp 0 with sy > 0: yin
+    const T* yPollSrc = warp > 0 ? ybuf + (size_t)(warp - 1) * levels * 2 : yin;   // + level * 2
+    const T* zLocalSrc = zin + (size_t)jl * 2;                                       // + x * kLwTile * 2
+    const T* zGlobalSrc = a.handoff + ((size_t)cta * nx * kLwTile + jl) * 2;         // + x * kLwTile * 2
+    // ... and where this lane's results go (one row each)
+    T* const zGlobalDst = hasZDown && !zDownLocal ? a.handoff + ((size_t)zDown * nx * kLwTile + jl) * 2 + r : nullptr;
+    const uint32_t zInDownBase =
+        (zDownLocal ? lwMapa(lwSmemAddr(zin), zDown % cs) : 0u) + (uint32_t)(((size_t)jl * 2 + r) * sizeof(T));
+    const bool yPub = j == kLwLinesPerWarp - 1 && (warp < kLwWarps - 1 || hasYDown);
+    const uint32_t yPubBase = (warp < kLwWarps - 1 ? lwSmemAddr(ybuf + (size_t)warp * levels * 2)
+                                                   : (hasYDown ? lwMapa(lwSmemAddr(yin), (cta + 1) % cs) : 0u)) +
+                              (uint32_t)(r * sizeof(T));
+
+    // the register ring: records of step s in entry (s - first step) % PF
+    P rX[PF], rY[PF], rZ[PF], rD[PF];
+    T rV[PF];
+    auto load = [&](int s, int k) {
+        const int sx = s - jl;
+        const bool act = lineOk && sx >= 0 && sx < nx;
+        const int x = DIR > 0 ? sx : nx - 1 - sx;
+        P zero;
+        zero.x = 0;
+        zero.y = 0;
+        rX[k] = act && sx > 0 ? lwLdg2(srcX + 4 * x) : zero;
+        rY[k] = act && hasY ? lwLdg2(srcY + 4 * x) : zero;
+        rZ[k] = act && hasZ ? lwLdg2(srcZ + 4 * x) : zero;
+        if (DIR < 0) rD[k] = act ? lwLdg2(srcD + 4 * x) : zero;
+        rV[k] = act ? __ldg(srcV + 2 * x) : T(0);
     };
 
     const bool warpWorks = working && !skip && sy0 + warp * kLwLinesPerWarp < ny;
     if (warpWorks) {
-#pragma unroll
-        for (int s = 0; s < PF; ++s) issue(s);
+        // line jl starts at step jl; the warp's lines are done after its last line's nx cells
+        const int sBegin = warp * kLwLinesPerWarp;
+        const int sEnd = min(nSteps, sBegin + kLwLinesPerWarp - 1 + nx);
         T prev = 0;
-        // inter-cluster z values: loaded one step ahead, so the load's latency overlaps the
-        // step before (an early load that still saw the empty pattern is repeated)
-        T gz0 = lwEmpty<T>(), gz1 = lwEmpty<T>();
-        const bool zGlobalIn = hasZUp && !zUpLocal;
-        if (zGlobalIn && cellX(0) >= 0) {
-            gz0 = lwLdRelaxedGpu(zGlobal + (size_t)cellX(0) * kLwTile * 2);
-            gz1 = lwLdRelaxedGpu(zGlobal + (size_t)cellX(0) * kLwTile * 2 + 1);
-        }
-        for (int s = 0; s < nSteps; ++s) {
+        // the inter-cluster z pair of the next step, loaded a step early (a load that still saw
+        // the empty pattern is repeated by the poll)
+        P gz;
+        gz.x = lwEmpty<T>();
+        gz.y = gz.x;
+        if (zGlobalIn && lineOk && sBegin - jl >= 0) gz = lwLdPairGpu(zGlobalSrc + (size_t)(sBegin - jl) * kLwTile * 2);
+
+        auto step = [&](int s, int k) {
+            const int sx = s - jl;
+            const bool act = lineOk && sx >= 0 && sx < nx;
             const int L = Lfirst + s;
-            const int sx = cellX(s);
-            const bool active = sx >= 0;
-            lwCpWait<PF - 1>();
+            // this step's records out of the ring, whose entry is refilled right away (the
+            // loads issue ahead of the step's dependent chain; measured faster than refilling
+            // after the step)
+            const P cX = rX[k], cY = rY[k], cZ = rZ[k];
+            P cD;
+            if (DIR < 0) cD = rD[k];
+            const T cV = rV[k];
+            load(s + PF, k);
             // x neighbour: this line's previous cell (other row from the partner lane); y
-            // neighbour: line j-1 at the level before (same row two lanes down, other row from
+            // neighbour: line j-1 at the step before (same row two lanes down, other row from
             // lane 2j-2+(1-r)); three independent shuffles of the previous results
             const T other = __shfl_xor_sync(0xffffffffu, prev, 1);
             const T ySame = __shfl_up_sync(0xffffffffu, prev, 2);
             const T yOther = __shfl_sync(0xffffffffu, prev, (lane - 1 - 2 * r) & 31);
-            const T zx0 = r == 0 ? prev : other, zx1 = r == 0 ? other : prev;
-            T zy0 = r == 0 ? ySame : yOther, zy1 = r == 0 ? yOther : ySame;
+            T acc = cV;
+            acc = fma(-cX.x, r == 0 ? prev : other, acc);
+            acc = fma(-cX.y, r == 0 ? other : prev, acc);
+            T zy0 = hasY ? (r == 0 ? ySame : yOther) : T(0);
+            T zy1 = hasY ? (r == 0 ? yOther : ySame) : T(0);
+            if (act && yPoll) {
+                const T* src = yPollSrc + (size_t)(L - 1) * 2;
+                P v = lwLdPairShared(src);
+                if (lwPairEmpty<T>(v)) v = lwWaitPair(src, false, &stopFlag, a.err, a.waitNs);
+                zy0 = v.x;
+                zy1 = v.y;
+            }
+            acc = fma(-cY.x, zy0, acc);
+            acc = fma(-cY.y, zy1, acc);
             T zz0 = 0, zz1 = 0;
-            bool ok = true;
-            if (active && j == 0 && sy > 0 && (warp > 0 || hasYUp)) {
-                const T* src = warp > 0 ? ybuf + ((size_t)(warp - 1) * levels + (L - 1)) * 2 : yin + (size_t)(L - 1) * 2;
-                ok = waitFor([&] {
-                    zy0 = lwLdRelaxedShared(src);
-                    zy1 = lwLdRelaxedShared(src + 1);
-                    return !lwIsEmpty(zy0) && !lwIsEmpty(zy1);
-                });
-            }
-            if (hasZUp && active) {
-                if (zUpLocal) {
-                    const T* src = zin + ((size_t)sx * kLwTile + jl) * 2;
-                    ok = waitFor([&] {
-                        zz0 = lwLdRelaxedShared(src);
-                        zz1 = lwLdRelaxedShared(src + 1);
-                        return !lwIsEmpty(zz0) && !lwIsEmpty(zz1);
-                    }) && ok;
-                } else {
-                    const T* src = zGlobal + (size_t)sx * kLwTile * 2;
-                    zz0 = gz0;
-                    zz1 = gz1;
-                    if (lwIsEmpty(zz0) || lwIsEmpty(zz1))
-                        ok = waitFor([&] {
-                            zz0 = lwLdRelaxedGpu(src);
-                            zz1 = lwLdRelaxedGpu(src + 1);
-                            return !lwIsEmpty(zz0) && !lwIsEmpty(zz1);
-                        }) && ok;
+            if (zLocalIn) {
+                if (act) {
+                    const T* src = zLocalSrc + (size_t)sx * kLwTile * 2;
+                    P v = lwLdPairShared(src);
+                    if (lwPairEmpty<T>(v)) v = lwWaitPair(src, false, &stopFlag, a.err, a.waitNs);
+                    zz0 = v.x;
+                    zz1 = v.y;
                 }
-            }
-            if (zGlobalIn) {
-                const int sxn = cellX(s + 1);
-                if (sxn >= 0) {
-                    gz0 = lwLdRelaxedGpu(zGlobal + (size_t)sxn * kLwTile * 2);
-                    gz1 = lwLdRelaxedGpu(zGlobal + (size_t)sxn * kLwTile * 2 + 1);
+            } else if (zGlobalIn) {
+                const T* src = zGlobalSrc + (int64_t)sx * kLwTile * 2;
+                if (act) {
+                    P v = gz;
+                    if (lwPairEmpty<T>(v)) v = lwWaitPair(src, true, &stopFlag, a.err, a.waitNs);
+                    zz0 = v.x;
+                    zz1 = v.y;
                 }
+                if (lineOk && sx + 1 >= 0 && sx + 1 < nx) gz = lwLdPairGpu(src + kLwTile * 2);
+                // both lanes of the line hold the pair: put the empty pattern back
+                __syncwarp();
+                if (act && r == 0) lwStPairGpu(const_cast<T*>(src), lwEmpty<T>(), lwEmpty<T>());
             }
-            if (__any_sync(0xffffffffu, !ok)) break;
-            // both lanes of the line hold the inter-cluster values: restore the pattern
-            if (zGlobalIn && active && r == 0) {
-                T* src = a.handoff + (((size_t)cta * nx + sx) * kLwTile + jl) * 2;
-                lwStRelaxedGpu(src, lwEmpty<T>());
-                lwStRelaxedGpu(src + 1, lwEmpty<T>());
-            }
-            const T* rec = ring + ((size_t)(s % PF) * kLwThreads + threadIdx.x) * REC;
-            T acc = 0;
-            if (active) {
-                acc = rec[DIR > 0 ? 6 : 8];
-                if (sx > 0) {
-                    acc = fma(-rec[0], zx0, acc);
-                    acc = fma(-rec[1], zx1, acc);
-                }
-                if (sy > 0) {
-                    acc = fma(-rec[2], zy0, acc);
-                    acc = fma(-rec[3], zy1, acc);
-                }
-                if (sz > 0) {
-                    acc = fma(-rec[4], zz0, acc);
-                    acc = fma(-rec[5], zz1, acc);
-                }
-            }
+            acc = fma(-cZ.x, zz0, acc);
+            acc = fma(-cZ.y, zz1, acc);
             T res = acc;
             if (DIR < 0) {
                 const T accOther = __shfl_xor_sync(0xffffffffu, acc, 1);
                 const T a0 = r == 0 ? acc : accOther, a1 = r == 0 ? accOther : acc;
-                T t = rec[6] * a0;
-                t = fma(rec[7], a1, t);
+                T t = cD.x * a0;
+                t = fma(cD.y, a1, t);
                 res = t;
             }
-            if (active) {
-                const int64_t i = cellIndex(sx);
-                a.v[i * 2 + r] = res;
+            if (act) {
+                const int x = DIR > 0 ? sx : nx - 1 - sx;
+                a.v[(lineBase + x) * 2 + r] = res;
                 if (zDownLocal)
-                    lwStRemote<T>(zinDown + (uint32_t)((((size_t)sx * kLwTile + jl) * 2 + r) * sizeof(T)), res);
+                    lwStRemote<T>(zInDownBase + (uint32_t)((size_t)sx * kLwTile * 2 * sizeof(T)), res);
                 else if (hasZDown)
-                    lwStRelaxedGpu(a.handoff + (((size_t)zDown * nx + sx) * kLwTile + jl) * 2 + r, res);
-                if (j == kLwLinesPerWarp - 1) {
-                    if (warp < kLwWarps - 1)
-                        lwStRemote<T>(lwSmemAddr(&ybuf[((size_t)warp * levels + L) * 2 + r]), res);
-                    else if (hasYDown)
-                        lwStRemote<T>(yinDown + (uint32_t)(((size_t)L * 2 + r) * sizeof(T)), res);
-                }
+                    lwStRelaxedGpu(zGlobalDst + (size_t)sx * kLwTile * 2, res);
+                if (yPub) lwStRemote<T>(yPubBase + (uint32_t)((size_t)L * 2 * sizeof(T)), res);
                 prev = res;
             }
-            issue(s + PF);
+        };
+
+#pragma unroll
+        for (int k = 0; k < PF; ++k) load(sBegin + k, k);
+        for (int s0 = sBegin; s0 < sEnd; s0 += PF) {
+#pragma unroll
+            for (int k = 0; k < PF; ++k) {
+                step(s0 + k, k);
+            }
         }
-        lwCpWait<0>();
     }
     // no CTA may leave while another can still write into its shared memory
     cluster.sync();
@@ -388,7 +415,7 @@ template <class T, int DIR, int PF>
 cudaError_t lwLaunchOne(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
 {
     auto kern = laneWaveKernel<T, DIR, PF>;
-    const size_t smem = lwSmem(a.nx, a.nx + a.ny + a.nz - 2, (int)sizeof(T), LwRec<DIR>::n, PF).total;
+    const size_t smem = lwSmem(a.nx, a.nx + a.ny + a.nz - 2, (int)sizeof(T)).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLwSmemLimit);
@@ -420,23 +447,11 @@ cudaError_t lwDispatch(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_t
 {
     const int pf = DIR > 0 ? p.pfFwd : p.pfBwd;
     switch (pf) {
-        case 8: return lwLaunchOne<T, DIR, 8>(p, a, st, query, fits);
         case 4: return lwLaunchOne<T, DIR, 4>(p, a, st, query, fits);
-        case 2: return lwLaunchOne<T, DIR, 2>(p, a, st, query, fits);
         default:
             if (fits) *fits = 0;
             return query ? cudaSuccess : cudaErrorInvalidConfiguration;
     }
-}
-
-template <class T>
-int lwDepth(int nx, int levels, int dir)
-{
-    for (int pf : {8, 4, 2}) {
-        const size_t sm = lwSmem(nx, levels, (int)sizeof(T), dir > 0 ? LwRec<1>::n : LwRec<-1>::n, pf).total;
-        if (sm <= kLwSmemLimit) return pf;
-    }
-    return 0;
 }
 
 }  // namespace
@@ -450,9 +465,11 @@ LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b)
     if (p.nyb > 16) return p;
     p.ctas = nz * p.nyb;
     const int levels = nx + ny + nz - 2;
-    p.pfFwd = lwDepth<T>(nx, levels, 1);
-    p.pfBwd = lwDepth<T>(nx, levels, -1);
-    if (!p.pfFwd || !p.pfBwd) return p;
+    if (lwSmem(nx, levels, (int)sizeof(T)).total > kLwSmemLimit) return p;
+    // register ring depth 4: measured on GB300 at 64x64x32 (FP64, per apply): 0.195 ms with
+    // depth 4, 0.194 ms with 5, 0.201 ms with 3, 0.223 ms with 6 (spills)
+    p.pfFwd = 4;
+    p.pfBwd = 4;
     LaneWaveArgs<T> dummy{};
     dummy.nx = nx;
     dummy.ny = ny;
