@@ -30,6 +30,7 @@ UNITS = {
     "amg.cu": [],
     "mpfa.cu": ["--fmad=false"],
     "stencilwave.cu": [],
+    "stencillane.cu": [],
 }
 
 

@@ -913,17 +913,18 @@ MpfaArgs mpfaArgs(const dxg_ctx* c)
 
 // The MPFA-O preconditioner apply: 1 the one-CTA line sweeps (2D with up to 1024 lines:
 // DXG_ILU_WAVEFRONT or auto), 2 the cluster line sweeps (2D: DXG_ILU_LANES, or auto beyond
-// 1024 lines), 0 the level-by-level kernel (3D, DXG_ILU_LEVELS, or when neither fits).  On
-// 256 x 256 the one-CTA sweeps took 1.09 ms per apply, the cluster sweeps (two CTAs, polled
-// hand-offs between warps) 1.0-2.4 ms.
+// 1024 lines), 3 the 3D cluster sweeps (one z-plane per CTA: DXG_ILU_LANES or auto), 0 the
+// level-by-level kernel (DXG_ILU_LEVELS, or when none fits).  On 256 x 256 the one-CTA sweeps
+// took 1.09 ms per apply, the cluster sweeps (two CTAs, polled hand-offs between warps)
+// 1.0-2.4 ms.
 int mpfaSweep(const dxg_ctx* c, const StencilArgs& sa)
 {
-    const bool lanes = stencilLane2dFits(sa), wave = stencilWave2dFits(sa);
+    const bool lanes = stencilLane2dFits(sa), wave = stencilWave2dFits(sa), lanes3 = stencilLane3dFits(sa);
     switch (c->iluKernel) {
     case DXG_ILU_LEVELS: return 0;
-    case DXG_ILU_LANES: return lanes ? 2 : 0;
+    case DXG_ILU_LANES: return lanes ? 2 : lanes3 ? 3 : 0;
     case DXG_ILU_WAVEFRONT: return wave ? 1 : 0;
-    default: return wave ? 1 : lanes ? 2 : 0;
+    default: return wave ? 1 : lanes ? 2 : lanes3 ? 3 : 0;
     }
 }
 
@@ -1348,6 +1349,7 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
             if (c->mpfa) {
                 TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep);
                 switch (mpfaSweep(c, sa)) {
+                case 3: launchStencilLane3d(sa, in, yOut, st); return 2;
                 case 2: launchStencilLane2d(sa, in, yOut, st); return 2;
                 case 1: launchStencilWave2d(sa, in, yOut, st); return 2;
                 default: launchStencilApplyLevels(sa, in, yOut, st); return 1;
@@ -2020,7 +2022,10 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
         sa.nz = c->pcHost.nz;
         const int k = mpfaSweep(c, sa);
         out = std::string("MPFA-O, ") + std::to_string(c->mpLayout.S) + "-point stencil; ILU(0): natural order, " +
-              (k == 2   ? "line sweeps (one thread per grid line, levels x+2y) over a cluster of " +
+              (k == 3   ? "line sweeps (one lane per grid line and block row, levels x+2y+4z), one z-plane "
+                          "per CTA over a cluster of " +
+                            std::to_string(sa.nz) + " CTAs"
+               : k == 2 ? "line sweeps (one thread per grid line, levels x+2y) over a cluster of " +
                             std::to_string((sa.ny + 127) / 128) + " CTAs"
                : k == 1 ? "line sweeps (one thread per grid line, levels x+2y) in one CTA"
                         : "hyperplanes x+2y+4z level by level in one CTA");

@@ -153,6 +153,10 @@ bool stencilWave2dFits(const StencilArgs& a);
 // warps, point-to-point hand-offs through shared-memory histories
 bool stencilLane2dFits(const StencilArgs& a);
 void launchStencilLane2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+// 3D 27-point sweeps over a cluster (stencillane.cu): one z-plane per CTA (nz <= 16), one lane
+// per grid line and block row
+bool stencilLane3dFits(const StencilArgs& a);
+void launchStencilLane3d(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
 
 template <class MT, class VT, class XT = VT>
 void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);

@@ -123,6 +123,65 @@ def test_mpfa_line_sweeps_equal_level_kernel(cells):
         assert np.array_equal(out[kind][1], out["levels"][1])
 
 
+@pytest.mark.parametrize("b,cells", [(1, (9, 7, 5)), (1, (6, 40, 3)), (1, (5, 5, 16)), (1, (4, 3, 20)),
+                                     (2, (8, 6, 5)), (2, (6, 20, 4)), (2, (10, 40, 3)), (2, (32, 32, 16))])
+def test_mpfa_3d_line_sweeps_equal_level_kernel(b, cells):
+    """The 3D sweeps over a cluster (one z-plane per CTA, one lane per grid line and block
+    row; (6, 40, 3) and (6, 20, 4) with b = 2 hand line histories between warps, (5, 5, 16) fills
+    a 16-CTA cluster) and the level-by-level kernel compute the same preconditioner bit for
+    bit; with more than 16 planes the sweeps fall back to the level kernel."""
+    if b == 1:
+        K = ((2.0, 0.3, 0.1), (0.3, 1.0, 0.2), (0.1, 0.2, 1.5))
+        desc, u0, _ = problems.mpfa_linear_field_problem(cells=cells, K=K, spacing_seed=3)
+        u = u0
+    else:
+        desc, u0 = problems.dnapl_2p_mpfa(cells=cells, seed=5)
+        u = u0.reshape(-1, 2).copy()
+        u[:, 1] = np.random.default_rng(4).uniform(0, 0.4, len(u))
+        u = u.reshape(-1)
+    out = {}
+    for kind in ("lanes", "levels"):
+        ctx = Context(desc)
+        ctx.set_ilu_kernel(kind)
+        ctx.set_solution(u)
+        ctx.set_prev_solution(u0)
+        if b == 2:
+            ctx.set_time_step(250.0)
+        ctx.assemble_jacobian_and_residual()
+        res = ctx.linear_solve(1e-12, 3000)
+        assert res["converged"]
+        out[kind] = (res["iterations"], ctx.update(), ctx.describe())
+    assert "level by level" in out["levels"][2]
+    if cells[2] <= 16:
+        assert "one z-plane per CTA" in out["lanes"][2]
+    else:
+        assert "level by level" in out["lanes"][2]
+    assert out["lanes"][0] == out["levels"][0]
+    assert np.array_equal(out["lanes"][1], out["levels"][1])
+
+
+def test_mpfa_3d_cluster_sweep_wait_limit_expires_and_recovers():
+    """The 3D cluster sweeps under a 1 us wait limit give up (each plane waits for the plane
+    before far longer), the solve reports DXG_ERR_TIMEOUT, and with the limit restored the same
+    context solves to the same bits."""
+    desc, u0 = problems.dnapl_2p_mpfa(cells=(16, 16, 12), seed=5)
+    ctx = Context(desc)
+    ctx.set_ilu_kernel("lanes")
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    ctx.set_time_step(250.0)
+    ctx.assemble_jacobian_and_residual()
+    first = ctx.linear_solve(1e-12, 3000)
+    assert first["converged"] and "one z-plane per CTA" in ctx.describe()
+    x0 = ctx.update()
+    ctx.set_wait_limit(1e-6)
+    with pytest.raises(Exception, match="timed out"):
+        ctx.linear_solve(1e-12, 3000)
+    ctx.set_wait_limit(0.5)
+    again = ctx.linear_solve(1e-12, 3000)
+    assert again["iterations"] == first["iterations"] and np.array_equal(ctx.update(), x0)
+
+
 def test_mpfa_cluster_sweep_wait_limit_expires_and_recovers():
     """A 1 us wait limit: the cluster line sweeps give up (later warps wait for their
     neighbours' first results far longer), the solve reports DXG_ERR_TIMEOUT, and with the
