@@ -1556,8 +1556,15 @@ static unsigned stencilThreads(const StencilArgs& a)
     return (unsigned)std::min(1024, std::max(32, t));
 }
 
+// 3D (27-point) stencils: the cluster factorisation (the rows carry up to 101 update triples;
+// one CTA level by level took 23 ms for a 2p 32x32x16 factor on GB300, the cluster version
+// with one warp per row spreads a level over 16 SMs); 2D stencils (12 triples): one CTA
 void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
 {
+    if (a.S == 27) {
+        launchStencilFactorCluster(a, st);
+        return;
+    }
     if (a.b == 2) stencilFactor2Kernel<<<1, stencilThreads(a), 0, st>>>(a);
     else stencilFactorKernel<<<1, stencilThreads(a), 0, st>>>(a);
     DXG_CUDA(cudaGetLastError());

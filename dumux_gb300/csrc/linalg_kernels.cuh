@@ -157,6 +157,9 @@ void launchStencilLane2d(const StencilArgs& a, const double* d, double* v, cudaS
 // per grid line and block row
 bool stencilLane3dFits(const StencilArgs& a);
 void launchStencilLane3d(const StencilArgs& a, const double* d, double* v, cudaStream_t st);
+// ILU(0) factorisation of a 3D (27-point) stencil matrix over a cluster of 16 CTAs, one warp per
+// row of a level (stencillane.cu)
+void launchStencilFactorCluster(const StencilArgs& a, cudaStream_t st);
 
 template <class MT, class VT, class XT = VT>
 void launchSpmv(const SpmvArgs<MT, VT, XT>& a, int b, int dim, int mode, cudaStream_t st);

@@ -327,7 +327,158 @@ cudaError_t slLaunch(const StencilArgs& a, const double* d, double* v, cudaStrea
     return cudaLaunchKernelEx(&cfg, kern, a, d, v);
 }
 
+// ---------------------------------------------------------------- factorisation
+// ILU(0) of a 3D stencil matrix over a cluster of 16 CTAs, level by level (hyperplanes
+// x + 2y + 4z), one warp per row.  The row's blocks are staged in shared memory; its lower
+// slots s are taken in ascending order (every lane forms the multiplier l = a_is Dinv_j, lane 0
+// stores it) and the update triples (s, t, u) of one s, whose targets t differ, run on separate
+// lanes; a cluster barrier ends each level.  Products, operand order and FMAs are those of
+// stencilFactorKernel / stencilFactor2Kernel, so the factors are the same bits.  Rows of earlier
+// levels are read past L1 (ld.global.cg): another SM of the cluster wrote them.
+constexpr int kSfWarps = 16;
+constexpr int kSfCtas = 16;
+
+// the k-th row of level L (lines ordered by z, then y), or false
+__device__ __forceinline__ bool sfLevelRow(int L, int k, int nx, int ny, int nz, int64_t& i)
+{
+    const int zLo = max(0, (L - (nx - 1) - 2 * (ny - 1) + 3) >> 2);
+    const int zHi = min(nz - 1, L >> 2);
+    for (int zz = zLo; zz <= zHi; ++zz) {
+        const int rest = L - 4 * zz;
+        const int yLo = max(0, (rest - (nx - 1) + 1) >> 1);
+        const int yHi = min(ny - 1, rest >> 1);
+        const int cnt = yHi - yLo + 1;
+        if (cnt <= 0) continue;
+        if (k < cnt) {
+            const int yy = yLo + k;
+            i = ((int64_t)zz * ny + yy) * nx + (rest - 2 * yy);
+            return true;
+        }
+        k -= cnt;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void sfMul2(const double* X, const double* Y, double* Z)
+{
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            double t = 0.0;
+            t = fma(X[r * 2 + 0], Y[0 * 2 + c], t);
+            t = fma(X[r * 2 + 1], Y[1 * 2 + c], t);
+            Z[r * 2 + c] = t;
+        }
+}
+
+template <int B>
+__global__ void __launch_bounds__(kSfWarps * 32) stencilFactorClusterKernel(StencilArgs a)
+{
+    constexpr int BB = B * B;
+    __shared__ double rowBuf[kSfWarps][27 * BB];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nW = (int)gridDim.x * kSfWarps;
+    const int gw = (int)blockIdx.x * kSfWarps + warp;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int64_t N = a.N;
+    const int S = a.S, center = a.center;
+    const int levels = (nx - 1) + 2 * (ny - 1) + 4 * (nz - 1) + 1;
+    double* R = rowBuf[warp];
+    for (int L = 0; L < levels; ++L) {
+        int64_t i;
+        for (int k = gw; sfLevelRow(L, k, nx, ny, nz, i); k += nW) {
+            for (int e = lane; e < S * BB; e += 32) R[e] = a.A[((int64_t)(e / BB) * N + i) * BB + e % BB];
+            __syncwarp();
+            const uint32_t m = a.mask[i];
+            int t0 = 0;
+            for (int s = 0; s < center; ++s) {
+                if (!((m >> s) & 1u)) continue;
+                const int64_t j = i + a.off[s];
+                double l[BB];
+                if constexpr (B == 1) {
+                    l[0] = R[s] * __ldcg(a.Dinv + j);
+                } else {
+                    double dj[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) dj[e] = __ldcg(a.Dinv + j * 4 + e);
+                    sfMul2(R + s * 4, dj, l);
+                }
+                __syncwarp();
+                if (lane == 0)
+#pragma unroll
+                    for (int e = 0; e < BB; ++e) R[s * BB + e] = l[e];
+                const uint32_t mj = __ldg(a.mask + j);
+                while (t0 < a.nTri && a.tri[t0][0] < s) ++t0;
+                for (int k2 = t0 + lane; k2 < a.nTri && a.tri[k2][0] == s; k2 += 32) {
+                    const int t = a.tri[k2][1], u = a.tri[k2][2];
+                    if (((m >> t) & 1u) && ((mj >> u) & 1u)) {
+                        if constexpr (B == 1) {
+                            R[t] = fma(-l[0], __ldcg(a.LU + (int64_t)u * N + j), R[t]);
+                        } else {
+                            double uj[4], pr[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) uj[e] = __ldcg(a.LU + ((int64_t)u * N + j) * 4 + e);
+                            sfMul2(l, uj, pr);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) R[t * 4 + e] -= pr[e];
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            for (int e = lane; e < S * BB; e += 32) a.LU[((int64_t)(e / BB) * N + i) * BB + e % BB] = R[e];
+            if (lane == 0) {
+                const double* D = R + center * BB;
+                if constexpr (B == 1) {
+                    if (D[0] == 0.0) atomicExch(a.singular, 1);
+                    a.Dinv[i] = 1.0 / D[0];
+                } else {
+                    const double p12 = D[1] * D[2];
+                    const double det = fma(D[0], D[3], -p12);
+                    if (det == 0.0) atomicExch(a.singular, 1);
+                    const double di = 1.0 / det;
+                    a.Dinv[i * 4 + 0] = D[3] * di;
+                    a.Dinv[i * 4 + 1] = -D[1] * di;
+                    a.Dinv[i * 4 + 2] = -D[2] * di;
+                    a.Dinv[i * 4 + 3] = D[0] * di;
+                }
+            }
+            __syncwarp();
+        }
+        cluster.sync();
+    }
+}
+
+template <int B>
+cudaError_t sfLaunch(const StencilArgs& a, cudaStream_t st)
+{
+    auto kern = stencilFactorClusterKernel<B>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kSfCtas);
+    cfg.blockDim = dim3(kSfWarps * 32);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kSfCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
 }  // namespace
+
+void launchStencilFactorCluster(const StencilArgs& a, cudaStream_t st)
+{
+    if (a.b == 2) DXG_CUDA(sfLaunch<2>(a, st));
+    else DXG_CUDA(sfLaunch<1>(a, st));
+}
 
 // 3D 27-point stencils of 1x1 or 2x2 blocks whose planes fit one cluster (nz <= 16), whose
 // lines and block rows fit one CTA of at most 256 threads, and whose plane copy and warp

@@ -160,6 +160,35 @@ def test_mpfa_3d_line_sweeps_equal_level_kernel(b, cells):
     assert np.array_equal(out["lanes"][1], out["levels"][1])
 
 
+@pytest.mark.parametrize("b,cells", [(1, (9, 7, 5)), (2, (8, 6, 5)), (2, (5, 40, 4))])
+def test_mpfa_3d_linear_solve_matches_oracle(b, cells):
+    """ILU(0)-BiCGSTAB on a 3D MPFA-O Jacobian: the cluster factorisation (one warp per row of
+    a level) and the cluster sweeps against the oracle's SeqILU + BiCGSTAB on the same matrix."""
+    if b == 1:
+        K = ((2.0, 0.3, 0.1), (0.3, 1.0, 0.2), (0.1, 0.2, 1.5))
+        desc, u0, _ = problems.mpfa_linear_field_problem(cells=cells, K=K, spacing_seed=2)
+        u = u0
+    else:
+        desc, u0 = problems.dnapl_2p_mpfa(cells=cells, seed=6)
+        u = u0.reshape(-1, 2).copy()
+        u[:, 1] = np.random.default_rng(9).uniform(0, 0.4, len(u))
+        u = u.reshape(-1)
+    ctx = Context(desc)
+    ctx.set_solution(u)
+    ctx.set_prev_solution(u0)
+    if b == 2:
+        ctx.set_time_step(250.0)
+    ctx.assemble_jacobian_and_residual()
+    res = ctx.linear_solve(1e-13, 1000)
+    assert res["converged"] and "one z-plane per CTA" in ctx.describe()
+    x = ctx.update()
+    row_ptr, col, vals = ctx.jacobian()
+    st, xo, ores = oracle.linear_solve(row_ptr, col, vals, ctx.residual(), b, reduction=1e-13, max_iter=1000)
+    assert st == 0
+    assert np.max(np.abs(x - xo)) <= 1e-8 * np.max(np.abs(xo))
+    assert abs(res["iterations"] - ores.iterations) <= max(2, 0.1 * ores.iterations)
+
+
 def test_mpfa_3d_cluster_sweep_wait_limit_expires_and_recovers():
     """The 3D cluster sweeps under a 1 us wait limit give up (each plane waits for the plane
     before far longer), the solve reports DXG_ERR_TIMEOUT, and with the limit restored the same
