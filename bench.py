@@ -1079,6 +1079,7 @@ def main():
     sweep_flops = sweep_flops_per_apply(cells, desc.num_eq)
     asm_n, asm_ms, asm_bytes = ctx.kernel_timing("assembly")
     spmv_n, spmv_ms, spmv_bytes = ctx.kernel_timing("spmv")
+    fac_n, fac_ms, fac_bytes = ctx.kernel_timing("ilu_factor")
     ctx.set_kernel_timing(False)
     timed_ms = sweep_ms + asm_ms + spmv_ms
 
@@ -1096,7 +1097,8 @@ def main():
         rnote = "bandwidth-bound passes, latency bound at small grids"
     elif args.workload in ("mpfa", "mpfa2p"):
         dsc = ctx.describe()
-        kname = ("stencilLane2dKernel" if "over a cluster" in dsc else
+        kname = ("stencilLane3dKernel" if "one z-plane per CTA" in dsc else
+                 "stencilLane2dKernel" if "over a cluster" in dsc else
                  "stencilWave2dKernel" if "line sweeps" in dsc else "stencilApplyKernel")
         rkernel = f"{kname} (ILU(0) forward+backward sweep of the MPFA-O stencil, one apply)"
         rnote = ("latency-bound natural-order sweeps (nx + 2 ny - 1 levels each), far below the HBM roof; "
@@ -1123,6 +1125,9 @@ def main():
         "assembly": {"launches": asm_n, "ms": asm_ms,
                      "gbs": (asm_bytes / (asm_ms / 1e3) / 1e9) if asm_ms else None},
         "spmv": {"launches": spmv_n, "ms": spmv_ms, "gbs": (spmv_bytes / (spmv_ms / 1e3) / 1e9) if spmv_ms else None},
+        # the preconditioner setup: ILU(0) factorisation (red-black pivots, AMG hierarchy)
+        "ilu_factor": {"launches": fac_n, "ms": fac_ms,
+                       "gbs": (fac_bytes / (fac_ms / 1e3) / 1e9) if fac_ms else None},
     }
 
     line = {

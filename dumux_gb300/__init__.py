@@ -277,8 +277,9 @@ class Context:
         self._check(self._L.dxg_set_kernel_timing(self._h, int(bool(enable))))
 
     def kernel_timing(self, kind):
-        """(launches, total device ms, algorithmic bytes) of 'ilu_sweep' / 'assembly' / 'spmv'."""
-        k = {"ilu_sweep": 0, "assembly": 1, "spmv": 2}[kind]
+        """(launches, total device ms, algorithmic bytes) of 'ilu_sweep' / 'assembly' / 'spmv' /
+        'ilu_factor'."""
+        k = {"ilu_sweep": 0, "assembly": 1, "spmv": 2, "ilu_factor": 3}[kind]
         n = C.c_int64(); ms = C.c_double(); by = C.c_double()
         self._check(self._L.dxg_get_kernel_timing(self._h, k, C.byref(n), C.byref(ms), C.byref(by)))
         return n.value, ms.value, by.value
@@ -522,8 +523,8 @@ class Batch:
         self._check(self._L.dxg_batch_set_kernel_timing(self._h, int(bool(enable))))
 
     def kernel_timing(self, kind):
-        """(launches, device ms, algorithmic bytes) of 'ilu_sweep', 'assembly' or 'spmv'."""
-        kc = {"ilu_sweep": 0, "assembly": 1, "spmv": 2}[kind]
+        """(launches, device ms, algorithmic bytes) of 'ilu_sweep', 'assembly', 'spmv' or 'ilu_factor'."""
+        kc = {"ilu_sweep": 0, "assembly": 1, "spmv": 2, "ilu_factor": 3}[kind]
         n = C.c_int64(); ms = C.c_double(); by = C.c_double()
         self._check(self._L.dxg_batch_get_kernel_timing(self._h, kc, C.byref(n), C.byref(ms), C.byref(by)))
         return n.value, ms.value, by.value

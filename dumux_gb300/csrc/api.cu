@@ -512,6 +512,8 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
         c->bytesSweep = (offBlocks * bb8 + N * (v8 + v8)) + (N * bb8 + N * (v8 + v8));
         // SpMV: all blocks + neighbour mask + x + y
         c->bytesSpmv = nnzb * bb8 + N * 1.0 + 2.0 * N * v8;
+        // factor: lower and diagonal blocks read, lower factor and inverted pivots written
+        c->bytesFactor = (double)N * bb8 * (2.0 * dim + 2.0);
         // assembly: u read, volume variables written and read back, coefficients,
         // Jacobian rows and residual written
         const int NS = method == 3 ? 1 : 1 + statesPerPv(method) * b;
@@ -718,6 +720,7 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     c->bytesAssembly = (double)N * (8.0 * L.F * (L.K + 1) + L.F + 4.0 + 8.0 * (L.S + 3) + 8.0 * L.S + 8.0);
     c->bytesSpmv = (double)nnz * 8.0 + N * 4.0 + 2.0 * N * 8.0;
     c->bytesSweep = (double)nnz * 8.0 + N * (8.0 + 4.0 * 8.0);
+    c->bytesFactor = (double)nnz * 16.0 + N * 8.0;
 
     cudaStream_t st = c->stream;
     c->uploadBlock.release();
@@ -849,6 +852,7 @@ void tabulateMpfa2p(dxg_ctx* c, const dxg_problem_desc* d)
     c->bytesAssembly += (double)N * (8.0 * L.F * (L.K + 2) + L.F + 4.0);
     c->bytesSpmv = (double)nnz * 32.0 + N * 4.0 + 2.0 * N * 16.0;
     c->bytesSweep = (double)nnz * 32.0 + N * (32.0 + 4.0 * 16.0);
+    c->bytesFactor = (double)nnz * 64.0 + N * 32.0;
     cudaStream_t st = c->stream;
     upload(c->mpMask, mask, st);
     upload(c->mpCoef, coef, st);
@@ -1276,6 +1280,7 @@ dxg_linear_result bicgstab(dxg_ctx* c, const double* rhs, double reduction, int 
     PT* PD = mixed ? (PT*)c->Dinvf.get() : (PT*)c->Dinv.get();
     IluArgs<PT, PT> ia = iluArgs<PT>(c, PA, PL, PD);
     if (refactor) {
+        TimedScope factorScope(c, DXG_KC_ILU_FACTOR, c->bytesFactor);
         if (mixed) {
             const int64_t nA = (int64_t)c->slots * c->N * c->bb;
             launchToFloat(ToFloatArgs{c->A.get(), c->Af.get(), nA}, st);

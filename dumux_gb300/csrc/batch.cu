@@ -209,9 +209,9 @@ struct dxg_batch {
     bool timing = false;
     std::vector<Timed> pending;
     std::vector<cudaEvent_t> eventPool;
-    int64_t kcLaunches[DXG_KC_COUNT] = {0, 0, 0};
-    double kcMs[DXG_KC_COUNT] = {0, 0, 0};
-    double kcBytes[DXG_KC_COUNT] = {0, 0, 0};
+    int64_t kcLaunches[DXG_KC_COUNT] = {};
+    double kcMs[DXG_KC_COUNT] = {};
+    double kcBytes[DXG_KC_COUNT] = {};
 
     double clock() const
     {

@@ -127,10 +127,11 @@ struct dxg_ctx {
     bool timing = false;
     std::vector<TimedLaunch> pending;
     std::vector<cudaEvent_t> eventPool;
-    int64_t kcLaunches[DXG_KC_COUNT] = {0, 0, 0};
-    double kcMs[DXG_KC_COUNT] = {0, 0, 0};
-    double kcBytes[DXG_KC_COUNT] = {0, 0, 0};
+    int64_t kcLaunches[DXG_KC_COUNT] = {};
+    double kcMs[DXG_KC_COUNT] = {};
+    double kcBytes[DXG_KC_COUNT] = {};
     double bytesSweep = 0, bytesAssembly = 0, bytesSpmv = 0;   // algorithmic bytes per launch (FP64 sizes)
+    double bytesFactor = 0;   // factorisation: matrix read, factor and pivots written once
 
     dxg::AssemblyArgs asmArgs() const;
     dxg::ReduceScratch scratch() const { return {partials.get(), counters.get()}; }

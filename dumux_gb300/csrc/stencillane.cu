@@ -333,8 +333,11 @@ cudaError_t slLaunch(const StencilArgs& a, const double* d, double* v, cudaStrea
 // slots s are taken in ascending order (every lane forms the multiplier l = a_is Dinv_j, lane 0
 // stores it) and the update triples (s, t, u) of one s, whose targets t differ, run on separate
 // lanes; a cluster barrier ends each level.  Products, operand order and FMAs are those of
-// stencilFactorKernel / stencilFactor2Kernel, so the factors are the same bits.  Rows of earlier
-// levels are read past L1 (ld.global.cg): another SM of the cluster wrote them.
+// stencilFactorKernel / stencilFactor2Kernel, so the factors are the same bits.  Before a row's
+// elimination its warp stages everything the row reads (its blocks, the lower neighbours'
+// pivots, masks and the neighbour blocks of every update triple) in shared memory with all loads
+// in flight together: one memory latency per row instead of one per lower slot.  Rows of
+// earlier levels are read past L1 (ld.global.cg): another SM of the cluster wrote them.
 constexpr int kSfWarps = 16;
 constexpr int kSfCtas = 16;
 
@@ -359,70 +362,92 @@ __device__ __forceinline__ bool sfLevelRow(int L, int k, int nx, int ny, int nz,
     return false;
 }
 
-__device__ __forceinline__ void sfMul2(const double* X, const double* Y, double* Z)
+// shared memory of one warp: the row's blocks [27], the inverted pivots of its 13 lower
+// neighbours, per update triple the neighbour's block it reads [104], the neighbours' slot masks
+template <int B>
+__host__ __device__ constexpr size_t sfWarpBytes()
 {
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            double t = 0.0;
-            t = fma(X[r * 2 + 0], Y[0 * 2 + c], t);
-            t = fma(X[r * 2 + 1], Y[1 * 2 + c], t);
-            Z[r * 2 + c] = t;
-        }
+    return (size_t)(27 + 13 + 104) * B * B * sizeof(double) + 64;
 }
 
 template <int B>
 __global__ void __launch_bounds__(kSfWarps * 32) stencilFactorClusterKernel(StencilArgs a)
 {
     constexpr int BB = B * B;
-    __shared__ double rowBuf[kSfWarps][27 * BB];
+    extern __shared__ __align__(16) unsigned char sfRaw[];
+    // the update triples in shared memory: lanes read different triples, which from the kernel
+    // parameters (constant bank) would serialise
+    __shared__ int8_t tri[104][3];
+    for (int e = threadIdx.x; e < a.nTri * 3; e += blockDim.x) tri[e / 3][e % 3] = a.tri[e / 3][e % 3];
+    __syncthreads();
     cg::cluster_group cluster = cg::this_cluster();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nW = (int)gridDim.x * kSfWarps;
     const int gw = (int)blockIdx.x * kSfWarps + warp;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int64_t N = a.N;
-    const int S = a.S, center = a.center;
+    const int S = a.S, center = a.center, nTri = a.nTri;
     const int levels = (nx - 1) + 2 * (ny - 1) + 4 * (nz - 1) + 1;
-    double* R = rowBuf[warp];
+    double* R = reinterpret_cast<double*>(sfRaw + (size_t)warp * sfWarpBytes<B>());
+    double* Dn = R + 27 * BB;
+    double* Un = Dn + 13 * BB;
+    uint32_t* Mn = reinterpret_cast<uint32_t*>(Un + 104 * BB);
     for (int L = 0; L < levels; ++L) {
         int64_t i;
         for (int k = gw; sfLevelRow(L, k, nx, ny, nz, i); k += nW) {
+            const uint32_t m = __ldg(a.mask + i);
+            // everything the row reads, staged with all loads in flight together
             for (int e = lane; e < S * BB; e += 32) R[e] = a.A[((int64_t)(e / BB) * N + i) * BB + e % BB];
+            for (int e = lane; e < center * BB; e += 32) {
+                const int s = e / BB;
+                Dn[e] = ((m >> s) & 1u) ? __ldcg(a.Dinv + (i + a.off[s]) * BB + e % BB) : 0.0;
+            }
+            for (int s = lane; s < center; s += 32) Mn[s] = ((m >> s) & 1u) ? __ldg(a.mask + i + a.off[s]) : 0u;
+            for (int e = lane; e < nTri * BB; e += 32) {
+                const int kk = e / BB;
+                const int s = tri[kk][0], t = tri[kk][1], u = tri[kk][2];
+                Un[e] = (((m >> s) & 1u) && ((m >> t) & 1u))
+                            ? __ldcg(a.LU + ((int64_t)u * N + i + a.off[s]) * BB + e % BB)
+                            : 0.0;
+            }
             __syncwarp();
-            const uint32_t m = a.mask[i];
             int t0 = 0;
+            // 2x2 blocks: lane q works on entry e = q % 4 (row er, column ec) of update triple
+            // t0 + q / 4 + 8 n; every entry of a block product is its own two-FMA chain, so this
+            // is the arithmetic of the whole-block products with 3 FP64 instructions per lane and
+            // lower slot instead of 12 per triple
+            const int e4 = lane & 3, er = e4 >> 1, ec = e4 & 1;
             for (int s = 0; s < center; ++s) {
                 if (!((m >> s) & 1u)) continue;
-                const int64_t j = i + a.off[s];
-                double l[BB];
+                const uint32_t mj = Mn[s];
+                while (t0 < nTri && tri[t0][0] < s) ++t0;
                 if constexpr (B == 1) {
-                    l[0] = R[s] * __ldcg(a.Dinv + j);
+                    const double l = R[s] * Dn[s];
+                    __syncwarp();
+                    if (lane == 0) R[s] = l;
+                    for (int k2 = t0 + lane; k2 < nTri && tri[k2][0] == s; k2 += 32) {
+                        const int t = tri[k2][1], u = tri[k2][2];
+                        if (((m >> t) & 1u) && ((mj >> u) & 1u)) R[t] = fma(-l, Un[k2], R[t]);
+                    }
                 } else {
-                    double dj[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) dj[e] = __ldcg(a.Dinv + j * 4 + e);
-                    sfMul2(R + s * 4, dj, l);
-                }
-                __syncwarp();
-                if (lane == 0)
-#pragma unroll
-                    for (int e = 0; e < BB; ++e) R[s * BB + e] = l[e];
-                const uint32_t mj = __ldg(a.mask + j);
-                while (t0 < a.nTri && a.tri[t0][0] < s) ++t0;
-                for (int k2 = t0 + lane; k2 < a.nTri && a.tri[k2][0] == s; k2 += 32) {
-                    const int t = a.tri[k2][1], u = a.tri[k2][2];
-                    if (((m >> t) & 1u) && ((mj >> u) & 1u)) {
-                        if constexpr (B == 1) {
-                            R[t] = fma(-l[0], __ldcg(a.LU + (int64_t)u * N + j), R[t]);
-                        } else {
-                            double uj[4], pr[4];
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) uj[e] = __ldcg(a.LU + ((int64_t)u * N + j) * 4 + e);
-                            sfMul2(l, uj, pr);
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) R[t * 4 + e] -= pr[e];
+                    // row er of the multiplier l = a_is Dinv_j (the entries this lane needs)
+                    const double* X = R + s * 4;
+                    const double* Y = Dn + s * 4;
+                    double l0 = 0.0, l1 = 0.0;
+                    l0 = fma(X[er * 2 + 0], Y[0 * 2 + 0], l0);
+                    l0 = fma(X[er * 2 + 1], Y[1 * 2 + 0], l0);
+                    l1 = fma(X[er * 2 + 0], Y[0 * 2 + 1], l1);
+                    l1 = fma(X[er * 2 + 1], Y[1 * 2 + 1], l1);
+                    __syncwarp();
+                    if (lane < 4) R[s * 4 + e4] = ec == 0 ? l0 : l1;
+                    for (int k2 = t0 + (lane >> 2); k2 < nTri && tri[k2][0] == s; k2 += 8) {
+                        const int t = tri[k2][1], u = tri[k2][2];
+                        if (((m >> t) & 1u) && ((mj >> u) & 1u)) {
+                            const double* U = Un + k2 * 4;
+                            double pr = 0.0;
+                            pr = fma(l0, U[0 * 2 + ec], pr);
+                            pr = fma(l1, U[1 * 2 + ec], pr);
+                            R[t * 4 + e4] -= pr;
                         }
                     }
                 }
@@ -455,12 +480,15 @@ template <int B>
 cudaError_t sfLaunch(const StencilArgs& a, cudaStream_t st)
 {
     auto kern = stencilFactorClusterKernel<B>;
+    const size_t smem = kSfWarps * sfWarpBytes<B>();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kSfCtas);
     cfg.blockDim = dim3(kSfWarps * 32);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

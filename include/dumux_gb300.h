@@ -294,11 +294,12 @@ int dxg_describe(const dxg_ctx* ctx, char* buf, int64_t len);
 void* dxg_stream_handle(const dxg_ctx* ctx);
 /* Per-kernel-class event timing on the context stream (off by default).  Classes:
  * DXG_KC_ILU_SWEEP (ILU(0) forward+backward sweeps), DXG_KC_ASSEMBLY (volume
- * variables + residual/Jacobian rows), DXG_KC_SPMV.  Reports launches, summed device
+ * variables + residual/Jacobian rows), DXG_KC_SPMV, DXG_KC_ILU_FACTOR (the preconditioner's
+ * setup: ILU(0) factorisation, red-black pivots or the AMG hierarchy).  Reports launches, summed device
  * milliseconds and the algorithmic bytes those launches move (each matrix block,
  * vector entry and coefficient read or written once).  No counterpart in the
  * reference. */
-enum { DXG_KC_ILU_SWEEP = 0, DXG_KC_ASSEMBLY = 1, DXG_KC_SPMV = 2, DXG_KC_COUNT = 3 };
+enum { DXG_KC_ILU_SWEEP = 0, DXG_KC_ASSEMBLY = 1, DXG_KC_SPMV = 2, DXG_KC_ILU_FACTOR = 3, DXG_KC_COUNT = 4 };
 int dxg_set_kernel_timing(dxg_ctx* ctx, int enable);
 int dxg_get_kernel_timing(dxg_ctx* ctx, int kernel_class, int64_t* launches, double* total_ms, double* bytes);
 /* ---- allocation-free norm --------------------------------------------------------------- */

@@ -173,3 +173,21 @@ def test_newton_line_search_and_residual_criterion_match_oracle(criterion):
         rn_g, rn_o = np.array(rg["residual_norm"]), np.array(ro["residual_norm"])
         assert np.all(np.abs(rn_g - rn_o) <= 1e-9 * rg["initial_residual"])
     assert np.max(np.abs(u_gpu - u_orc)) <= 1e-9 * np.max(np.abs(u_orc))
+
+
+@pytest.mark.parametrize("mpfa", [False, True])
+def test_kernel_timing_classes_cover_the_factorisation(mpfa):
+    """Per-class event timing: sweeps, assembly, SpMV and the preconditioner setup (one ILU(0)
+    factorisation per Newton iteration) all report launches, time and algorithmic bytes."""
+    d, u0 = (problems.dnapl_2p_mpfa(cells=(8, 6, 5), seed=2) if mpfa else
+             problems.dnapl_2p(cells=(8, 6, 5), seed=2))
+    ctx = Context(d)
+    ctx.set_solution(u0)
+    ctx.set_prev_solution(u0)
+    ctx.set_kernel_timing(True)
+    rep = ctx.newton_solve(250.0, newton_params())
+    assert rep["converged"]
+    for kind in ("ilu_sweep", "assembly", "spmv", "ilu_factor"):
+        n, ms, by = ctx.kernel_timing(kind)
+        assert n > 0 and ms > 0 and by > 0, kind
+    assert ctx.kernel_timing("ilu_factor")[0] == rep["iterations"]
