@@ -70,6 +70,7 @@ def lib():
         L.dxg_suggest_time_step.argtypes = [vp, C.c_double, C.POINTER(NewtonParamsC)]
         L.dxg_suggest_time_step.restype = C.c_double
         L.dxg_advance_time_step.argtypes = [vp]
+        L.dxg_set_lane_ring.argtypes = [vp, C.c_int]
         L.dxg_set_ilu_kernel.argtypes = [vp, C.c_int]
         L.dxg_set_wait_limit.argtypes = [vp, C.c_double]
         L.dxg_set_linear_solver.argtypes = [vp, C.c_int]
@@ -251,6 +252,11 @@ class Context:
     def suggest_time_step(self, old_dt, params=None):
         p = params if params is not None else newton_params()
         return self._L.dxg_suggest_time_step(self._h, float(old_dt), C.byref(p))
+
+    def set_lane_ring(self, form):
+        """Form of the lane sweeps: 'auto' (timed at the first factorisation), 'registers' or
+        'ring' (shared-memory prefetch ring); both give the same bits."""
+        self._check(self._L.dxg_set_lane_ring(self._h, {"auto": 0, "registers": 1, "ring": 2}[form]))
 
     def set_ilu_kernel(self, kind):
         """'auto' / 'wavefront' (one cluster launch per sweep), 'lanes' (two lanes per grid line,

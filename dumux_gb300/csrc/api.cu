@@ -1176,7 +1176,8 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
     c->waveTuned = true;
     const std::vector<WavePlan> cand = wavePlanCandidates(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
                                                           (int)c->pcHost.nz, c->b, sizeof(T) == 8);
-    if (cand.size() < 2 && !(c->lanePlan.ok && c->iluKernel == DXG_ILU_AUTO)) return;
+    const bool lanes = c->lanePlan.ok && (c->iluKernel == DXG_ILU_AUTO || c->iluKernel == DXG_ILU_LANES);
+    if (cand.size() < 2 && !lanes) return;
     cudaStream_t st = c->stream;
     cudaEvent_t e0, e1;
     DXG_CUDA(cudaEventCreate(&e0));
@@ -1209,23 +1210,39 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
             best = p;
         }
     }
-    // the lane sweeps (3D, 2x2 blocks), when their plan fits
-    if (c->lanePlan.ok && c->iluKernel == DXG_ILU_AUTO) {
+    // the lane sweeps (3D, 2x2 blocks), when their plan fits: the register form and, where it
+    // fits, the shared-memory-ring form (faster where most z hand-offs cross clusters), unless
+    // dxg_set_lane_ring fixed one
+    if (lanes) {
         LaneWaveArgs<T> lt = laneArgs<T>(c, A, L, Dinv, in, out);
         lt.ks = nullptr;   // never skip while timing
-        launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);   // warm-up
-        DXG_CUDA(cudaEventRecord(e0, st));
-        for (int r = 0; r < kReps; ++r) launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);
-        DXG_CUDA(cudaEventRecord(e1, st));
-        DXG_CUDA(cudaEventSynchronize(e1));
-        c->launches += 2 * (1 + kReps);
-        float ms = 0.f;
-        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        ms /= kReps;
-        c->laneTuneMs = ms;
+        c->laneFormMs[0] = c->laneFormMs[1] = 0.0;
+        float laneBest = 0.f;
+        int form = 0;
+        for (int f = 0; f < 2; ++f) {
+            if (f == 1 && !c->lanePlan.ringOk) continue;
+            if (c->laneRingMode != 0 && c->laneRingMode != f + 1) continue;
+            c->lanePlan.ring = f;
+            launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);   // warm-up
+            DXG_CUDA(cudaEventRecord(e0, st));
+            for (int r = 0; r < kReps; ++r) launchLaneWaveApply<T>(c->lanePlan, lt, lt, st);
+            DXG_CUDA(cudaEventRecord(e1, st));
+            DXG_CUDA(cudaEventSynchronize(e1));
+            c->launches += 2 * (1 + kReps);
+            float ms = 0.f;
+            DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            ms /= kReps;
+            c->laneFormMs[f] = ms;
+            if (laneBest == 0.f || ms < laneBest) {
+                laneBest = ms;
+                form = f;
+            }
+        }
+        c->lanePlan.ring = form;
+        c->laneTuneMs = laneBest;
         int flag = 0;
         DXG_CUDA(cudaMemcpy(&flag, c->singular.get() + 1, sizeof(int), cudaMemcpyDeviceToHost));
-        c->laneWave = flag == 0 && ms < bestMs;
+        c->laneWave = flag == 0 && (bestMs == 0.f || laneBest < bestMs);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1993,6 +2010,21 @@ int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
     return DXG_OK;
 }
 
+int dxg_set_lane_ring(dxg_ctx* c, int form)
+{
+    if (!c || form < 0 || form > 2) return DXG_ERR_ARG;
+    if (form == 2 && c->uploaded && !c->lanePlan.ringOk) {
+        c->err = "the shared-memory-ring form of the lane sweeps does not fit this grid";
+        return DXG_ERR_ARG;
+    }
+    c->laneRingMode = form;
+    // time (or fix) the form again at the next factorisation; captured chunks hold the old one
+    c->waveTuned = false;
+    c->haveFactor = false;
+    c->dropGraphs();
+    return DXG_OK;
+}
+
 int dxg_set_wait_limit(dxg_ctx* c, double seconds)
 {
     if (!c || !(seconds > 0.0) || seconds > 60.0) return DXG_ERR_ARG;
@@ -2043,12 +2075,17 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
     else if (useLane(c)) {
         const LanePlan& p = c->lanePlan;
         char tmp[200];
-        std::snprintf(tmp, sizeof tmp, "ILU(0): lane wavefront, %d CTAs of 128 threads in clusters of %d", p.ctas,
-                      p.clusterSize);
+        std::snprintf(tmp, sizeof tmp, "ILU(0): lane wavefront (%s), %d CTAs of 128 threads in clusters of %d",
+                      p.ring == 1 ? "shared-memory ring" : "register ring", p.ctas, p.clusterSize);
         out = tmp;
         if (c->laneTuneMs > 0) {
             std::snprintf(tmp, sizeof tmp, ", tuned (ms per apply: lanes %.3f", c->laneTuneMs);
             out += tmp;
+            if (c->laneFormMs[0] > 0 && c->laneFormMs[1] > 0) {
+                std::snprintf(tmp, sizeof tmp, " (register ring %.3f, shared-memory ring %.3f)", c->laneFormMs[0],
+                              c->laneFormMs[1]);
+                out += tmp;
+            }
             for (int k = 0; k < c->waveTuneCount; ++k) {
                 std::snprintf(tmp, sizeof tmp, ", cluster wavefront %d CTAs %.3f", c->waveTuneCtas[k], c->waveTuneMs[k]);
                 out += tmp;

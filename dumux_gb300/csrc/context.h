@@ -112,7 +112,9 @@ struct dxg_ctx {
     // (DXG_ILU_AUTO) or forced (DXG_ILU_LANES); their inter-cluster hand-off buffer
     dxg::LanePlan lanePlan;
     bool laneWave = false;
-    double laneTuneMs = 0.0;
+    double laneTuneMs = 0.0;       // the lane sweeps' time per apply at the tuning (the form run)
+    double laneFormMs[2] = {0.0, 0.0};   // per form: 0 registers, 1 shared-memory ring
+    int laneRingMode = 0;          // 0 timed, 1 register form, 2 shared-memory-ring form
     dxg::DevBuf<unsigned char> laneHandoff;
     size_t laneHandoffBytes = 0;
     // limit of every bounded wait of the sweeps (0: the kernels' default, 0.5 s)

@@ -205,6 +205,61 @@ __device__ __noinline__ typename LwPair<T>::type lwWaitPair(const T* p, bool glo
     return zero;
 }
 
+
+// ---- the shared-memory-ring form (laneRingKernel)
+template <int DIR>
+struct LwRec {
+    static constexpr int n = DIR > 0 ? 8 : 10;
+};
+
+struct LrSmem {
+    size_t zin, ybuf, yin, ring, total;
+};
+__host__ __device__ inline LrSmem lrSmem(int nx, int levels, int tsize, int recElems, int pf)
+{
+    LrSmem s{};
+    size_t o = 0;
+    s.zin = o;
+    o += (size_t)nx * kLwTile * 2 * tsize;
+    s.ybuf = o;
+    o += (size_t)kLwWarps * levels * 2 * tsize;
+    s.yin = o;
+    o += (size_t)levels * 2 * tsize;
+    o = (o + 15) & ~(size_t)15;
+    s.ring = o;
+    o += (size_t)pf * kLwThreads * recElems * tsize;
+    s.total = o;
+    return s;
+}
+template <class T>
+__device__ __forceinline__ T lwLdRelaxedShared(const T* p)
+{
+    T v;
+    if constexpr (sizeof(T) == 8)
+        asm volatile("ld.relaxed.cluster.shared::cta.f64 %0, [%1];" : "=d"(v) : "r"(lwSmemAddr(p)) : "memory");
+    else
+        asm volatile("ld.relaxed.cluster.shared::cta.f32 %0, [%1];" : "=f"(v) : "r"(lwSmemAddr(p)) : "memory");
+    return v;
+}
+// The "not written yet" pattern of the hand-off histories: all bits set (a NaN that no
+// arithmetic yields; cudaMemset with 0xff produces it).
+template <class T>
+__device__ __forceinline__ T lwLdRelaxedGpu(const T* p)
+{
+    T v;
+    if constexpr (sizeof(T) == 8) asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    else asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+template <int BYTES>
+__device__ __forceinline__ void lwCpAsync(uint32_t dst, const void* src)
+{
+    if constexpr (BYTES == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void lwCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void lwCpWait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 }  // namespace
 
 // One sweep: DIR +1 forward (z_i = d_i - L_ix z_x - L_iy z_y - L_iz z_z), DIR -1 backward
@@ -408,14 +463,256 @@ __global__ void __launch_bounds__(kLwThreads) laneWaveKernel(LaneWaveArgs<T> a)
     cluster.sync();
 }
 
+// The shared-memory-ring form of the same sweeps: each step's records are copied PF steps
+// ahead into a shared-memory ring with cp.async, the y and z hand-offs are polled before the
+// step's FMAs, and a vote per step stops the warp on an expired wait.  Same arithmetic, same
+// bits.  On grids whose z hand-offs mostly cross clusters (128x128x64 in clusters of 4: 0.97
+// against 1.24 ms per apply) it is the faster form; the context times both.
+template <class T, int DIR, int PF>
+__global__ void __launch_bounds__(kLwThreads) laneRingKernel(LaneWaveArgs<T> a)
+{
+    constexpr int REC = LwRec<DIR>::n;
+    constexpr int RB = 2 * (int)sizeof(T);   // bytes of one block row
+    extern __shared__ __align__(16) unsigned char lwRaw[];
+    __shared__ int abortFlag;
+
+    cg::cluster_group cluster = cg::this_cluster();
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int levels = nx + ny + nz - 2;
+    const LrSmem lay = lrSmem(nx, levels, (int)sizeof(T), REC, PF);
+    T* zin = reinterpret_cast<T*>(lwRaw + lay.zin);     // [nx][kLwTile][2]
+    T* ybuf = reinterpret_cast<T*>(lwRaw + lay.ybuf);   // [kLwWarps][levels][2]
+    T* yin = reinterpret_cast<T*>(lwRaw + lay.yin);     // [levels][2]
+    T* ring = reinterpret_cast<T*>(lwRaw + lay.ring);   // [PF][kLwThreads][REC]
+
+    const int cta = (int)blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = lane >> 1, r = lane & 1;
+    const int jl = warp * kLwLinesPerWarp + j;           // line within the tile
+    const bool working = cta < a.ctas;
+    // tile in sweep coordinates (the backward sweep mirrors x, y and z)
+    const int sz = working ? cta / a.nyb : 0;
+    const int syb = working ? cta % a.nyb : 0;
+    const int sy0 = syb * kLwTile;
+    const int sy = sy0 + jl;
+    const bool lineOk = working && sy < ny;
+    const int z = DIR > 0 ? sz : nz - 1 - sz;
+    const int y = DIR > 0 ? sy : ny - 1 - sy;
+    const int64_t N = a.N;
+    const int64_t lineBase = lineOk ? ((int64_t)z * ny + y) * nx : 0;
+    const int cs = a.clusterSize;
+    const bool hasZUp = working && sz > 0;
+    const int zUp = cta - a.nyb;
+    const bool zUpLocal = hasZUp && zUp / cs == cta / cs;
+    const int zDown = cta + a.nyb;
+    const bool hasZDown = working && zDown < a.ctas;
+    const bool zDownLocal = hasZDown && zDown / cs == cta / cs;
+    const bool hasYUp = working && syb > 0;
+    const bool hasYDown = working && syb + 1 < a.nyb;
+    const int lastLine = min(sy0 + kLwTile, ny) - 1;
+    const int Lfirst = sy0 + sz;
+    const int nSteps = working ? lastLine + nx - sy0 : 0;
+
+    // the incoming histories start empty (before any CTA of the cluster writes into them)
+    if (hasZUp && zUpLocal)
+        for (int k = threadIdx.x; k < nx * kLwTile * 2; k += kLwThreads) zin[k] = lwEmpty<T>();
+    for (int k = threadIdx.x; k < kLwWarps * levels * 2; k += kLwThreads) ybuf[k] = lwEmpty<T>();
+    if (hasYUp)
+        for (int k = threadIdx.x; k < levels * 2; k += kLwThreads) yin[k] = lwEmpty<T>();
+    if (threadIdx.x == 0) abortFlag = 0;
+    cluster.sync();
+    const bool skip = a.ks && a.ks->status != KS_RUNNING;
+
+    const uint32_t zinDown = zDownLocal ? lwMapa(lwSmemAddr(zin), zDown % cs) : 0u;
+    const uint32_t yinDown = hasYDown ? lwMapa(lwSmemAddr(yin), (cta + 1) % cs) : 0u;
+
+    // cell of step s on this lane's line (sweep x), or -1
+    const int sx0 = Lfirst - sy - sz;
+    auto cellX = [&](int s) -> int {
+        const int sx = sx0 + s;
+        return (lineOk && s < nSteps && sx >= 0 && sx < nx) ? sx : -1;
+    };
+    auto cellIndex = [&](int sx) -> int64_t { return lineBase + (DIR > 0 ? sx : nx - 1 - sx); };
+    // record sources of this lane's line at x = 0 (slots: forward -x 2, -y 1, -z 0; backward
+    // +x 4, +y 5, +z 6); a cell adds 4 (blocks) or 2 (vectors) elements per x
+    const T* mat = DIR > 0 ? a.Lf : a.A;
+    const T* srcX = mat + ((int64_t)(DIR > 0 ? 2 : 4) * N + lineBase) * 4 + 2 * r;
+    const T* srcY = mat + ((int64_t)(DIR > 0 ? 1 : 5) * N + lineBase) * 4 + 2 * r;
+    const T* srcZ = mat + ((int64_t)(DIR > 0 ? 0 : 6) * N + lineBase) * 4 + 2 * r;
+    const T* srcD = a.Dinv + lineBase * 4 + 2 * r;
+    const T* srcV = (DIR > 0 ? a.rhs : a.v) + lineBase * 2 + r;
+    const uint32_t ringBase = lwSmemAddr(ring + (size_t)threadIdx.x * REC);
+    // copies of the records of step s into ring slot s % PF
+    auto issue = [&](int s) {
+        const int sx = cellX(s);
+        if (sx >= 0) {
+            const int x = DIR > 0 ? sx : nx - 1 - sx;
+            const uint32_t rec = ringBase + (uint32_t)((s % PF) * kLwThreads * REC * (int)sizeof(T));
+            if (sx > 0) lwCpAsync<RB>(rec + 0 * RB, srcX + 4 * x);
+            if (sy > 0) lwCpAsync<RB>(rec + 1 * RB, srcY + 4 * x);
+            if (sz > 0) lwCpAsync<RB>(rec + 2 * RB, srcZ + 4 * x);
+            if (DIR > 0) {
+                lwCpAsync<(int)sizeof(T)>(rec + 3 * RB, srcV + 2 * x);
+            } else {
+                lwCpAsync<RB>(rec + 3 * RB, srcD + 4 * x);
+                lwCpAsync<(int)sizeof(T)>(rec + 4 * RB, srcV + 2 * x);
+            }
+        }
+        lwCommit();
+    };
+    // inter-cluster hand-off entries of this lane's line
+    const T* zGlobal = a.handoff + ((size_t)cta * nx * kLwTile + jl) * 2;
+    // bounded wait; false when it gave up or another warp stopped the sweep
+    auto waitFor = [&](auto&& ready) -> bool {
+        if (ready()) return true;
+        const unsigned long long deadline = lwTimer() + a.waitNs;
+        while (!ready()) {
+            if (*(volatile int*)&abortFlag) return false;
+            if (lwTimer() > deadline) {
+                atomicExch(a.err, DXG_ERR_TIMEOUT);
+                abortFlag = 1;
+                return false;
+            }
+        }
+        return true;
+    };
+
+    const bool warpWorks = working && !skip && sy0 + warp * kLwLinesPerWarp < ny;
+    if (warpWorks) {
+#pragma unroll
+        for (int s = 0; s < PF; ++s) issue(s);
+        T prev = 0;
+        // inter-cluster z values: loaded one step ahead, so the load's latency overlaps the
+        // step before (an early load that still saw the empty pattern is repeated)
+        T gz0 = lwEmpty<T>(), gz1 = lwEmpty<T>();
+        const bool zGlobalIn = hasZUp && !zUpLocal;
+        if (zGlobalIn && cellX(0) >= 0) {
+            gz0 = lwLdRelaxedGpu(zGlobal + (size_t)cellX(0) * kLwTile * 2);
+            gz1 = lwLdRelaxedGpu(zGlobal + (size_t)cellX(0) * kLwTile * 2 + 1);
+        }
+        for (int s = 0; s < nSteps; ++s) {
+            const int L = Lfirst + s;
+            const int sx = cellX(s);
+            const bool active = sx >= 0;
+            lwCpWait<PF - 1>();
+            // x neighbour: this line's previous cell (other row from the partner lane); y
+            // neighbour: line j-1 at the level before (same row two lanes down, other row from
+            // lane 2j-2+(1-r)); three independent shuffles of the previous results
+            const T other = __shfl_xor_sync(0xffffffffu, prev, 1);
+            const T ySame = __shfl_up_sync(0xffffffffu, prev, 2);
+            const T yOther = __shfl_sync(0xffffffffu, prev, (lane - 1 - 2 * r) & 31);
+            const T zx0 = r == 0 ? prev : other, zx1 = r == 0 ? other : prev;
+            T zy0 = r == 0 ? ySame : yOther, zy1 = r == 0 ? yOther : ySame;
+            T zz0 = 0, zz1 = 0;
+            bool ok = true;
+            if (active && j == 0 && sy > 0 && (warp > 0 || hasYUp)) {
+                const T* src = warp > 0 ? ybuf + ((size_t)(warp - 1) * levels + (L - 1)) * 2 : yin + (size_t)(L - 1) * 2;
+                ok = waitFor([&] {
+                    zy0 = lwLdRelaxedShared(src);
+                    zy1 = lwLdRelaxedShared(src + 1);
+                    return !lwIsEmpty(zy0) && !lwIsEmpty(zy1);
+                });
+            }
+            if (hasZUp && active) {
+                if (zUpLocal) {
+                    const T* src = zin + ((size_t)sx * kLwTile + jl) * 2;
+                    ok = waitFor([&] {
+                        zz0 = lwLdRelaxedShared(src);
+                        zz1 = lwLdRelaxedShared(src + 1);
+                        return !lwIsEmpty(zz0) && !lwIsEmpty(zz1);
+                    }) && ok;
+                } else {
+                    const T* src = zGlobal + (size_t)sx * kLwTile * 2;
+                    zz0 = gz0;
+                    zz1 = gz1;
+                    if (lwIsEmpty(zz0) || lwIsEmpty(zz1))
+                        ok = waitFor([&] {
+                            zz0 = lwLdRelaxedGpu(src);
+                            zz1 = lwLdRelaxedGpu(src + 1);
+                            return !lwIsEmpty(zz0) && !lwIsEmpty(zz1);
+                        }) && ok;
+                }
+            }
+            if (zGlobalIn) {
+                const int sxn = cellX(s + 1);
+                if (sxn >= 0) {
+                    gz0 = lwLdRelaxedGpu(zGlobal + (size_t)sxn * kLwTile * 2);
+                    gz1 = lwLdRelaxedGpu(zGlobal + (size_t)sxn * kLwTile * 2 + 1);
+                }
+            }
+            if (__any_sync(0xffffffffu, !ok)) break;
+            // both lanes of the line hold the inter-cluster values: restore the pattern
+            if (zGlobalIn && active && r == 0) {
+                T* src = a.handoff + (((size_t)cta * nx + sx) * kLwTile + jl) * 2;
+                lwStRelaxedGpu(src, lwEmpty<T>());
+                lwStRelaxedGpu(src + 1, lwEmpty<T>());
+            }
+            const T* rec = ring + ((size_t)(s % PF) * kLwThreads + threadIdx.x) * REC;
+            T acc = 0;
+            if (active) {
+                acc = rec[DIR > 0 ? 6 : 8];
+                if (sx > 0) {
+                    acc = fma(-rec[0], zx0, acc);
+                    acc = fma(-rec[1], zx1, acc);
+                }
+                if (sy > 0) {
+                    acc = fma(-rec[2], zy0, acc);
+                    acc = fma(-rec[3], zy1, acc);
+                }
+                if (sz > 0) {
+                    acc = fma(-rec[4], zz0, acc);
+                    acc = fma(-rec[5], zz1, acc);
+                }
+            }
+            T res = acc;
+            if (DIR < 0) {
+                const T accOther = __shfl_xor_sync(0xffffffffu, acc, 1);
+                const T a0 = r == 0 ? acc : accOther, a1 = r == 0 ? accOther : acc;
+                T t = rec[6] * a0;
+                t = fma(rec[7], a1, t);
+                res = t;
+            }
+            if (active) {
+                const int64_t i = cellIndex(sx);
+                a.v[i * 2 + r] = res;
+                if (zDownLocal)
+                    lwStRemote<T>(zinDown + (uint32_t)((((size_t)sx * kLwTile + jl) * 2 + r) * sizeof(T)), res);
+                else if (hasZDown)
+                    lwStRelaxedGpu(a.handoff + (((size_t)zDown * nx + sx) * kLwTile + jl) * 2 + r, res);
+                if (j == kLwLinesPerWarp - 1) {
+                    if (warp < kLwWarps - 1)
+                        lwStRemote<T>(lwSmemAddr(&ybuf[((size_t)warp * levels + L) * 2 + r]), res);
+                    else if (hasYDown)
+                        lwStRemote<T>(yinDown + (uint32_t)(((size_t)L * 2 + r) * sizeof(T)), res);
+                }
+                prev = res;
+            }
+            issue(s + PF);
+        }
+        lwCpWait<0>();
+    }
+    // no CTA may leave while another can still write into its shared memory
+    cluster.sync();
+}
+
 // ---------------------------------------------------------------- host side
 namespace {
 
-template <class T, int DIR, int PF>
+// One launch of either form (RING 0: registers, laneWaveKernel; 1: shared memory,
+// laneRingKernel), or the occupancy query of its launch shape.
+template <class T, int DIR, int PF, int RING>
 cudaError_t lwLaunchOne(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
 {
-    auto kern = laneWaveKernel<T, DIR, PF>;
-    const size_t smem = lwSmem(a.nx, a.nx + a.ny + a.nz - 2, (int)sizeof(T)).total;
+    void (*kern)(LaneWaveArgs<T>);
+    size_t smem;
+    const int levels = a.nx + a.ny + a.nz - 2;
+    if constexpr (RING != 0) {
+        kern = laneRingKernel<T, DIR, PF>;
+        smem = lrSmem(a.nx, levels, (int)sizeof(T), LwRec<DIR>::n, PF).total;
+    } else {
+        kern = laneWaveKernel<T, DIR, PF>;
+        smem = lwSmem(a.nx, levels, (int)sizeof(T)).total;
+    }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLwSmemLimit);
@@ -443,15 +740,41 @@ cudaError_t lwLaunchOne(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_
 }
 
 template <class T, int DIR>
-cudaError_t lwDispatch(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
+cudaError_t lwDispatch(const LanePlan& p, int ring, const LaneWaveArgs<T>& a, cudaStream_t st, bool query, int* fits)
 {
-    const int pf = DIR > 0 ? p.pfFwd : p.pfBwd;
-    switch (pf) {
-        case 4: return lwLaunchOne<T, DIR, 4>(p, a, st, query, fits);
-        default:
-            if (fits) *fits = 0;
-            return query ? cudaSuccess : cudaErrorInvalidConfiguration;
+    if (ring == 0) {
+        if ((DIR > 0 ? p.pfFwd : p.pfBwd) == 4) return lwLaunchOne<T, DIR, 4, 0>(p, a, st, query, fits);
+    } else {
+        switch (DIR > 0 ? p.pfRingFwd : p.pfRingBwd) {
+            case 8: return lwLaunchOne<T, DIR, 8, 1>(p, a, st, query, fits);
+            case 4: return lwLaunchOne<T, DIR, 4, 1>(p, a, st, query, fits);
+            case 2: return lwLaunchOne<T, DIR, 2, 1>(p, a, st, query, fits);
+            default: break;
+        }
     }
+    if (fits) *fits = 0;
+    return query ? cudaSuccess : cudaErrorInvalidConfiguration;
+}
+
+// prefetch depth of the shared-memory ring: the deepest of {8, 4, 2} within the budget, else 0
+template <class T>
+int lrDepth(int nx, int levels, int dir)
+{
+    for (int pf : {8, 4, 2}) {
+        const size_t sm = lrSmem(nx, levels, (int)sizeof(T), dir > 0 ? LwRec<1>::n : LwRec<-1>::n, pf).total;
+        if (sm <= kLwSmemLimit) return pf;
+    }
+    return 0;
+}
+
+// every cluster of the launch shape resident at once, for both sweeps of form `ring`
+template <class T>
+bool lwResident(const LanePlan& p, int ring, const LaneWaveArgs<T>& dummy)
+{
+    int f1 = 0, f2 = 0;
+    lwDispatch<T, 1>(p, ring, dummy, 0, true, &f1);
+    lwDispatch<T, -1>(p, ring, dummy, 0, true, &f2);
+    return f1 >= p.grid / p.clusterSize && f2 >= p.grid / p.clusterSize;
 }
 
 }  // namespace
@@ -470,6 +793,8 @@ LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b)
     // depth 4, 0.194 ms with 5, 0.201 ms with 3, 0.223 ms with 6 (spills)
     p.pfFwd = 4;
     p.pfBwd = 4;
+    p.pfRingFwd = lrDepth<T>(nx, levels, 1);
+    p.pfRingBwd = lrDepth<T>(nx, levels, -1);
     LaneWaveArgs<T> dummy{};
     dummy.nx = nx;
     dummy.ny = ny;
@@ -478,12 +803,9 @@ LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b)
         if (cs % p.nyb != 0) continue;
         p.clusterSize = cs;
         p.grid = (p.ctas + cs - 1) / cs * cs;
-        int f1 = 0, f2 = 0;
-        lwDispatch<T, 1>(p, dummy, 0, true, &f1);
-        lwDispatch<T, -1>(p, dummy, 0, true, &f2);
-        // every cluster resident at once
-        if (f1 >= p.grid / cs && f2 >= p.grid / cs) {
+        if (lwResident<T>(p, 0, dummy)) {
             p.ok = true;
+            p.ringOk = p.pfRingFwd > 0 && p.pfRingBwd > 0 && lwResident<T>(p, 1, dummy);
             return p;
         }
     }
@@ -494,8 +816,9 @@ LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b)
 template <class T>
 void launchLaneWaveApply(const LanePlan& p, const LaneWaveArgs<T>& fwd, const LaneWaveArgs<T>& bwd, cudaStream_t st)
 {
-    DXG_CUDA((lwDispatch<T, 1>(p, fwd, st, false, nullptr)));
-    DXG_CUDA((lwDispatch<T, -1>(p, bwd, st, false, nullptr)));
+    const int ring = p.ring == 1 && p.ringOk ? 1 : 0;
+    DXG_CUDA((lwDispatch<T, 1>(p, ring, fwd, st, false, nullptr)));
+    DXG_CUDA((lwDispatch<T, -1>(p, ring, bwd, st, false, nullptr)));
 }
 
 template LanePlan makeLanePlan<double>(int, int, int, int, int);

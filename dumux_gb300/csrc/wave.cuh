@@ -46,6 +46,11 @@ struct LaneWaveArgs {
 struct LanePlan {
     bool ok = false;
     int nyb = 0, ctas = 0, clusterSize = 0, grid = 0, pfFwd = 0, pfBwd = 0;
+    // the shared-memory-ring form (laneRingKernel): fits beside the register form (same
+    // launch shape), its prefetch depths, and which form the sweeps run (0 registers, 1 ring)
+    bool ringOk = false;
+    int pfRingFwd = 0, pfRingBwd = 0;
+    int ring = 0;
 };
 // Plan of the lane sweeps for a dim-D grid of b x b blocks (ok only for 3D, b == 2, grids whose
 // sweeps fit: every cluster resident at once, the plane history in shared memory).

@@ -267,6 +267,12 @@ enum { DXG_ILU_AUTO = 0, DXG_ILU_WAVEFRONT = 1, DXG_ILU_LEVELS = 2, DXG_ILU_REDB
  * the same factors and arithmetic per cell as DXG_ILU_WAVEFRONT, so the same results.
  * DXG_ILU_AUTO takes it when the timing at the first factorisation finds it faster. */
 int dxg_set_ilu_kernel(dxg_ctx* ctx, int kind);
+/* Form of the lane sweeps: 0 (default) times both at the first factorisation and keeps the
+ * faster, 1 the register form (each step's records in a register ring, no vote per step), 2 the
+ * shared-memory-ring form (records copied ahead with cp.async, faster where most plane
+ * hand-offs cross thread-block clusters); both give the same bits.  DXG_ERR_ARG for 2 when it
+ * does not fit the grid.  No counterpart in the reference. */
+int dxg_set_lane_ring(dxg_ctx* ctx, int form);
 /* Limit of every bounded wait inside the ILU(0) sweeps, in seconds (default 0.5; at most
  * 60).  A wait that runs out ends the sweep with DXG_ERR_TIMEOUT, which the Newton driver
  * treats like a failed linear solve (a time-step retry).  Raise it where the GPU is

@@ -481,6 +481,7 @@ public:
     // (red-black ordered ILU(0): not the reference's preconditioner, faster per time step);
     // takes effect at the assembler's next factorisation
     void setIluKernel(GpuFVAssembler& A, int kind) { A.handle().check(dxg_set_ilu_kernel(A.context(), kind)); }
+    void setLaneRing(GpuFVAssembler& A, int form) { A.handle().check(dxg_set_lane_ring(A.context(), form)); }
     // x = A^-1 b from x = 0: A and b are the assembler's device system (the b handle must
     // be that assembler's residual); x receives the update on the host
     GpuSolverResult solve(const GpuJacobian& A, std::vector<double>& x, const GpuResidual& b)

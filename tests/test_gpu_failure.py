@@ -45,7 +45,8 @@ def test_failing_problem_is_isolated_in_a_batch():
     assert np.array_equal(batch.solution(p_ok), ctx.solution())
 
 
-def test_lane_sweep_wait_limit_expires_and_the_context_recovers():
+@pytest.mark.parametrize("form", ["registers", "ring"])
+def test_lane_sweep_wait_limit_expires_and_the_context_recovers(form):
     """A wait limit far below the hand-off latency of the lane sweeps (plane 31 of a 32-plane
     grid receives its first value after 31 plane steps): the sweeps give up and the solve
     reports DXG_ERR_TIMEOUT; with the limit restored, the same context solves to the same
@@ -55,6 +56,7 @@ def test_lane_sweep_wait_limit_expires_and_the_context_recovers():
     u[:, 1] = np.random.default_rng(5).uniform(0.0, 0.4, len(u))
     ctx = Context(desc)
     ctx.set_ilu_kernel("lanes")
+    ctx.set_lane_ring(form)
     ctx.set_solution(u.reshape(-1))
     ctx.set_prev_solution(u0)
     ctx.set_time_step(250.0)

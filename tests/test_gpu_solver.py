@@ -136,10 +136,13 @@ def test_wavefront_ilu_equals_level_scheduled(dims, precision):
     smax = 0.3 if max(dims) >= 37 or (len(dims) == 3 and dims[1] >= 70) else 0.6
     u[:, 1] = np.random.default_rng(2).uniform(0, smax, len(u))
     out = {}
-    kinds = ("levels", "wavefront", "lanes") if len(dims) == 3 else ("levels", "wavefront")
+    kinds = (("levels", "wavefront", "lanes", "lanes-registers", "lanes-ring") if len(dims) == 3
+             else ("levels", "wavefront"))
     for kind in kinds:
         ctx = Context(d, precision=precision)
-        ctx.set_ilu_kernel(kind)
+        ctx.set_ilu_kernel(kind.split("-")[0])
+        if kind != "lanes" and kind.startswith("lanes"):
+            ctx.set_lane_ring(kind.split("-")[1])
         ctx.set_solution(u.reshape(-1))
         ctx.set_prev_solution(u0)
         ctx.set_time_step(250.0)
@@ -151,11 +154,13 @@ def test_wavefront_ilu_equals_level_scheduled(dims, precision):
     assert abs(rl["iterations"] - rw["iterations"]) <= 2
     tol = 1e-7 if precision == "fp64" else 1e-3
     assert np.max(np.abs(xl - xw)) <= tol * np.max(np.abs(xl))
-    if "lanes" in out:
-        # the same arithmetic per cell as the cluster wavefront: the same bits
-        rn, xn = out["lanes"]
-        assert rn["iterations"] == rw["iterations"]
-        assert np.array_equal(xn, xw)
+    for kind in ("lanes", "lanes-registers", "lanes-ring"):
+        if kind in out:
+            # both forms of the lane sweeps: the same arithmetic per cell as the cluster
+            # wavefront, the same bits
+            rn, xn = out[kind]
+            assert rn["iterations"] == rw["iterations"]
+            assert np.array_equal(xn, xw)
 
 
 @pytest.mark.parametrize("criterion", ["line_search", "residual"])
