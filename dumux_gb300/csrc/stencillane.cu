@@ -267,8 +267,13 @@ __global__ void __launch_bounds__(kSlMaxThreads) stencilLane3dKernel(StencilArgs
                     } else {
                         val = o;
                     }
-                    const V mul = ok ? m[q] : slZero<B>();
-                    val = ok ? val : slZero<B>();
+                    // a slot outside the row's pattern holds +0 in the factor (the assembly
+                    // kernels and dxg_set_linear_system write +0 there, the factorisation never
+                    // updates it) and its plane-below value was not loaded (+0), so no select is
+                    // needed for it: -(+0) * (+0) leaves the accumulator's bits unchanged; the
+                    // line-below and own-line values come from shuffles and are zeroed
+                    const V mul = m[q];
+                    if (q >= 9) val = ok ? val : slZero<B>();
                     if constexpr (B == 1) {
                         acc = fma(-mul, val, acc);
                     } else {
