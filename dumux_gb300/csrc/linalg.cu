@@ -1258,23 +1258,19 @@ __global__ void __launch_bounds__(1024) stencilApplyKernel(StencilArgs a, const 
 // L+3).  Every thread keeps its last three results; a warp passes them on by shuffle, the
 // boundary lane of each warp through a double-buffered shared-memory slot, and one CTA
 // barrier ends each level.  The cells' factor entries, right-hand side (and pivot) are
-// copied PF levels ahead into a shared-memory ring with cp.async.  The arithmetic is that
-// of stencilApplyKernel (same operand order, explicit FMAs), so both give the same bits.
-__device__ __forceinline__ void stCpAsync8(uint32_t dst, const void* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void stCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void stCpWait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+// loaded PF levels ahead into a register ring (a shared-memory ring filled with cp.async took
+// 1.09-1.11 ms per apply at 256 x 256).  The arithmetic is that of stencilApplyKernel (same
+// operand order, explicit FMAs), so both give the same bits.
 
-template <int DIR, int PF>
-__global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const double* __restrict__ d,
+template <int DIR, int PF, int MAXT>
+__global__ void __launch_bounds__(MAXT) stencilWave2dKernel(StencilArgs a, const double* __restrict__ d,
                                                              double* __restrict__ v)
 {
-    // record per cell: forward L0..L3 (slots 0..3), d; backward U5..U8 (slots 5..8), Dinv, v
+    // record per cell: forward L0..L3 (slots 0..3), d; backward U5..U8 (slots 5..8), Dinv, v;
+    // held PF steps ahead in a register ring whose entry is refilled at the start of the step
+    // that empties it (the loads issue ahead of the step's chain); the ring's depth follows the
+    // registers a thread has at MAXT threads
     constexpr int REC = DIR > 0 ? 5 : 6;
-    extern __shared__ __align__(16) double stRing[];   // [PF][blockDim][REC]
     __shared__ double hist[32][2][3];                  // per warp, level parity: boundary lane's r1..r3
     if (a.ks && a.ks->status != KS_RUNNING) return;
     const int nx = a.nx, ny = a.ny;
@@ -1284,88 +1280,85 @@ __global__ void __launch_bounds__(1024) stencilWave2dKernel(StencilArgs a, const
     const int Lmax = (nx - 1) + 2 * (ny - 1);
     const int64_t N = a.N;
     const int64_t rowBase = (int64_t)y * nx;
-    const uint32_t ringBase = (uint32_t)__cvta_generic_to_shared(stRing + (size_t)threadIdx.x * REC);
-    const uint32_t slotBytes = blockDim.x * REC * 8u;
     // sweep step s: level L = s (forward) or Lmax - s (backward)
     auto cellX = [&](int s) -> int {
         const int L = DIR > 0 ? s : Lmax - s;
         const int x = L - 2 * y;
         return (lineOk && s <= Lmax && x >= 0 && x < nx) ? x : -1;
     };
-    auto issue = [&](int s) {
+    double ring[PF][REC];
+    auto load = [&](int s, int k) {
         const int x = cellX(s);
-        if (x >= 0) {
-            const int64_t i = rowBase + x;
-            const uint32_t rec = ringBase + (uint32_t)(s % PF) * slotBytes;
-            if (DIR > 0) {
-                for (int k = 0; k < 4; ++k) stCpAsync8(rec + 8u * k, a.LU + (int64_t)k * N + i);
-                stCpAsync8(rec + 32u, d + i);
-            } else {
-                for (int k = 0; k < 4; ++k) stCpAsync8(rec + 8u * k, a.LU + (int64_t)(5 + k) * N + i);
-                stCpAsync8(rec + 32u, a.Dinv + i);
-                stCpAsync8(rec + 40u, v + i);
-            }
+        const int64_t i = rowBase + (x >= 0 ? x : 0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ring[k][e] = x >= 0 ? __ldg(a.LU + (int64_t)((DIR > 0 ? 0 : 5) + e) * N + i) : 0.0;
+        if (DIR > 0) {
+            ring[k][4] = x >= 0 ? __ldg(d + i) : 0.0;
+        } else {
+            ring[k][4] = x >= 0 ? __ldg(a.Dinv + i) : 0.0;
+            ring[k][5] = x >= 0 ? __ldg(v + i) : 0.0;
         }
-        stCommit();
     };
 #pragma unroll
-    for (int s = 0; s < PF; ++s) issue(s);
+    for (int k = 0; k < PF; ++k) load(k, k);
     double r1 = 0.0, r2 = 0.0, r3 = 0.0;
-    for (int s = 0; s <= Lmax; ++s) {
-        // the neighbour line's results of two and three levels back first, then the last
-        // level's (see stencilLane2dKernel): the same operand order as stencilApplyKernel
-        double n3 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r3, 1) : __shfl_down_sync(0xffffffffu, r3, 1);
-        double n2 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r2, 1) : __shfl_down_sync(0xffffffffu, r2, 1);
-        double n1 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r1, 1) : __shfl_down_sync(0xffffffffu, r1, 1);
-        const int par = (s - 1) & 1;
-        if (DIR > 0 && lane == 0 && warp > 0 && s > 0) {
-            n1 = hist[warp - 1][par][0];
-            n2 = hist[warp - 1][par][1];
-            n3 = hist[warp - 1][par][2];
-        } else if (DIR < 0 && lane == 31 && s > 0 && (warp + 1) * 32 < (int)blockDim.x) {
-            n1 = hist[warp + 1][par][0];
-            n2 = hist[warp + 1][par][1];
-            n3 = hist[warp + 1][par][2];
-        }
-        stCpWait<PF - 1>();
-        const int x = cellX(s);
-        double res = 0.0;
-        if (x >= 0) {
-            const double* rec = stRing + ((size_t)(s % PF) * blockDim.x + threadIdx.x) * REC;
-            const int64_t i = rowBase + x;
-            if (DIR > 0) {
-                double acc = rec[4];
-                if (x > 0 && y > 0) acc = fma(-rec[0], n3, acc);        // (x-1, y-1)
-                if (y > 0) acc = fma(-rec[1], n2, acc);                 // (x,   y-1)
-                if (x < nx - 1 && y > 0) acc = fma(-rec[2], n1, acc);   // (x+1, y-1)
-                if (x > 0) acc = fma(-rec[3], r1, acc);                 // (x-1, y)
-                res = acc;
-            } else {
-                double acc = rec[5];
-                if (x < nx - 1 && y < ny - 1) acc = fma(-rec[3], n3, acc);   // (x+1, y+1)
-                if (y < ny - 1) acc = fma(-rec[2], n2, acc);                 // (x,   y+1)
-                if (x > 0 && y < ny - 1) acc = fma(-rec[1], n1, acc);        // (x-1, y+1)
-                if (x < nx - 1) acc = fma(-rec[0], r1, acc);                  // (x+1, y)
-                res = rec[4] * acc;
+    for (int s0 = 0; s0 <= Lmax; s0 += PF) {
+#pragma unroll
+        for (int k = 0; k < PF; ++k) {
+            const int s = s0 + k;
+            double rec[REC];
+#pragma unroll
+            for (int e = 0; e < REC; ++e) rec[e] = ring[k][e];
+            load(s + PF, k);
+            // the neighbour line's results of two and three levels back first, then the last
+            // level's (see stencilLane2dKernel): the same operand order as stencilApplyKernel
+            double n3 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r3, 1) : __shfl_down_sync(0xffffffffu, r3, 1);
+            double n2 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r2, 1) : __shfl_down_sync(0xffffffffu, r2, 1);
+            double n1 = DIR > 0 ? __shfl_up_sync(0xffffffffu, r1, 1) : __shfl_down_sync(0xffffffffu, r1, 1);
+            const int par = (s - 1) & 1;
+            if (DIR > 0 && lane == 0 && warp > 0 && s > 0) {
+                n1 = hist[warp - 1][par][0];
+                n2 = hist[warp - 1][par][1];
+                n3 = hist[warp - 1][par][2];
+            } else if (DIR < 0 && lane == 31 && s > 0 && (warp + 1) * 32 < (int)blockDim.x) {
+                n1 = hist[warp + 1][par][0];
+                n2 = hist[warp + 1][par][1];
+                n3 = hist[warp + 1][par][2];
             }
-            v[i] = res;
+            const int x = cellX(s);
+            double res = 0.0;
+            if (x >= 0) {
+                const int64_t i = rowBase + x;
+                if (DIR > 0) {
+                    double acc = rec[4];
+                    if (x > 0 && y > 0) acc = fma(-rec[0], n3, acc);        // (x-1, y-1)
+                    if (y > 0) acc = fma(-rec[1], n2, acc);                 // (x,   y-1)
+                    if (x < nx - 1 && y > 0) acc = fma(-rec[2], n1, acc);   // (x+1, y-1)
+                    if (x > 0) acc = fma(-rec[3], r1, acc);                 // (x-1, y)
+                    res = acc;
+                } else {
+                    double acc = rec[5];
+                    if (x < nx - 1 && y < ny - 1) acc = fma(-rec[3], n3, acc);   // (x+1, y+1)
+                    if (y < ny - 1) acc = fma(-rec[2], n2, acc);                 // (x,   y+1)
+                    if (x > 0 && y < ny - 1) acc = fma(-rec[1], n1, acc);        // (x-1, y+1)
+                    if (x < nx - 1) acc = fma(-rec[0], r1, acc);                  // (x+1, y)
+                    res = rec[4] * acc;
+                }
+                v[i] = res;
+            }
+            r3 = r2;
+            r2 = r1;
+            r1 = res;
+            if ((DIR > 0 && lane == 31) || (DIR < 0 && lane == 0)) {
+                hist[warp][s & 1][0] = r1;
+                hist[warp][s & 1][1] = r2;
+                hist[warp][s & 1][2] = r3;
+            }
+            __syncthreads();
         }
-        r3 = r2;
-        r2 = r1;
-        r1 = res;
-        if ((DIR > 0 && lane == 31) || (DIR < 0 && lane == 0)) {
-            hist[warp][s & 1][0] = r1;
-            hist[warp][s & 1][1] = r2;
-            hist[warp][s & 1][2] = r3;
-        }
-        issue(s + PF);
-        __syncthreads();
     }
-    stCpWait<0>();
 }
 
-// dynamic shared memory of the 2D sweeps at prefetch depth pf
-static size_t wave2dSmem(unsigned threads, int pf) { return (size_t)pf * threads * 6 * sizeof(double); }
 
 // 2x2 blocks over the same stencil (the 2p MPFA-O Jacobian, A[slot][row][4] row-major
 // blocks): SpMV with the same fused dots, and the block ILU(0) factor and sweeps level by
@@ -1574,28 +1567,17 @@ bool stencilWave2dFits(const StencilArgs& a) { return a.b == 1 && a.S == 9 && a.
 
 void launchStencilWave2d(const StencilArgs& a, const double* d, double* v, cudaStream_t st)
 {
+    // ring depth by CTA size: 8 steps up to 256 lines, 4 up to 512, 2 up to 1024
     const unsigned threads = (unsigned)((a.ny + 31) / 32 * 32);
-    const int pf = threads <= 512 ? 8 : 4;
-    const size_t smem = wave2dSmem(threads, pf);
-    // the opt-in shared-memory size, once per device
-    static bool attrSet[64] = {};
-    int dev = 0;
-    DXG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) throw Error(DXG_ERR_ARG, "device index out of range");
-    if (!attrSet[dev]) {
-        const int maxSmem = (int)wave2dSmem(512, 8);
-        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<-1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-        DXG_CUDA(cudaFuncSetAttribute(stencilWave2dKernel<-1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmem));
-        attrSet[dev] = true;
-    }
-    if (pf == 8) {
-        stencilWave2dKernel<1, 8><<<1, threads, smem, st>>>(a, d, v);
-        stencilWave2dKernel<-1, 8><<<1, threads, smem, st>>>(a, d, v);
+    if (threads <= 256) {
+        stencilWave2dKernel<1, 8, 256><<<1, threads, 0, st>>>(a, d, v);
+        stencilWave2dKernel<-1, 8, 256><<<1, threads, 0, st>>>(a, d, v);
+    } else if (threads <= 512) {
+        stencilWave2dKernel<1, 4, 512><<<1, threads, 0, st>>>(a, d, v);
+        stencilWave2dKernel<-1, 4, 512><<<1, threads, 0, st>>>(a, d, v);
     } else {
-        stencilWave2dKernel<1, 4><<<1, threads, smem, st>>>(a, d, v);
-        stencilWave2dKernel<-1, 4><<<1, threads, smem, st>>>(a, d, v);
+        stencilWave2dKernel<1, 2, 1024><<<1, threads, 0, st>>>(a, d, v);
+        stencilWave2dKernel<-1, 2, 1024><<<1, threads, 0, st>>>(a, d, v);
     }
     DXG_CUDA(cudaGetLastError());
 }
