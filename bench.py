@@ -223,9 +223,10 @@ def measured_peaks():
 
 # dram__bytes_read.sum + dram__bytes_write.sum per ILU(0) apply (forward + backward sweep)
 # of the 64x64x32 FP64 system, from ncu captures of the sweeps (cold-cache, serialised
-# launches): the cluster wavefront kernels and the lane sweeps.
+# launches): the cluster wavefront kernels and the lane sweeps (register-ring form, the one
+# the context picks at this size).
 ILU_TRAFFIC_PER_APPLY_64x64x32 = 14537472 + 18714112
-LANE_TRAFFIC_PER_APPLY_64x64x32 = 14533376 + 18735616
+LANE_TRAFFIC_PER_APPLY_64x64x32 = 14520320 + 18721792
 # DRAM bytes per cell of one batched FP32 apply (forward + backward sweep), from an ncu capture
 # of a 32-problem ensemble (2,379,154 cells); traffic scales with the cells swept (each block
 # and vector entry is moved once)
