@@ -31,6 +31,7 @@ UNITS = {
     "mpfa.cu": ["--fmad=false"],
     "stencilwave.cu": [],
     "stencillane.cu": [],
+    "linesweep.cu": [],
 }
 
 

@@ -590,6 +590,9 @@ void tabulate(dxg_ctx* c, const dxg_problem_desc* d)
     c->waveTuned = false;
     c->laneWave = false;
     c->laneTuneMs = 0.0;
+    c->line2dOk = tpfaLine2dFits(dim, (int)g.n[0], (int)g.n[1], b);
+    c->line2d = false;
+    c->line2dMs = 0.0;
     c->laneHandoff.release();
     c->laneHandoffBytes = 0;
     c->waveTuneCount = 0;
@@ -752,6 +755,7 @@ void tabulateMpfa(dxg_ctx* c, const dxg_problem_desc* d)
     c->singular.alloc(2);
     c->wavePlan = WavePlan{};
     c->lanePlan = LanePlan{};
+    c->line2dOk = c->line2d = false;
     c->waveTuned = true;
     c->laneWave = false;
     c->laneTuneMs = 0.0;
@@ -865,6 +869,7 @@ void tabulateMpfa2p(dxg_ctx* c, const dxg_problem_desc* d)
     DXG_CUDA(cudaStreamSynchronize(st));
     c->wavePlan = WavePlan{};
     c->lanePlan = LanePlan{};
+    c->line2dOk = c->line2d = false;
     c->waveTuned = true;
     c->laneWave = false;
     c->dropGraphs();
@@ -1059,6 +1064,31 @@ bool useLane(const dxg_ctx* c)
            (c->iluKernel == DXG_ILU_LANES || (c->iluKernel == DXG_ILU_AUTO && c->laneWave));
 }
 
+// The one-CTA line sweeps of 2D TPFA systems apply the preconditioner (DXG_ILU_LANES on a 2D
+// grid, or DXG_ILU_AUTO when the timing at the first factorisation found them faster).
+bool useLine2d(const dxg_ctx* c)
+{
+    return c->line2dOk && c->linearSolver == DXG_LINEAR_SOLVER_ILU_BICGSTAB &&
+           (c->iluKernel == DXG_ILU_LANES || (c->iluKernel == DXG_ILU_AUTO && c->line2d));
+}
+
+template <class T>
+LaneWaveArgs<T> line2dArgs(dxg_ctx* c, const T* A, const T* L, const T* Dinv, const T* rhs, T* v)
+{
+    LaneWaveArgs<T> w{};
+    w.nx = c->pcHost.nx;
+    w.ny = c->pcHost.ny;
+    w.nz = 1;
+    w.N = c->N;
+    w.Lf = L;
+    w.A = A;
+    w.Dinv = Dinv;
+    w.rhs = rhs;
+    w.v = v;
+    w.ks = c->ks.get();
+    return w;
+}
+
 // The hand-off buffer of the lane sweeps between clusters, all bits set (the kernels' "not
 // written yet" pattern); made on first use, refilled after a sweep gave up waiting.
 template <class T>
@@ -1177,7 +1207,8 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
     const std::vector<WavePlan> cand = wavePlanCandidates(c->dim, (int)c->pcHost.nx, (int)c->pcHost.ny,
                                                           (int)c->pcHost.nz, c->b, sizeof(T) == 8);
     const bool lanes = c->lanePlan.ok && (c->iluKernel == DXG_ILU_AUTO || c->iluKernel == DXG_ILU_LANES);
-    if (cand.size() < 2 && !lanes) return;
+    const bool lines2d = c->line2dOk && (c->iluKernel == DXG_ILU_AUTO || c->iluKernel == DXG_ILU_LANES);
+    if (cand.size() < 2 && !lanes && !lines2d) return;
     cudaStream_t st = c->stream;
     cudaEvent_t e0, e1;
     DXG_CUDA(cudaEventCreate(&e0));
@@ -1244,6 +1275,22 @@ void tuneWavePlan(dxg_ctx* c, const T* A, T* L, T* Dinv, const T* in, T* out)
         DXG_CUDA(cudaMemcpy(&flag, c->singular.get() + 1, sizeof(int), cudaMemcpyDeviceToHost));
         c->laneWave = flag == 0 && (bestMs == 0.f || laneBest < bestMs);
     }
+    // the one-CTA line sweeps of 2D grids
+    if (lines2d) {
+        LaneWaveArgs<T> lt = line2dArgs<T>(c, A, L, Dinv, in, out);
+        lt.ks = nullptr;   // never skip while timing
+        launchTpfaLine2d<T>(lt, lt, c->b, st);   // warm-up
+        DXG_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < kReps; ++r) launchTpfaLine2d<T>(lt, lt, c->b, st);
+        DXG_CUDA(cudaEventRecord(e1, st));
+        DXG_CUDA(cudaEventSynchronize(e1));
+        c->launches += 2 * (1 + kReps);
+        float ms = 0.f;
+        DXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= kReps;
+        c->line2dMs = ms;
+        c->line2d = bestMs == 0.f || ms < bestMs;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->wavePlan = best;
@@ -1254,6 +1301,11 @@ int64_t iluApply(dxg_ctx* c, const IluArgs<T, T>& ia, const T* A, T* L, T* Dinv,
 {
     TimedScope ts(c, DXG_KC_ILU_SWEEP, c->bytesSweep * sizeof(T) / 8.0);
     if (c->iluKernel == DXG_ILU_REDBLACK) return launchRbApply<T>(rbArgs<T>(c, A, Dinv), c->b, c->dim, d, v, c->stream);
+    if (useLine2d(c)) {
+        const LaneWaveArgs<T> la = line2dArgs<T>(c, A, L, Dinv, d, v);
+        launchTpfaLine2d<T>(la, la, c->b, c->stream);
+        return 2;
+    }
     if (useLane(c)) {
         const LaneWaveArgs<T> la = laneArgs<T>(c, A, L, Dinv, d, v);
         launchLaneWaveApply<T>(c->lanePlan, la, la, c->stream);
@@ -2001,8 +2053,8 @@ int dxg_set_ilu_kernel(dxg_ctx* c, int kind)
         c->err = "no wavefront plan fits this grid";
         return DXG_ERR_ARG;
     }
-    if (kind == DXG_ILU_LANES && c->uploaded && !c->lanePlan.ok) {
-        c->err = "the lane sweeps need a 3D grid of 2x2 blocks that fits them";
+    if (kind == DXG_ILU_LANES && c->uploaded && !c->lanePlan.ok && !c->line2dOk) {
+        c->err = "the lane sweeps need a 3D grid of 2x2 blocks or a 2D grid of up to 512 lines that fits them";
         return DXG_ERR_ARG;
     }
     c->iluKernel = kind;
@@ -2072,6 +2124,19 @@ int dxg_describe(const dxg_ctx* c, char* buf, int64_t len)
                                                                (int)c->pcHost.nz).size() + 1) +
               " levels of 2x2(x2) aggregation, damped block-Jacobi smoothing";
     else if (c->iluKernel == DXG_ILU_REDBLACK) out = "ILU(0): red-black ordering, two parallel passes per sweep";
+    else if (useLine2d(c)) {
+        out = "ILU(0): line sweeps in one CTA (one thread per grid line, levels x+y)";
+        if (c->line2dMs > 0) {
+            char tmp[96];
+            std::snprintf(tmp, sizeof tmp, ", tuned (ms per apply: line sweeps %.3f", c->line2dMs);
+            out += tmp;
+            for (int k = 0; k < c->waveTuneCount; ++k) {
+                std::snprintf(tmp, sizeof tmp, ", cluster wavefront %d CTAs %.3f", c->waveTuneCtas[k], c->waveTuneMs[k]);
+                out += tmp;
+            }
+            out += ")";
+        }
+    }
     else if (useLane(c)) {
         const LanePlan& p = c->lanePlan;
         char tmp[200];

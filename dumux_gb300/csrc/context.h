@@ -115,6 +115,9 @@ struct dxg_ctx {
     double laneTuneMs = 0.0;       // the lane sweeps' time per apply at the tuning (the form run)
     double laneFormMs[2] = {0.0, 0.0};   // per form: 0 registers, 1 shared-memory ring
     int laneRingMode = 0;          // 0 timed, 1 register form, 2 shared-memory-ring form
+    bool line2dOk = false;         // the one-CTA line sweeps of 2D TPFA systems fit
+    bool line2d = false;           // ... and the timing at the first factorisation chose them
+    double line2dMs = 0.0;
     dxg::DevBuf<unsigned char> laneHandoff;
     size_t laneHandoffBytes = 0;
     // limit of every bounded wait of the sweeps (0: the kernels' default, 0.5 s)

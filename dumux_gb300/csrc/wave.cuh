@@ -58,6 +58,11 @@ template <class T>
 LanePlan makeLanePlan(int dim, int nx, int ny, int nz, int b);
 template <class T>
 void launchLaneWaveApply(const LanePlan& p, const LaneWaveArgs<T>& fwd, const LaneWaveArgs<T>& bwd, cudaStream_t st);
+// One-CTA line sweeps of 2D cc-TPFA systems (linesweep.cu): one thread per grid line, both block
+// rows, for grids of up to 512 lines; uses nx, ny, N, Lf, A, Dinv, rhs, v and ks of the args.
+bool tpfaLine2dFits(int dim, int nx, int ny, int b);
+template <class T>
+void launchTpfaLine2d(const LaneWaveArgs<T>& fwd, const LaneWaveArgs<T>& bwd, int b, cudaStream_t st);
 
 struct WavePlan {
     int ctas = 0, linesPerCta = 0, haloLines = 0, threads = 0, lpt = 0;

@@ -120,7 +120,8 @@ def test_newton_2p_mixed_precision_within_1e6():
     assert np.max(np.abs(um[:, 1] - uo[:, 1])) / max(np.max(np.abs(uo[:, 1])), 1e-12) <= 1e-6
 
 
-@pytest.mark.parametrize("dims,precision", [((13, 11), "fp64"), ((7, 6, 9), "fp64"), ((64, 64, 32), "fp64"),
+@pytest.mark.parametrize("dims,precision", [((13, 11), "fp64"), ((100, 100), "fp64"), ((37, 300), "fp64"),
+                                            ((33, 70), "mixed"), ((7, 6, 9), "fp64"), ((64, 64, 32), "fp64"),
                                             ((7, 6, 9), "mixed"), ((40, 1, 3), "fp64"), ((1, 5, 4), "fp64"),
                                             ((9, 70, 5), "fp64"), ((6, 5, 37), "fp64"), ((6, 5, 37), "mixed"),
                                             ((5, 100, 19), "fp64")])
@@ -136,8 +137,9 @@ def test_wavefront_ilu_equals_level_scheduled(dims, precision):
     smax = 0.3 if max(dims) >= 37 or (len(dims) == 3 and dims[1] >= 70) else 0.6
     u[:, 1] = np.random.default_rng(2).uniform(0, smax, len(u))
     out = {}
+    # 2D "lanes": the one-CTA line sweeps (one thread per grid line)
     kinds = (("levels", "wavefront", "lanes", "lanes-registers", "lanes-ring") if len(dims) == 3
-             else ("levels", "wavefront"))
+             else ("levels", "wavefront", "lanes"))
     for kind in kinds:
         ctx = Context(d, precision=precision)
         ctx.set_ilu_kernel(kind.split("-")[0])
