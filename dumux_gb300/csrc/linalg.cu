@@ -1551,10 +1551,11 @@ static unsigned stencilThreads(const StencilArgs& a)
 
 // 3D (27-point) stencils: the cluster factorisation (the rows carry up to 101 update triples;
 // one CTA level by level took 23 ms for a 2p 32x32x16 factor on GB300, the cluster version
-// with one warp per row spreads a level over 16 SMs); 2D stencils (12 triples): one CTA
+// with one warp per row spreads a level over 16 SMs); 2D stencils (12 triples): the cluster
+// factorisation from 4096 cells, one CTA below
 void launchStencilFactor(const StencilArgs& a, cudaStream_t st)
 {
-    if (a.S == 27) {
+    if (a.S == 27 || a.N >= 4096) {
         launchStencilFactorCluster(a, st);
         return;
     }
