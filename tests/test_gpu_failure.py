@@ -71,3 +71,23 @@ def test_lane_sweep_wait_limit_expires_and_the_context_recovers(form):
     again = ctx.linear_solve(1e-10, 500)
     assert again["converged"] and again["iterations"] == first["iterations"]
     assert np.array_equal(ctx.update(), x0)
+
+
+def test_lane_ring_form_refused_where_it_does_not_fit():
+    """A grid whose lane sweeps fit only in the register form (200-cell lines: the
+    shared-memory ring would not fit beside the plane history): dxg_set_lane_ring refuses the
+    ring form with DXG_ERR_ARG and the context keeps working with the register form."""
+    desc, u0 = problems.dnapl_2p(cells=(200, 8, 4), seed=3)
+    u = u0.reshape(-1, 2).copy()
+    u[:, 1] = np.random.default_rng(1).uniform(0.0, 0.3, len(u))
+    ctx = Context(desc)
+    ctx.set_ilu_kernel("lanes")
+    with pytest.raises(Exception):
+        ctx.set_lane_ring("ring")
+    ctx.set_lane_ring("registers")
+    ctx.set_solution(u.reshape(-1))
+    ctx.set_prev_solution(u0)
+    ctx.set_time_step(250.0)
+    ctx.assemble_jacobian_and_residual()
+    res = ctx.linear_solve(1e-10, 1000)
+    assert res["converged"] and "register ring" in ctx.describe()
