@@ -316,6 +316,12 @@ __global__ void __launch_bounds__(kLwThreads) laneWaveKernel(LaneWaveArgs<T> a)
         for (int k = threadIdx.x; k < levels * 2; k += kLwThreads) yin[k] = lwEmpty<T>();
     if (threadIdx.x == 0) stopFlag = 0;
     cluster.sync();
+    // The backward sweep reads the forward sweep's output.  It is launched as a programmatic
+    // dependent of the forward sweep: its CTAs start and fill their histories while the forward
+    // sweep runs (whose CTAs allow that right after their own start) and wait here until it has
+    // completed and its writes are visible.
+    if (DIR < 0) asm volatile("griddepcontrol.wait;" ::: "memory");
+    else asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const bool skip = a.ks && a.ks->status != KS_RUNNING;
 
     // record sources of this lane's line at x = 0 (slots: forward -x 2, -y 1, -z 0; backward
@@ -521,6 +527,12 @@ __global__ void __launch_bounds__(kLwThreads) laneRingKernel(LaneWaveArgs<T> a)
         for (int k = threadIdx.x; k < levels * 2; k += kLwThreads) yin[k] = lwEmpty<T>();
     if (threadIdx.x == 0) abortFlag = 0;
     cluster.sync();
+    // The backward sweep reads the forward sweep's output.  It is launched as a programmatic
+    // dependent of the forward sweep: its CTAs start and fill their histories while the forward
+    // sweep runs (whose CTAs allow that right after their own start) and wait here until it has
+    // completed and its writes are visible.
+    if (DIR < 0) asm volatile("griddepcontrol.wait;" ::: "memory");
+    else asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const bool skip = a.ks && a.ks->status != KS_RUNNING;
 
     const uint32_t zinDown = zDownLocal ? lwMapa(lwSmemAddr(zin), zDown % cs) : 0u;
@@ -722,13 +734,16 @@ cudaError_t lwLaunchOne(const LanePlan& p, const LaneWaveArgs<T>& a, cudaStream_
     cfg.blockDim = dim3(kLwThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = p.clusterSize;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    // the backward sweep as a programmatic dependent of the forward sweep before it
+    cfg.numAttrs = (DIR < 0 && !query) ? 2 : 1;
     if (query) {
         int n = 0;
         e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
