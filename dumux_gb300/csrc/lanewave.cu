@@ -16,6 +16,10 @@
 //   * no vote and no barrier per step: a wait that expires records DXG_ERR_TIMEOUT and sets the
 //     CTA's stop flag, after which every wait of the CTA returns at once (the sweep runs out on
 //     stale values, which the error discards).
+// A second form (laneRingKernel, below) copies the records ahead into a shared-memory ring with
+// cp.async and polls before the step's FMAs; it is faster where most plane hand-offs cross
+// clusters, and the context times both.  The backward sweep of either form is launched as a
+// programmatic dependent of the forward one, so its prologue overlaps the forward sweep.
 //
 // Dependencies of cell (x, y, z) at level x+y+z: (x-1, y, z), (x, y-1, z), (x, y, z-1) at the
 // level before (forward; mirrored for the backward sweep).
